@@ -1,0 +1,100 @@
+"""Locates (and builds on demand) oracle/_ref/libpvref.so: pieces of the reference CPU
+path compiled from the reference source tree.  Only available where the reference
+tree is mounted; tests that need it skip elsewhere."""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+REF_ROOT = os.environ.get("OPENPV_REFERENCE", "/root/reference")
+LIB = os.path.join(ROOT, "oracle", "_ref", "libpvref.so")
+
+
+class RefLoc(C.Structure):
+    _fields_ = [("nbatch", C.c_int), ("nx", C.c_int), ("ny", C.c_int), ("nf", C.c_int),
+                ("lt", C.c_int), ("rt", C.c_int), ("dn", C.c_int), ("up", C.c_int)]
+
+    @staticmethod
+    def of(loc):
+        h = loc.halo
+        return RefLoc(loc.nbatch, loc.nx, loc.ny, loc.nf, h.lt, h.rt, h.dn, h.up)
+
+
+_lib = None
+
+
+def available():
+    return os.path.exists(LIB) or os.path.isdir(os.path.join(REF_ROOT, "src", "components"))
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if os.path.isdir(os.path.join(REF_ROOT, "src")):
+            subprocess.check_call(["make", "-s", "-f", os.path.join(ROOT, "oracle", "Makefile.ref"),
+                                   f"REF={REF_ROOT}"])
+        _lib = C.CDLL(LIB)
+        vp = C.c_void_p
+        lp = C.POINTER(RefLoc)
+        _lib.pvr_patch_geometry.restype = C.c_int
+        _lib.pvr_patch_geometry.argtypes = [lp, lp, C.c_int, C.c_int] + [vp] * 7
+        _lib.pvr_lca_update.restype = None
+        _lib.pvr_lca_update.argtypes = [lp, C.c_int, vp, C.c_float, vp, vp, vp]
+        _lib.pvr_gsyn_accumulate.restype = None
+        _lib.pvr_gsyn_accumulate.argtypes = [C.c_int, C.c_int, vp, vp, vp]
+        _lib.pvr_apply_vertices.restype = None
+        _lib.pvr_apply_vertices.argtypes = [lp, C.c_int, vp, vp, vp, vp, vp]
+        _lib.pvr_cost.restype = C.c_double
+        _lib.pvr_cost.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double]
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+def patch_geometry(pre, post, nxp, nyp):
+    n = pre.num_ext
+    nxs = np.zeros(n, np.uint16)
+    nys = np.zeros(n, np.uint16)
+    off = np.zeros(n, np.uint32)
+    gs = np.zeros(n, np.int64)
+    ap = np.zeros(n, np.int64)
+    us = np.zeros(n, np.int64)
+    nkx = pre.nx // post.nx if pre.nx > post.nx else 1
+    nky = pre.ny // post.ny if pre.ny > post.ny else 1
+    ti = np.zeros(nkx * nky * pre.nf * nxp * nyp * post.nf, np.int32)
+    rc = lib().pvr_patch_geometry(C.byref(RefLoc.of(pre)), C.byref(RefLoc.of(post)), nxp, nyp, _p(nxs), _p(nys),
+                                  _p(off), _p(gs), _p(ap), _p(us), _p(ti))
+    if rc != 0:
+        raise ValueError("reference rejected geometry")
+    return nxs, nys, off, gs, ap, us, ti
+
+
+def lca_update(loc, g, a_ext, v, dt_adapt, tau, self_interact=True):
+    v = np.ascontiguousarray(v, np.float32).copy()
+    lib().pvr_lca_update(C.byref(RefLoc.of(loc)), int(self_interact),
+                         _p(np.ascontiguousarray(dt_adapt, np.float64)), tau,
+                         _p(np.ascontiguousarray(g, np.float32)), _p(np.ascontiguousarray(a_ext, np.float32)), _p(v))
+    return v
+
+
+def gsyn_accumulate(gsyn, coeffs):
+    g = np.ascontiguousarray(gsyn, np.float32)
+    out = np.zeros(g.shape[1:], np.float32)
+    lib().pvr_gsyn_accumulate(g[0].size, g.shape[0], _p(np.ascontiguousarray(coeffs, np.float32)), _p(g), _p(out))
+    return out
+
+
+def apply_vertices(loc, v, vV, vA, slopes):
+    a = np.zeros(loc.ext_shape(), np.float32)
+    lib().pvr_apply_vertices(C.byref(RefLoc.of(loc)), len(vV), _p(np.ascontiguousarray(vV, np.float32)),
+                             _p(np.ascontiguousarray(vA, np.float32)), _p(np.ascontiguousarray(slopes, np.float32)),
+                             _p(np.ascontiguousarray(v, np.float32)), _p(a))
+    return a
+
+
+def cost(kind, p0, p1, x):
+    return lib().pvr_cost(kind, p0, p1, float(x))

@@ -1,0 +1,115 @@
+"""Pins the CPU oracle against the reference's own code compiled from its source tree
+(oracle/_ref/libpvref.so): PatchGeometry tables, the .kpp update kernels and the
+energy cost functions, compared bit for bit.  Skips where the reference tree is absent."""
+import numpy as np
+import pytest
+
+from tests import refbuild
+
+pytestmark = pytest.mark.skipif(not refbuild.available(), reason="reference source tree not mounted")
+
+
+def L(O, nb, nx, ny, nf, mx, my=None):
+    return O.Loc.make(nb, nx, ny, nf, mx, my)
+
+
+# (pre nx, ny, nf, halo x, halo y), (post nx, ny, nf, halo x, halo y), nxp, nyp
+GEOMETRIES = [
+    ((16, 16, 64, 2, 2), (32, 32, 1, 3, 3), 8, 8),       # LCA V1 -> error (one-to-many x2)
+    ((32, 32, 1, 3, 3), (16, 16, 64, 2, 2), 4, 4),       # error -> V1 (many-to-one x2, post patch)
+    ((16, 16, 512, 2, 2), (32, 32, 3, 3, 3), 8, 8),      # batched LCA, 3 colour channels
+    ((16, 16, 256, 2, 2), (64, 64, 1, 6, 6), 16, 16),    # stride-4 dictionary (one-to-many x4)
+    ((64, 64, 1, 6, 6), (16, 16, 256, 2, 2), 4, 4),      # many-to-one x4
+    ((64, 32, 24, 4, 4), (128, 64, 1, 8, 8), 18, 18),    # the reference GPU LCA system test
+    ((32, 32, 16, 3, 3), (32, 32, 8, 0, 0), 7, 7),       # one-to-one, delivery microbench shape
+    ((12, 9, 3, 0, 0), (12, 9, 2, 0, 0), 5, 3),          # one-to-one, no halo: shrunken patches
+    ((8, 8, 2, 5, 5), (8, 8, 3, 1, 1), 3, 3),            # halo wider than the margin
+    ((6, 10, 2, 1, 1), (12, 20, 4, 2, 2), 6, 4),         # one-to-many, unequal axes
+    ((24, 16, 2, 3, 3), (6, 4, 3, 0, 0), 3, 3),          # many-to-one x4, no post halo
+]
+
+
+@pytest.mark.parametrize("g", GEOMETRIES)
+def test_patch_geometry_bitexact(oracle, g):
+    (a, b, c, d, e), (f, h, i, j, k), nxp, nyp = g
+    pre, post = L(oracle, 1, a, b, c, d, e), L(oracle, 1, f, h, i, j, k)
+    patches, gs, ap, us = oracle.patch_geometry(pre, post, nxp, nyp)
+    rnx, rny, roff, rgs, rap, rus, _ = refbuild.patch_geometry(pre, post, nxp, nyp)
+    assert np.array_equal(patches["nx"], rnx)
+    assert np.array_equal(patches["ny"], rny)
+    assert np.array_equal(patches["offset"], roff)
+    assert np.array_equal(gs, rgs)
+    assert np.array_equal(ap, rap)
+    assert np.array_equal(us, rus)
+
+
+@pytest.mark.parametrize("bad", [((16, 16, 1, 0, 0), (16, 16, 1, 0, 0), 4, 4),   # even one-to-one
+                                 ((16, 16, 1, 0, 0), (48, 48, 1, 0, 0), 6, 6),   # ratio 3
+                                 ((16, 16, 1, 0, 0), (32, 32, 1, 0, 0), 5, 5)])  # patch not multiple of 2
+def test_patch_geometry_rejects_like_reference(oracle, bad):
+    (a, b, c, d, e), (f, h, i, j, k), nxp, nyp = bad
+    pre, post = L(oracle, 1, a, b, c, d, e), L(oracle, 1, f, h, i, j, k)
+    with pytest.raises(ValueError):
+        refbuild.patch_geometry(pre, post, nxp, nyp)
+    with pytest.raises(ValueError):
+        oracle.patch_geometry(pre, post, nxp, nyp)
+
+
+@pytest.mark.parametrize("halo", [(0, 0), (2, 2), (3, 1)])
+@pytest.mark.parametrize("self_interact", [True, False])
+def test_lca_update_bitexact(oracle, halo, self_interact):
+    rng = np.random.default_rng(7)
+    loc = L(oracle, 3, 11, 7, 5, *halo)
+    v = rng.normal(size=loc.res_shape()).astype(np.float32)
+    g = rng.normal(size=loc.res_shape()).astype(np.float32)
+    a = rng.normal(size=loc.ext_shape()).astype(np.float32)
+    dt = np.array([1.0, 0.5, 0.37], np.float64)
+    mine = oracle.lca_update(loc, g, a, v, dt, 100.0, self_interact)
+    ref = refbuild.lca_update(loc, g, a, v, dt, 100.0, self_interact)
+    assert np.array_equal(mine.view(np.uint32), ref.view(np.uint32))
+
+
+@pytest.mark.parametrize("nch", [1, 2, 3])
+def test_gsyn_accumulate_bitexact(oracle, nch):
+    rng = np.random.default_rng(nch)
+    gs = rng.normal(size=(nch, 4, 9, 5)).astype(np.float32)
+    coeffs = np.array([1.0, -1.0, 0.5][:nch], np.float32)
+    assert np.array_equal(oracle.gsyn_accumulate(gs, coeffs).view(np.uint32),
+                          refbuild.gsyn_accumulate(gs, coeffs).view(np.uint32))
+
+
+THRESHOLDS = [  # VThresh, AMin, AMax, AShift, VWidth
+    (0.1, 0.0, np.inf, 0.1, 0.0),        # soft threshold (LCA)
+    (0.15, 0.0, np.inf, 0.15, 0.0),
+    (0.025, 0.0, np.inf, 0.0, 0.025),    # firm threshold (reference LCA system tests)
+    (0.5, 0.0, np.inf, 0.0, 0.0),        # hard threshold
+    (0.1, 0.0, 0.7, 0.1, 0.0),           # soft threshold clipped at AMax
+    (-np.inf, -np.inf, np.inf, 0.0, 0.0),  # identity (error layers)
+]
+
+
+@pytest.mark.parametrize("th", THRESHOLDS)
+def test_threshold_cpu_form_matches_reference_vertex_form(oracle, th):
+    """The reference's CPU form (applyVThresh) and its GPU vertex form give the same
+    activity values (up to the sign of zero and rounding in the linear ramp)."""
+    rng = np.random.default_rng(3)
+    loc = L(oracle, 2, 13, 6, 4, 2, 1)
+    v = (rng.normal(size=loc.res_shape()) * 0.5).astype(np.float32)
+    a_cpu = oracle.ann_activity(loc, v, *[np.float32(x) for x in th])
+    vV, vA, sl = oracle.ann_vertices(*[np.float32(x) for x in th])
+    a_vert = refbuild.apply_vertices(loc, v, vV, vA, sl)
+    np.testing.assert_allclose(a_cpu, a_vert, rtol=2e-6, atol=1e-7)
+
+
+@pytest.mark.parametrize("kind,p0,p1", [(0, 0, 0), (1, 0, 0), (2, 0.025, 0.025), (2, 0.1, 0.0)])
+def test_cost_functions_match_reference(oracle, kind, p0, p1):
+    rng = np.random.default_rng(11)
+    loc = L(oracle, 2, 5, 4, 3, 1)
+    buf = (rng.normal(size=loc.ext_shape()) * 0.1).astype(np.float32)
+    mine = oracle.cost_sum(loc, buf, kind, p0, p1)
+    for b in range(2):
+        ref = 0.0
+        res = buf[b, 1:-1, 1:-1, :].ravel()
+        for x in res:
+            ref += refbuild.cost(kind, p0, p1, float(x))
+        assert mine[b] == ref
