@@ -1,0 +1,227 @@
+/*
+ * pvgpu.h -- C ABI of the GB300-native (sm_103a) synaptic-delivery + LCA-update path.
+ *
+ * One shared library, libpvgpu.so, built from openpv_gb300/csrc.  Every entry point:
+ *   - takes device pointers in the OpenPV layouts (activity [nbatch][nyExt][nxExt][nf],
+ *     GSyn channel [nbatch][ny][nx][nf], shared weights [kernel][nyp][nxp][nfp], all FP32
+ *     unless stated),
+ *   - takes an explicit CUDA stream (a cudaStream_t passed as void*; NULL = legacy default
+ *     stream) and never synchronises it, so a sequence of calls can be captured in a CUDA
+ *     graph,
+ *   - returns a pvgpu_status and never aborts.  The reference's handleError
+ *     (arch/cuda/cuda_util.hpp:14-27) turns every CUDA error into Fatal(); adapters that
+ *     want that behaviour test the status and call their own Fatal.
+ *
+ * Each declaration names the reference interface it replaces (paths relative to the
+ * OpenPV source tree).
+ */
+#ifndef PVGPU_H_
+#define PVGPU_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+   PVGPU_OK = 0,
+   PVGPU_ERR_BAD_ARG = 1,           /* null pointer, negative size, inconsistent locs */
+   PVGPU_ERR_OOM = 2,               /* device allocation failed */
+   PVGPU_ERR_LAUNCH = 3,            /* kernel launch or CUDA runtime error */
+   PVGPU_ERR_TIMEOUT = 4,           /* a bounded device-side wait gave up */
+   PVGPU_ERR_UNSUPPORTED_SHAPE = 5, /* legal OpenPV geometry this build does not handle */
+   PVGPU_ERR_ILLEGAL_GEOMETRY = 6   /* geometry OpenPV itself rejects (PatchGeometry::verifyPatchSize) */
+} pvgpu_status;
+
+/* PVHalo / PVLayerLoc (include/PVLayerLoc.h:14-26), batch-local fields. */
+typedef struct {
+   int lt, rt, dn, up;
+} pvgpu_halo;
+
+typedef struct {
+   int nbatch, nx, ny, nf;
+   pvgpu_halo halo;
+} pvgpu_loc;
+
+/* SparseList<float>::Entry (structures/SparseList.hpp:19-22): extended index + value. */
+typedef struct {
+   uint32_t index;
+   float value;
+} pvgpu_entry;
+
+/* Connection geometry shared by the delivery calls: the presynaptic (source) layer,
+ * the postsynaptic (target) layer and the presynaptic patch size nxp x nyp (nfp is
+ * post.nf).  Mirrors the geometry fields of recv_pre_params / recv_post_params
+ * (cudakernels/CudaRecvPre.hpp:19-45, cudakernels/CudaRecvPost.hpp:18-80). */
+typedef struct {
+   pvgpu_loc pre;
+   pvgpu_loc post;
+   int nxp, nyp;
+   float dt_factor; /* 1 for convolve delivery (HyPerDelivery.cpp:26-81) */
+} pvgpu_conn_desc;
+
+/* Delivery numerics. */
+enum {
+   PVGPU_DELIVER_FAST = 0,           /* FP32 with fused multiply-add, tiled order */
+   PVGPU_DELIVER_REFERENCE_ORDER = 1 /* FP32, separately rounded products and sums in the
+                                        reference's single-thread order: bit-identical to the
+                                        reference CPU path run with -t 1 */
+};
+
+/* ---- library ------------------------------------------------------------ */
+const char *pvgpu_version(void);
+const char *pvgpu_status_string(pvgpu_status s);
+/* Last CUDA error string recorded by a failing call on this thread. */
+const char *pvgpu_last_error(void);
+
+/* ---- a1: active-index compaction ------------------------------------------------------
+ * Replaces DataStore::updateActiveIndices (columns/DataStore.cpp:46-66), which the reference
+ * runs on the host after a device->host copy.  Stable: entries of each batch element are in
+ * ascending extended index, value = the exact activity float; numActive[b] (long in the
+ * reference) receives the count.  entries has capacity numExt per batch element.
+ * Scratch: uses `scratch` (device, >= pvgpu_compact_scratch_bytes) for per-chunk counts. */
+size_t pvgpu_compact_scratch_bytes(int nbatch, int64_t numExt);
+pvgpu_status pvgpu_compact_active(
+      const float *aExt,
+      int nbatch,
+      int64_t numExt,
+      pvgpu_entry *entries,
+      int64_t *numActive,
+      void *scratch,
+      size_t scratchBytes,
+      void *stream);
+
+/* ---- a4: presynaptic-perspective delivery -----------------------------------------------
+ * Replaces CudaRecvPre::do_run / HyPerLayer_recv_pre (cudakernels/CudaRecvPre.cu:10-101)
+ * driven by PresynapticPerspectiveGPUDelivery::deliver (delivery/PresynapticPerspectiveGPUDelivery.cpp:198-270),
+ * with the CPU semantics of PresynapticPerspectiveConvolveDelivery::deliver
+ * (delivery/PresynapticPerspectiveConvolveDelivery.cpp:61-192).  Shared weights, one arbor.
+ * Sparse input: entries/numActive (SparseList per batch element, stride numPreExt); pass
+ * entries = NULL to read the dense activity aExt instead (zeros skipped).  GSyn of the
+ * channel ([nbatch][post restricted]) is accumulated into.  No atomics: each GSyn element
+ * is owned by one thread and receives its contributions in the reference's order
+ * (patch row, then ascending presynaptic index). */
+pvgpu_status pvgpu_deliver_pre(
+      const pvgpu_conn_desc *conn,
+      const pvgpu_entry *entries,
+      const int64_t *numActive,
+      const float *aExt,
+      const float *weights,
+      float *gsyn,
+      int mode,
+      void *stream);
+
+/* ---- a5: postsynaptic-perspective delivery ----------------------------------------------
+ * Replaces CudaRecvPost::do_run (cudnnConvolutionForward plus the NHWC<->NCHW permutes,
+ * cudakernels/CudaRecvPost.cpp:357-389, arch/cuda/CudaKernel.cu:20-135) driven by
+ * PostsynapticPerspectiveGPUDelivery::deliver (delivery/PostsynapticPerspectiveGPUDelivery.cpp:239-281),
+ * with the semantics of PostsynapticPerspectiveConvolveDelivery::deliver
+ * (delivery/PostsynapticPerspectiveConvolveDelivery.cpp:56-151).
+ * conn describes the connection pre->post; postWeights are the post-perspective weights
+ * (kernels of the post->pre geometry, patch nxpPost x nypPost x pre.nf, as produced by
+ * TransposeWeights::transposeShared, or the original connection's weights for a
+ * TransposeConn).  Reads the whole unshrunken receptive field from the extended
+ * presynaptic activity, which needs pre.halo >= the connection's margin. */
+pvgpu_status pvgpu_deliver_post(
+      const pvgpu_conn_desc *conn,
+      const float *aExt,
+      const float *postWeights,
+      float *gsyn,
+      int mode,
+      void *stream);
+
+/* Post weights from pre weights: TransposeWeights::transposeShared (utils/TransposeWeights.cpp:56-115)
+ * on the device, for WeightsPair::finalizeUpdate (components/WeightsPair.cpp:261-277). */
+pvgpu_status pvgpu_transpose_weights(const pvgpu_conn_desc *conn, const float *preWeights, float *postWeights, void *stream);
+
+/* ---- a6..a9: layer update ------------------------------------------------------------- */
+/* updateGSynAccumulatorOnGPU (components/GSynAccumulator.kpp:16-44): G = sum_ch coeff[ch]*GSyn[ch].
+ * coeffs is a host array of numChannels floats. */
+pvgpu_status pvgpu_gsyn_accumulate(
+      int64_t numNeuronsAcrossBatch,
+      int numChannels,
+      const float *coeffs,
+      const float *gsyn,
+      float *g,
+      void *stream);
+
+/* updateHyPerLCAOnGPU (components/HyPerLCAInternalStateBuffer.kpp:18-63):
+ * V = e*V + (1-e)*(G + selfInteract*A_ext), e = (float)exp(-dtAdapt[b]/tau).  dtAdapt is a
+ * device array of nbatch doubles.  Products and sums are rounded as the CPU path rounds them. */
+pvgpu_status pvgpu_lca_update(
+      const pvgpu_loc *loc,
+      int selfInteract,
+      const double *dtAdapt,
+      float tau,
+      const float *g,
+      const float *aExt,
+      float *v,
+      void *stream);
+
+/* ANNActivityBuffer threshold, CPU form (components/ANNActivityBuffer.cpp:432-558; the
+ * reference GPU runs the vertex form of ANNActivityBuffer.kpp:16-77 instead): A_ext = T(V) on
+ * the restricted region; the halo is left untouched. */
+pvgpu_status pvgpu_ann_activity(
+      const pvgpu_loc *loc,
+      const float *v,
+      float VThresh,
+      float AMin,
+      float AMax,
+      float AShift,
+      float VWidth,
+      float *aExt,
+      void *stream);
+
+/* The three update kernels fused (HyPerActivityComponent::updateActivity,
+ * components/HyPerActivityComponent.tpp:81-90, running GSynAccumulator -> HyPerLCAInternalStateBuffer
+ * -> ANNActivityBuffer): one pass over the layer.  gsyn holds numChannels channels. */
+typedef struct {
+   pvgpu_loc loc;
+   int numChannels;
+   float coeffs[4];
+   int selfInteract;
+   float tau;
+   float VThresh, AMin, AMax, AShift, VWidth;
+} pvgpu_lca_layer_desc;
+
+pvgpu_status pvgpu_lca_layer_update(
+      const pvgpu_lca_layer_desc *desc,
+      const float *gsyn,
+      const double *dtAdapt,
+      float *v,
+      float *aExt,
+      void *stream);
+
+/* ---- a11: energy probes, FP64 on the device ------------------------------------------------
+ * CostFunctionSum<C>::calculateSumNoMask (probes/CostFunctionSum.hpp:86-108) per batch element:
+ * kind 0 = L2 (x^2), 1 = L1 (|x|), 2 = firm threshold (p0 = VThresh, p1 = VWidth,
+ * probes/CostFunctions.hpp:32-49).  out: device array of nbatch doubles (overwritten).
+ * Deterministic fixed-order reduction. */
+pvgpu_status pvgpu_cost_sum(
+      const pvgpu_loc *loc,
+      const float *bufExt,
+      int kind,
+      double p0,
+      double p1,
+      double *out,
+      void *stream);
+
+/* ---- a12: Hebbian weight update and the adjoint of delivery ------------------------------
+ * HebbianUpdater::update_dW / updateInd_dW (weightupdaters/HebbianUpdater.cpp:476-629), shared
+ * weights, summed over the batch, normalize_dW off: dW[kernel][item] = dWMax * sum pre*post.
+ * dw ([numKernels][nyp][nxp][post.nf]) is overwritten.  Deterministic (no atomics). */
+pvgpu_status pvgpu_hebbian_dw(
+      const pvgpu_conn_desc *conn,
+      float dWMax,
+      const float *preExt,
+      const float *postExt,
+      float *dw,
+      void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PVGPU_H_ */

@@ -1,0 +1,213 @@
+"""ctypes binding of libpvgpu.so (include/pvgpu.h).
+
+This is the same C ABI a reference-side adapter binds; the Python tests and bench
+call through it exactly as a C++ host would.  Device memory and streams come from
+PyTorch (plumbing only): tensors are passed as raw device pointers and the current
+torch stream as the cudaStream_t.
+
+The library must exist: importing this module on a machine without libpvgpu.so
+raises, there is no CPU fallback.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libpvgpu.so")
+
+PVGPU_OK = 0
+DELIVER_FAST = 0
+DELIVER_REFERENCE_ORDER = 1
+COST_L2, COST_L1, COST_FIRM = 0, 1, 2
+
+
+class PvgpuError(RuntimeError):
+    def __init__(self, status, what):
+        self.status = status
+        super().__init__(f"{what}: {status_string(status)} ({last_error()})")
+
+
+class Halo(C.Structure):
+    _fields_ = [("lt", C.c_int), ("rt", C.c_int), ("dn", C.c_int), ("up", C.c_int)]
+
+
+class Loc(C.Structure):
+    _fields_ = [("nbatch", C.c_int), ("nx", C.c_int), ("ny", C.c_int), ("nf", C.c_int), ("halo", Halo)]
+
+    @staticmethod
+    def make(nbatch, nx, ny, nf, mx=0, my=None):
+        my = mx if my is None else my
+        return Loc(nbatch, nx, ny, nf, Halo(mx, mx, my, my))
+
+    @property
+    def nx_ext(self):
+        return self.nx + self.halo.lt + self.halo.rt
+
+    @property
+    def ny_ext(self):
+        return self.ny + self.halo.dn + self.halo.up
+
+    @property
+    def num_ext(self):
+        return self.nx_ext * self.ny_ext * self.nf
+
+    @property
+    def num_res(self):
+        return self.nx * self.ny * self.nf
+
+    def ext_shape(self):
+        return (self.nbatch, self.ny_ext, self.nx_ext, self.nf)
+
+    def res_shape(self):
+        return (self.nbatch, self.ny, self.nx, self.nf)
+
+
+class ConnDesc(C.Structure):
+    _fields_ = [("pre", Loc), ("post", Loc), ("nxp", C.c_int), ("nyp", C.c_int), ("dt_factor", C.c_float)]
+
+
+class LcaLayerDesc(C.Structure):
+    _fields_ = [("loc", Loc), ("numChannels", C.c_int), ("coeffs", C.c_float * 4), ("selfInteract", C.c_int),
+                ("tau", C.c_float), ("VThresh", C.c_float), ("AMin", C.c_float), ("AMax", C.c_float),
+                ("AShift", C.c_float), ("VWidth", C.c_float)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: build it with openpv_gb300.build.build() "
+                               "(there is no CPU fallback)")
+        _lib = C.CDLL(LIB_PATH)
+        _declare(_lib)
+    return _lib
+
+
+def _declare(L):
+    vp, i, f, d, i64, sz = C.c_void_p, C.c_int, C.c_float, C.c_double, C.c_int64, C.c_size_t
+    cp = C.POINTER(ConnDesc)
+    lp = C.POINTER(Loc)
+    sig = {
+        "pvgpu_version": (C.c_char_p, []),
+        "pvgpu_status_string": (C.c_char_p, [i]),
+        "pvgpu_last_error": (C.c_char_p, []),
+        "pvgpu_compact_scratch_bytes": (sz, [i, i64]),
+        "pvgpu_compact_active": (i, [vp, i, i64, vp, vp, vp, sz, vp]),
+        "pvgpu_deliver_pre": (i, [cp, vp, vp, vp, vp, vp, i, vp]),
+        "pvgpu_deliver_post": (i, [cp, vp, vp, vp, i, vp]),
+        "pvgpu_transpose_weights": (i, [cp, vp, vp, vp]),
+        "pvgpu_gsyn_accumulate": (i, [i64, i, vp, vp, vp, vp]),
+        "pvgpu_lca_update": (i, [lp, i, vp, f, vp, vp, vp, vp]),
+        "pvgpu_ann_activity": (i, [lp, vp, f, f, f, f, f, vp, vp]),
+        "pvgpu_lca_layer_update": (i, [C.POINTER(LcaLayerDesc), vp, vp, vp, vp, vp]),
+        "pvgpu_cost_sum": (i, [lp, vp, i, d, d, vp, vp]),
+        "pvgpu_hebbian_dw": (i, [cp, f, vp, vp, vp, vp]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+
+
+def exported_symbols():
+    """Names of the pvgpu_* functions declared in include/pvgpu.h."""
+    import re
+    hdr = os.path.join(os.path.dirname(HERE), "include", "pvgpu.h")
+    txt = open(hdr).read()
+    return sorted(set(re.findall(r"\b(pvgpu_[a-z0-9_]+)\s*\(", txt)))
+
+
+def version():
+    return lib().pvgpu_version().decode()
+
+
+def status_string(s):
+    return lib().pvgpu_status_string(s).decode()
+
+
+def last_error():
+    return lib().pvgpu_last_error().decode()
+
+
+def check(status, what):
+    if status != PVGPU_OK:
+        raise PvgpuError(status, what)
+
+
+# ---- torch plumbing ---------------------------------------------------------------------
+
+def _ptr(t):
+    if t is None:
+        return None
+    assert t.is_cuda and t.is_contiguous(), "device tensors must be contiguous CUDA tensors"
+    return C.c_void_p(t.data_ptr())
+
+
+def _stream(stream=None):
+    import torch
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return C.c_void_p(s.cuda_stream)
+
+
+def conn_desc(pre, post, nxp, nyp, dt_factor=1.0):
+    return ConnDesc(pre, post, nxp, nyp, dt_factor)
+
+
+def compact_active(a_ext, nbatch, num_ext, entries, num_active, scratch=None, stream=None):
+    """entries: uint8/int64 tensor viewed as [nbatch][num_ext] {u32 index, f32 value}."""
+    import torch
+    need = lib().pvgpu_compact_scratch_bytes(nbatch, num_ext)
+    if scratch is None:
+        scratch = torch.empty(max(need, 1), dtype=torch.uint8, device=a_ext.device)
+    check(lib().pvgpu_compact_active(_ptr(a_ext), nbatch, num_ext, _ptr(entries), _ptr(num_active), _ptr(scratch),
+                                     scratch.numel() * scratch.element_size(), _stream(stream)), "compact_active")
+
+
+def deliver_pre(conn, weights, gsyn, entries=None, num_active=None, a_ext=None, mode=DELIVER_FAST, stream=None):
+    check(lib().pvgpu_deliver_pre(C.byref(conn), _ptr(entries), _ptr(num_active), _ptr(a_ext), _ptr(weights),
+                                  _ptr(gsyn), mode, _stream(stream)), "deliver_pre")
+
+
+def deliver_post(conn, a_ext, post_weights, gsyn, mode=DELIVER_FAST, stream=None):
+    check(lib().pvgpu_deliver_post(C.byref(conn), _ptr(a_ext), _ptr(post_weights), _ptr(gsyn), mode,
+                                   _stream(stream)), "deliver_post")
+
+
+def transpose_weights(conn, w_pre, w_post, stream=None):
+    check(lib().pvgpu_transpose_weights(C.byref(conn), _ptr(w_pre), _ptr(w_post), _stream(stream)), "transpose")
+
+
+def gsyn_accumulate(n, coeffs, gsyn, g, stream=None):
+    c = (C.c_float * len(coeffs))(*coeffs)
+    check(lib().pvgpu_gsyn_accumulate(n, len(coeffs), c, _ptr(gsyn), _ptr(g), _stream(stream)), "gsyn_accumulate")
+
+
+def lca_update(loc, self_interact, dt_adapt, tau, g, a_ext, v, stream=None):
+    check(lib().pvgpu_lca_update(C.byref(loc), int(self_interact), _ptr(dt_adapt), tau, _ptr(g), _ptr(a_ext), _ptr(v),
+                                 _stream(stream)), "lca_update")
+
+
+def ann_activity(loc, v, VThresh, AMin, AMax, AShift, VWidth, a_ext, stream=None):
+    check(lib().pvgpu_ann_activity(C.byref(loc), _ptr(v), VThresh, AMin, AMax, AShift, VWidth, _ptr(a_ext),
+                                   _stream(stream)), "ann_activity")
+
+
+def lca_layer_update(desc, gsyn, dt_adapt, v, a_ext, stream=None):
+    check(lib().pvgpu_lca_layer_update(C.byref(desc), _ptr(gsyn), _ptr(dt_adapt), _ptr(v), _ptr(a_ext),
+                                       _stream(stream)), "lca_layer_update")
+
+
+def cost_sum(loc, buf_ext, kind, p0, p1, out, stream=None):
+    check(lib().pvgpu_cost_sum(C.byref(loc), _ptr(buf_ext), kind, p0, p1, _ptr(out), _stream(stream)), "cost_sum")
+
+
+def hebbian_dw(conn, dw_max, pre_ext, post_ext, dw, stream=None):
+    check(lib().pvgpu_hebbian_dw(C.byref(conn), dw_max, _ptr(pre_ext), _ptr(post_ext), _ptr(dw), _stream(stream)),
+          "hebbian_dw")
+
+
+ENTRY_DTYPE = np.dtype([("index", np.uint32), ("value", np.float32)])

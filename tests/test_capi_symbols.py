@@ -1,0 +1,50 @@
+"""CPU checks of the C ABI: libpvgpu.so builds, loads and exports every entry point
+include/pvgpu.h declares (no compute call: there is no GPU here)."""
+import ctypes as C
+import os
+
+import pytest
+
+
+@pytest.fixture(scope="module")
+def built():
+    from openpv_gb300 import build
+    try:
+        build.nvcc()
+    except RuntimeError:
+        pytest.skip("nvcc not available")
+    return build.build()
+
+
+def test_library_exports_every_declared_symbol(built):
+    from openpv_gb300 import capi
+    lib = C.CDLL(built)
+    declared = capi.exported_symbols()
+    assert len(declared) >= 10
+    missing = [s for s in declared if not hasattr(lib, s)]
+    assert not missing, f"declared in include/pvgpu.h but not exported: {missing}"
+
+
+def test_status_strings_and_version(built):
+    from openpv_gb300 import capi
+    assert "sm_103a" in capi.version()
+    assert capi.status_string(0) == "ok"
+    for s in range(1, 7):
+        assert capi.status_string(s) != "unknown status"
+
+
+def test_bad_arguments_rejected_without_gpu(built):
+    """Argument checks run on the host before any CUDA call."""
+    from openpv_gb300 import capi
+    L = capi.lib()
+    pre = capi.Loc.make(1, 16, 16, 4, 2)
+    post = capi.Loc.make(1, 32, 32, 1, 3)
+    bad = capi.ConnDesc(pre, post, 8, 8, 1.0)
+    # null weights / gsyn
+    assert L.pvgpu_deliver_pre(C.byref(bad), None, None, None, None, None, 0, None) == 1
+    # a geometry OpenPV rejects: one-to-many with a patch that is not a multiple of the ratio
+    illegal = capi.ConnDesc(pre, post, 7, 7, 1.0)
+    dummy = C.c_void_p(16)
+    assert L.pvgpu_deliver_pre(C.byref(illegal), None, None, dummy, dummy, dummy, 0, None) == 6
+    assert L.pvgpu_compact_active(None, 1, 10, None, None, None, 0, None) == 1
+    assert L.pvgpu_cost_sum(None, None, 0, 0.0, 0.0, None, None) == 1

@@ -1,0 +1,264 @@
+"""GPU parity of the delivery / update kernels against the CPU oracle, called through
+the C ABI (libpvgpu.so).  Integer work (compaction, geometry) and the update kernels are
+compared bit for bit; FP32 delivery sums within 1e-5 relative in FAST mode and bit for
+bit in REFERENCE_ORDER mode (the reference's single-thread order)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+RTOL_FP32 = 1e-5  # FP32 sums in a different order than the reference
+
+
+@pytest.fixture(scope="module")
+def cuda():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from openpv_gb300 import build
+    build.build()
+    from openpv_gb300 import capi
+    capi.lib()
+    return torch
+
+
+def T(torch, a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def H(t):
+    return t.cpu().numpy()
+
+
+def OL(O, loc):
+    return O.Loc.make(loc.nbatch, loc.nx, loc.ny, loc.nf, loc.halo.lt, loc.halo.dn)
+
+
+def sparse_activity(rng, loc, p, zero_halo=True):
+    a = np.zeros(loc.ext_shape(), np.float32)
+    h = loc.halo
+    core = (rng.random(loc.res_shape()) < p) * rng.uniform(1e-3, 1.0, loc.res_shape())
+    a[:, h.up:h.up + loc.ny, h.lt:h.lt + loc.nx, :] = core
+    if not zero_halo:
+        a += (rng.random(loc.ext_shape()) < p) * rng.uniform(1e-3, 1.0, loc.ext_shape())
+    return a.astype(np.float32)
+
+
+# ---- a1: compaction --------------------------------------------------------------------
+
+@pytest.mark.parametrize("nb,n,p", [(3, 25600, 0.05), (2, 4097, 0.5), (1, 4096, 1.0), (4, 777, 0.0),
+                                    (2, 204800, 0.02), (1, 1, 1.0)])
+def test_compaction_bitexact(cuda, oracle, nb, n, p):
+    torch = cuda
+    from openpv_gb300 import capi
+    rng = np.random.default_rng(n)
+    a = ((rng.random((nb, n)) < p) * rng.normal(size=(nb, n))).astype(np.float32)
+    ent_ref, num_ref = oracle.compact(a)
+    ent = torch.zeros((nb, n, 2), dtype=torch.int32, device="cuda")
+    num = torch.full((nb,), -7, dtype=torch.int64, device="cuda")
+    capi.compact_active(T(torch, a), nb, n, ent, num)
+    num_h = H(num)
+    ent_h = H(ent).view(np.uint8).reshape(nb, n, 8).view(capi.ENTRY_DTYPE).reshape(nb, n)
+    assert np.array_equal(num_h, num_ref)
+    for b in range(nb):
+        k = num_ref[b]
+        assert np.array_equal(ent_h[b, :k]["index"], ent_ref[b, :k]["index"])
+        assert np.array_equal(ent_h[b, :k]["value"].view(np.uint32), ent_ref[b, :k]["value"].view(np.uint32))
+
+
+# ---- a4: presynaptic delivery ------------------------------------------------------------
+
+# (pre nb,nx,ny,nf,halo), (post nx,ny,nf,halo), nxp, nyp
+PRE_CASES = [
+    ((2, 16, 16, 64, 2), (32, 32, 1, 3), 8, 8),     # LCA reconstruction V1 -> error
+    ((2, 16, 16, 24, 2), (32, 32, 3, 3), 8, 8),     # colour reconstruction
+    ((2, 24, 20, 16, 3), (24, 20, 8, 0), 7, 7),     # one-to-one, shrunken at borders
+    ((1, 32, 32, 4, 6), (8, 8, 5, 0), 4, 4),        # many-to-one x4
+    ((3, 12, 8, 3, 1), (24, 16, 2, 2), 6, 4),       # one-to-many, unequal axes
+    ((1, 20, 20, 40, 0), (20, 20, 600, 0), 3, 3),   # post features above one tile
+]
+
+
+@pytest.mark.parametrize("case", PRE_CASES)
+@pytest.mark.parametrize("sparse", [True, False])
+def test_deliver_pre_matches_oracle(cuda, oracle, case, sparse):
+    torch = cuda
+    from openpv_gb300 import capi
+    (nb, nx, ny, nf, h), (qx, qy, qf, qh), nxp, nyp = case
+    pre = capi.Loc.make(nb, nx, ny, nf, h)
+    post = capi.Loc.make(nb, qx, qy, qf, qh)
+    rng = np.random.default_rng(nx * 7 + qf)
+    a = sparse_activity(rng, pre, 0.1, zero_halo=False)
+    nk = (nx // qx if nx > qx else 1) * (ny // qy if ny > qy else 1) * nf
+    w = rng.normal(0, 0.05, (nk, nyp, nxp, qf)).astype(np.float32)
+    g0 = rng.normal(size=post.res_shape()).astype(np.float32)
+    ent, num = oracle.compact(a.reshape(nb, -1))
+    ref = oracle.deliver_pre(OL(oracle, pre), OL(oracle, post), nxp, nyp, w, entries=ent, num_active=num,
+                             gsyn=g0.copy())
+    conn = capi.conn_desc(pre, post, nxp, nyp)
+    for mode in (capi.DELIVER_FAST, capi.DELIVER_REFERENCE_ORDER):
+        g = T(torch, g0)
+        if sparse:
+            ent_d = T(torch, ent.view(np.uint8))
+            capi.deliver_pre(conn, T(torch, w), g, entries=ent_d, num_active=T(torch, num), mode=mode)
+        else:
+            capi.deliver_pre(conn, T(torch, w), g, a_ext=T(torch, a), mode=mode)
+        out = H(g)
+        if mode == capi.DELIVER_REFERENCE_ORDER:
+            assert np.array_equal(out.view(np.uint32), ref.view(np.uint32))
+        else:
+            np.testing.assert_allclose(out, ref, rtol=RTOL_FP32, atol=1e-5 * np.abs(ref).max())
+
+
+def test_deliver_pre_empty_activity(cuda, oracle):
+    torch = cuda
+    from openpv_gb300 import capi
+    pre = capi.Loc.make(2, 16, 16, 8, 2)
+    post = capi.Loc.make(2, 32, 32, 1, 3)
+    g0 = np.arange(2 * 32 * 32, dtype=np.float32).reshape(post.res_shape())
+    g = T(torch, g0)
+    ent = torch.zeros((2, pre.num_ext, 2), dtype=torch.int32, device="cuda")
+    num = torch.zeros(2, dtype=torch.int64, device="cuda")
+    capi.deliver_pre(capi.conn_desc(pre, post, 8, 8), torch.ones(8 * 64, device="cuda"), g, entries=ent,
+                     num_active=num)
+    assert np.array_equal(H(g), g0)
+
+
+# ---- a5: postsynaptic delivery ------------------------------------------------------------
+
+# conn pre -> post with the pre layer's halo at least the post-perspective margin
+POST_CASES = [
+    ((2, 32, 32, 1, 3), (16, 16, 64, 2), 8, 8),     # error -> V1 (LCA), many-to-one x2
+    ((2, 32, 32, 3, 3), (16, 16, 48, 2), 8, 8),     # colour LCA
+    ((1, 24, 24, 16, 3), (24, 24, 8, 0), 7, 7),     # one-to-one
+    ((2, 8, 8, 6, 2), (16, 16, 4, 1), 4, 4),        # one-to-many x2 (kernel phases)
+    ((1, 64, 64, 1, 6), (16, 16, 32, 2), 16, 16),   # stride-4 dictionary
+]
+
+
+@pytest.mark.parametrize("case", POST_CASES)
+def test_deliver_post_matches_oracle(cuda, oracle, case):
+    torch = cuda
+    from openpv_gb300 import capi
+    (nb, nx, ny, nf, h), (qx, qy, qf, qh), nxp, nyp = case
+    pre = capi.Loc.make(nb, nx, ny, nf, h)
+    post = capi.Loc.make(nb, qx, qy, qf, qh)
+    rng = np.random.default_rng(qf + nx)
+    a = rng.normal(size=pre.ext_shape()).astype(np.float32)
+    nk = (nx // qx if nx > qx else 1) * (ny // qy if ny > qy else 1) * nf
+    w = rng.normal(0, 0.05, (nk, nyp, nxp, qf)).astype(np.float32)
+    w_post = oracle.transpose_shared(OL(oracle, pre), OL(oracle, post), nxp, nyp, w)
+    # the GPU transpose agrees with the oracle bit for bit
+    conn = capi.conn_desc(pre, post, nxp, nyp)
+    w_post_d = torch.zeros(w_post.size, dtype=torch.float32, device="cuda")
+    capi.transpose_weights(conn, T(torch, w), w_post_d)
+    assert np.array_equal(H(w_post_d).reshape(w_post.shape), w_post)
+    g0 = rng.normal(size=post.res_shape()).astype(np.float32)
+    nxpP = oracle.post_patch_size(nxp, nx, qx)
+    nypP = oracle.post_patch_size(nyp, ny, qy)
+    ref = oracle.deliver_post(OL(oracle, pre), OL(oracle, post), nxpP, nypP, w_post, a, gsyn=g0.copy())
+    for mode in (capi.DELIVER_FAST, capi.DELIVER_REFERENCE_ORDER):
+        g = T(torch, g0)
+        capi.deliver_post(conn, T(torch, a), w_post_d, g, mode=mode)
+        out = H(g)
+        if mode == capi.DELIVER_REFERENCE_ORDER:
+            assert np.array_equal(out.view(np.uint32), ref.view(np.uint32))
+        else:
+            np.testing.assert_allclose(out, ref, rtol=RTOL_FP32, atol=1e-5 * np.abs(ref).max())
+
+
+def test_pre_and_post_perspective_agree(cuda, oracle):
+    """ReceiveFromPostTest's property: pre- and post-perspective delivery of the same
+    connection give the same GSyn (tolerance n*2^-24, input/postTest.params:176)."""
+    torch = cuda
+    from openpv_gb300 import capi
+    pre = capi.Loc.make(2, 32, 32, 8, 3)
+    post = capi.Loc.make(2, 16, 16, 16, 0)
+    rng = np.random.default_rng(5)
+    a = sparse_activity(rng, pre, 0.3)
+    w = rng.normal(0, 0.1, (4 * 8, 4, 4, 16)).astype(np.float32)
+    conn = capi.conn_desc(pre, post, 4, 4)
+    g_pre = torch.zeros(post.res_shape(), device="cuda")
+    capi.deliver_pre(conn, T(torch, w), g_pre, a_ext=T(torch, a))
+    w_post = torch.zeros(w.size, device="cuda")
+    capi.transpose_weights(conn, T(torch, w), w_post)
+    g_post = torch.zeros(post.res_shape(), device="cuda")
+    capi.deliver_post(conn, T(torch, a), w_post, g_post)
+    n_inputs = 8 * 8 * 8
+    np.testing.assert_allclose(H(g_pre), H(g_post), atol=n_inputs * 2.0 ** -24 * np.abs(H(g_pre)).max())
+
+
+# ---- a6..a9: layer update ------------------------------------------------------------------
+
+def test_update_kernels_bitexact(cuda, oracle):
+    torch = cuda
+    from openpv_gb300 import capi
+    rng = np.random.default_rng(9)
+    loc = capi.Loc.make(5, 16, 16, 64, 2)
+    ol = OL(oracle, loc)
+    v = rng.normal(0, 0.3, loc.res_shape()).astype(np.float32)
+    gs = rng.normal(0, 0.3, (2,) + loc.res_shape()).astype(np.float32)
+    a = oracle.ann_activity(ol, rng.normal(0, 0.3, loc.res_shape()).astype(np.float32), 0.1, 0.0, np.inf, 0.1, 0.0)
+    dt = np.array([1.0, 0.5, 0.25, 2.0, 1.0], np.float64)
+    coeffs = np.array([1.0, -1.0], np.float32)
+    # accumulate
+    g_ref = oracle.gsyn_accumulate(gs, coeffs)
+    g = torch.zeros(loc.res_shape(), device="cuda")
+    capi.gsyn_accumulate(loc.num_res * 5, [1.0, -1.0], T(torch, gs), g)
+    assert np.array_equal(H(g).view(np.uint32), g_ref.view(np.uint32))
+    # LCA membrane update
+    v_ref = oracle.lca_update(ol, g_ref, a, v, dt, 100.0)
+    vd = T(torch, v)
+    capi.lca_update(loc, True, T(torch, dt), 100.0, g, T(torch, a), vd)
+    assert np.array_equal(H(vd).view(np.uint32), v_ref.view(np.uint32))
+    # thresholds: soft, firm, clipped, identity
+    for th in [(0.1, 0.0, np.inf, 0.1, 0.0), (0.025, 0.0, np.inf, 0.0, 0.025), (0.1, 0.0, 0.2, 0.1, 0.0),
+               (-np.inf, -np.inf, np.inf, 0.0, 0.0)]:
+        a_ref = oracle.ann_activity(ol, v_ref, *th, a_ext=a)
+        ad = T(torch, a)
+        capi.ann_activity(loc, vd, *th, ad)
+        assert np.array_equal(H(ad).view(np.uint32), a_ref.view(np.uint32)), th
+    # fused
+    import ctypes
+    desc = capi.LcaLayerDesc(loc, 2, (ctypes.c_float * 4)(1.0, -1.0, 0.0, 0.0), 1, 100.0, 0.1, 0.0, np.inf, 0.1, 0.0)
+    a2_ref = oracle.ann_activity(ol, v_ref, 0.1, 0.0, np.inf, 0.1, 0.0, a_ext=a)
+    vd2 = T(torch, v)
+    ad2 = T(torch, a)
+    capi.lca_layer_update(desc, T(torch, gs), T(torch, dt), vd2, ad2)
+    assert np.array_equal(H(vd2).view(np.uint32), v_ref.view(np.uint32))
+    assert np.array_equal(H(ad2).view(np.uint32), a2_ref.view(np.uint32))
+
+
+# ---- a11: energy ---------------------------------------------------------------------------
+
+@pytest.mark.parametrize("kind,p0,p1", [(0, 0.0, 0.0), (1, 0.0, 0.0), (2, 0.025, 0.025)])
+def test_cost_sum_fp64(cuda, oracle, kind, p0, p1):
+    torch = cuda
+    from openpv_gb300 import capi
+    rng = np.random.default_rng(kind)
+    loc = capi.Loc.make(4, 16, 16, 64, 2)
+    buf = rng.normal(0, 0.1, loc.ext_shape()).astype(np.float32)
+    ref = oracle.cost_sum(OL(oracle, loc), buf, kind, p0, p1)
+    out = torch.zeros(4, dtype=torch.float64, device="cuda")
+    capi.cost_sum(loc, T(torch, buf), kind, p0, p1, out)
+    np.testing.assert_allclose(H(out), ref, rtol=1e-12)
+
+
+# ---- a12: Hebbian ----------------------------------------------------------------------------
+
+@pytest.mark.parametrize("case", [((3, 16, 16, 8, 2), (32, 32, 1, 3), 8, 8),
+                                  ((2, 10, 10, 4, 1), (10, 10, 3, 1), 3, 3),
+                                  ((2, 16, 16, 4, 3), (8, 8, 2, 0), 2, 2)])
+def test_hebbian_bitexact(cuda, oracle, case):
+    torch = cuda
+    from openpv_gb300 import capi
+    (nb, nx, ny, nf, h), (qx, qy, qf, qh), nxp, nyp = case
+    pre = capi.Loc.make(nb, nx, ny, nf, h)
+    post = capi.Loc.make(nb, qx, qy, qf, qh)
+    rng = np.random.default_rng(2)
+    a = sparse_activity(rng, pre, 0.3)
+    r = rng.normal(size=post.ext_shape()).astype(np.float32)
+    ref = oracle.hebbian_dw(OL(oracle, pre), OL(oracle, post), nxp, nyp, a, r, 1.0)
+    dw = torch.zeros(ref.size, device="cuda")
+    capi.hebbian_dw(capi.conn_desc(pre, post, nxp, nyp), 1.0, T(torch, a), T(torch, r), dw)
+    assert np.array_equal(H(dw).reshape(ref.shape).view(np.uint32), ref.view(np.uint32))
