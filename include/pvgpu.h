@@ -220,6 +220,14 @@ pvgpu_status pvgpu_hebbian_dw(
       float *dw,
       void *stream);
 
+/* ---- diagnostics ----------------------------------------------------------------------------
+ * No counterpart in the reference.  C[M][N] (FP32) = A[M][K] * B[N][K]^T with BF16 row-major
+ * operands on the tcgen05 tensor cores through TMA and TMEM: the building block of the BF16
+ * LCA kernels, exposed so a test can check it against a host GEMM.  M % 128 == 0,
+ * 16 <= N <= 256 with N % 16 == 0, K % 64 == 0; A, B 16-byte aligned.  *errFlag (device int)
+ * is set to 1 if a bounded device wait gave up. */
+pvgpu_status pvgpu_tc_gemm_bf16(const void *A, const void *B, float *C, int M, int N, int K, int *errFlag, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

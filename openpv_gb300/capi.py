@@ -106,6 +106,7 @@ def _declare(L):
         "pvgpu_lca_layer_update": (i, [C.POINTER(LcaLayerDesc), vp, vp, vp, vp, vp]),
         "pvgpu_cost_sum": (i, [lp, vp, i, d, d, vp, vp]),
         "pvgpu_hebbian_dw": (i, [cp, f, vp, vp, vp, vp]),
+        "pvgpu_tc_gemm_bf16": (i, [vp, vp, vp, i, i, i, vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -208,6 +209,10 @@ def cost_sum(loc, buf_ext, kind, p0, p1, out, stream=None):
 def hebbian_dw(conn, dw_max, pre_ext, post_ext, dw, stream=None):
     check(lib().pvgpu_hebbian_dw(C.byref(conn), dw_max, _ptr(pre_ext), _ptr(post_ext), _ptr(dw), _stream(stream)),
           "hebbian_dw")
+
+
+def tc_gemm_bf16(A, B, C, M, N, K, err, stream=None):
+    check(lib().pvgpu_tc_gemm_bf16(_ptr(A), _ptr(B), _ptr(C), M, N, K, _ptr(err), _stream(stream)), "tc_gemm_bf16")
 
 
 ENTRY_DTYPE = np.dtype([("index", np.uint32), ("value", np.float32)])

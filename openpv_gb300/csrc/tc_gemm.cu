@@ -1,0 +1,121 @@
+// tc_gemm.cu -- diagnostic: C[M][N] = A[M][K] * B[N][K]^T with BF16 operands and FP32
+// accumulation on the 5th-generation tensor cores (TMA -> SW128 shared tiles ->
+// tcgen05.mma -> TMEM -> tcgen05.ld).  It exercises the exact descriptor, pipeline and
+// TMEM conventions the fused LCA kernels use, on a plain GEMM that a test compares with
+// a host reference.  One CTA per 128-row tile, all N (<= 256) columns; 2-stage TMA ring.
+#include "pvgpu_internal.cuh"
+#include "tc_ptx.cuh"
+#include "tmap.cuh"
+
+namespace {
+
+using namespace pvgpu::tc;
+
+constexpr int kBM = 128, kBK = 64;
+
+__global__ void __launch_bounds__(128) tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA,
+                                                      const __grid_constant__ CUtensorMap tmB, float *__restrict__ C,
+                                                      int M, int N, int K, int *__restrict__ err) {
+   extern __shared__ uint8_t smem_raw[];
+   uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+   const int bytesA = kBM * kBK * 2, bytesB = N * kBK * 2;
+   uint8_t *sA[2] = {smem, smem + bytesA + bytesB};
+   uint8_t *sB[2] = {smem + bytesA, smem + 2 * bytesA + bytesB};
+   __shared__ __align__(8) uint64_t full[2], empty[2], done;
+   __shared__ uint32_t tmemBase;
+   __shared__ int failed;
+
+   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+   const int m0 = blockIdx.x * kBM;
+   const uint32_t ncols = N <= 32 ? 32 : (N <= 64 ? 64 : (N <= 128 ? 128 : 256));
+   if (threadIdx.x == 0) {
+      mbar_init(&full[0], 1);
+      mbar_init(&full[1], 1);
+      mbar_init(&empty[0], 1);
+      mbar_init(&empty[1], 1);
+      mbar_init(&done, 1);
+      fence_mbar_init();
+      failed = 0;
+      prefetch_tmap(&tmA);
+      prefetch_tmap(&tmB);
+   }
+   if (warp == 0) tmem_alloc(&tmemBase, ncols);
+   tc_fence_before();
+   __syncthreads();
+   tc_fence_after();
+   const uint32_t tmem = tmemBase;
+
+   const int nk = K / kBK;
+   if (threadIdx.x == 0) {
+      const uint32_t idesc = idesc_bf16(kBM, N);
+      int issued = 0, consumed = 0;  // TMA stage loads issued / waited for
+      for (int kc = 0; kc < nk && kc < 2; kc++, issued++) {
+         mbar_arrive_expect_tx(&full[kc], bytesA + bytesB);
+         tma_load_2d(sA[kc], &tmA, &full[kc], kc * kBK, m0);
+         tma_load_2d(sB[kc], &tmB, &full[kc], kc * kBK, 0);
+      }
+      bool ok = true;
+      for (int kc = 0; kc < nk && ok; kc++) {
+         const int s = kc & 1;
+         const uint32_t ph = (kc >> 1) & 1;
+         if (!mbar_wait(&full[s], ph)) { ok = false; break; }
+         consumed++;
+         tc_fence_after();
+         const uint32_t a0 = smem_u32(sA[s]), b0 = smem_u32(sB[s]);
+#pragma unroll
+         for (int k = 0; k < kBK / 16; k++)
+            mma_bf16(tmem, sdesc_sw128(a0 + k * 32), sdesc_sw128(b0 + k * 32), idesc, (kc | k) != 0);
+         mma_commit(&empty[s]);
+         if (kc + 2 < nk) {
+            if (!mbar_wait(&empty[s], ph)) { ok = false; break; }
+            mbar_arrive_expect_tx(&full[s], bytesA + bytesB);
+            tma_load_2d(sA[s], &tmA, &full[s], (kc + 2) * kBK, m0);
+            tma_load_2d(sB[s], &tmB, &full[s], (kc + 2) * kBK, 0);
+            issued++;
+         }
+      }
+      mma_commit(&done);
+      if (!ok) {
+         failed = 1;
+         // let the copies still in flight land before the CTA's shared memory goes away
+         for (int i = consumed; i < issued; i++) mbar_wait(&full[i & 1], (i >> 1) & 1);
+      }
+   }
+   __syncthreads();
+   bool ok = failed == 0 && mbar_wait(&done, 0);
+   tc_fence_after();
+   if (ok) {
+      const int row = m0 + warp * 32 + lane;
+      for (int c = 0; c < N; c += 32) {
+         float v[32];
+         tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + c, v);
+         if (row < M) {
+#pragma unroll
+            for (int j = 0; j < 32; j++)
+               if (c + j < N) C[(size_t)row * N + c + j] = v[j];
+         }
+      }
+   } else if (threadIdx.x == 0) {
+      atomicExch(err, 1);
+   }
+   tc_fence_before();
+   __syncthreads();
+   if (warp == 0) tmem_dealloc(tmem, ncols);
+}
+
+}  // namespace
+
+extern "C" pvgpu_status pvgpu_tc_gemm_bf16(const void *A, const void *B, float *C, int M, int N, int K, int *errFlag,
+                                           void *stream) {
+   if (!A || !B || !C || !errFlag || M <= 0 || N < 16 || N > 256 || (N % 16) || K < 64 || (K % 64) || (M % 128))
+      return PVGPU_ERR_BAD_ARG;
+   CUtensorMap tmA, tmB;
+   if (!pvgpu::make_tmap_bf16_sw128(&tmA, A, M, K, K, kBM) || !pvgpu::make_tmap_bf16_sw128(&tmB, B, N, K, K, N))
+      return PVGPU_ERR_BAD_ARG;
+   size_t smem = 2 * (size_t)(kBM * kBK * 2 + N * kBK * 2) + 1024;
+   cudaError_t e = cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+   if (e != cudaSuccess) return pvgpu::record_cuda_error(e, "tc_gemm attr");
+   tc_gemm_kernel<<<M / kBM, 128, smem, pvgpu::as_stream(stream)>>>(tmA, tmB, C, M, N, K, errFlag);
+   PVGPU_CHECK_LAUNCH("tc_gemm");
+   return PVGPU_OK;
+}

@@ -1,0 +1,157 @@
+// tc_ptx.cuh -- inline-PTX building blocks for the Blackwell (sm_103a) tensor-core path:
+// mbarriers with bounded waits, TMA tile loads, tcgen05 TMEM allocation, tcgen05.mma
+// (kind::f16, BF16 inputs, FP32 accumulation in TMEM), tcgen05.commit and tcgen05.ld.
+//
+// Shared-memory operand layout: K-major, 128-byte swizzle (the layout a TMA load with
+// CU_TENSOR_MAP_SWIZZLE_128B writes for a box whose inner extent is 64 BF16 elements).
+// Rows are 128 B; the 16-byte chunk c of row r sits at chunk c ^ (r % 8); 8-row atoms are
+// 1024 B apart.  Tiles start on 1024-byte boundaries.
+#pragma once
+
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+namespace pvgpu {
+namespace tc {
+
+// Iteration limit of every device-side wait: well beyond any legitimate latency
+// (a few ms at ~1 ns per probe); after it the kernel records a timeout and returns.
+constexpr uint32_t kWaitLimit = 1u << 22;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// ---- mbarrier -------------------------------------------------------------------------
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init() {
+   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
+   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+   uint32_t ok;
+   asm volatile(
+         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+         : "=r"(ok)
+         : "r"(smem_u32(bar)), "r"(parity)
+         : "memory");
+   return ok != 0;
+}
+
+// Bounded wait for the phase with the given parity; false on timeout.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+   for (uint32_t i = 0; i < kWaitLimit; i++) {
+      if (mbar_try_wait(bar, parity)) return true;
+   }
+   return false;
+}
+
+// ---- TMA -------------------------------------------------------------------------------
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, uint64_t *bar, int c0, int c1) {
+   asm volatile(
+         "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+         ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(smem_u32(bar))
+         : "memory");
+}
+
+__device__ __forceinline__ void prefetch_tmap(const CUtensorMap *map) {
+   asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map)) : "memory");
+}
+
+// Generic-proxy shared-memory writes become visible to the async proxy (tcgen05.mma operands).
+__device__ __forceinline__ void fence_proxy_async_smem() {
+   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// ---- TMEM ------------------------------------------------------------------------------
+// Whole warp: allocate ncols (power of two, >= 32) TMEM columns; the address lands in *dst.
+__device__ __forceinline__ void tmem_alloc(uint32_t *dst, uint32_t ncols) {
+   asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst)), "r"(ncols)
+                : "memory");
+   asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+   asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() {
+   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+
+__device__ __forceinline__ void tc_fence_after() {
+   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+// ---- descriptors -------------------------------------------------------------------------
+// Shared-memory matrix descriptor, K-major with 128-byte swizzle: start address, leading
+// byte offset (unused for this layout, 16 B), stride byte offset 1024 B between 8-row
+// atoms, descriptor version 1, swizzle mode 2 (128B).
+__device__ __forceinline__ uint64_t sdesc_sw128(uint32_t smem_addr) {
+   uint64_t d = 0;
+   d |= (uint64_t)((smem_addr >> 4) & 0x3FFFu);
+   d |= (uint64_t)(16u >> 4) << 16;
+   d |= (uint64_t)(1024u >> 4) << 32;
+   d |= (uint64_t)1 << 46;
+   d |= (uint64_t)2 << 61;
+   return d;
+}
+
+// Instruction descriptor, kind::f16: D = FP32, A = B = BF16, both K-major, M x N.
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+   return (1u << 4)                        // D format F32
+          | (1u << 7)                      // A format BF16
+          | (1u << 10)                     // B format BF16
+          | ((uint32_t)(N >> 3) << 17)     // N / 8
+          | ((uint32_t)(M >> 4) << 24);    // M / 16
+}
+
+// D[tmem] (+)= A[smem] * B[smem]^T, one instruction (M x N x 16), issued by one thread.
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accumulate) {
+   asm volatile(
+         "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+         " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+         "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+         : "memory");
+}
+
+// Arrive on *bar once every tcgen05.mma this thread issued so far has completed.
+__device__ __forceinline__ void mma_commit(uint64_t *bar) {
+   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                : "memory");
+}
+
+// Warp-collective: 32 consecutive FP32 columns of this warp's 32 TMEM lanes.
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v) {
+   uint32_t r[32];
+   asm volatile(
+         "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+         "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+           "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+           "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+           "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+         : "r"(taddr));
+   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+   for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
+}
+
+// Byte offset of element (row, k) of a K-major SW128 BF16 tile with 64-element rows.
+__host__ __device__ __forceinline__ uint32_t sw128_offset(int row, int k) {
+   int chunk = k >> 3;  // 8 BF16 = 16 B
+   return (uint32_t)(row * 128 + (((chunk ^ (row & 7)) << 4)) + ((k & 7) << 1));
+}
+
+}  // namespace tc
+}  // namespace pvgpu

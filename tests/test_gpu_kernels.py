@@ -128,11 +128,11 @@ def test_deliver_pre_empty_activity(cuda, oracle):
 
 # conn pre -> post with the pre layer's halo at least the post-perspective margin
 POST_CASES = [
-    ((2, 32, 32, 1, 3), (16, 16, 64, 2), 8, 8),     # error -> V1 (LCA), many-to-one x2
-    ((2, 32, 32, 3, 3), (16, 16, 48, 2), 8, 8),     # colour LCA
+    ((2, 32, 32, 1, 3), (16, 16, 64, 2), 4, 4),     # error -> V1 (LCA), many-to-one x2, 8x8 receptive field
+    ((2, 32, 32, 3, 3), (16, 16, 48, 2), 4, 4),     # colour LCA
     ((1, 24, 24, 16, 3), (24, 24, 8, 0), 7, 7),     # one-to-one
     ((2, 8, 8, 6, 2), (16, 16, 4, 1), 4, 4),        # one-to-many x2 (kernel phases)
-    ((1, 64, 64, 1, 6), (16, 16, 32, 2), 16, 16),   # stride-4 dictionary
+    ((1, 64, 64, 1, 6), (16, 16, 32, 2), 4, 4),     # stride-4 dictionary, 16x16 receptive field
 ]
 
 
@@ -262,3 +262,23 @@ def test_hebbian_bitexact(cuda, oracle, case):
     dw = torch.zeros(ref.size, device="cuda")
     capi.hebbian_dw(capi.conn_desc(pre, post, nxp, nyp), 1.0, T(torch, a), T(torch, r), dw)
     assert np.array_equal(H(dw).reshape(ref.shape).view(np.uint32), ref.view(np.uint32))
+
+
+# ---- tcgen05 building block ------------------------------------------------------------------
+
+@pytest.mark.parametrize("M,N,K", [(128, 64, 64), (256, 192, 512), (384, 256, 192), (128, 16, 128)])
+def test_tc_gemm_bf16(cuda, M, N, K):
+    """TMA -> SW128 smem -> tcgen05.mma -> TMEM -> tcgen05.ld against an FP32 host GEMM of
+    the same BF16 values (FP32 accumulation: only summation order differs)."""
+    torch = cuda
+    from openpv_gb300 import capi
+    g = torch.Generator().manual_seed(M + N + K)
+    A = torch.randn(M, K, generator=g).to(torch.bfloat16)
+    B = torch.randn(N, K, generator=g).to(torch.bfloat16)
+    ref = A.float() @ B.float().T
+    C = torch.zeros(M, N, device="cuda")
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    capi.tc_gemm_bf16(A.cuda(), B.cuda(), C, M, N, K, err)
+    torch.cuda.synchronize()
+    assert int(err.item()) == 0, "a bounded device wait timed out"
+    np.testing.assert_allclose(C.cpu().numpy(), ref.numpy(), rtol=1e-4, atol=1e-3)
