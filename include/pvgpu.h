@@ -220,6 +220,61 @@ pvgpu_status pvgpu_hebbian_dw(
       float *dw,
       void *stream);
 
+/* ---- the batched LCA module ------------------------------------------------------------------
+ * The per-timestep layer sequence of an LCA module (input -> error <-> V1; the LCA-CIFAR
+ * topology of tutorials/LCA-CIFAR and tests/GPULCATest), replacing, per step, the reference's
+ *   error layer:  IdentDelivery (ch0) + PresynapticPerspectiveConvolveDelivery of V1 (ch1),
+ *                 GSynAccumulator, ErrScaleInternalStateBuffer, ANNActivityBuffer (identity);
+ *   V1:           PostsynapticPerspectiveConvolveDelivery of the error (TransposeConn),
+ *                 GSynAccumulator, HyPerLCAInternalStateBuffer, ANNActivityBuffer
+ * driven by HyPerCol::advanceTime (columns/HyPerCol.cpp:659-790), with the host round trips of
+ * the reference GPU path (datastore H->D, SparseList on the host, V/A/GSyn D->H) removed.
+ * Each timestep is two fused kernels: (1) reconstruction W^T a as a GEMM + deterministic fold,
+ * (2) residual + post-perspective delivery GEMM + LCA update + threshold in the epilogue.
+ * Supported geometry: V1 stride S = inNx / v1Nx in {2, 4}, square patch nxp, with
+ * (S, nxp, inNf) in {(2, 8, 1), (2, 8, 3), (4, 16, 1)}, v1Nx * v1Ny a multiple of 128, 128 a
+ * multiple of v1Nx, v1Nf a multiple of 64. */
+typedef struct {
+   int nbatch;
+   int inNx, inNy, inNf;   /* input / error layer, restricted */
+   int v1Nx, v1Ny, v1Nf;   /* V1, restricted */
+   int nxp;                /* V1 -> error patch (square), nfp = inNf */
+   float VThresh, AMin, AMax, AShift, VWidth;  /* ANNActivityBuffer parameters of V1 */
+   float tau;              /* timeConstantTau / dt (HyPerLCAInternalStateBuffer.cpp:104-112) */
+   float dt;               /* the time step handed to the update (dtAdapt without an adaptive probe) */
+   int selfInteract;
+} pvgpu_lca_solver_desc;
+
+typedef struct pvgpu_lca_solver pvgpu_lca_solver;
+
+enum {
+   PVGPU_LCA_FP32 = 0, /* FP32 SIMT GEMMs, FP32 activity: the plain form */
+   PVGPU_LCA_BF16 = 1  /* tcgen05 BF16 GEMMs with FP32 accumulation, FP32 residual and V */
+};
+
+/* Allocates the solver's device state (V, activity, reconstruction partials, weight copies). */
+pvgpu_status pvgpu_lca_solver_create(const pvgpu_lca_solver_desc *desc, pvgpu_lca_solver **out);
+pvgpu_status pvgpu_lca_solver_destroy(pvgpu_lca_solver *s);
+/* w: device FP32 [v1Nf][nxp][nxp][inNf], the V1 -> error weights (already normalised). */
+pvgpu_status pvgpu_lca_solver_set_weights(pvgpu_lca_solver *s, const float *w, void *stream);
+/* V = v0 (device FP32 [nbatch][v1Ny][v1Nx][v1Nf]) or zeros when v0 is NULL; A = T(V). */
+pvgpu_status pvgpu_lca_solver_reset(pvgpu_lca_solver *s, const float *v0, void *stream);
+/* numSteps timesteps on input x (device FP32 [nbatch][inNy][inNx][inNf]); in BF16 precision the
+ * last numX3Steps run with BF16x3 split products (hi*hi + hi*lo + lo*hi). */
+pvgpu_status pvgpu_lca_solver_run(pvgpu_lca_solver *s, const float *x, int numSteps, int numX3Steps, int precision,
+                                  void *stream);
+/* Energy of the last step as the reference's ColumnEnergyProbe computes it
+ * (probes/ColumnEnergyProbe.cpp:60-70): l2Coeff * sum(err^2) (L2NormProbe) + costCoeff *
+ * sum(cost(A_V1)), cost = |a| (costKind 1, L1NormLCAProbe) or the firm-threshold cost
+ * (costKind 2, FirmThresholdCostFnLCAProbe); FP64, energy = device array of nbatch doubles. */
+pvgpu_status pvgpu_lca_solver_energy(pvgpu_lca_solver *s, const float *x, double l2Coeff, int costKind,
+                                     double costThresh, double costWidth, double costCoeff, double *energy,
+                                     void *stream);
+/* Copies V and/or A = T(V) (device FP32, restricted layout) out of the solver; either may be NULL. */
+pvgpu_status pvgpu_lca_solver_state(pvgpu_lca_solver *s, float *v, float *a, void *stream);
+/* Reads (synchronously) the solver's device error flag: nonzero if a bounded device wait gave up. */
+pvgpu_status pvgpu_lca_solver_error_flag(pvgpu_lca_solver *s, int *hostFlag);
+
 /* ---- diagnostics ----------------------------------------------------------------------------
  * No counterpart in the reference.  C[M][N] (FP32) = A[M][K] * B[N][K]^T with BF16 row-major
  * operands on the tcgen05 tensor cores through TMA and TMEM: the building block of the BF16

@@ -73,6 +73,16 @@ class LcaLayerDesc(C.Structure):
                 ("AShift", C.c_float), ("VWidth", C.c_float)]
 
 
+class LcaSolverDesc(C.Structure):
+    _fields_ = [("nbatch", C.c_int), ("inNx", C.c_int), ("inNy", C.c_int), ("inNf", C.c_int),
+                ("v1Nx", C.c_int), ("v1Ny", C.c_int), ("v1Nf", C.c_int), ("nxp", C.c_int),
+                ("VThresh", C.c_float), ("AMin", C.c_float), ("AMax", C.c_float), ("AShift", C.c_float),
+                ("VWidth", C.c_float), ("tau", C.c_float), ("dt", C.c_float), ("selfInteract", C.c_int)]
+
+
+LCA_FP32 = 0
+LCA_BF16 = 1
+
 _lib = None
 
 
@@ -107,6 +117,14 @@ def _declare(L):
         "pvgpu_cost_sum": (i, [lp, vp, i, d, d, vp, vp]),
         "pvgpu_hebbian_dw": (i, [cp, f, vp, vp, vp, vp]),
         "pvgpu_tc_gemm_bf16": (i, [vp, vp, vp, i, i, i, vp, vp]),
+        "pvgpu_lca_solver_create": (i, [C.POINTER(LcaSolverDesc), C.POINTER(vp)]),
+        "pvgpu_lca_solver_destroy": (i, [vp]),
+        "pvgpu_lca_solver_set_weights": (i, [vp, vp, vp]),
+        "pvgpu_lca_solver_reset": (i, [vp, vp, vp]),
+        "pvgpu_lca_solver_run": (i, [vp, vp, i, i, i, vp]),
+        "pvgpu_lca_solver_energy": (i, [vp, vp, d, i, d, d, d, vp, vp]),
+        "pvgpu_lca_solver_state": (i, [vp, vp, vp, vp]),
+        "pvgpu_lca_solver_error_flag": (i, [vp, C.POINTER(i)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -216,3 +234,55 @@ def tc_gemm_bf16(A, B, C, M, N, K, err, stream=None):
 
 
 ENTRY_DTYPE = np.dtype([("index", np.uint32), ("value", np.float32)])
+
+
+class LcaSolver:
+    """The batched LCA module (pvgpu_lca_solver_*): input -> error <-> V1, two fused kernels per
+    timestep.  Inputs, weights and state are device tensors in the OpenPV layouts."""
+
+    def __init__(self, nbatch, in_shape, v1_shape, nxp, VThresh, AMin=0.0, AMax=float("inf"), AShift=None,
+                 VWidth=0.0, tau=100.0, dt=1.0, self_interact=True):
+        iny, inx, inf_ = in_shape
+        vy, vx, vf = v1_shape
+        self.desc = LcaSolverDesc(nbatch, inx, iny, inf_, vx, vy, vf, nxp, VThresh, AMin, AMax,
+                                  VThresh if AShift is None else AShift, VWidth, tau, dt, int(self_interact))
+        h = C.c_void_p()
+        check(lib().pvgpu_lca_solver_create(C.byref(self.desc), C.byref(h)), "lca_solver_create")
+        self.h = h
+        self.nbatch = nbatch
+        self.v1_shape = (nbatch, vy, vx, vf)
+
+    def close(self):
+        if self.h:
+            lib().pvgpu_lca_solver_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_weights(self, w, stream=None):
+        check(lib().pvgpu_lca_solver_set_weights(self.h, _ptr(w), _stream(stream)), "lca_solver_set_weights")
+
+    def reset(self, v0=None, stream=None):
+        check(lib().pvgpu_lca_solver_reset(self.h, _ptr(v0), _stream(stream)), "lca_solver_reset")
+
+    def run(self, x, steps, x3_steps=0, precision=LCA_BF16, stream=None):
+        check(lib().pvgpu_lca_solver_run(self.h, _ptr(x), steps, x3_steps, precision, _stream(stream)),
+              "lca_solver_run")
+
+    def energy(self, x, out, l2_coeff=0.5, cost_kind=COST_L1, cost_thresh=0.0, cost_width=0.0, cost_coeff=None,
+               stream=None):
+        cc = float(np.float32(self.desc.VThresh)) if cost_coeff is None else cost_coeff
+        check(lib().pvgpu_lca_solver_energy(self.h, _ptr(x), l2_coeff, cost_kind, cost_thresh, cost_width, cc,
+                                            _ptr(out), _stream(stream)), "lca_solver_energy")
+
+    def state(self, v=None, a=None, stream=None):
+        check(lib().pvgpu_lca_solver_state(self.h, _ptr(v), _ptr(a), _stream(stream)), "lca_solver_state")
+
+    def error_flag(self):
+        f = C.c_int(0)
+        check(lib().pvgpu_lca_solver_error_flag(self.h, C.byref(f)), "lca_solver_error_flag")
+        return f.value

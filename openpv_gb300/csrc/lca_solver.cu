@@ -1,0 +1,745 @@
+// lca_solver.cu -- the batched LCA module (input -> error <-> V1) as two fused kernels per
+// timestep, on the tcgen05 tensor cores (BF16 operands, FP32 accumulation) or, for the
+// plain FP32 form, on the FP32 pipes with the same structure.
+//
+// Reference path (per timestep, HyPerCol::advanceTime, columns/HyPerCol.cpp:659-790):
+//   error layer (phase 1): G = input - W^T a(t-1)   IdentConn ch0 + HyPerConn V1->Error ch1
+//                                                      (PresynapticPerspectiveConvolveDelivery)
+//   V1 (phase 2):         G = W . err               TransposeConn, PostsynapticPerspectiveConvolveDelivery
+//                          V = e V + (1-e)(G + A)    HyPerLCAInternalStateBuffer.kpp:18-63
+//                          A = T(V)                  ANNActivityBuffer.cpp:490-558
+//
+// Kernel R ("recon"): one CTA per (image, block of 128 V1 positions).  GEMM
+//   D[pos][k] = sum_f A[pos][f] * W[f][k],  k = (ky*P + kx)*C + c  (M = 128, N = P*P*C, K = F)
+// A and W^T stream by TMA into 128B-swizzled shared tiles, tcgen05.mma accumulates in TMEM.
+// The fold of D into the error image (patch (ky,kx) of position (y,x) lands on pixel
+// (S*y - E + ky, S*x - E + kx)) runs in 16 tap groups; one group holds one tap of each
+// pixel-parity class, so no two threads touch a pixel inside a group and every pixel sums
+// its contributions in the same fixed group order -- deterministic, no atomics.  The
+// block's partial reconstruction goes to HBM.
+//
+// Kernel P ("post"): one CTA per (image, block of 128 positions, block of NT features).
+//   residual r = x - sum of the image's partial reconstructions (FP32, fixed order),
+//   staged for the block's receptive-field window in shared memory;
+//   im2col of r into a 128B-swizzled BF16 operand by the CTA's threads;
+//   D[pos][f] = sum_k r[pos][k] * W[f][k] on tcgen05 (TMEM accumulator);
+//   epilogue per (position, feature): A_old = T(V_old); V = e V_old + (1-e)(D + A_old);
+//   A = T(V) -> BF16 for the next step's kernel R.  V is prefetched by TMA at kernel start.
+// BF16x3 mode adds the hi*lo and lo*hi products (operands split as x = hi + lo).
+#include "lca_common.cuh"
+#include "tc_ptx.cuh"
+#include "tmap.cuh"
+
+#include <cuda_bf16.h>
+
+#include <cfloat>
+#include <cstdio>
+#include <cstring>
+#include <new>
+
+namespace {
+
+using namespace pvgpu::tc;
+using bf16 = __nv_bfloat16;
+
+using pvgpu::LcaGeom;
+using pvgpu::rwin_cols;
+using pvgpu::rwin_rows;
+
+__device__ __forceinline__ uint8_t *align1024(uint8_t *p) {
+   return reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(p) + 1023) & ~uintptr_t(1023));
+}
+
+__device__ __forceinline__ float thresh(float v, const LcaGeom &g) { return pvgpu::lca_thresh(v, g); }
+
+// Issue nchunks x8 TMEM loads (8 columns each) then wait once.
+template <int N>
+__device__ __forceinline__ void tmem_ld_cols(uint32_t taddr, float *v) {
+   static_assert(N % 8 == 0, "columns in multiples of 8");
+   uint32_t r[N];
+#pragma unroll
+   for (int c = 0; c < N; c += 8) {
+      asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                   : "=r"(r[c + 0]), "=r"(r[c + 1]), "=r"(r[c + 2]), "=r"(r[c + 3]), "=r"(r[c + 4]),
+                     "=r"(r[c + 5]), "=r"(r[c + 6]), "=r"(r[c + 7])
+                   : "r"(taddr + c));
+   }
+   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+   for (int i = 0; i < N; i++) v[i] = __uint_as_float(r[i]);
+}
+
+// -------------------------------------------------------------------------------------------
+// Kernel R: reconstruction partials
+// -------------------------------------------------------------------------------------------
+template <int S, int P, int C, bool X3>
+__global__ void __launch_bounds__(128) recon_tc_kernel(const __grid_constant__ CUtensorMap tmA,
+                                                       const __grid_constant__ CUtensorMap tmAlo,
+                                                       const __grid_constant__ CUtensorMap tmWt,
+                                                       const __grid_constant__ CUtensorMap tmWtlo, LcaGeom g,
+                                                       float *__restrict__ partials, int *__restrict__ err) {
+   constexpr int KP = P * P * C;
+   constexpr int E = (P - S) / 2;
+   constexpr uint32_t NCOLS = KP <= 32 ? 32 : (KP <= 64 ? 64 : (KP <= 128 ? 128 : 256));
+   constexpr int BYTES_A = 128 * 64 * 2, BYTES_W = KP * 64 * 2, STAGE = BYTES_A + BYTES_W;
+   extern __shared__ uint8_t smem_raw[];
+   uint8_t *smem = align1024(smem_raw);
+   uint8_t *sA[2] = {smem, smem + STAGE};
+   uint8_t *sW[2] = {smem + BYTES_A, smem + STAGE + BYTES_A};
+   float *recon = reinterpret_cast<float *>(smem + 2 * STAGE);
+   __shared__ __align__(8) uint64_t full[2], empty[2], done;
+   __shared__ uint32_t tmemBase;
+   __shared__ int failed;
+
+   const int tid = threadIdx.x, warp = tid >> 5;
+   const int b = blockIdx.x / g.MB, mb = blockIdx.x % g.MB;
+   const int rowA = b * g.Npos + mb * 128;
+   if (tid == 0) {
+      mbar_init(&full[0], 1);
+      mbar_init(&full[1], 1);
+      mbar_init(&empty[0], 1);
+      mbar_init(&empty[1], 1);
+      mbar_init(&done, 1);
+      fence_mbar_init();
+      failed = 0;
+   }
+   if (warp == 0) tmem_alloc(&tmemBase, NCOLS);
+   tc_fence_before();
+   __syncthreads();
+   tc_fence_after();
+   const uint32_t tmem = tmemBase;
+
+   if (tid == 0) {
+      const int nkc = g.F / 64;
+      const int total = (X3 ? 3 : 1) * nkc;
+      const uint32_t idesc = idesc_bf16(128, KP);
+      auto issue = [&](int j, int s) {
+         const int pass = j / nkc, kc = j % nkc;
+         const CUtensorMap *ma = (X3 && pass == 2) ? &tmAlo : &tmA;
+         const CUtensorMap *mw = (X3 && pass == 1) ? &tmWtlo : &tmWt;
+         mbar_arrive_expect_tx(&full[s], STAGE);
+         tma_load_2d(sA[s], ma, &full[s], kc * 64, rowA);
+         tma_load_2d(sW[s], mw, &full[s], kc * 64, 0);
+      };
+      int issued = 0, consumed = 0;
+      for (; issued < total && issued < 2; issued++) issue(issued, issued);
+      bool ok = true;
+      for (int j = 0; j < total; j++) {
+         const int s = j & 1;
+         const uint32_t ph = (j >> 1) & 1;
+         if (!mbar_wait(&full[s], ph)) {
+            ok = false;
+            break;
+         }
+         consumed++;
+         tc_fence_after();
+         const uint32_t a0 = smem_u32(sA[s]), w0 = smem_u32(sW[s]);
+#pragma unroll
+         for (int k = 0; k < 4; k++) mma_bf16(tmem, sdesc_sw128(a0 + k * 32), sdesc_sw128(w0 + k * 32), idesc, (j | k) != 0);
+         mma_commit(&empty[s]);
+         if (j + 2 < total) {
+            if (!mbar_wait(&empty[s], ph)) {
+               ok = false;
+               break;
+            }
+            issue(j + 2, s);
+            issued++;
+         }
+      }
+      mma_commit(&done);
+      if (!ok) {
+         failed = 1;
+         for (int i = consumed; i < issued; i++) mbar_wait(&full[i & 1], (i >> 1) & 1);
+      }
+   }
+   const int nPix = g.inNx * g.inNy * C;
+   for (int i = tid; i < nPix; i += 128) recon[i] = 0.0f;
+   __syncthreads();
+   const bool ok = __syncthreads_and(failed == 0 && mbar_wait(&done, 0));
+   tc_fence_after();
+   if (ok) {
+      // fold: thread = position (TMEM lane)
+      const uint32_t lanes = tmem + ((uint32_t)(warp * 32) << 16);
+      const int pos = mb * 128 + tid;
+      const int y1 = pos / g.v1Nx, x1 = pos % g.v1Nx;
+      const int py0 = S * y1 - E, px0 = S * x1 - E;
+#pragma unroll 1
+      for (int ty = 0; ty < P / S; ty++) {
+         float rowv[S][P * C];
+#pragma unroll
+         for (int dy = 0; dy < S; dy++) tmem_ld_cols<P * C>(lanes + (uint32_t)((S * ty + dy) * P * C), rowv[dy]);
+#pragma unroll
+         for (int tx = 0; tx < P / S; tx++) {
+#pragma unroll
+            for (int dy = 0; dy < S; dy++) {
+               const int py = py0 + S * ty + dy;
+#pragma unroll
+               for (int dx = 0; dx < S; dx++) {
+                  const int kx = S * tx + dx, px = px0 + kx;
+                  if (py >= 0 && py < g.inNy && px >= 0 && px < g.inNx) {
+                     float *rp = recon + (py * g.inNx + px) * C;
+#pragma unroll
+                     for (int c = 0; c < C; c++) rp[c] += rowv[dy][kx * C + c];
+                  }
+               }
+            }
+            __syncthreads();
+         }
+      }
+      float *out = partials + ((size_t)b * g.MB + mb) * nPix;
+      for (int i = tid; i < nPix; i += 128) out[i] = recon[i];
+   } else if (tid == 0) {
+      atomicExch(err, 1);
+   }
+   tc_fence_before();
+   __syncthreads();
+   if (warp == 0) tmem_dealloc(tmem, NCOLS);
+}
+
+// -------------------------------------------------------------------------------------------
+// Kernel P: residual, post-perspective delivery and the LCA update
+// -------------------------------------------------------------------------------------------
+template <int S, int P, int C, int NT, bool X3>
+struct PostLayout {
+   static constexpr int KP = P * P * C;
+   static constexpr int NKC = KP / 64;
+   static constexpr int IM2COL = NKC * 128 * 128;  // one K chunk = 128 rows x 128 B
+   static constexpr int WTILE = NKC * NT * 128;
+   static constexpr bool PREFETCH_V = !X3;
+   static constexpr int VTILE = PREFETCH_V ? 128 * NT * 4 : 0;
+   static constexpr int OFF_A = 0;
+   static constexpr int OFF_ALO = OFF_A + IM2COL;
+   static constexpr int OFF_W = OFF_ALO + (X3 ? IM2COL : 0);
+   static constexpr int OFF_WLO = OFF_W + WTILE;
+   static constexpr int OFF_V = OFF_WLO + (X3 ? WTILE : 0);
+   static constexpr int OFF_RWIN = OFF_V + VTILE;
+};
+
+__device__ __forceinline__ uint32_t pack2(float lo, float hi) {
+   __nv_bfloat162 h = __floats2bfloat162_rn(lo, hi);
+   return *reinterpret_cast<uint32_t *>(&h);
+}
+
+template <int S, int P, int C, int NT, bool X3>
+__global__ void __launch_bounds__(128) post_tc_kernel(const __grid_constant__ CUtensorMap tmW,
+                                                      const __grid_constant__ CUtensorMap tmWlo,
+                                                      const __grid_constant__ CUtensorMap tmV, LcaGeom g,
+                                                      const float *__restrict__ x,
+                                                      const float *__restrict__ partials, float *__restrict__ V,
+                                                      bf16 *__restrict__ A, bf16 *__restrict__ Alo,
+                                                      int *__restrict__ err) {
+   using L = PostLayout<S, P, C, NT, X3>;
+   constexpr int KP = L::KP, NKC = L::NKC, E = (P - S) / 2;
+   extern __shared__ uint8_t smem_raw[];
+   uint8_t *smem = align1024(smem_raw);
+   float *rwin = reinterpret_cast<float *>(smem + L::OFF_RWIN);
+   __shared__ __align__(8) uint64_t wfull, vfull, done;
+   __shared__ uint32_t tmemBase;
+   __shared__ int failed;
+
+   const int tid = threadIdx.x, warp = tid >> 5;
+   const int nTilesN = g.F / NT;
+   const int b = blockIdx.x / (g.MB * nTilesN);
+   const int rem = blockIdx.x % (g.MB * nTilesN);
+   const int mb = rem / nTilesN, nt = rem % nTilesN;
+   const int f0 = nt * NT;
+   const int rowV = b * g.Npos + mb * 128;
+
+   if (tid == 0) {
+      mbar_init(&wfull, 1);
+      mbar_init(&vfull, 1);
+      mbar_init(&done, 1);
+      fence_mbar_init();
+      failed = 0;
+      // operands first: the weight tiles (L2-resident) and the V tile (HBM)
+      mbar_arrive_expect_tx(&wfull, (X3 ? 2 : 1) * L::WTILE);
+      for (int kc = 0; kc < NKC; kc++) {
+         tma_load_2d(smem + L::OFF_W + kc * NT * 128, &tmW, &wfull, kc * 64, f0);
+         if (X3) tma_load_2d(smem + L::OFF_WLO + kc * NT * 128, &tmWlo, &wfull, kc * 64, f0);
+      }
+      if (L::PREFETCH_V) {
+         mbar_arrive_expect_tx(&vfull, L::VTILE);
+         for (int c = 0; c < NT / 32; c++) tma_load_2d(smem + L::OFF_V + c * 128 * 128, &tmV, &vfull, f0 + c * 32, rowV);
+      }
+   }
+   if (warp == 0) tmem_alloc(&tmemBase, NT);
+
+   const int RWC = rwin_cols(S, P, g.v1Nx);
+   pvgpu::build_residual_window<S, P, C, 128>(g, b, mb, x, partials, rwin);
+   tc_fence_before();
+   __syncthreads();
+   tc_fence_after();
+   const uint32_t tmem = tmemBase;
+
+   // im2col: thread = position; row tid of each K chunk, 8 BF16 (16 B) per store
+   {
+      const int yl = tid / g.v1Nx, x1 = tid % g.v1Nx;
+      const float *wbase = rwin + ((S * yl) * RWC + S * x1) * C;
+#pragma unroll 1
+      for (int kc = 0; kc < NKC; kc++) {
+#pragma unroll
+         for (int c8 = 0; c8 < 8; c8++) {
+            float vals[8];
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+               const int k = kc * 64 + c8 * 8 + j;
+               const int ky = k / (P * C), kr = k % (P * C);
+               vals[j] = wbase[(ky * RWC) * C + kr];
+            }
+            uint4 hi;
+            hi.x = pack2(vals[0], vals[1]);
+            hi.y = pack2(vals[2], vals[3]);
+            hi.z = pack2(vals[4], vals[5]);
+            hi.w = pack2(vals[6], vals[7]);
+            const uint32_t off = kc * 16384 + sw128_offset(tid, c8 * 8);
+            *reinterpret_cast<uint4 *>(smem + L::OFF_A + off) = hi;
+            if (X3) {
+               uint4 lo;
+               const __nv_bfloat162 *h2 = reinterpret_cast<const __nv_bfloat162 *>(&hi);
+               float2 f01 = __bfloat1622float2(h2[0]), f23 = __bfloat1622float2(h2[1]);
+               float2 f45 = __bfloat1622float2(h2[2]), f67 = __bfloat1622float2(h2[3]);
+               lo.x = pack2(vals[0] - f01.x, vals[1] - f01.y);
+               lo.y = pack2(vals[2] - f23.x, vals[3] - f23.y);
+               lo.z = pack2(vals[4] - f45.x, vals[5] - f45.y);
+               lo.w = pack2(vals[6] - f67.x, vals[7] - f67.y);
+               *reinterpret_cast<uint4 *>(smem + L::OFF_ALO + off) = lo;
+            }
+         }
+      }
+   }
+   fence_proxy_async_smem();
+   __syncthreads();
+
+   if (tid == 0) {
+      bool ok = mbar_wait(&wfull, 0);
+      if (ok) {
+         tc_fence_after();
+         const uint32_t idesc = idesc_bf16(128, NT);
+         const int npass = X3 ? 3 : 1;
+         for (int pass = 0; pass < npass; pass++) {
+            const uint32_t a0 = smem_u32(smem + ((X3 && pass == 2) ? L::OFF_ALO : L::OFF_A));
+            const uint32_t w0 = smem_u32(smem + ((X3 && pass == 1) ? L::OFF_WLO : L::OFF_W));
+            for (int kc = 0; kc < NKC; kc++)
+#pragma unroll
+               for (int k = 0; k < 4; k++)
+                  mma_bf16(tmem, sdesc_sw128(a0 + kc * 16384 + k * 32), sdesc_sw128(w0 + kc * NT * 128 + k * 32),
+                           idesc, (pass | kc | k) != 0);
+         }
+      } else {
+         failed = 1;
+      }
+      mma_commit(&done);
+      if (L::PREFETCH_V && !ok) mbar_wait(&vfull, 0);
+   }
+   __syncthreads();
+   bool ok = failed == 0 && mbar_wait(&done, 0);
+   if (L::PREFETCH_V) ok = ok && mbar_wait(&vfull, 0);
+   ok = __syncthreads_and(ok);
+   tc_fence_after();
+   if (ok) {
+      const uint32_t lanes = tmem + ((uint32_t)(warp * 32) << 16);
+      const size_t row = (size_t)(rowV + tid) * g.F + f0;
+      float *vrow = V + row;
+#pragma unroll 1
+      for (int c = 0; c < NT / 32; c++) {
+         float d[32], vo[32];
+         tmem_ld32(lanes + c * 32, d);
+         if (L::PREFETCH_V) {
+            const uint8_t *vt = smem + L::OFF_V + c * 16384 + tid * 128;
+#pragma unroll
+            for (int q = 0; q < 8; q++) {
+               float4 t = *reinterpret_cast<const float4 *>(vt + ((q ^ (tid & 7)) << 4));
+               vo[4 * q] = t.x;
+               vo[4 * q + 1] = t.y;
+               vo[4 * q + 2] = t.z;
+               vo[4 * q + 3] = t.w;
+            }
+         } else {
+#pragma unroll
+            for (int q = 0; q < 8; q++) {
+               float4 t = *reinterpret_cast<const float4 *>(vrow + c * 32 + 4 * q);
+               vo[4 * q] = t.x;
+               vo[4 * q + 1] = t.y;
+               vo[4 * q + 2] = t.z;
+               vo[4 * q + 3] = t.w;
+            }
+         }
+         float vn[32];
+         uint32_t ah[16], al[16];
+#pragma unroll
+         for (int j = 0; j < 32; j++) {
+            const float aold = thresh(vo[j], g);
+            vn[j] = fmaf(g.e, vo[j], (1.0f - g.e) * (d[j] + g.si * aold));
+         }
+#pragma unroll
+         for (int j = 0; j < 32; j += 2) {
+            const float a0 = thresh(vn[j], g), a1 = thresh(vn[j + 1], g);
+            __nv_bfloat162 h = __floats2bfloat162_rn(a0, a1);
+            ah[j / 2] = *reinterpret_cast<uint32_t *>(&h);
+            if (X3) {
+               float2 hf = __bfloat1622float2(h);
+               al[j / 2] = pack2(a0 - hf.x, a1 - hf.y);
+            }
+         }
+#pragma unroll
+         for (int q = 0; q < 8; q++)
+            *reinterpret_cast<float4 *>(vrow + c * 32 + 4 * q) =
+                  make_float4(vn[4 * q], vn[4 * q + 1], vn[4 * q + 2], vn[4 * q + 3]);
+         uint4 *ap = reinterpret_cast<uint4 *>(A + row + c * 32);
+#pragma unroll
+         for (int q = 0; q < 4; q++) ap[q] = make_uint4(ah[4 * q], ah[4 * q + 1], ah[4 * q + 2], ah[4 * q + 3]);
+         if (X3) {
+            uint4 *lp = reinterpret_cast<uint4 *>(Alo + row + c * 32);
+#pragma unroll
+            for (int q = 0; q < 4; q++) lp[q] = make_uint4(al[4 * q], al[4 * q + 1], al[4 * q + 2], al[4 * q + 3]);
+         }
+      }
+   } else if (tid == 0) {
+      atomicExch(err, 1);
+   }
+   tc_fence_before();
+   __syncthreads();
+   if (warp == 0) tmem_dealloc(tmem, NT);
+}
+
+// -------------------------------------------------------------------------------------------
+// Probe energy: l2Coeff * sum r^2 + costCoeff * sum cost(T(V)), per image, FP64
+// (ColumnEnergyProbe.cpp:60-70 over L2NormProbe and L1NormLCAProbe / FirmThresholdCostFnLCAProbe)
+// -------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) energy_kernel(LcaGeom g, int C, const float *__restrict__ x,
+                                                     const float *__restrict__ partials, const float *__restrict__ V,
+                                                     double l2Coeff, int costKind, double cp0, double cp1,
+                                                     double costCoeff, double *__restrict__ out) {
+   const int b = blockIdx.x;
+   const int nPix = g.inNx * g.inNy * C;
+   const float *pb = partials + (size_t)b * g.MB * nPix;
+   double l2 = 0.0, cost = 0.0;
+   for (int i = threadIdx.x; i < nPix; i += 256) {
+      float rec = pb[i];
+      for (int m = 1; m < g.MB; m++) rec = __fadd_rn(rec, pb[(size_t)m * nPix + i]);
+      double r = (double)__fadd_rn(x[(size_t)b * nPix + i], -rec);
+      l2 += r * r;
+   }
+   const double tw = cp0 + cp1, maxc = 0.5 * tw, qc = 0.5 / tw;
+   const float *vb = V + (size_t)b * g.Npos * g.F;
+   for (int i = threadIdx.x; i < g.Npos * g.F; i += 256) {
+      double a = fabs((double)thresh(vb[i], g));
+      cost += costKind == 1 ? a : (a < tw ? a * (1.0 - qc * a) : maxc);
+   }
+   __shared__ double s1[256], s2[256];
+   s1[threadIdx.x] = l2;
+   s2[threadIdx.x] = cost;
+   __syncthreads();
+   for (int w = 128; w > 0; w >>= 1) {
+      if (threadIdx.x < w) {
+         s1[threadIdx.x] += s1[threadIdx.x + w];
+         s2[threadIdx.x] += s2[threadIdx.x + w];
+      }
+      __syncthreads();
+   }
+   if (threadIdx.x == 0) {
+      double e = 0.0;
+      e += l2Coeff * s1[0];
+      e += costCoeff * s2[0];
+      out[b] = e;
+   }
+}
+
+// -------------------------------------------------------------------------------------------
+// state / weight preparation
+// -------------------------------------------------------------------------------------------
+// W [F][KP] (FP32, the pre weights V1->error) -> BF16 hi/lo [F][KP] and transposed [KP][F]
+__global__ void prep_weights_kernel(const float *__restrict__ w, int F, int KP, bf16 *Wh, bf16 *Wl, bf16 *Wth,
+                                    bf16 *Wtl, float *W32, float *Wt32) {
+   int i = blockIdx.x * blockDim.x + threadIdx.x;
+   if (i >= F * KP) return;
+   int f = i / KP, k = i % KP;
+   float v = w[i];
+   bf16 h = __float2bfloat16_rn(v);
+   bf16 l = __float2bfloat16_rn(v - __bfloat162float(h));
+   Wh[i] = h;
+   Wl[i] = l;
+   Wth[(size_t)k * F + f] = h;
+   Wtl[(size_t)k * F + f] = l;
+   W32[i] = v;
+   Wt32[(size_t)k * F + f] = v;
+}
+
+// A = T(V) for the initial state, BF16 hi/lo and FP32
+__global__ void init_activity_kernel(LcaGeom g, const float *__restrict__ V, bf16 *A, bf16 *Alo, float *A32) {
+   size_t n = (size_t)g.nb * g.Npos * g.F;
+   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+      float a = thresh(V[i], g);
+      bf16 h = __float2bfloat16_rn(a);
+      A[i] = h;
+      Alo[i] = __float2bfloat16_rn(a - __bfloat162float(h));
+      A32[i] = a;
+   }
+}
+
+__global__ void activity_out_kernel(LcaGeom g, const float *__restrict__ V, float *__restrict__ out) {
+   size_t n = (size_t)g.nb * g.Npos * g.F;
+   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+      out[i] = thresh(V[i], g);
+}
+
+}  // namespace
+
+// The SIMT FP32 form lives in lca_solver_fp32.cu and shares LcaGeom through this hook.
+namespace pvgpu {
+pvgpu_status lca_fp32_step(int S, int P, int C, const LcaGeom &g, const float *x, const float *W32, const float *Wt32,
+                           float *partials, float *V, float *A32, cudaStream_t s);
+}
+
+struct pvgpu_lca_solver {
+   pvgpu_lca_solver_desc d;
+   LcaGeom g;
+   int S, P, C, KP;
+   int stepsRun;
+   float *V = nullptr, *partials = nullptr, *A32 = nullptr, *W32 = nullptr, *Wt32 = nullptr;
+   bf16 *A = nullptr, *Alo = nullptr, *W = nullptr, *Wlo = nullptr, *Wt = nullptr, *Wtlo = nullptr;
+   int *err = nullptr;
+   CUtensorMap tmA, tmAlo, tmWt, tmWtlo, tmW, tmWlo, tmV;
+   bool weightsSet = false;
+};
+
+namespace {
+
+template <int S, int P, int C>
+struct Launcher {
+   static size_t recon_smem(const pvgpu_lca_solver *s) {
+      constexpr int KP = P * P * C;
+      return 1024 + 2 * (size_t)(128 * 64 * 2 + KP * 64 * 2) + (size_t)s->g.inNx * s->g.inNy * C * 4;
+   }
+   template <int NT, bool X3>
+   static size_t post_smem(const pvgpu_lca_solver *s) {
+      using L = PostLayout<S, P, C, NT, X3>;
+      return 1024 + L::OFF_RWIN +
+             (size_t)rwin_rows(S, P, s->g.rowsPerBlock) * rwin_cols(S, P, s->g.v1Nx) * C * 4;
+   }
+   template <int NT, bool X3>
+   static pvgpu_status step(pvgpu_lca_solver *s, const float *x, cudaStream_t st) {
+      size_t rs = recon_smem(s);
+      auto rk = recon_tc_kernel<S, P, C, X3>;
+      cudaError_t e = cudaFuncSetAttribute(rk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rs);
+      if (e != cudaSuccess) return pvgpu::record_cuda_error(e, "lca recon attr");
+      rk<<<s->g.nb * s->g.MB, 128, rs, st>>>(s->tmA, s->tmAlo, s->tmWt, s->tmWtlo, s->g, s->partials, s->err);
+      PVGPU_CHECK_LAUNCH("lca recon");
+      size_t ps = post_smem<NT, X3>(s);
+      auto pk = post_tc_kernel<S, P, C, NT, X3>;
+      e = cudaFuncSetAttribute(pk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ps);
+      if (e != cudaSuccess) return pvgpu::record_cuda_error(e, "lca post attr");
+      pk<<<s->g.nb * s->g.MB * (s->g.F / NT), 128, ps, st>>>(s->tmW, s->tmWlo, s->tmV, s->g, x, s->partials, s->V,
+                                                              s->A, s->Alo, s->err);
+      PVGPU_CHECK_LAUNCH("lca post");
+      return PVGPU_OK;
+   }
+   static bool fits(const pvgpu_lca_solver *s, bool x3) {
+      size_t lim = 227 * 1024;
+      if (recon_smem(s) > lim) return false;
+      if (s->g.NT == 128) return (x3 ? post_smem<128, true>(s) : post_smem<128, false>(s)) <= lim;
+      return (x3 ? post_smem<64, true>(s) : post_smem<64, false>(s)) <= lim;
+   }
+   static pvgpu_status run_step(pvgpu_lca_solver *s, const float *x, bool x3, cudaStream_t st) {
+      if (s->g.NT == 128) return x3 ? step<128, true>(s, x, st) : step<128, false>(s, x, st);
+      return x3 ? step<64, true>(s, x, st) : step<64, false>(s, x, st);
+   }
+};
+
+template <typename Fn>
+pvgpu_status dispatch(int S, int P, int C, Fn &&fn) {
+   if (S == 2 && P == 8 && C == 1) return fn(Launcher<2, 8, 1>());
+   if (S == 2 && P == 8 && C == 3) return fn(Launcher<2, 8, 3>());
+   if (S == 4 && P == 16 && C == 1) return fn(Launcher<4, 16, 1>());
+   return PVGPU_ERR_UNSUPPORTED_SHAPE;
+}
+
+void free_solver(pvgpu_lca_solver *s) {
+   void *ptrs[] = {s->V, s->partials, s->A32, s->W32, s->Wt32, s->A, s->Alo, s->W, s->Wlo, s->Wt, s->Wtlo, s->err};
+   for (void *p : ptrs)
+      if (p) cudaFree(p);
+   delete s;
+}
+
+}  // namespace
+
+extern "C" pvgpu_status pvgpu_lca_solver_create(const pvgpu_lca_solver_desc *d, pvgpu_lca_solver **out) {
+   if (!d || !out) return PVGPU_ERR_BAD_ARG;
+   *out = nullptr;
+   if (d->nbatch <= 0 || d->inNx <= 0 || d->inNy <= 0 || d->inNf <= 0 || d->v1Nx <= 0 || d->v1Ny <= 0 ||
+       d->v1Nf <= 0 || d->nxp <= 0 || d->tau <= 0.0f)
+      return PVGPU_ERR_BAD_ARG;
+   if (d->inNx % d->v1Nx || d->inNy % d->v1Ny || d->inNx / d->v1Nx != d->inNy / d->v1Ny) return PVGPU_ERR_UNSUPPORTED_SHAPE;
+   const int S = d->inNx / d->v1Nx;
+   if (!pvgpu::axis_legal(d->v1Nx, d->inNx, d->nxp)) return PVGPU_ERR_ILLEGAL_GEOMETRY;
+   const int P = d->nxp, C = d->inNf, KP = P * P * C;
+   const int Npos = d->v1Nx * d->v1Ny;
+   if (Npos % 128 || 128 % d->v1Nx || KP % 64 || KP > 256 || d->v1Nf % 64) return PVGPU_ERR_UNSUPPORTED_SHAPE;
+   if (dispatch(S, P, C, [](auto) { return PVGPU_OK; }) != PVGPU_OK) return PVGPU_ERR_UNSUPPORTED_SHAPE;
+   pvgpu_lca_solver *s = new (std::nothrow) pvgpu_lca_solver();
+   if (!s) return PVGPU_ERR_OOM;
+   s->d = *d;
+   s->S = S;
+   s->P = P;
+   s->C = C;
+   s->KP = KP;
+   s->stepsRun = 0;
+   LcaGeom &g = s->g;
+   g.nb = d->nbatch;
+   g.inNx = d->inNx;
+   g.inNy = d->inNy;
+   g.v1Nx = d->v1Nx;
+   g.v1Ny = d->v1Ny;
+   g.F = d->v1Nf;
+   g.Npos = Npos;
+   g.MB = Npos / 128;
+   g.rowsPerBlock = 128 / d->v1Nx;
+   g.NT = d->v1Nf % 128 == 0 ? 128 : 64;
+   float vt = d->VThresh, vw = d->VWidth;
+   if (vw < 0) {
+      vt += vw;
+      vw = -vw;
+   }
+   g.VThresh = vt;
+   g.AMin = d->AMin;
+   g.AMax = d->AMax;
+   g.AShift = d->AShift;
+   g.VWidth = vw;
+   g.e = (float)exp(-(double)d->dt / (double)d->tau);
+   g.si = d->selfInteract ? 1.0f : 0.0f;
+   const size_t nState = (size_t)g.nb * Npos * g.F;
+   const size_t nPart = (size_t)g.nb * g.MB * d->inNx * d->inNy * C;
+   const size_t nW = (size_t)g.F * KP;
+   bool ok = cudaMalloc(&s->V, nState * 4) == cudaSuccess && cudaMalloc(&s->A32, nState * 4) == cudaSuccess &&
+             cudaMalloc(&s->A, nState * 2) == cudaSuccess && cudaMalloc(&s->Alo, nState * 2) == cudaSuccess &&
+             cudaMalloc(&s->partials, nPart * 4) == cudaSuccess && cudaMalloc(&s->W, nW * 2) == cudaSuccess &&
+             cudaMalloc(&s->Wlo, nW * 2) == cudaSuccess && cudaMalloc(&s->Wt, nW * 2) == cudaSuccess &&
+             cudaMalloc(&s->Wtlo, nW * 2) == cudaSuccess && cudaMalloc(&s->W32, nW * 4) == cudaSuccess &&
+             cudaMalloc(&s->Wt32, nW * 4) == cudaSuccess && cudaMalloc(&s->err, sizeof(int)) == cudaSuccess;
+   if (!ok) {
+      cudaGetLastError();
+      free_solver(s);
+      return PVGPU_ERR_OOM;
+   }
+   cudaMemset(s->err, 0, sizeof(int));
+   const uint64_t rowsA = (uint64_t)g.nb * Npos;
+   ok = pvgpu::make_tmap_bf16_sw128(&s->tmA, s->A, rowsA, g.F, g.F, 128) &&
+        pvgpu::make_tmap_bf16_sw128(&s->tmAlo, s->Alo, rowsA, g.F, g.F, 128) &&
+        pvgpu::make_tmap_bf16_sw128(&s->tmWt, s->Wt, KP, g.F, g.F, KP) &&
+        pvgpu::make_tmap_bf16_sw128(&s->tmWtlo, s->Wtlo, KP, g.F, g.F, KP) &&
+        pvgpu::make_tmap_bf16_sw128(&s->tmW, s->W, g.F, KP, KP, g.NT) &&
+        pvgpu::make_tmap_bf16_sw128(&s->tmWlo, s->Wlo, g.F, KP, KP, g.NT);
+   if (ok) {  // V tile: FP32 [rows][F], box 32 x 128, 128-byte swizzle
+      pvgpu::EncodeTiledFn enc = pvgpu::encode_tiled_fn();
+      cuuint64_t dims[2] = {(cuuint64_t)g.F, rowsA};
+      cuuint64_t strides[1] = {(cuuint64_t)g.F * 4};
+      cuuint32_t box[2] = {32, 128};
+      cuuint32_t estr[2] = {1, 1};
+      ok = enc && enc(&s->tmV, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, s->V, dims, strides, box, estr,
+                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+   }
+   if (!ok) {
+      free_solver(s);
+      return PVGPU_ERR_LAUNCH;
+   }
+   bool fits = true;
+   dispatch(S, P, C, [&](auto L) {
+      fits = L.fits(s, false);
+      return PVGPU_OK;
+   });
+   if (!fits) {
+      free_solver(s);
+      return PVGPU_ERR_UNSUPPORTED_SHAPE;
+   }
+   *out = s;
+   return PVGPU_OK;
+}
+
+extern "C" pvgpu_status pvgpu_lca_solver_destroy(pvgpu_lca_solver *s) {
+   if (!s) return PVGPU_ERR_BAD_ARG;
+   free_solver(s);
+   return PVGPU_OK;
+}
+
+extern "C" pvgpu_status pvgpu_lca_solver_set_weights(pvgpu_lca_solver *s, const float *w, void *stream) {
+   if (!s || !w) return PVGPU_ERR_BAD_ARG;
+   int n = s->g.F * s->KP;
+   prep_weights_kernel<<<(n + 255) / 256, 256, 0, pvgpu::as_stream(stream)>>>(w, s->g.F, s->KP, s->W, s->Wlo, s->Wt,
+                                                                           s->Wtlo, s->W32, s->Wt32);
+   PVGPU_CHECK_LAUNCH("lca set_weights");
+   s->weightsSet = true;
+   return PVGPU_OK;
+}
+
+extern "C" pvgpu_status pvgpu_lca_solver_reset(pvgpu_lca_solver *s, const float *v0, void *stream) {
+   if (!s) return PVGPU_ERR_BAD_ARG;
+   cudaStream_t st = pvgpu::as_stream(stream);
+   size_t n = (size_t)s->g.nb * s->g.Npos * s->g.F;
+   if (v0) PVGPU_CUDA(cudaMemcpyAsync(s->V, v0, n * 4, cudaMemcpyDeviceToDevice, st), "lca reset");
+   else PVGPU_CUDA(cudaMemsetAsync(s->V, 0, n * 4, st), "lca reset");
+   init_activity_kernel<<<152 * 8, 256, 0, st>>>(s->g, s->V, s->A, s->Alo, s->A32);
+   PVGPU_CHECK_LAUNCH("lca reset");
+   PVGPU_CUDA(cudaMemsetAsync(s->err, 0, sizeof(int), st), "lca reset");
+   s->stepsRun = 0;
+   return PVGPU_OK;
+}
+
+extern "C" pvgpu_status pvgpu_lca_solver_run(pvgpu_lca_solver *s, const float *x, int numSteps, int numX3Steps,
+                                             int precision, void *stream) {
+   if (!s || !x || numSteps < 0 || numX3Steps < 0 || numX3Steps > numSteps) return PVGPU_ERR_BAD_ARG;
+   if (!s->weightsSet) return PVGPU_ERR_BAD_ARG;
+   cudaStream_t st = pvgpu::as_stream(stream);
+   if (precision == PVGPU_LCA_FP32) {
+      for (int t = 0; t < numSteps; t++) {
+         pvgpu_status r = pvgpu::lca_fp32_step(s->S, s->P, s->C, s->g, x, s->W32, s->Wt32, s->partials, s->V, s->A32, st);
+         if (r != PVGPU_OK) return r;
+      }
+      s->stepsRun += numSteps;
+      return PVGPU_OK;
+   }
+   if (precision != PVGPU_LCA_BF16) return PVGPU_ERR_BAD_ARG;
+   bool x3ok = true;
+   if (numX3Steps > 0) {
+      dispatch(s->S, s->P, s->C, [&](auto L) {
+         x3ok = L.fits(s, true);
+         return PVGPU_OK;
+      });
+      if (!x3ok) return PVGPU_ERR_UNSUPPORTED_SHAPE;
+   }
+   for (int t = 0; t < numSteps; t++) {
+      const bool x3 = t >= numSteps - numX3Steps;
+      pvgpu_status r = dispatch(s->S, s->P, s->C, [&](auto L) { return L.run_step(s, x, x3, st); });
+      if (r != PVGPU_OK) return r;
+   }
+   s->stepsRun += numSteps;
+   return PVGPU_OK;
+}
+
+extern "C" pvgpu_status pvgpu_lca_solver_energy(pvgpu_lca_solver *s, const float *x, double l2Coeff, int costKind,
+                                                double costThresh, double costWidth, double costCoeff,
+                                                double *energy, void *stream) {
+   if (!s || !x || !energy || (costKind != 1 && costKind != 2)) return PVGPU_ERR_BAD_ARG;
+   energy_kernel<<<s->g.nb, 256, 0, pvgpu::as_stream(stream)>>>(s->g, s->C, x, s->partials, s->V, l2Coeff, costKind,
+                                                                costThresh, costWidth, costCoeff, energy);
+   PVGPU_CHECK_LAUNCH("lca energy");
+   return PVGPU_OK;
+}
+
+extern "C" pvgpu_status pvgpu_lca_solver_state(pvgpu_lca_solver *s, float *v, float *a, void *stream) {
+   if (!s) return PVGPU_ERR_BAD_ARG;
+   cudaStream_t st = pvgpu::as_stream(stream);
+   size_t n = (size_t)s->g.nb * s->g.Npos * s->g.F;
+   if (v) PVGPU_CUDA(cudaMemcpyAsync(v, s->V, n * 4, cudaMemcpyDeviceToDevice, st), "lca state");
+   if (a) {
+      activity_out_kernel<<<152 * 8, 256, 0, st>>>(s->g, s->V, a);
+      PVGPU_CHECK_LAUNCH("lca state");
+   }
+   return PVGPU_OK;
+}
+
+extern "C" pvgpu_status pvgpu_lca_solver_error_flag(pvgpu_lca_solver *s, int *hostFlag) {
+   if (!s || !hostFlag) return PVGPU_ERR_BAD_ARG;
+   PVGPU_CUDA(cudaMemcpy(hostFlag, s->err, sizeof(int), cudaMemcpyDeviceToHost), "lca error flag");
+   return PVGPU_OK;
+}

@@ -82,7 +82,7 @@ __global__ void __launch_bounds__(128) tc_gemm_kernel(const __grid_constant__ CU
       }
    }
    __syncthreads();
-   bool ok = failed == 0 && mbar_wait(&done, 0);
+   bool ok = __syncthreads_and(failed == 0 && mbar_wait(&done, 0));
    tc_fence_after();
    if (ok) {
       const int row = m0 + warp * 32 + lane;

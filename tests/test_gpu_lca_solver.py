@@ -1,0 +1,127 @@
+"""The fused LCA solver (both precisions) against the CPU oracle's LCA module
+(pvo_lca_run: input -> error <-> V1 in the reference's phase order), through the C ABI.
+
+FP32 form: same math as the reference path, only GEMM summation order differs -> V, A and
+the probe energy agree with the FP32 oracle to ~1e-5 relative.  BF16 form: the final energy
+must be within 1e-3 relative of the FP64 oracle (the stated BF16 bar)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def torch():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from openpv_gb300 import build
+    build.build()
+    return torch
+
+
+def dictionary(rng, nf, p, c):
+    w = rng.normal(size=(nf, p, p, c))
+    w /= np.sqrt((w ** 2).sum(axis=(1, 2, 3), keepdims=True))
+    return w.astype(np.float32)
+
+
+def one_over_f(rng, nb, ny, nx, c):
+    fy = np.fft.fftfreq(ny)[:, None]
+    fx = np.fft.fftfreq(nx)[None, :]
+    f = np.sqrt(fy ** 2 + fx ** 2)
+    f[0, 0] = 1.0
+    amp = 1.0 / f
+    amp[0, 0] = 0.0
+    out = np.zeros((nb, ny, nx, c))
+    for b in range(nb):
+        for ch in range(c):
+            ph = rng.uniform(0, 2 * np.pi, (ny, nx))
+            img = np.real(np.fft.ifft2(amp * np.exp(1j * ph)))
+            out[b, :, :, ch] = img
+        out[b] = (out[b] - out[b].mean()) / out[b].std()
+    return out.astype(np.float32)
+
+
+CASES = {
+    # name: nb, (in y,x,c), (v1 y,x,f), nxp, VThresh, steps
+    "plain_lca": (2, (32, 32, 1), (16, 16, 64), 8, 0.1, 30),
+    "colour": (2, (32, 32, 3), (16, 16, 128), 8, 0.15, 30),
+    "stride4": (1, (64, 64, 1), (16, 16, 64), 16, 0.1, 20),
+}
+
+
+def setup(oracle, name, seed=3):
+    nb, ins, v1s, nxp, vth, steps = CASES[name]
+    rng = np.random.default_rng(seed)
+    w = dictionary(rng, v1s[2], nxp, ins[2])
+    x = one_over_f(rng, nb, *ins)
+    p = oracle.lca_params(nbatch=nb, inNx=ins[1], inNy=ins[0], inNf=ins[2], v1Nx=v1s[1], v1Ny=v1s[0],
+                          v1Nf=v1s[2], nxp=nxp, nyp=nxp, VThresh=vth, AShift=vth, AMin=0.0, VWidth=0.0, tau=100.0,
+                          dtFixed=1.0)
+    return nb, ins, v1s, nxp, vth, steps, w, x, p
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_lca_fp32_form_matches_oracle(torch, oracle, name):
+    from openpv_gb300 import capi
+    nb, ins, v1s, nxp, vth, steps, w, x, p = setup(oracle, name)
+    v0 = np.zeros((nb,) + v1s, np.float32)
+    v_ref, a_ref, _, e_ref = oracle.lca_run(p, w, x[None], steps, v0, want_recon=False)
+    s = capi.LcaSolver(nb, ins, v1s, nxp, vth)
+    s.set_weights(torch.from_numpy(w).cuda())
+    s.reset()
+    xd = torch.from_numpy(x).cuda()
+    s.run(xd, steps, precision=capi.LCA_FP32)
+    v = torch.zeros((nb,) + v1s, device="cuda")
+    a = torch.zeros((nb,) + v1s, device="cuda")
+    s.state(v, a)
+    e = torch.zeros(nb, dtype=torch.float64, device="cuda")
+    s.energy(xd, e)
+    torch.cuda.synchronize()
+    assert s.error_flag() == 0
+    vs = np.abs(v_ref).max()
+    np.testing.assert_allclose(v.cpu().numpy(), v_ref, rtol=1e-4, atol=1e-5 * vs)
+    np.testing.assert_allclose(a.cpu().numpy(), a_ref, rtol=1e-4, atol=1e-5 * vs)
+    np.testing.assert_allclose(e.cpu().numpy(), e_ref[-1], rtol=1e-5)
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_lca_bf16_form_energy_within_1e3_of_fp64(torch, oracle, name):
+    from openpv_gb300 import capi
+    nb, ins, v1s, nxp, vth, steps, w, x, p = setup(oracle, name)
+    v0 = np.zeros((nb,) + v1s)
+    _, _, _, e64 = oracle.lca_run(p, w.astype(np.float64), x[None].astype(np.float64), steps, v0, f64=True,
+                                  want_recon=False)
+    s = capi.LcaSolver(nb, ins, v1s, nxp, vth)
+    s.set_weights(torch.from_numpy(w).cuda())
+    xd = torch.from_numpy(x).cuda()
+    e = torch.zeros(nb, dtype=torch.float64, device="cuda")
+    for x3 in (0, 5):
+        s.reset()
+        s.run(xd, steps, x3_steps=x3, precision=capi.LCA_BF16)
+        s.energy(xd, e)
+        torch.cuda.synchronize()
+        assert s.error_flag() == 0
+        rel = np.abs(e.cpu().numpy() - e64[-1]) / np.abs(e64[-1])
+        assert rel.max() < 1e-3, (x3, rel)
+
+
+def test_lca_bf16_x3_closer_than_bf16(torch, oracle):
+    """BF16x3 split products bring the state closer to the FP32 oracle than plain BF16."""
+    from openpv_gb300 import capi
+    nb, ins, v1s, nxp, vth, steps, w, x, p = setup(oracle, "colour")
+    v0 = np.zeros((nb,) + v1s, np.float32)
+    v_ref, _, _, _ = oracle.lca_run(p, w, x[None], steps, v0, want_recon=False)
+    s = capi.LcaSolver(nb, ins, v1s, nxp, vth)
+    s.set_weights(torch.from_numpy(w).cuda())
+    xd = torch.from_numpy(x).cuda()
+    errs = []
+    for x3 in (0, steps):
+        s.reset()
+        s.run(xd, steps, x3_steps=x3, precision=capi.LCA_BF16)
+        v = torch.zeros((nb,) + v1s, device="cuda")
+        s.state(v)
+        torch.cuda.synchronize()
+        errs.append(np.abs(v.cpu().numpy() - v_ref).max())
+    assert errs[1] < 0.25 * errs[0], errs
