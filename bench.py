@@ -1,0 +1,460 @@
+"""Benchmark of the batched LCA module on one GB300 (and N replicas under torchrun).
+
+Workload (the headline metric's configuration): 256 images of 32x32x3 with a seeded 1/f
+amplitude spectrum and random phase, each normalised to zero mean and unit std; an LCA
+layer of 16x16x512 (stride 2) with a dictionary of 512 features of 8x8x3, N(0,1) then
+L2-normalised; VThresh = AShift = 0.15, AMin = 0, tau = 100, dt = 1; 400 timesteps per
+solve, the last 50 with BF16x3 split products.  One bench step = one full solve of the
+batch (reset, 400 timesteps, the FP64 probe energy).  Synthetic data stands in for
+natural images; inputs are generated here from fixed seeds.
+
+Metric: images*timesteps per second of the BF16 tensor-core form (value, device-resident
+inputs), the same through the C ABI with host buffers (e2e), the plain FP32 form beside it,
+the final-energy error against the FP64 oracle, the dominant kernel's roofline fraction
+(CUDA events around every launch in the timed region), the presynaptic sparse-delivery
+microbenchmark, and the CPU oracle timed on this host's cores.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+CFG = dict(nbatch=256, in_shape=(32, 32, 3), v1_shape=(16, 16, 512), nxp=8, VThresh=0.15, AMin=0.0, AShift=0.15,
+           VWidth=0.0, tau=100.0, dt=1.0, timesteps=400, x3_steps=50, seed=1237)
+METRIC = "LCA images*steps/s BF16-TC vs plain FP32 at <=1e-3 energy err; delivery HBM GB/s"
+PEAKS_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return {"hbm_gbs": d["hbm_gbs"], "bf16_tflops": d["bf16_tflops"], "source": "measured"}
+    return dict(PEAKS_FALLBACK, source="fallback")
+
+
+# ---------------------------------------------------------------------------------------------
+# synthetic inputs
+# ---------------------------------------------------------------------------------------------
+def one_over_f_images(rng, nb, ny, nx, c):
+    fy = np.fft.fftfreq(ny)[:, None]
+    fx = np.fft.fftfreq(nx)[None, :]
+    f = np.sqrt(fy ** 2 + fx ** 2)
+    f[0, 0] = 1.0
+    amp = 1.0 / f
+    amp[0, 0] = 0.0
+    ph = rng.uniform(0, 2 * np.pi, (nb, c, ny, nx))
+    img = np.real(np.fft.ifft2(amp[None, None] * np.exp(1j * ph)))  # [nb][c][ny][nx]
+    img = np.transpose(img, (0, 2, 3, 1))
+    mu = img.mean(axis=(1, 2, 3), keepdims=True)
+    sd = img.std(axis=(1, 2, 3), keepdims=True)
+    return ((img - mu) / sd).astype(np.float32)
+
+
+def dictionary(rng, nf, p, c):
+    w = rng.normal(size=(nf, p, p, c))
+    w /= np.sqrt((w ** 2).sum(axis=(1, 2, 3), keepdims=True))
+    return w.astype(np.float32)
+
+
+def make_inputs(cfg, nb=None, seed_offset=0):
+    rng = np.random.default_rng(cfg["seed"] + seed_offset)
+    nb = cfg["nbatch"] if nb is None else nb
+    w = dictionary(rng, cfg["v1_shape"][2], cfg["nxp"], cfg["in_shape"][2])
+    x = one_over_f_images(rng, nb, *cfg["in_shape"])
+    return w, x
+
+
+# ---------------------------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------------------------
+class ClockSampler:
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            f = [t.strip() for t in l.split(",")]
+            try:
+                sm.append(float(f[0]))
+                mx = float(f[1])
+            except (ValueError, IndexError):
+                continue
+            for n, v in zip(names, f[3:7]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------------------------
+# CPU oracle timing (the reference's CPU path restated; test infrastructure)
+# ---------------------------------------------------------------------------------------------
+def oracle_lca_params(O, cfg, nb):
+    (iy, ix, ic), (vy, vx, vf) = cfg["in_shape"], cfg["v1_shape"]
+    return O.lca_params(nbatch=nb, inNx=ix, inNy=iy, inNf=ic, v1Nx=vx, v1Ny=vy, v1Nf=vf, nxp=cfg["nxp"],
+                        nyp=cfg["nxp"], VThresh=cfg["VThresh"], AShift=cfg["AShift"], AMin=cfg["AMin"],
+                        VWidth=cfg["VWidth"], tau=cfg["tau"], dtFixed=cfg["dt"])
+
+
+def cpu_sample(cfg, threads, warm_steps, timed_steps):
+    """The oracle (FP32, reference order) on `threads` images, one per thread: warm_steps untimed
+    timesteps into the dynamics, then timed_steps timed.  Returns images*steps/s."""
+    from oracle import oracle as O
+    O.build()
+    w, x = make_inputs(cfg, nb=threads, seed_offset=100)
+    p = oracle_lca_params(O, cfg, threads)
+    v = np.zeros((threads,) + cfg["v1_shape"], np.float32)
+    if warm_steps:
+        v, _, _, _ = O.lca_run(p, w, x[None], warm_steps, v, threads=threads, want_recon=False)
+    t0 = time.perf_counter()
+    O.lca_run(p, w, x[None], timed_steps, v, threads=threads, want_recon=False)
+    dt = time.perf_counter() - t0
+    return threads * timed_steps / dt, dt
+
+
+def fp64_energy(cfg, x, w, nimg, threads):
+    from oracle import oracle as O
+    O.build()
+    p = oracle_lca_params(O, cfg, nimg)
+    v0 = np.zeros((nimg,) + cfg["v1_shape"])
+    _, _, _, e = O.lca_run(p, w.astype(np.float64), x[None, :nimg].astype(np.float64), cfg["timesteps"], v0,
+                           f64=True, threads=threads, want_recon=False)
+    return e[-1]
+
+
+# ---------------------------------------------------------------------------------------------
+# reference arm
+# ---------------------------------------------------------------------------------------------
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    cfg = CFG
+    from oracle import oracle as O
+    O.build()
+    w, x = make_inputs(cfg, nb=cores, seed_offset=100)
+    p = oracle_lca_params(O, cfg, cores)
+    v = np.zeros((cores,) + cfg["v1_shape"], np.float32)
+    per_step = 25  # timesteps per bench step; the dynamics continue from step to step
+    for _ in range(args.warmup):
+        v, _, _, _ = O.lca_run(p, w, x[None], per_step, v, threads=cores, want_recon=False)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        v, _, _, _ = O.lca_run(p, w, x[None], per_step, v, threads=cores, want_recon=False)
+    dt = time.perf_counter() - t0
+    value = cores * per_step * args.steps / dt
+    sample = (f"{cores} images x {per_step} timesteps per step (one image per thread), continuing the dynamics "
+              f"after {args.warmup * per_step} warm-up timesteps; same layer sizes as the GPU workload")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "images*steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * dt / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "batched LCA 256x32x32x3 -> 16x16x512, 8x8x3 dictionary, 400 timesteps",
+                       "reference_sample": sample},
+            "cpu_baseline": {"value": value, "unit": "images*steps/s", "cores": cores, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": "images*steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------------------------
+# delivery microbenchmark (presynaptic sparse delivery, 128x128x256 -> 128x128x64, 7x7, batch 16)
+# ---------------------------------------------------------------------------------------------
+def delivery_bench(torch, capi, reps=5):
+    nb = 16
+    pre = capi.Loc.make(nb, 128, 128, 256, 3)
+    post = capi.Loc.make(nb, 128, 128, 64, 0)
+    conn = capi.conn_desc(pre, post, 7, 7)
+    g = torch.Generator(device="cuda").manual_seed(1234 + 2)
+    w = (torch.randn(256 * 7 * 7 * 64, device="cuda", generator=g) * 0.05).contiguous()
+    gsyn = torch.zeros(post.res_shape(), device="cuda")
+    entries = torch.empty((nb, pre.num_ext, 2), dtype=torch.int32, device="cuda")
+    num = torch.zeros(nb, dtype=torch.int64, device="cuda")
+    out = {}
+    for p in (0.01, 0.05, 0.2):
+        a = torch.zeros(pre.ext_shape(), device="cuda")
+        core = (torch.rand((nb, 128, 128, 256), device="cuda", generator=g) < p).float() * \
+            (1.0 - torch.rand((nb, 128, 128, 256), device="cuda", generator=g))
+        a[:, 3:131, 3:131, :] = core
+        capi.compact_active(a, nb, pre.num_ext, entries, num)
+        torch.cuda.synchronize()
+        nnz = int(num.sum().item())
+        # warm-up, then reps timed with events
+        capi.deliver_pre(conn, w, gsyn, entries=entries, num_active=num)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            capi.deliver_pre(conn, w, gsyn, entries=entries, num_active=num)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        # algorithmic bytes: entries read, GSyn read+write, weights once
+        byts = 8 * nnz + 8 * post.num_res * nb + 4 * w.numel()
+        flops = 2 * nnz * 7 * 7 * 64
+        # compaction of the dense activity (HBM-bound integer work)
+        c0, c1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        c0.record()
+        for _ in range(reps):
+            capi.compact_active(a, nb, pre.num_ext, entries, num)
+        c1.record()
+        torch.cuda.synchronize()
+        cms = c0.elapsed_time(c1) / reps
+        cbytes = 2 * 4 * pre.num_ext * nb + 8 * nnz  # two passes over the activity + entries written
+        out[str(p)] = {"nnz_per_image": nnz / nb, "ms": ms, "GB_s": byts / ms / 1e6, "GFLOP_s": flops / ms / 1e6,
+                       "compaction_ms": cms, "compaction_GB_s": cbytes / cms / 1e6}
+    return out
+
+
+# ---------------------------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------------------------
+def run_ours(args, rank, world, local_rank):
+    import torch
+    from openpv_gb300 import build
+    build.build()
+    from openpv_gb300 import capi
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+    cfg = dict(CFG)
+    if args.timesteps:
+        cfg["timesteps"] = args.timesteps
+        cfg["x3_steps"] = min(cfg["x3_steps"], args.timesteps // 8)
+    nb, T, X3 = cfg["nbatch"], cfg["timesteps"], cfg["x3_steps"]
+    w_np, x_np = make_inputs(cfg, seed_offset=rank)  # each rank solves its own batch shard
+    vshape = (nb,) + cfg["v1_shape"]
+    solver = capi.LcaSolver(nb, cfg["in_shape"], cfg["v1_shape"], cfg["nxp"], cfg["VThresh"], AMin=cfg["AMin"],
+                            AShift=cfg["AShift"], VWidth=cfg["VWidth"], tau=cfg["tau"], dt=cfg["dt"])
+    w = torch.from_numpy(w_np).to(dev)
+    x = torch.from_numpy(x_np).to(dev)
+    solver.set_weights(w)
+    energy = torch.zeros(nb, dtype=torch.float64, device=dev)
+
+    def solve(xd, precision=capi.LCA_BF16, x3=X3):
+        solver.reset()
+        solver.run(xd, T, x3_steps=x3, precision=precision)
+        solver.energy(xd, energy)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        solve(x)
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    solver.profile_begin(args.steps * T)
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        e0.record()
+        for _ in range(args.steps):
+            solve(x)
+        e1.record()
+        torch.cuda.synchronize()
+    recon_ms, post_ms, nprof = solver.profile_end()
+    barrier()
+    ms = e0.elapsed_time(e1) / args.steps
+    ms_all = ms
+    if dist is not None:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_all = float(t.item())
+    value = world * nb * T / (ms_all / 1000.0)
+    assert solver.error_flag() == 0, "a bounded device wait timed out"
+    e_gpu = energy.cpu().numpy().copy()
+
+    # end to end through the C ABI with host buffers: H2D input, solve, D2H activity + energy
+    x_host = torch.from_numpy(x_np).pin_memory()
+    a_host = torch.empty(vshape, dtype=torch.float32).pin_memory()
+    en_host = torch.empty(nb, dtype=torch.float64).pin_memory()
+    x_dev = torch.empty_like(x)
+    a_dev = torch.empty(vshape, device=dev)
+
+    def e2e_step():
+        x_dev.copy_(x_host, non_blocking=True)
+        solve(x_dev)
+        solver.state(a=a_dev)
+        a_host.copy_(a_dev, non_blocking=True)
+        en_host.copy_(energy, non_blocking=True)
+
+    e2e_step()
+    barrier()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record()
+    for _ in range(args.steps):
+        e2e_step()
+    t1.record()
+    torch.cuda.synchronize()
+    e2e_ms = t0.elapsed_time(t1) / args.steps
+    if dist is not None:
+        t = torch.tensor([e2e_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    e2e_value = world * nb * T / (e2e_ms / 1000.0)
+    h2d = x_np.nbytes
+    d2h = a_host.numel() * 4 + nb * 8
+
+    if rank != 0 or args.quick:
+        if dist is not None:
+            dist.barrier()
+            dist.destroy_process_group()
+        if args.quick and rank == 0:
+            print(json.dumps({"quick": True, "value": value, "ms_per_step": ms_all, "timesteps": T,
+                              "recon_ms": recon_ms / max(nprof, 1), "post_ms": post_ms / max(nprof, 1)}))
+        return
+
+    # plain FP32 form, same structure, no tensor cores
+    solve(x, precision=capi.LCA_FP32, x3=0)
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps32 = max(1, min(args.steps, 3))
+    f0.record()
+    for _ in range(reps32):
+        solve(x, precision=capi.LCA_FP32, x3=0)
+    f1.record()
+    torch.cuda.synchronize()
+    ms32 = f0.elapsed_time(f1) / reps32
+    value32 = nb * T / (ms32 / 1000.0)
+    e_fp32 = energy.cpu().numpy().copy()
+
+    # final-energy error against the FP64 oracle on the first images
+    nchk = int(os.environ.get("PVGPU_BENCH_FP64_IMAGES", "4"))
+    cores = os.cpu_count() or 1
+    e64 = fp64_energy(cfg, x_np, w_np, nchk, min(nchk, cores))
+    rel_bf16 = float(np.max(np.abs(e_gpu[:nchk] - e64) / np.abs(e64)))
+    rel_fp32 = float(np.max(np.abs(e_fp32[:nchk] - e64) / np.abs(e64)))
+
+    # dominant kernel roofline: the post-delivery + update kernel (HBM-bound)
+    pk = peaks()
+    npos, F = cfg["v1_shape"][0] * cfg["v1_shape"][1], cfg["v1_shape"][2]
+    npix = int(np.prod(cfg["in_shape"]))
+    mb = npos // 128
+    x3_frac = X3 / T
+    # per image-timestep: V read + write (FP32), A written (BF16; + BF16 lo in BF16x3 steps),
+    # the input and the partial reconstructions read once
+    post_bytes_unit = npos * F * (4 + 4 + 2 + 2 * x3_frac) + (mb + 1) * npix * 4
+    post_bytes_launch = post_bytes_unit * nb
+    post_avg_ms = post_ms / nprof
+    achieved = post_bytes_launch / (post_avg_ms / 1000.0) / 1e9
+    recon_bytes_unit = npos * F * (2 + 2 * x3_frac) + mb * npix * 4
+    recon_avg_ms = recon_ms / nprof
+    recon_flops_launch = 2 * npos * F * (cfg["nxp"] ** 2 * cfg["in_shape"][2]) * nb * (1 + 2 * x3_frac)
+
+    trafficf = os.path.join(ROOT, "profiles", "post_kernel_traffic.json")
+    traffic = None
+    if os.path.exists(trafficf):
+        try:
+            traffic = json.load(open(trafficf)).get("bytes_per_launch")
+        except (ValueError, OSError):
+            traffic = None
+
+    cpu_val, cpu_dt = cpu_sample(cfg, cores, warm_steps=25, timed_steps=25)
+    deliv = delivery_bench(torch, capi)
+    clocks = clk.summary()
+
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "images*steps/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_all,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "bf16",
+        "data": "synthetic",
+        "config": {"workload": "batched LCA: 256 images 32x32x3 (1/f, unit std) -> V1 16x16x512 stride 2, "
+                               "dictionary 512 x 8x8x3, VThresh=AShift=0.15, tau=100, 400 timesteps, BF16x3 last 50",
+                   "global_batch": nb * world, "timesteps_per_step": T, "parallelism": f"replicas{world}",
+                   "l2": "state streamed each timestep (V 134 MB + activity 67 MB per step > 129 MB L2)"},
+        "gpu_launches": args.steps * (2 * T + 2),
+        "e2e": {"value": e2e_value, "unit": "images*steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "roofline": {"bound": "hbm", "kernel": "post_tc_kernel (residual + post delivery GEMM + LCA update)",
+                     "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": achieved / pk["hbm_gbs"],
+                     "peak_source": pk["source"], "traffic": traffic, "bytes_per_launch": post_bytes_launch,
+                     "avg_launch_ms": post_avg_ms, "share_of_step": post_ms / (post_ms + recon_ms)},
+        "recon_kernel": {"avg_launch_ms": recon_avg_ms, "GB_s": recon_bytes_unit * nb / (recon_avg_ms / 1e3) / 1e9,
+                         "TFLOP_s": recon_flops_launch / (recon_avg_ms / 1e3) / 1e12},
+        "fp32_form": {"value": value32, "unit": "images*steps/s", "speedup_bf16_over_fp32": value / world / value32,
+                      "final_energy_rel_err_vs_fp64": rel_fp32},
+        "final_energy_rel_err_vs_fp64": rel_bf16,
+        "energy_check_images": nchk,
+        "cpu_baseline": {"value": cpu_val, "unit": "images*steps/s", "cores": cores, "kind": "port",
+                         "sample": f"oracle FP32 LCA, {cores} images (one per thread) x 25 timesteps after 25 "
+                                   f"warm-up timesteps, same layer sizes ({cpu_dt:.1f} s)"},
+        "delivery": {"workload": "presynaptic sparse delivery 16 x (128x128x256 -> 128x128x64), 7x7 shared weights",
+                     "by_density": deliv, "hbm_peak_gbs": pk["hbm_gbs"]},
+        "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--timesteps", type=int, default=0, help="override the 400 LCA timesteps (profiling runs)")
+    ap.add_argument("--quick", action="store_true", help="time the solve only (profiling runs; not a bench line)")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", str(args.gpus if args.impl == "ours" else 1)))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if world != args.gpus and "WORLD_SIZE" not in os.environ:
+        world = 1
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world, local_rank)
+
+
+if __name__ == "__main__":
+    main()

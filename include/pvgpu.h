@@ -274,6 +274,12 @@ pvgpu_status pvgpu_lca_solver_energy(pvgpu_lca_solver *s, const float *x, double
 pvgpu_status pvgpu_lca_solver_state(pvgpu_lca_solver *s, float *v, float *a, void *stream);
 /* Reads (synchronously) the solver's device error flag: nonzero if a bounded device wait gave up. */
 pvgpu_status pvgpu_lca_solver_error_flag(pvgpu_lca_solver *s, int *hostFlag);
+/* Per-kernel timing of the next maxSteps timesteps with CUDA events on the run's stream (the
+ * counterpart of the reference's CudaTimer around recvsyn / update, arch/cuda/CudaTimer.hpp:23-63).
+ * profile_end synchronises on the last event and returns the summed milliseconds of the
+ * reconstruction kernel and of the post-delivery/update kernel over the recorded steps. */
+pvgpu_status pvgpu_lca_solver_profile_begin(pvgpu_lca_solver *s, int maxSteps);
+pvgpu_status pvgpu_lca_solver_profile_end(pvgpu_lca_solver *s, double *reconMs, double *postMs, int *steps);
 
 /* ---- diagnostics ----------------------------------------------------------------------------
  * No counterpart in the reference.  C[M][N] (FP32) = A[M][K] * B[N][K]^T with BF16 row-major

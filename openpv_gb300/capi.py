@@ -125,6 +125,8 @@ def _declare(L):
         "pvgpu_lca_solver_energy": (i, [vp, vp, d, i, d, d, d, vp, vp]),
         "pvgpu_lca_solver_state": (i, [vp, vp, vp, vp]),
         "pvgpu_lca_solver_error_flag": (i, [vp, C.POINTER(i)]),
+        "pvgpu_lca_solver_profile_begin": (i, [vp, i]),
+        "pvgpu_lca_solver_profile_end": (i, [vp, C.POINTER(d), C.POINTER(d), C.POINTER(i)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -281,6 +283,15 @@ class LcaSolver:
 
     def state(self, v=None, a=None, stream=None):
         check(lib().pvgpu_lca_solver_state(self.h, _ptr(v), _ptr(a), _stream(stream)), "lca_solver_state")
+
+    def profile_begin(self, max_steps):
+        check(lib().pvgpu_lca_solver_profile_begin(self.h, max_steps), "lca_solver_profile_begin")
+
+    def profile_end(self):
+        """(recon ms, post ms, steps) summed over the profiled timesteps."""
+        r, p, n = C.c_double(), C.c_double(), C.c_int()
+        check(lib().pvgpu_lca_solver_profile_end(self.h, C.byref(r), C.byref(p), C.byref(n)), "lca_solver_profile_end")
+        return r.value, p.value, n.value
 
     def error_flag(self):
         f = C.c_int(0)

@@ -36,6 +36,7 @@
 #include <cstdio>
 #include <cstring>
 #include <new>
+#include <vector>
 
 namespace {
 
@@ -488,7 +489,7 @@ __global__ void activity_out_kernel(LcaGeom g, const float *__restrict__ V, floa
 // The SIMT FP32 form lives in lca_solver_fp32.cu and shares LcaGeom through this hook.
 namespace pvgpu {
 pvgpu_status lca_fp32_step(int S, int P, int C, const LcaGeom &g, const float *x, const float *W32, const float *Wt32,
-                           float *partials, float *V, float *A32, cudaStream_t s);
+                           float *partials, float *V, float *A32, cudaStream_t s, cudaEvent_t mid);
 }
 
 struct pvgpu_lca_solver {
@@ -501,6 +502,10 @@ struct pvgpu_lca_solver {
    int *err = nullptr;
    CUtensorMap tmA, tmAlo, tmWt, tmWtlo, tmW, tmWlo, tmV;
    bool weightsSet = false;
+   // optional per-kernel timing: events before kernel R, between R and P, after P
+   std::vector<cudaEvent_t> ev;
+   size_t evNext = 0;
+   bool profiling = false;
 };
 
 namespace {
@@ -518,13 +523,14 @@ struct Launcher {
              (size_t)rwin_rows(S, P, s->g.rowsPerBlock) * rwin_cols(S, P, s->g.v1Nx) * C * 4;
    }
    template <int NT, bool X3>
-   static pvgpu_status step(pvgpu_lca_solver *s, const float *x, cudaStream_t st) {
+   static pvgpu_status step(pvgpu_lca_solver *s, const float *x, cudaStream_t st, cudaEvent_t mid) {
       size_t rs = recon_smem(s);
       auto rk = recon_tc_kernel<S, P, C, X3>;
       cudaError_t e = cudaFuncSetAttribute(rk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rs);
       if (e != cudaSuccess) return pvgpu::record_cuda_error(e, "lca recon attr");
       rk<<<s->g.nb * s->g.MB, 128, rs, st>>>(s->tmA, s->tmAlo, s->tmWt, s->tmWtlo, s->g, s->partials, s->err);
       PVGPU_CHECK_LAUNCH("lca recon");
+      if (mid) cudaEventRecord(mid, st);
       size_t ps = post_smem<NT, X3>(s);
       auto pk = post_tc_kernel<S, P, C, NT, X3>;
       e = cudaFuncSetAttribute(pk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ps);
@@ -540,9 +546,9 @@ struct Launcher {
       if (s->g.NT == 128) return (x3 ? post_smem<128, true>(s) : post_smem<128, false>(s)) <= lim;
       return (x3 ? post_smem<64, true>(s) : post_smem<64, false>(s)) <= lim;
    }
-   static pvgpu_status run_step(pvgpu_lca_solver *s, const float *x, bool x3, cudaStream_t st) {
-      if (s->g.NT == 128) return x3 ? step<128, true>(s, x, st) : step<128, false>(s, x, st);
-      return x3 ? step<64, true>(s, x, st) : step<64, false>(s, x, st);
+   static pvgpu_status run_step(pvgpu_lca_solver *s, const float *x, bool x3, cudaStream_t st, cudaEvent_t mid) {
+      if (s->g.NT == 128) return x3 ? step<128, true>(s, x, st, mid) : step<128, false>(s, x, st, mid);
+      return x3 ? step<64, true>(s, x, st, mid) : step<64, false>(s, x, st, mid);
    }
 };
 
@@ -555,6 +561,7 @@ pvgpu_status dispatch(int S, int P, int C, Fn &&fn) {
 }
 
 void free_solver(pvgpu_lca_solver *s) {
+   for (cudaEvent_t e : s->ev) cudaEventDestroy(e);
    void *ptrs[] = {s->V, s->partials, s->A32, s->W32, s->Wt32, s->A, s->Alo, s->W, s->Wlo, s->Wt, s->Wtlo, s->err};
    for (void *p : ptrs)
       if (p) cudaFree(p);
@@ -692,8 +699,15 @@ extern "C" pvgpu_status pvgpu_lca_solver_run(pvgpu_lca_solver *s, const float *x
    cudaStream_t st = pvgpu::as_stream(stream);
    if (precision == PVGPU_LCA_FP32) {
       for (int t = 0; t < numSteps; t++) {
-         pvgpu_status r = pvgpu::lca_fp32_step(s->S, s->P, s->C, s->g, x, s->W32, s->Wt32, s->partials, s->V, s->A32, st);
+         const bool rec = s->profiling && s->evNext + 3 <= s->ev.size();
+         if (rec) cudaEventRecord(s->ev[s->evNext], st);
+         pvgpu_status r = pvgpu::lca_fp32_step(s->S, s->P, s->C, s->g, x, s->W32, s->Wt32, s->partials, s->V, s->A32,
+                                               st, rec ? s->ev[s->evNext + 1] : nullptr);
          if (r != PVGPU_OK) return r;
+         if (rec) {
+            cudaEventRecord(s->ev[s->evNext + 2], st);
+            s->evNext += 3;
+         }
       }
       s->stepsRun += numSteps;
       return PVGPU_OK;
@@ -709,8 +723,16 @@ extern "C" pvgpu_status pvgpu_lca_solver_run(pvgpu_lca_solver *s, const float *x
    }
    for (int t = 0; t < numSteps; t++) {
       const bool x3 = t >= numSteps - numX3Steps;
-      pvgpu_status r = dispatch(s->S, s->P, s->C, [&](auto L) { return L.run_step(s, x, x3, st); });
+      const bool rec = s->profiling && s->evNext + 3 <= s->ev.size();
+      if (rec) cudaEventRecord(s->ev[s->evNext], st);
+      pvgpu_status r = dispatch(s->S, s->P, s->C, [&](auto L) {
+         return L.run_step(s, x, x3, st, rec ? s->ev[s->evNext + 1] : nullptr);
+      });
       if (r != PVGPU_OK) return r;
+      if (rec) {
+         cudaEventRecord(s->ev[s->evNext + 2], st);
+         s->evNext += 3;
+      }
    }
    s->stepsRun += numSteps;
    return PVGPU_OK;
@@ -741,5 +763,38 @@ extern "C" pvgpu_status pvgpu_lca_solver_state(pvgpu_lca_solver *s, float *v, fl
 extern "C" pvgpu_status pvgpu_lca_solver_error_flag(pvgpu_lca_solver *s, int *hostFlag) {
    if (!s || !hostFlag) return PVGPU_ERR_BAD_ARG;
    PVGPU_CUDA(cudaMemcpy(hostFlag, s->err, sizeof(int), cudaMemcpyDeviceToHost), "lca error flag");
+   return PVGPU_OK;
+}
+
+extern "C" pvgpu_status pvgpu_lca_solver_profile_begin(pvgpu_lca_solver *s, int maxSteps) {
+   if (!s || maxSteps < 0) return PVGPU_ERR_BAD_ARG;
+   size_t need = (size_t)maxSteps * 3;
+   while (s->ev.size() < need) {
+      cudaEvent_t e;
+      PVGPU_CUDA(cudaEventCreate(&e), "lca profile");
+      s->ev.push_back(e);
+   }
+   s->evNext = 0;
+   s->profiling = true;
+   return PVGPU_OK;
+}
+
+extern "C" pvgpu_status pvgpu_lca_solver_profile_end(pvgpu_lca_solver *s, double *reconMs, double *postMs, int *steps) {
+   if (!s || !reconMs || !postMs || !steps) return PVGPU_ERR_BAD_ARG;
+   s->profiling = false;
+   double r = 0.0, p = 0.0;
+   int n = (int)(s->evNext / 3);
+   if (n > 0) PVGPU_CUDA(cudaEventSynchronize(s->ev[s->evNext - 1]), "lca profile");
+   for (int i = 0; i < n; i++) {
+      float a = 0.0f, b = 0.0f;
+      PVGPU_CUDA(cudaEventElapsedTime(&a, s->ev[3 * i], s->ev[3 * i + 1]), "lca profile");
+      PVGPU_CUDA(cudaEventElapsedTime(&b, s->ev[3 * i + 1], s->ev[3 * i + 2]), "lca profile");
+      r += a;
+      p += b;
+   }
+   *reconMs = r;
+   *postMs = p;
+   *steps = n;
+   s->evNext = 0;
    return PVGPU_OK;
 }

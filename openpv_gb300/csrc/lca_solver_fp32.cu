@@ -176,7 +176,7 @@ __global__ void __launch_bounds__(kThreads) post32_kernel(LcaGeom g, const float
 
 template <int S, int P, int C>
 pvgpu_status step(const LcaGeom &g, const float *x, const float *Wt32, float *partials, float *V, float *A32,
-                  cudaStream_t st) {
+                  cudaStream_t st, cudaEvent_t mid) {
    constexpr int KP = P * P * C;
    const size_t rs = sizeof(float) * (16 * 128 + 16 * KP + 128 * (KP + 1) + (size_t)g.inNx * g.inNy * C);
    auto rk = recon32_kernel<S, P, C>;
@@ -184,6 +184,7 @@ pvgpu_status step(const LcaGeom &g, const float *x, const float *Wt32, float *pa
    if (e != cudaSuccess) return pvgpu::record_cuda_error(e, "lca32 recon attr");
    rk<<<g.nb * g.MB, kThreads, rs, st>>>(g, A32, Wt32, partials);
    PVGPU_CHECK_LAUNCH("lca32 recon");
+   if (mid) cudaEventRecord(mid, st);
    const size_t win = (size_t)pvgpu::rwin_rows(S, P, g.rowsPerBlock) * rwin_cols(S, P, g.v1Nx) * C;
    if (g.NT == 128) {
       const size_t ps = sizeof(float) * (16 * 128 + 16 * 128 + win);
@@ -207,11 +208,11 @@ pvgpu_status step(const LcaGeom &g, const float *x, const float *Wt32, float *pa
 namespace pvgpu {
 
 pvgpu_status lca_fp32_step(int S, int P, int C, const LcaGeom &g, const float *x, const float *W32, const float *Wt32,
-                           float *partials, float *V, float *A32, cudaStream_t st) {
+                           float *partials, float *V, float *A32, cudaStream_t st, cudaEvent_t mid) {
    (void)W32;
-   if (S == 2 && P == 8 && C == 1) return step<2, 8, 1>(g, x, Wt32, partials, V, A32, st);
-   if (S == 2 && P == 8 && C == 3) return step<2, 8, 3>(g, x, Wt32, partials, V, A32, st);
-   if (S == 4 && P == 16 && C == 1) return step<4, 16, 1>(g, x, Wt32, partials, V, A32, st);
+   if (S == 2 && P == 8 && C == 1) return step<2, 8, 1>(g, x, Wt32, partials, V, A32, st, mid);
+   if (S == 2 && P == 8 && C == 3) return step<2, 8, 3>(g, x, Wt32, partials, V, A32, st, mid);
+   if (S == 4 && P == 16 && C == 1) return step<4, 16, 1>(g, x, Wt32, partials, V, A32, st, mid);
    return PVGPU_ERR_UNSUPPORTED_SHAPE;
 }
 
