@@ -58,7 +58,7 @@ def one_over_f_images(rng, nb, ny, nx, c):
     img = np.transpose(img, (0, 2, 3, 1))
     mu = img.mean(axis=(1, 2, 3), keepdims=True)
     sd = img.std(axis=(1, 2, 3), keepdims=True)
-    return ((img - mu) / sd).astype(np.float32)
+    return np.ascontiguousarray(((img - mu) / sd).astype(np.float32))
 
 
 def dictionary(rng, nf, p, c):

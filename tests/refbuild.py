@@ -46,6 +46,10 @@ def lib():
         _lib.pvr_gsyn_accumulate.argtypes = [C.c_int, C.c_int, vp, vp, vp]
         _lib.pvr_apply_vertices.restype = None
         _lib.pvr_apply_vertices.argtypes = [lp, C.c_int, vp, vp, vp, vp, vp]
+        _lib.pvr_deliver_pre.restype = C.c_int
+        _lib.pvr_deliver_pre.argtypes = [lp, lp, C.c_int, C.c_int, vp, vp, vp, vp, vp]
+        _lib.pvr_deliver_post.restype = C.c_int
+        _lib.pvr_deliver_post.argtypes = [lp, lp, C.c_int, C.c_int, vp, vp, vp]
         _lib.pvr_cost.restype = C.c_double
         _lib.pvr_cost.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double]
     return _lib
@@ -98,3 +102,32 @@ def apply_vertices(loc, v, vV, vA, slopes):
 
 def cost(kind, p0, p1, x):
     return lib().pvr_cost(kind, p0, p1, float(x))
+
+
+def deliver_pre(pre, post, nxp, nyp, w, a_ext=None, entries=None, num_active=None, gsyn=None):
+    """The reference's PresynapticPerspectiveConvolveDelivery::deliver, single-threaded."""
+    g = np.zeros(post.res_shape(), np.float32) if gsyn is None else gsyn
+    w = np.ascontiguousarray(w, np.float32)
+    if entries is not None:
+        e = np.ascontiguousarray(entries)
+        n = np.ascontiguousarray(num_active, np.int64)
+        rc = lib().pvr_deliver_pre(C.byref(RefLoc.of(pre)), C.byref(RefLoc.of(post)), nxp, nyp, _p(w), _p(e), _p(n),
+                                   None, _p(g))
+    else:
+        a = np.ascontiguousarray(a_ext, np.float32)
+        rc = lib().pvr_deliver_pre(C.byref(RefLoc.of(pre)), C.byref(RefLoc.of(post)), nxp, nyp, _p(w), None, None,
+                                   _p(a), _p(g))
+    if rc != 0:
+        raise ValueError("reference rejected geometry")
+    return g
+
+
+def deliver_post(src, tgt, nxp_post, nyp_post, w_post, a_ext, gsyn=None):
+    """The reference's PostsynapticPerspectiveConvolveDelivery::deliver, single-threaded."""
+    g = np.zeros(tgt.res_shape(), np.float32) if gsyn is None else gsyn
+    rc = lib().pvr_deliver_post(C.byref(RefLoc.of(src)), C.byref(RefLoc.of(tgt)), nxp_post, nyp_post,
+                                _p(np.ascontiguousarray(w_post, np.float32)), _p(np.ascontiguousarray(a_ext, np.float32)),
+                                _p(g))
+    if rc != 0:
+        raise ValueError("reference rejected geometry")
+    return g

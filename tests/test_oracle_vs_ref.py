@@ -113,3 +113,65 @@ def test_cost_functions_match_reference(oracle, kind, p0, p1):
         for x in res:
             ref += refbuild.cost(kind, p0, p1, float(x))
         assert mine[b] == ref
+
+
+# ---- the delivery loops, against the reference's own deliver() compiled from its source ----
+
+DELIVERY_CASES = [  # (pre nb,nx,ny,nf,halo), (post nx,ny,nf,halo), nxp, nyp
+    ((2, 16, 16, 8, 2), (32, 32, 1, 3), 8, 8),     # V1 -> error (LCA reconstruction)
+    ((2, 16, 16, 6, 2), (32, 32, 3, 3), 8, 8),     # colour
+    ((1, 24, 20, 5, 3), (24, 20, 4, 0), 7, 7),     # one-to-one, shrunken at the borders
+    ((2, 32, 32, 2, 6), (8, 8, 3, 0), 4, 4),       # many-to-one x4
+    ((1, 12, 8, 3, 1), (24, 16, 2, 2), 6, 4),      # one-to-many, unequal axes
+    ((1, 16, 16, 4, 2), (64, 64, 1, 6), 16, 16),   # one-to-many x4
+]
+
+
+def _activity(rng, loc, p):
+    a = ((rng.random(loc.ext_shape()) < p) * rng.uniform(1e-3, 1.0, loc.ext_shape())).astype(np.float32)
+    return a
+
+
+@pytest.mark.parametrize("case", DELIVERY_CASES)
+@pytest.mark.parametrize("sparse", [True, False])
+def test_deliver_pre_bitexact_vs_reference(oracle, case, sparse):
+    (nb, nx, ny, nf, h), (qx, qy, qf, qh), nxp, nyp = case
+    pre, post = L(oracle, nb, nx, ny, nf, h), L(oracle, nb, qx, qy, qf, qh)
+    rng = np.random.default_rng(nx + qf)
+    a = _activity(rng, pre, 0.3)
+    nk = (nx // qx if nx > qx else 1) * (ny // qy if ny > qy else 1) * nf
+    w = rng.normal(0, 0.1, (nk, nyp, nxp, qf)).astype(np.float32)
+    g0 = rng.normal(size=post.res_shape()).astype(np.float32)
+    if sparse:
+        ent, num = oracle.compact(a.reshape(nb, -1))
+        mine = oracle.deliver_pre(pre, post, nxp, nyp, w, entries=ent, num_active=num, gsyn=g0.copy())
+        ref = refbuild.deliver_pre(pre, post, nxp, nyp, w, entries=ent, num_active=num, gsyn=g0.copy())
+    else:
+        mine = oracle.deliver_pre(pre, post, nxp, nyp, w, a_ext=a, gsyn=g0.copy())
+        ref = refbuild.deliver_pre(pre, post, nxp, nyp, w, a_ext=a, gsyn=g0.copy())
+    assert np.array_equal(mine.view(np.uint32), ref.view(np.uint32))
+
+
+POST_CASES = [  # connection pre -> post, delivered from the post perspective
+    ((2, 32, 32, 1, 3), (16, 16, 8, 2), 4, 4),
+    ((2, 32, 32, 3, 3), (16, 16, 6, 2), 4, 4),
+    ((1, 24, 24, 5, 3), (24, 24, 4, 0), 7, 7),
+    ((2, 8, 8, 3, 2), (16, 16, 2, 1), 4, 4),
+    ((1, 64, 64, 1, 6), (16, 16, 4, 2), 4, 4),
+]
+
+
+@pytest.mark.parametrize("case", POST_CASES)
+def test_deliver_post_bitexact_vs_reference(oracle, case):
+    (nb, nx, ny, nf, h), (qx, qy, qf, qh), nxp, nyp = case
+    pre, post = L(oracle, nb, nx, ny, nf, h), L(oracle, nb, qx, qy, qf, qh)
+    rng = np.random.default_rng(nx * 3 + qf)
+    a = rng.normal(size=pre.ext_shape()).astype(np.float32)
+    nk = (nx // qx if nx > qx else 1) * (ny // qy if ny > qy else 1) * nf
+    w = rng.normal(0, 0.1, (nk, nyp, nxp, qf)).astype(np.float32)
+    w_post = oracle.transpose_shared(pre, post, nxp, nyp, w)
+    nxpP, nypP = oracle.post_patch_size(nxp, nx, qx), oracle.post_patch_size(nyp, ny, qy)
+    g0 = rng.normal(size=post.res_shape()).astype(np.float32)
+    mine = oracle.deliver_post(pre, post, nxpP, nypP, w_post, a, gsyn=g0.copy())
+    ref = refbuild.deliver_post(pre, post, nxpP, nypP, w_post, a, gsyn=g0.copy())
+    assert np.array_equal(mine.view(np.uint32), ref.view(np.uint32))
