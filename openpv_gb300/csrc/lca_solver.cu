@@ -32,6 +32,7 @@
 
 #include <cuda_bf16.h>
 
+#include <algorithm>
 #include <cfloat>
 #include <cstdio>
 #include <cstring>
@@ -198,22 +199,28 @@ __global__ void __launch_bounds__(128) recon_tc_kernel(const __grid_constant__ C
 }
 
 // -------------------------------------------------------------------------------------------
-// Kernel P: residual, post-perspective delivery and the LCA update
+// Kernel P: residual, post-perspective delivery and the LCA update (persistent)
+//
+// Work unit ("tile"): one image, 128 V1 positions, 64 features.  Grid = (F/64) x G CTAs, one
+// per SM; a CTA keeps its 64-feature block, loads that block's weights once, and walks the
+// (image, position block) tiles g, g+G, ...  Per tile, one thread issues every global read as
+// an async copy on one mbarrier: the V tile (TMA, 128B swizzle), the rows of the input and of
+// the reconstruction partials that the tile's receptive fields cover (bulk copies).  With two
+// buffer sets the next tile's copies fly while this tile computes.  The 8 warps then build
+// the im2col operand of r = x - sum(partials) in shared memory, one thread issues the
+// tcgen05.mma chain (M=128, N=64, K=P*P*C) into TMEM, and the epilogue (warp w: TMEM lanes
+// 32*(w%4).., features 32*(w/4)..) updates V in place in the shared tile and stages A; TMA
+// stores write both back.
 // -------------------------------------------------------------------------------------------
-template <int S, int P, int C, int NT, bool X3>
-struct PostLayout {
-   static constexpr int KP = P * P * C;
-   static constexpr int NKC = KP / 64;
-   static constexpr int IM2COL = NKC * 128 * 128;  // one K chunk = 128 rows x 128 B
-   static constexpr int WTILE = NKC * NT * 128;
-   static constexpr bool PREFETCH_V = !X3;
-   static constexpr int VTILE = PREFETCH_V ? 128 * NT * 4 : 0;
-   static constexpr int OFF_A = 0;
-   static constexpr int OFF_ALO = OFF_A + IM2COL;
-   static constexpr int OFF_W = OFF_ALO + (X3 ? IM2COL : 0);
-   static constexpr int OFF_WLO = OFF_W + WTILE;
-   static constexpr int OFF_V = OFF_WLO + (X3 ? WTILE : 0);
-   static constexpr int OFF_RWIN = OFF_V + VTILE;
+constexpr int kPostNT = 64;
+
+struct PostPlan {
+   int nbuf;                          // 1 or 2 buffer sets (next-tile prefetch when 2)
+   int G;                             // CTAs per feature block
+   uint32_t offW, offWlo, offIM, offIMlo, offAST, offASTlo;
+   uint32_t offVT[2], offST[2];
+   uint32_t stArrBytes;               // one staged array (x or one partial), rounded to 16 B
+   uint32_t total;                    // dynamic shared memory incl. alignment slack
 };
 
 __device__ __forceinline__ uint32_t pack2(float lo, float hi) {
@@ -221,186 +228,243 @@ __device__ __forceinline__ uint32_t pack2(float lo, float hi) {
    return *reinterpret_cast<uint32_t *>(&h);
 }
 
-template <int S, int P, int C, int NT, bool X3>
-__global__ void __launch_bounds__(128) post_tc_kernel(const __grid_constant__ CUtensorMap tmW,
-                                                      const __grid_constant__ CUtensorMap tmWlo,
-                                                      const __grid_constant__ CUtensorMap tmV, LcaGeom g,
-                                                      const float *__restrict__ x,
-                                                      const float *__restrict__ partials, float *__restrict__ V,
-                                                      bf16 *__restrict__ A, bf16 *__restrict__ Alo,
-                                                      int *__restrict__ err) {
-   using L = PostLayout<S, P, C, NT, X3>;
-   constexpr int KP = L::KP, NKC = L::NKC, E = (P - S) / 2;
+template <int S, int P, int C, bool X3>
+__global__ void __launch_bounds__(256, 1) post_tc_kernel(const __grid_constant__ CUtensorMap tmW,
+                                                         const __grid_constant__ CUtensorMap tmWlo,
+                                                         const __grid_constant__ CUtensorMap tmV,
+                                                         const __grid_constant__ CUtensorMap tmA,
+                                                         const __grid_constant__ CUtensorMap tmAlo, LcaGeom g,
+                                                         PostPlan pl, const float *__restrict__ x,
+                                                         const float *__restrict__ partials, int *__restrict__ err) {
+   constexpr int KP = P * P * C, NKC = KP / 64, E = (P - S) / 2;
    extern __shared__ uint8_t smem_raw[];
    uint8_t *smem = align1024(smem_raw);
-   float *rwin = reinterpret_cast<float *>(smem + L::OFF_RWIN);
-   __shared__ __align__(8) uint64_t wfull, vfull, done;
+   __shared__ __align__(8) uint64_t wbar, vbar[2], done;
    __shared__ uint32_t tmemBase;
-   __shared__ int failed;
 
-   const int tid = threadIdx.x, warp = tid >> 5;
-   const int nTilesN = g.F / NT;
-   const int b = blockIdx.x / (g.MB * nTilesN);
-   const int rem = blockIdx.x % (g.MB * nTilesN);
-   const int mb = rem / nTilesN, nt = rem % nTilesN;
-   const int f0 = nt * NT;
-   const int rowV = b * g.Npos + mb * 128;
+   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+   const int nTilesN = g.F / kPostNT;
+   const int nt = blockIdx.x % nTilesN, grp = blockIdx.x / nTilesN;
+   const int f0 = nt * kPostNT;
+   const int nTiles = g.nb * g.MB;
+   const int RWR = rwin_rows(S, P, g.rowsPerBlock);
+   const int rowElems = g.inNx * C;
+   const int nPix = g.inNy * rowElems;
 
    if (tid == 0) {
-      mbar_init(&wfull, 1);
-      mbar_init(&vfull, 1);
+      mbar_init(&wbar, 1);
+      mbar_init(&vbar[0], 1);
+      mbar_init(&vbar[1], 1);
       mbar_init(&done, 1);
       fence_mbar_init();
-      failed = 0;
-      // operands first: the weight tiles (L2-resident) and the V tile (HBM)
-      mbar_arrive_expect_tx(&wfull, (X3 ? 2 : 1) * L::WTILE);
-      for (int kc = 0; kc < NKC; kc++) {
-         tma_load_2d(smem + L::OFF_W + kc * NT * 128, &tmW, &wfull, kc * 64, f0);
-         if (X3) tma_load_2d(smem + L::OFF_WLO + kc * NT * 128, &tmWlo, &wfull, kc * 64, f0);
-      }
-      if (L::PREFETCH_V) {
-         mbar_arrive_expect_tx(&vfull, L::VTILE);
-         for (int c = 0; c < NT / 32; c++) tma_load_2d(smem + L::OFF_V + c * 128 * 128, &tmV, &vfull, f0 + c * 32, rowV);
-      }
    }
-   if (warp == 0) tmem_alloc(&tmemBase, NT);
-
-   const int RWC = rwin_cols(S, P, g.v1Nx);
-   pvgpu::build_residual_window<S, P, C, 128>(g, b, mb, x, partials, rwin);
+   if (warp == 0) tmem_alloc(&tmemBase, kPostNT);
    tc_fence_before();
    __syncthreads();
    tc_fence_after();
    const uint32_t tmem = tmemBase;
 
-   // im2col: thread = position; row tid of each K chunk, 8 BF16 (16 B) per store
-   {
-      const int yl = tid / g.v1Nx, x1 = tid % g.v1Nx;
-      const float *wbase = rwin + ((S * yl) * RWC + S * x1) * C;
-#pragma unroll 1
+   auto tile_rows = [&](int mb, int &ylo, int &yhi) {
+      const int top = S * mb * g.rowsPerBlock - E;
+      ylo = top < 0 ? 0 : top;
+      yhi = top + RWR > g.inNy ? g.inNy : top + RWR;
+   };
+   // thread 0 only: copies of tile j into buffer set s
+   auto issue_tile = [&](int j, int s) {
+      const int b = j / g.MB, mb = j % g.MB;
+      const int rowV = b * g.Npos + mb * 128;
+      int ylo, yhi;
+      tile_rows(mb, ylo, yhi);
+      const uint32_t nbytes = (uint32_t)((yhi - ylo) * rowElems * 4);
+      mbar_arrive_expect_tx(&vbar[s], 2 * 16384 + (uint32_t)(g.MB + 1) * nbytes);
+      uint8_t *vt = smem + pl.offVT[s];
+      tma_load_2d(vt, &tmV, &vbar[s], f0, rowV);
+      tma_load_2d(vt + 16384, &tmV, &vbar[s], f0 + 32, rowV);
+      uint8_t *st = smem + pl.offST[s];
+      bulk_load(st, x + (size_t)b * nPix + (size_t)ylo * rowElems, nbytes, &vbar[s]);
+      for (int m = 0; m < g.MB; m++)
+         bulk_load(st + (size_t)(1 + m) * pl.stArrBytes,
+                   partials + ((size_t)b * g.MB + m) * nPix + (size_t)ylo * rowElems, nbytes, &vbar[s]);
+   };
+   auto buf_of = [&](int i) { return pl.nbuf == 2 ? (i & 1) : 0; };
+   auto par_of = [&](int i) { return (uint32_t)(pl.nbuf == 2 ? ((i >> 1) & 1) : (i & 1)); };
+
+   int issued = 0;  // tiles whose copies thread 0 has issued (local indices 0..issued-1)
+   if (tid == 0) {
+      mbar_arrive_expect_tx(&wbar, (X3 ? 2 : 1) * NKC * kPostNT * 128);
       for (int kc = 0; kc < NKC; kc++) {
-#pragma unroll
-         for (int c8 = 0; c8 < 8; c8++) {
+         tma_load_2d(smem + pl.offW + kc * kPostNT * 128, &tmW, &wbar, kc * 64, f0);
+         if (X3) tma_load_2d(smem + pl.offWlo + kc * kPostNT * 128, &tmWlo, &wbar, kc * 64, f0);
+      }
+      if (grp < nTiles) {
+         issue_tile(grp, 0);
+         issued = 1;
+      }
+   }
+
+   bool ok = true;
+   int waited = 0;
+   int i = 0;
+   for (int j = grp; j < nTiles; j += pl.G, i++) {
+      const int s = buf_of(i);
+      if (tid == 0) {
+         if (i > 0) bulk_wait_read_all();  // the previous tile's stores have read their shared tiles
+         if (pl.nbuf == 2 && j + pl.G < nTiles) {
+            issue_tile(j + pl.G, s ^ 1);
+            issued++;
+         }
+      }
+      bool lok = mbar_wait(&vbar[s], par_of(i));
+      if (i == 0) lok = lok && mbar_wait(&wbar, 0);
+      ok = __syncthreads_and(lok);
+      if (!ok) break;
+      waited = i + 1;
+
+      // ---- im2col of r = x - sum(partials), BF16 (and the low part in BF16x3) ----
+      const int b = j / g.MB, mb = j % g.MB;
+      int ylo, yhi;
+      tile_rows(mb, ylo, yhi);
+      {
+         const int p = tid & 127, half = tid >> 7;
+         const int yl = p / g.v1Nx, x1 = p % g.v1Nx;
+         const int ybase = S * (mb * g.rowsPerBlock + yl) - E, xbase = S * x1 - E;
+         const float *st = reinterpret_cast<const float *>(smem + pl.offST[s]);
+         const int stride = pl.stArrBytes / 4;
+         constexpr int NC8 = KP / 8;
+#pragma unroll 2
+         for (int c8 = half * (NC8 / 2); c8 < (half + 1) * (NC8 / 2); c8++) {
             float vals[8];
 #pragma unroll
-            for (int j = 0; j < 8; j++) {
-               const int k = kc * 64 + c8 * 8 + j;
+            for (int jj = 0; jj < 8; jj++) {
+               const int k = c8 * 8 + jj;
                const int ky = k / (P * C), kr = k % (P * C);
-               vals[j] = wbase[(ky * RWC) * C + kr];
+               const int kx = kr / C, ch = kr % C;
+               const int ye = ybase + ky, xe = xbase + kx;
+               float v = 0.0f;
+               if (ye >= 0 && ye < g.inNy && xe >= 0 && xe < g.inNx) {
+                  const int idx = ((ye - ylo) * g.inNx + xe) * C + ch;
+                  float rec = st[stride + idx];
+                  for (int m = 1; m < g.MB; m++) rec = __fadd_rn(rec, st[(1 + m) * stride + idx]);
+                  v = __fadd_rn(st[idx], -rec);
+               }
+               vals[jj] = v;
             }
             uint4 hi;
             hi.x = pack2(vals[0], vals[1]);
             hi.y = pack2(vals[2], vals[3]);
             hi.z = pack2(vals[4], vals[5]);
             hi.w = pack2(vals[6], vals[7]);
-            const uint32_t off = kc * 16384 + sw128_offset(tid, c8 * 8);
-            *reinterpret_cast<uint4 *>(smem + L::OFF_A + off) = hi;
+            const uint32_t off = (c8 >> 3) * 16384 + sw128_offset(p, (c8 & 7) * 8);
+            *reinterpret_cast<uint4 *>(smem + pl.offIM + off) = hi;
             if (X3) {
-               uint4 lo;
                const __nv_bfloat162 *h2 = reinterpret_cast<const __nv_bfloat162 *>(&hi);
                float2 f01 = __bfloat1622float2(h2[0]), f23 = __bfloat1622float2(h2[1]);
                float2 f45 = __bfloat1622float2(h2[2]), f67 = __bfloat1622float2(h2[3]);
+               uint4 lo;
                lo.x = pack2(vals[0] - f01.x, vals[1] - f01.y);
                lo.y = pack2(vals[2] - f23.x, vals[3] - f23.y);
                lo.z = pack2(vals[4] - f45.x, vals[5] - f45.y);
                lo.w = pack2(vals[6] - f67.x, vals[7] - f67.y);
-               *reinterpret_cast<uint4 *>(smem + L::OFF_ALO + off) = lo;
+               *reinterpret_cast<uint4 *>(smem + pl.offIMlo + off) = lo;
             }
          }
       }
-   }
-   fence_proxy_async_smem();
-   __syncthreads();
+      fence_proxy_async_smem();
+      __syncthreads();
 
-   if (tid == 0) {
-      bool ok = mbar_wait(&wfull, 0);
-      if (ok) {
+      // ---- D[pos][f] on the tensor cores ----
+      if (tid == 0) {
          tc_fence_after();
-         const uint32_t idesc = idesc_bf16(128, NT);
+         const uint32_t idesc = idesc_bf16(128, kPostNT);
          const int npass = X3 ? 3 : 1;
          for (int pass = 0; pass < npass; pass++) {
-            const uint32_t a0 = smem_u32(smem + ((X3 && pass == 2) ? L::OFF_ALO : L::OFF_A));
-            const uint32_t w0 = smem_u32(smem + ((X3 && pass == 1) ? L::OFF_WLO : L::OFF_W));
+            const uint32_t a0 = smem_u32(smem + ((X3 && pass == 2) ? pl.offIMlo : pl.offIM));
+            const uint32_t w0 = smem_u32(smem + ((X3 && pass == 1) ? pl.offWlo : pl.offW));
             for (int kc = 0; kc < NKC; kc++)
 #pragma unroll
                for (int k = 0; k < 4; k++)
-                  mma_bf16(tmem, sdesc_sw128(a0 + kc * 16384 + k * 32), sdesc_sw128(w0 + kc * NT * 128 + k * 32),
+                  mma_bf16(tmem, sdesc_sw128(a0 + kc * 16384 + k * 32), sdesc_sw128(w0 + kc * kPostNT * 128 + k * 32),
                            idesc, (pass | kc | k) != 0);
          }
-      } else {
-         failed = 1;
+         mma_commit(&done);
       }
-      mma_commit(&done);
-      if (L::PREFETCH_V && !ok) mbar_wait(&vfull, 0);
-   }
-   __syncthreads();
-   bool ok = failed == 0 && mbar_wait(&done, 0);
-   if (L::PREFETCH_V) ok = ok && mbar_wait(&vfull, 0);
-   ok = __syncthreads_and(ok);
-   tc_fence_after();
-   if (ok) {
-      const uint32_t lanes = tmem + ((uint32_t)(warp * 32) << 16);
-      const size_t row = (size_t)(rowV + tid) * g.F + f0;
-      float *vrow = V + row;
-#pragma unroll 1
-      for (int c = 0; c < NT / 32; c++) {
+      ok = __syncthreads_and(mbar_wait(&done, (uint32_t)(i & 1)));
+      if (!ok) break;
+      tc_fence_after();
+
+      // ---- epilogue: V update in place in the shared V tile, A staged for the store ----
+      {
+         const int q = warp & 3, h = warp >> 2;
+         const int p = 32 * q + lane;
          float d[32], vo[32];
-         tmem_ld32(lanes + c * 32, d);
-         if (L::PREFETCH_V) {
-            const uint8_t *vt = smem + L::OFF_V + c * 16384 + tid * 128;
+         tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + 32 * h, d);
+         uint8_t *vt = smem + pl.offVT[s] + h * 16384 + p * 128;
 #pragma unroll
-            for (int q = 0; q < 8; q++) {
-               float4 t = *reinterpret_cast<const float4 *>(vt + ((q ^ (tid & 7)) << 4));
-               vo[4 * q] = t.x;
-               vo[4 * q + 1] = t.y;
-               vo[4 * q + 2] = t.z;
-               vo[4 * q + 3] = t.w;
-            }
-         } else {
-#pragma unroll
-            for (int q = 0; q < 8; q++) {
-               float4 t = *reinterpret_cast<const float4 *>(vrow + c * 32 + 4 * q);
-               vo[4 * q] = t.x;
-               vo[4 * q + 1] = t.y;
-               vo[4 * q + 2] = t.z;
-               vo[4 * q + 3] = t.w;
-            }
+         for (int qq = 0; qq < 8; qq++) {
+            const float4 t = *reinterpret_cast<const float4 *>(vt + ((qq ^ (p & 7)) << 4));
+            vo[4 * qq] = t.x;
+            vo[4 * qq + 1] = t.y;
+            vo[4 * qq + 2] = t.z;
+            vo[4 * qq + 3] = t.w;
          }
          float vn[32];
          uint32_t ah[16], al[16];
 #pragma unroll
-         for (int j = 0; j < 32; j++) {
-            const float aold = thresh(vo[j], g);
-            vn[j] = fmaf(g.e, vo[j], (1.0f - g.e) * (d[j] + g.si * aold));
-         }
+         for (int jj = 0; jj < 32; jj++) vn[jj] = fmaf(g.e, vo[jj], (1.0f - g.e) * (d[jj] + g.si * thresh(vo[jj], g)));
 #pragma unroll
-         for (int j = 0; j < 32; j += 2) {
-            const float a0 = thresh(vn[j], g), a1 = thresh(vn[j + 1], g);
-            __nv_bfloat162 h = __floats2bfloat162_rn(a0, a1);
-            ah[j / 2] = *reinterpret_cast<uint32_t *>(&h);
+         for (int jj = 0; jj < 32; jj += 2) {
+            const float a0 = thresh(vn[jj], g), a1 = thresh(vn[jj + 1], g);
+            __nv_bfloat162 hb = __floats2bfloat162_rn(a0, a1);
+            ah[jj / 2] = *reinterpret_cast<uint32_t *>(&hb);
             if (X3) {
-               float2 hf = __bfloat1622float2(h);
-               al[j / 2] = pack2(a0 - hf.x, a1 - hf.y);
+               const float2 hf = __bfloat1622float2(hb);
+               al[jj / 2] = pack2(a0 - hf.x, a1 - hf.y);
             }
          }
 #pragma unroll
-         for (int q = 0; q < 8; q++)
-            *reinterpret_cast<float4 *>(vrow + c * 32 + 4 * q) =
-                  make_float4(vn[4 * q], vn[4 * q + 1], vn[4 * q + 2], vn[4 * q + 3]);
-         uint4 *ap = reinterpret_cast<uint4 *>(A + row + c * 32);
+         for (int qq = 0; qq < 8; qq++)
+            *reinterpret_cast<float4 *>(vt + ((qq ^ (p & 7)) << 4)) =
+                  make_float4(vn[4 * qq], vn[4 * qq + 1], vn[4 * qq + 2], vn[4 * qq + 3]);
 #pragma unroll
-         for (int q = 0; q < 4; q++) ap[q] = make_uint4(ah[4 * q], ah[4 * q + 1], ah[4 * q + 2], ah[4 * q + 3]);
-         if (X3) {
-            uint4 *lp = reinterpret_cast<uint4 *>(Alo + row + c * 32);
-#pragma unroll
-            for (int q = 0; q < 4; q++) lp[q] = make_uint4(al[4 * q], al[4 * q + 1], al[4 * q + 2], al[4 * q + 3]);
+         for (int t = 0; t < 4; t++) {
+            const uint32_t off = p * 128 + ((((4 * h + t) ^ (p & 7))) << 4);
+            *reinterpret_cast<uint4 *>(smem + pl.offAST + off) =
+                  make_uint4(ah[4 * t], ah[4 * t + 1], ah[4 * t + 2], ah[4 * t + 3]);
+            if (X3)
+               *reinterpret_cast<uint4 *>(smem + pl.offASTlo + off) =
+                     make_uint4(al[4 * t], al[4 * t + 1], al[4 * t + 2], al[4 * t + 3]);
          }
       }
-   } else if (tid == 0) {
-      atomicExch(err, 1);
+      fence_proxy_async_smem();
+      tc_fence_before();
+      __syncthreads();
+      if (tid == 0) {
+         const int rowV = b * g.Npos + mb * 128;
+         uint8_t *vt = smem + pl.offVT[s];
+         tma_store_2d(&tmV, vt, f0, rowV);
+         tma_store_2d(&tmV, vt + 16384, f0 + 32, rowV);
+         tma_store_2d(&tmA, smem + pl.offAST, f0, rowV);
+         if (X3) tma_store_2d(&tmAlo, smem + pl.offASTlo, f0, rowV);
+         bulk_commit();
+         if (pl.nbuf == 1 && j + pl.G < nTiles) {
+            bulk_wait_read_all();
+            issue_tile(j + pl.G, 0);
+            issued++;
+         }
+      }
+   }
+   if (tid == 0) {
+      if (i == 0) mbar_wait(&wbar, 0);  // no tile ran: the weight copies still have to land
+      bulk_wait_all();
+      if (!ok) {
+         // let copies still in flight land before shared memory goes away
+         for (int t = waited; t < issued; t++) mbar_wait(&vbar[buf_of(t)], par_of(t));
+         atomicExch(err, 1);
+      }
    }
    tc_fence_before();
    __syncthreads();
-   if (warp == 0) tmem_dealloc(tmem, NT);
+   if (warp == 0) tmem_dealloc(tmem, kPostNT);
 }
 
 // -------------------------------------------------------------------------------------------
@@ -501,6 +565,7 @@ struct pvgpu_lca_solver {
    bf16 *A = nullptr, *Alo = nullptr, *W = nullptr, *Wlo = nullptr, *Wt = nullptr, *Wtlo = nullptr;
    int *err = nullptr;
    CUtensorMap tmA, tmAlo, tmWt, tmWtlo, tmW, tmWlo, tmV;
+   PostPlan plan, planX3;
    bool weightsSet = false;
    // optional per-kernel timing: events before kernel R, between R and P, after P
    std::vector<cudaEvent_t> ev;
@@ -510,19 +575,69 @@ struct pvgpu_lca_solver {
 
 namespace {
 
+int g_num_sms = 0;
+
+PostPlan make_post_plan(const LcaGeom &g, int S, int P, int C, bool x3, int numSms) {
+   const int KP = P * P * C, NKC = KP / 64;
+   auto al = [](uint32_t v) { return (v + 1023u) & ~1023u; };
+   PostPlan pl;
+   std::memset(&pl, 0, sizeof(pl));
+   const uint32_t RWR = (uint32_t)rwin_rows(S, P, g.rowsPerBlock);
+   pl.stArrBytes = ((RWR * g.inNx * C * 4) + 15u) & ~15u;
+   const uint32_t wB = NKC * kPostNT * 128, imB = NKC * 16384, astB = 16384, vtB = 2 * 16384;
+   const uint32_t stB = (uint32_t)(g.MB + 1) * pl.stArrBytes;
+   // Two buffer sets (next-tile prefetch) when they fit; otherwise one, with the A staging
+   // tiles placed inside the staged-rows region, which is dead by the epilogue (the rows are
+   // consumed by the im2col build, and the next tile's copies are issued only after the
+   // stores have read the staging tiles).
+   for (int nbuf = 2; nbuf >= 1; nbuf--) {
+      uint32_t o = 0;
+      pl.offW = o;
+      o = al(o + wB);
+      pl.offWlo = o;
+      if (x3) o = al(o + wB);
+      pl.offIM = o;
+      o = al(o + imB);
+      pl.offIMlo = o;
+      if (x3) o = al(o + imB);
+      if (nbuf == 2) {
+         pl.offAST = o;
+         o = al(o + astB);
+         pl.offASTlo = o;
+         if (x3) o = al(o + astB);
+      }
+      for (int b = 0; b < 2; b++) {
+         pl.offVT[b] = o;
+         if (b < nbuf) o = al(o + vtB);
+      }
+      const uint32_t stRegion = nbuf == 2 ? stB : std::max(stB, (x3 ? 2u : 1u) * astB);
+      for (int b = 0; b < 2; b++) {
+         pl.offST[b] = o;
+         if (b < nbuf) o = al(o + stRegion);
+      }
+      if (nbuf == 1) {
+         pl.offAST = pl.offST[0];
+         pl.offASTlo = pl.offST[0] + astB;
+      }
+      pl.total = o + 1024;
+      pl.nbuf = nbuf;
+      if (pl.total <= 227u * 1024u) break;
+   }
+   const int nTilesN = g.F / kPostNT;
+   int G = numSms / nTilesN;
+   if (G < 1) G = 1;
+   if (G > g.nb * g.MB) G = g.nb * g.MB;
+   pl.G = G;
+   return pl;
+}
+
 template <int S, int P, int C>
 struct Launcher {
    static size_t recon_smem(const pvgpu_lca_solver *s) {
       constexpr int KP = P * P * C;
       return 1024 + 2 * (size_t)(128 * 64 * 2 + KP * 64 * 2) + (size_t)s->g.inNx * s->g.inNy * C * 4;
    }
-   template <int NT, bool X3>
-   static size_t post_smem(const pvgpu_lca_solver *s) {
-      using L = PostLayout<S, P, C, NT, X3>;
-      return 1024 + L::OFF_RWIN +
-             (size_t)rwin_rows(S, P, s->g.rowsPerBlock) * rwin_cols(S, P, s->g.v1Nx) * C * 4;
-   }
-   template <int NT, bool X3>
+   template <bool X3>
    static pvgpu_status step(pvgpu_lca_solver *s, const float *x, cudaStream_t st, cudaEvent_t mid) {
       size_t rs = recon_smem(s);
       auto rk = recon_tc_kernel<S, P, C, X3>;
@@ -531,24 +646,22 @@ struct Launcher {
       rk<<<s->g.nb * s->g.MB, 128, rs, st>>>(s->tmA, s->tmAlo, s->tmWt, s->tmWtlo, s->g, s->partials, s->err);
       PVGPU_CHECK_LAUNCH("lca recon");
       if (mid) cudaEventRecord(mid, st);
-      size_t ps = post_smem<NT, X3>(s);
-      auto pk = post_tc_kernel<S, P, C, NT, X3>;
-      e = cudaFuncSetAttribute(pk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ps);
+      const PostPlan &pl = X3 ? s->planX3 : s->plan;
+      auto pk = post_tc_kernel<S, P, C, X3>;
+      e = cudaFuncSetAttribute(pk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.total);
       if (e != cudaSuccess) return pvgpu::record_cuda_error(e, "lca post attr");
-      pk<<<s->g.nb * s->g.MB * (s->g.F / NT), 128, ps, st>>>(s->tmW, s->tmWlo, s->tmV, s->g, x, s->partials, s->V,
-                                                              s->A, s->Alo, s->err);
+      pk<<<(s->g.F / kPostNT) * pl.G, 256, pl.total, st>>>(s->tmW, s->tmWlo, s->tmV, s->tmA, s->tmAlo, s->g, pl, x,
+                                                          s->partials, s->err);
       PVGPU_CHECK_LAUNCH("lca post");
       return PVGPU_OK;
    }
    static bool fits(const pvgpu_lca_solver *s, bool x3) {
       size_t lim = 227 * 1024;
       if (recon_smem(s) > lim) return false;
-      if (s->g.NT == 128) return (x3 ? post_smem<128, true>(s) : post_smem<128, false>(s)) <= lim;
-      return (x3 ? post_smem<64, true>(s) : post_smem<64, false>(s)) <= lim;
+      return (x3 ? s->planX3.total : s->plan.total) <= lim;
    }
    static pvgpu_status run_step(pvgpu_lca_solver *s, const float *x, bool x3, cudaStream_t st, cudaEvent_t mid) {
-      if (s->g.NT == 128) return x3 ? step<128, true>(s, x, st, mid) : step<128, false>(s, x, st, mid);
-      return x3 ? step<64, true>(s, x, st, mid) : step<64, false>(s, x, st, mid);
+      return x3 ? step<true>(s, x, st, mid) : step<false>(s, x, st, mid);
    }
 };
 
@@ -582,6 +695,7 @@ extern "C" pvgpu_status pvgpu_lca_solver_create(const pvgpu_lca_solver_desc *d, 
    const int P = d->nxp, C = d->inNf, KP = P * P * C;
    const int Npos = d->v1Nx * d->v1Ny;
    if (Npos % 128 || 128 % d->v1Nx || KP % 64 || KP > 256 || d->v1Nf % 64) return PVGPU_ERR_UNSUPPORTED_SHAPE;
+   if ((d->inNx * d->inNf) % 4) return PVGPU_ERR_UNSUPPORTED_SHAPE;  // input rows are bulk-copied (16-byte multiples)
    if (dispatch(S, P, C, [](auto) { return PVGPU_OK; }) != PVGPU_OK) return PVGPU_ERR_UNSUPPORTED_SHAPE;
    pvgpu_lca_solver *s = new (std::nothrow) pvgpu_lca_solver();
    if (!s) return PVGPU_ERR_OOM;
@@ -601,7 +715,7 @@ extern "C" pvgpu_status pvgpu_lca_solver_create(const pvgpu_lca_solver_desc *d, 
    g.Npos = Npos;
    g.MB = Npos / 128;
    g.rowsPerBlock = 128 / d->v1Nx;
-   g.NT = d->v1Nf % 128 == 0 ? 128 : 64;
+   g.NT = kPostNT;
    float vt = d->VThresh, vw = d->VWidth;
    if (vw < 0) {
       vt += vw;
@@ -650,6 +764,14 @@ extern "C" pvgpu_status pvgpu_lca_solver_create(const pvgpu_lca_solver_desc *d, 
       free_solver(s);
       return PVGPU_ERR_LAUNCH;
    }
+   if (!g_num_sms) {
+      int dev = 0, n = 0;
+      cudaGetDevice(&dev);
+      if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 148;
+      g_num_sms = n;
+   }
+   s->plan = make_post_plan(g, S, P, C, false, g_num_sms);
+   s->planX3 = make_post_plan(g, S, P, C, true, g_num_sms);
    bool fits = true;
    dispatch(S, P, C, [&](auto L) {
       fits = L.fits(s, false);

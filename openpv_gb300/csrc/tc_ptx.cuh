@@ -155,3 +155,33 @@ __host__ __device__ __forceinline__ uint32_t sw128_offset(int row, int k) {
 
 }  // namespace tc
 }  // namespace pvgpu
+
+namespace pvgpu {
+namespace tc {
+
+// ---- bulk copies and TMA stores ------------------------------------------------------------
+// Contiguous global -> shared copy (16-byte aligned addresses, size a multiple of 16) that
+// completes on an mbarrier.
+__device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+   asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(src)), "r"(bytes), "r"(smem_u32(bar))
+                : "memory");
+}
+
+// Tiled shared -> global store through a tensor map (bulk-group completion).
+__device__ __forceinline__ void tma_store_2d(const CUtensorMap *map, const void *src, int c0, int c1) {
+   asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%2, %3}], [%1];"
+                ::"l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(src)), "r"(c0), "r"(c1)
+                : "memory");
+}
+
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+
+// Wait until the bulk stores committed by this thread have finished reading shared memory.
+__device__ __forceinline__ void bulk_wait_read_all() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+
+// Wait until the bulk stores committed by this thread have completed.
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+
+}  // namespace tc
+}  // namespace pvgpu
