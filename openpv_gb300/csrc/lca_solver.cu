@@ -219,6 +219,7 @@ struct PostPlan {
    int G;                             // CTAs per feature block
    uint32_t offW, offWlo, offIM, offIMlo, offAST, offASTlo;
    uint32_t offVT[2], offST[2];
+   uint32_t offRW;                    // residual window of the current tile (FP32)
    uint32_t stArrBytes;               // one staged array (x or one partial), rounded to 16 B
    uint32_t total;                    // dynamic shared memory incl. alignment slack
 };
@@ -314,58 +315,76 @@ __global__ void __launch_bounds__(256, 1) post_tc_kernel(const __grid_constant__
             issued++;
          }
       }
-      bool lok = mbar_wait(&vbar[s], par_of(i));
-      if (i == 0) lok = lok && mbar_wait(&wbar, 0);
+      // one thread polls; the barrier hands its observation (and the copied data) to the CTA
+      bool lok = true;
+      if (tid == 0) {
+         lok = mbar_wait(&vbar[s], par_of(i));
+         if (i == 0) lok = lok && mbar_wait(&wbar, 0);
+      }
       ok = __syncthreads_and(lok);
       if (!ok) break;
       waited = i + 1;
 
-      // ---- im2col of r = x - sum(partials), BF16 (and the low part in BF16x3) ----
+      // ---- residual window r = x - sum(partials), once per tile (FP32, zero outside the layer) ----
       const int b = j / g.MB, mb = j % g.MB;
       int ylo, yhi;
       tile_rows(mb, ylo, yhi);
+      const int top = S * mb * g.rowsPerBlock - E;
+      const int RWC = rwin_cols(S, P, g.v1Nx);
+      float *rwin = reinterpret_cast<float *>(smem + pl.offRW);
       {
-         const int p = tid & 127, half = tid >> 7;
-         const int yl = p / g.v1Nx, x1 = p % g.v1Nx;
-         const int ybase = S * (mb * g.rowsPerBlock + yl) - E, xbase = S * x1 - E;
          const float *st = reinterpret_cast<const float *>(smem + pl.offST[s]);
          const int stride = pl.stArrBytes / 4;
-         constexpr int NC8 = KP / 8;
-#pragma unroll 2
-         for (int c8 = half * (NC8 / 2); c8 < (half + 1) * (NC8 / 2); c8++) {
-            float vals[8];
-#pragma unroll
-            for (int jj = 0; jj < 8; jj++) {
-               const int k = c8 * 8 + jj;
-               const int ky = k / (P * C), kr = k % (P * C);
-               const int kx = kr / C, ch = kr % C;
-               const int ye = ybase + ky, xe = xbase + kx;
-               float v = 0.0f;
-               if (ye >= 0 && ye < g.inNy && xe >= 0 && xe < g.inNx) {
-                  const int idx = ((ye - ylo) * g.inNx + xe) * C + ch;
-                  float rec = st[stride + idx];
-                  for (int m = 1; m < g.MB; m++) rec = __fadd_rn(rec, st[(1 + m) * stride + idx]);
-                  v = __fadd_rn(st[idx], -rec);
-               }
-               vals[jj] = v;
+         const int n = RWR * RWC * C;
+         for (int e = tid; e < n; e += 256) {
+            const int c = e % C, xr = (e / C) % RWC, yr = e / (C * RWC);
+            const int ye = top + yr, xe = xr - E;
+            float v = 0.0f;
+            if (ye >= 0 && ye < g.inNy && xe >= 0 && xe < g.inNx) {
+               const int idx = ((ye - ylo) * g.inNx + xe) * C + c;
+               float rec = st[stride + idx];
+               for (int m = 1; m < g.MB; m++) rec = __fadd_rn(rec, st[(1 + m) * stride + idx]);
+               v = __fadd_rn(st[idx], -rec);
             }
-            uint4 hi;
-            hi.x = pack2(vals[0], vals[1]);
-            hi.y = pack2(vals[2], vals[3]);
-            hi.z = pack2(vals[4], vals[5]);
-            hi.w = pack2(vals[6], vals[7]);
-            const uint32_t off = (c8 >> 3) * 16384 + sw128_offset(p, (c8 & 7) * 8);
-            *reinterpret_cast<uint4 *>(smem + pl.offIM + off) = hi;
-            if (X3) {
-               const __nv_bfloat162 *h2 = reinterpret_cast<const __nv_bfloat162 *>(&hi);
-               float2 f01 = __bfloat1622float2(h2[0]), f23 = __bfloat1622float2(h2[1]);
-               float2 f45 = __bfloat1622float2(h2[2]), f67 = __bfloat1622float2(h2[3]);
-               uint4 lo;
-               lo.x = pack2(vals[0] - f01.x, vals[1] - f01.y);
-               lo.y = pack2(vals[2] - f23.x, vals[3] - f23.y);
-               lo.z = pack2(vals[4] - f45.x, vals[5] - f45.y);
-               lo.w = pack2(vals[6] - f67.x, vals[7] - f67.y);
-               *reinterpret_cast<uint4 *>(smem + pl.offIMlo + off) = lo;
+            rwin[e] = v;
+         }
+      }
+      __syncthreads();
+      // ---- im2col: row ky of a position's receptive field is P*C contiguous window floats ----
+      {
+         constexpr int RUN = P * C;          // floats per patch row, a multiple of 8
+         constexpr int CPR = RUN / 8;        // 16-byte chunks per patch row
+         static_assert(RUN % 8 == 0, "patch rows must fill whole 16-byte chunks");
+         const int p = tid & 127, half = tid >> 7;
+         const int yl = p / g.v1Nx, x1 = p % g.v1Nx;
+         const float *src0 = rwin + ((S * yl) * RWC + S * x1) * C;
+#pragma unroll 1
+         for (int ky = half * (P / 2); ky < (half + 1) * (P / 2); ky++) {
+            const float *src = src0 + ky * RWC * C;
+#pragma unroll
+            for (int cc = 0; cc < CPR; cc++) {
+               float vals[8];
+#pragma unroll
+               for (int jj = 0; jj < 8; jj++) vals[jj] = src[cc * 8 + jj];
+               uint4 hi;
+               hi.x = pack2(vals[0], vals[1]);
+               hi.y = pack2(vals[2], vals[3]);
+               hi.z = pack2(vals[4], vals[5]);
+               hi.w = pack2(vals[6], vals[7]);
+               const int c8 = ky * CPR + cc;
+               const uint32_t off = (c8 >> 3) * 16384 + sw128_offset(p, (c8 & 7) * 8);
+               *reinterpret_cast<uint4 *>(smem + pl.offIM + off) = hi;
+               if (X3) {
+                  const __nv_bfloat162 *h2 = reinterpret_cast<const __nv_bfloat162 *>(&hi);
+                  float2 f01 = __bfloat1622float2(h2[0]), f23 = __bfloat1622float2(h2[1]);
+                  float2 f45 = __bfloat1622float2(h2[2]), f67 = __bfloat1622float2(h2[3]);
+                  uint4 lo;
+                  lo.x = pack2(vals[0] - f01.x, vals[1] - f01.y);
+                  lo.y = pack2(vals[2] - f23.x, vals[3] - f23.y);
+                  lo.z = pack2(vals[4] - f45.x, vals[5] - f45.y);
+                  lo.w = pack2(vals[6] - f67.x, vals[7] - f67.y);
+                  *reinterpret_cast<uint4 *>(smem + pl.offIMlo + off) = lo;
+               }
             }
          }
       }
@@ -388,7 +407,7 @@ __global__ void __launch_bounds__(256, 1) post_tc_kernel(const __grid_constant__
          }
          mma_commit(&done);
       }
-      ok = __syncthreads_and(mbar_wait(&done, (uint32_t)(i & 1)));
+      ok = __syncthreads_and(tid != 0 || mbar_wait(&done, (uint32_t)(i & 1)));
       if (!ok) break;
       tc_fence_after();
 
@@ -619,6 +638,8 @@ PostPlan make_post_plan(const LcaGeom &g, int S, int P, int C, bool x3, int numS
          pl.offAST = pl.offST[0];
          pl.offASTlo = pl.offST[0] + astB;
       }
+      pl.offRW = o;
+      o = al(o + (uint32_t)(RWR * rwin_cols(S, P, g.v1Nx) * C * 4));
       pl.total = o + 1024;
       pl.nbuf = nbuf;
       if (pl.total <= 227u * 1024u) break;
