@@ -93,6 +93,25 @@ pvgpu_status pvgpu_compact_active(
       size_t scratchBytes,
       void *stream);
 
+/* The same compaction with no device allocation and no caller scratch.  No counterpart in the
+ * reference: it exists for callers that cannot allocate device memory at the call site -- code
+ * in a host function enqueued on a stream, loops that must not incur cudaMalloc's implicit
+ * synchronisation, hosts whose device memory belongs to their own pool allocator.  The chunk
+ * counts live in a fixed 1 MiB array inside the library's device image (loaded once per device,
+ * kept until the process exits), which limits a call to nbatch * ceil(numExt / 4096) <= 262144;
+ * larger calls return PVGPU_ERR_BAD_ARG with a message in pvgpu_last_error().  The first call on
+ * a device looks up the array's device address (cudaGetSymbolAddress, with that device current)
+ * and caches it; make that first call before any stream capture.  All calls share the one array:
+ * calls that overlap on the GPU (concurrent streams, or several host threads) race on it and
+ * must be serialised by the caller.  Output equals pvgpu_compact_active's. */
+pvgpu_status pvgpu_compact_active_noalloc(
+      const float *aExt,
+      int nbatch,
+      int64_t numExt,
+      pvgpu_entry *entries,
+      int64_t *numActive,
+      void *stream);
+
 /* ---- a4: presynaptic-perspective delivery -----------------------------------------------
  * Replaces CudaRecvPre::do_run / HyPerLayer_recv_pre (cudakernels/CudaRecvPre.cu:10-101)
  * driven by PresynapticPerspectiveGPUDelivery::deliver (delivery/PresynapticPerspectiveGPUDelivery.cpp:198-270),

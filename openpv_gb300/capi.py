@@ -107,6 +107,7 @@ def _declare(L):
         "pvgpu_last_error": (C.c_char_p, []),
         "pvgpu_compact_scratch_bytes": (sz, [i, i64]),
         "pvgpu_compact_active": (i, [vp, i, i64, vp, vp, vp, sz, vp]),
+        "pvgpu_compact_active_noalloc": (i, [vp, i, i64, vp, vp, vp]),
         "pvgpu_deliver_pre": (i, [cp, vp, vp, vp, vp, vp, i, vp]),
         "pvgpu_deliver_post": (i, [cp, vp, vp, vp, i, vp]),
         "pvgpu_transpose_weights": (i, [cp, vp, vp, vp]),
@@ -186,6 +187,12 @@ def compact_active(a_ext, nbatch, num_ext, entries, num_active, scratch=None, st
         scratch = torch.empty(max(need, 1), dtype=torch.uint8, device=a_ext.device)
     check(lib().pvgpu_compact_active(_ptr(a_ext), nbatch, num_ext, _ptr(entries), _ptr(num_active), _ptr(scratch),
                                      scratch.numel() * scratch.element_size(), _stream(stream)), "compact_active")
+
+
+def compact_active_noalloc(a_ext, nbatch, num_ext, entries, num_active, stream=None):
+    """Compaction that allocates nothing (fixed scratch inside the library); see include/pvgpu.h."""
+    check(lib().pvgpu_compact_active_noalloc(_ptr(a_ext), nbatch, num_ext, _ptr(entries), _ptr(num_active),
+                                             _stream(stream)), "compact_active_noalloc")
 
 
 def deliver_pre(conn, weights, gsyn, entries=None, num_active=None, a_ext=None, mode=DELIVER_FAST, stream=None):

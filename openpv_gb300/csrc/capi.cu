@@ -14,6 +14,11 @@ pvgpu_status record_cuda_error(cudaError_t err, const char *where) {
    return PVGPU_ERR_LAUNCH;
 }
 
+pvgpu_status record_message(pvgpu_status status, const char *message) {
+   std::snprintf(g_last_error, sizeof(g_last_error), "%s", message);
+   return status;
+}
+
 }  // namespace pvgpu
 
 extern "C" const char *pvgpu_version(void) { return "pvgpu 0.1 (sm_103a)"; }

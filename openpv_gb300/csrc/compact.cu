@@ -10,6 +10,8 @@
 // produces them.  Integer/byte work: HBM-bound, 2 reads of the activity + 8 B per entry.
 #include "pvgpu_internal.cuh"
 
+#include <mutex>
+
 namespace {
 
 constexpr int kThreads = 256;
@@ -141,5 +143,74 @@ extern "C" pvgpu_status pvgpu_compact_active(const float *aExt, int nbatch, int6
    PVGPU_CHECK_LAUNCH("compact scan");
    write_kernel<<<grid, kThreads, 0, s>>>(aExt, numExt, nchunks, counts, entries);
    PVGPU_CHECK_LAUNCH("compact write");
+   return PVGPU_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Compaction without any device allocation.
+//
+// Some callers cannot hand this library a scratch buffer and must not make it allocate one:
+// code that runs inside a host function enqueued on a stream (CUDA API calls that allocate are
+// not allowed there), latency-critical loops that cannot afford the implicit device
+// synchronisation cudaMalloc/cudaFree may cause, and hosts whose device memory is entirely
+// owned by their own pool allocator.  For them the per-chunk counts live in a fixed array in
+// this library's device image, sized for kNoAllocMaxChunks chunks in total
+// (nbatch * ceil(numExt / 4096) <= 262144, i.e. up to 2^30 activity values per call).
+// The array is loaded with the library, once per device, and held until the process exits.
+// ---------------------------------------------------------------------------------------------
+namespace {
+
+constexpr int64_t kNoAllocMaxChunks = 1 << 18;  // 262144 x 4 bytes = 1 MiB per device
+
+static __device__ __align__(256) uint32_t g_compact_noalloc_scratch[kNoAllocMaxChunks];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+void *g_noalloc_addr[kMaxDevices] = {};
+
+// Device address of g_compact_noalloc_scratch on the current device.  The host-side symbol is
+// only a stand-in: a kernel handed its host address would read the wrong memory, so the
+// address is looked up with the device current, checked, and cached per device.
+pvgpu_status noalloc_scratch(uint32_t **out) {
+   int dev = 0;
+   cudaError_t e = cudaGetDevice(&dev);
+   if (e != cudaSuccess) return pvgpu::record_cuda_error(e, "compact_active_noalloc: cudaGetDevice");
+   if (dev < 0 || dev >= kMaxDevices)
+      return pvgpu::record_message(PVGPU_ERR_UNSUPPORTED_SHAPE, "compact_active_noalloc: device ordinal out of range");
+   std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+   if (!g_noalloc_addr[dev]) {
+      void *p = nullptr;
+      e = cudaGetSymbolAddress(&p, g_compact_noalloc_scratch);
+      if (e != cudaSuccess || !p) return pvgpu::record_cuda_error(e, "compact_active_noalloc: cudaGetSymbolAddress");
+      g_noalloc_addr[dev] = p;
+   }
+   *out = static_cast<uint32_t *>(g_noalloc_addr[dev]);
+   return PVGPU_OK;
+}
+
+}  // namespace
+
+extern "C" pvgpu_status pvgpu_compact_active_noalloc(const float *aExt, int nbatch, int64_t numExt,
+                                                     pvgpu_entry *entries, int64_t *numActive, void *stream) {
+   if (!aExt || !entries || !numActive || nbatch <= 0 || numExt <= 0 || numExt > 0xffffffffLL) return PVGPU_ERR_BAD_ARG;
+   if (nbatch > 65535) return PVGPU_ERR_UNSUPPORTED_SHAPE;
+   const int64_t nchunks = (numExt + kChunk - 1) / kChunk;
+   if ((int64_t)nbatch * nchunks > kNoAllocMaxChunks)
+      return pvgpu::record_message(PVGPU_ERR_BAD_ARG,
+                                   "compact_active_noalloc: nbatch * ceil(numExt / 4096) exceeds the fixed scratch "
+                                   "of 262144 chunk counts; use pvgpu_compact_active with caller scratch");
+   uint32_t *counts = nullptr;
+   pvgpu_status st = noalloc_scratch(&counts);
+   if (st != PVGPU_OK) return st;
+   // Every chunk count the kernels read is written earlier in the same call, so nothing has to
+   // be cleared between calls.
+   cudaStream_t s = pvgpu::as_stream(stream);
+   dim3 grid((unsigned)nchunks, nbatch);
+   count_kernel<<<grid, kThreads, 0, s>>>(aExt, numExt, (int)nchunks, counts);
+   PVGPU_CHECK_LAUNCH("compact_active_noalloc count");
+   scan_kernel<<<nbatch, 1024, 0, s>>>(counts, (int)nchunks, numActive);
+   PVGPU_CHECK_LAUNCH("compact_active_noalloc scan");
+   write_kernel<<<grid, kThreads, 0, s>>>(aExt, numExt, (int)nchunks, counts, entries);
+   PVGPU_CHECK_LAUNCH("compact_active_noalloc write");
    return PVGPU_OK;
 }

@@ -10,6 +10,8 @@ namespace pvgpu {
 
 // Records the CUDA error string for pvgpu_last_error() and maps it to a status.
 pvgpu_status record_cuda_error(cudaError_t err, const char *where);
+// Records a plain message for pvgpu_last_error() and returns status.
+pvgpu_status record_message(pvgpu_status status, const char *message);
 
 #define PVGPU_CHECK_LAUNCH(where)                                                  \
    do {                                                                            \
