@@ -19,6 +19,7 @@ struct LcaGeom {
    int NT;                      // feature tile of the post kernel
    float VThresh, AMin, AMax, AShift, VWidth;
    float e, si;                 // decay factor (float)exp(-dt/tau), selfInteract
+   int simple;                  // AMax = +inf and VWidth = 0: A = V < VThresh ? AMin : V - AShift
 };
 
 // ANNActivityBuffer::applyVThresh / applyAMax (components/ANNActivityBuffer.cpp:490-558)

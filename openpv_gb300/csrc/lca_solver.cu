@@ -201,25 +201,25 @@ __global__ void __launch_bounds__(128) recon_tc_kernel(const __grid_constant__ C
 // -------------------------------------------------------------------------------------------
 // Kernel P: residual, post-perspective delivery and the LCA update (persistent)
 //
-// Work unit ("tile"): one image, 128 V1 positions, 64 features.  Grid = (F/64) x G CTAs, one
-// per SM; a CTA keeps its 64-feature block, loads that block's weights once, and walks the
-// (image, position block) tiles g, g+G, ...  Per tile, one thread issues every global read as
-// an async copy on one mbarrier: the V tile (TMA, 128B swizzle), the rows of the input and of
-// the reconstruction partials that the tile's receptive fields cover (bulk copies).  With two
-// buffer sets the next tile's copies fly while this tile computes.  The 8 warps then build
-// the im2col operand of r = x - sum(partials) in shared memory, one thread issues the
-// tcgen05.mma chain (M=128, N=64, K=P*P*C) into TMEM, and the epilogue (warp w: TMEM lanes
-// 32*(w%4).., features 32*(w/4)..) updates V in place in the shared tile and stages A; TMA
-// stores write both back.
+// Tile: one image, 128 V1 positions, FT (<= 256) features, i.e. FT/64 MMA blocks of 64
+// features.  Grid: one CTA per SM walking tiles blockIdx.x, +G, ...  Per tile the 8 warps
+// build the residual window r = x - sum(partials) once (from input / partial rows bulk-copied
+// into shared memory during the previous tile) and its BF16 im2col operand; then, per block,
+// the block's weight tile and V tile arrive by TMA into a 2-slot ring (the next block's copies
+// fly during this block), one thread issues the tcgen05.mma chain (M=128, N=64, K=P*P*C) into
+// TMEM, and the epilogue (warp w: TMEM lanes 32*(w%4).., features 32*(w/4)..) updates V in
+// place in its shared tile (TMA-stored back) and writes A straight to global memory.
 // -------------------------------------------------------------------------------------------
 constexpr int kPostNT = 64;
 
 struct PostPlan {
-   int nbuf;                          // 1 or 2 buffer sets (next-tile prefetch when 2)
-   int G;                             // CTAs per feature block
-   uint32_t offW, offWlo, offIM, offIMlo, offAST, offASTlo;
-   uint32_t offVT[2], offST[2];
-   uint32_t offRW;                    // residual window of the current tile (FP32)
+   int G;                             // persistent CTAs
+   int FT;                            // features per tile (multiple of 64, <= 256)
+   int nslot;                         // ring slots for the per-block weight / V tiles (1 or 2)
+   uint32_t offIM, offIMlo;
+   uint32_t offW[2], offWlo[2];
+   uint32_t offVT[2];
+   uint32_t offST, offRW;
    uint32_t stArrBytes;               // one staged array (x or one partial), rounded to 16 B
    uint32_t total;                    // dynamic shared memory incl. alignment slack
 };
@@ -232,30 +232,31 @@ __device__ __forceinline__ uint32_t pack2(float lo, float hi) {
 template <int S, int P, int C, bool X3>
 __global__ void __launch_bounds__(256, 1) post_tc_kernel(const __grid_constant__ CUtensorMap tmW,
                                                          const __grid_constant__ CUtensorMap tmWlo,
-                                                         const __grid_constant__ CUtensorMap tmV,
-                                                         const __grid_constant__ CUtensorMap tmA,
-                                                         const __grid_constant__ CUtensorMap tmAlo, LcaGeom g,
+                                                         const __grid_constant__ CUtensorMap tmV, LcaGeom g,
                                                          PostPlan pl, const float *__restrict__ x,
-                                                         const float *__restrict__ partials, int *__restrict__ err) {
+                                                         const float *__restrict__ partials, bf16 *__restrict__ A,
+                                                         bf16 *__restrict__ Alo, int *__restrict__ err) {
    constexpr int KP = P * P * C, NKC = KP / 64, E = (P - S) / 2;
+   constexpr uint32_t WBYTES = NKC * kPostNT * 128;
    extern __shared__ uint8_t smem_raw[];
    uint8_t *smem = align1024(smem_raw);
-   __shared__ __align__(8) uint64_t wbar, vbar[2], done;
+   __shared__ __align__(8) uint64_t stbar, ldbar[2], done;
    __shared__ uint32_t tmemBase;
 
    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-   const int nTilesN = g.F / kPostNT;
-   const int nt = blockIdx.x % nTilesN, grp = blockIdx.x / nTilesN;
-   const int f0 = nt * kPostNT;
-   const int nTiles = g.nb * g.MB;
+   const int nFH = g.F / pl.FT, nBlk = pl.FT / kPostNT;
+   const int nTiles = g.nb * g.MB * nFH;
+   const int myTiles = blockIdx.x < nTiles ? (nTiles - 1 - blockIdx.x) / pl.G + 1 : 0;
+   const int Q = myTiles * nBlk;
    const int RWR = rwin_rows(S, P, g.rowsPerBlock);
+   const int RWC = rwin_cols(S, P, g.v1Nx);
    const int rowElems = g.inNx * C;
    const int nPix = g.inNy * rowElems;
 
    if (tid == 0) {
-      mbar_init(&wbar, 1);
-      mbar_init(&vbar[0], 1);
-      mbar_init(&vbar[1], 1);
+      mbar_init(&stbar, 1);
+      mbar_init(&ldbar[0], 1);
+      mbar_init(&ldbar[1], 1);
       mbar_init(&done, 1);
       fence_mbar_init();
    }
@@ -265,75 +266,72 @@ __global__ void __launch_bounds__(256, 1) post_tc_kernel(const __grid_constant__
    tc_fence_after();
    const uint32_t tmem = tmemBase;
 
+   auto tile_of = [&](int ti, int &b, int &mb, int &fh) {
+      const int j = blockIdx.x + ti * pl.G;
+      fh = j % nFH;
+      const int r = j / nFH;
+      mb = r % g.MB;
+      b = r / g.MB;
+   };
    auto tile_rows = [&](int mb, int &ylo, int &yhi) {
       const int top = S * mb * g.rowsPerBlock - E;
       ylo = top < 0 ? 0 : top;
       yhi = top + RWR > g.inNy ? g.inNy : top + RWR;
    };
-   // thread 0 only: copies of tile j into buffer set s
-   auto issue_tile = [&](int j, int s) {
-      const int b = j / g.MB, mb = j % g.MB;
-      const int rowV = b * g.Npos + mb * 128;
+   // thread 0 only: input / partial rows of tile ti
+   auto issue_rows = [&](int ti) {
+      int b, mb, fh;
+      tile_of(ti, b, mb, fh);
       int ylo, yhi;
       tile_rows(mb, ylo, yhi);
       const uint32_t nbytes = (uint32_t)((yhi - ylo) * rowElems * 4);
-      mbar_arrive_expect_tx(&vbar[s], 2 * 16384 + (uint32_t)(g.MB + 1) * nbytes);
-      uint8_t *vt = smem + pl.offVT[s];
-      tma_load_2d(vt, &tmV, &vbar[s], f0, rowV);
-      tma_load_2d(vt + 16384, &tmV, &vbar[s], f0 + 32, rowV);
-      uint8_t *st = smem + pl.offST[s];
-      bulk_load(st, x + (size_t)b * nPix + (size_t)ylo * rowElems, nbytes, &vbar[s]);
+      mbar_arrive_expect_tx(&stbar, (uint32_t)(g.MB + 1) * nbytes);
+      uint8_t *st = smem + pl.offST;
+      bulk_load(st, x + (size_t)b * nPix + (size_t)ylo * rowElems, nbytes, &stbar);
       for (int m = 0; m < g.MB; m++)
          bulk_load(st + (size_t)(1 + m) * pl.stArrBytes,
-                   partials + ((size_t)b * g.MB + m) * nPix + (size_t)ylo * rowElems, nbytes, &vbar[s]);
+                   partials + ((size_t)b * g.MB + m) * nPix + (size_t)ylo * rowElems, nbytes, &stbar);
    };
-   auto buf_of = [&](int i) { return pl.nbuf == 2 ? (i & 1) : 0; };
-   auto par_of = [&](int i) { return (uint32_t)(pl.nbuf == 2 ? ((i >> 1) & 1) : (i & 1)); };
-
-   int issued = 0;  // tiles whose copies thread 0 has issued (local indices 0..issued-1)
-   if (tid == 0) {
-      mbar_arrive_expect_tx(&wbar, (X3 ? 2 : 1) * NKC * kPostNT * 128);
+   // thread 0 only: weight tile and V tile of block q into ring slot q % nslot
+   auto issue_block = [&](int q) {
+      const int ti = q / nBlk, nb = q % nBlk, slot = q % pl.nslot;
+      int b, mb, fh;
+      tile_of(ti, b, mb, fh);
+      const int f0 = fh * pl.FT + nb * kPostNT, rowV = b * g.Npos + mb * 128;
+      mbar_arrive_expect_tx(&ldbar[slot], (X3 ? 2 : 1) * WBYTES + 2 * 16384);
       for (int kc = 0; kc < NKC; kc++) {
-         tma_load_2d(smem + pl.offW + kc * kPostNT * 128, &tmW, &wbar, kc * 64, f0);
-         if (X3) tma_load_2d(smem + pl.offWlo + kc * kPostNT * 128, &tmWlo, &wbar, kc * 64, f0);
+         tma_load_2d(smem + pl.offW[slot] + kc * kPostNT * 128, &tmW, &ldbar[slot], kc * 64, f0);
+         if (X3) tma_load_2d(smem + pl.offWlo[slot] + kc * kPostNT * 128, &tmWlo, &ldbar[slot], kc * 64, f0);
       }
-      if (grp < nTiles) {
-         issue_tile(grp, 0);
-         issued = 1;
-      }
-   }
+      uint8_t *vt = smem + pl.offVT[slot];
+      tma_load_2d(vt, &tmV, &ldbar[slot], f0, rowV);
+      tma_load_2d(vt + 16384, &tmV, &ldbar[slot], f0 + 32, rowV);
+   };
 
+   int rowsIssued = 0, rowsWaited = 0, blocksIssued = 0, blocksWaited = 0;
+   if (tid == 0 && Q > 0) {
+      issue_rows(0);
+      rowsIssued = 1;
+      issue_block(0);
+      blocksIssued = 1;
+   }
    bool ok = true;
-   int waited = 0;
-   int i = 0;
-   for (int j = grp; j < nTiles; j += pl.G, i++) {
-      const int s = buf_of(i);
-      if (tid == 0) {
-         if (i > 0) bulk_wait_read_all();  // the previous tile's stores have read their shared tiles
-         if (pl.nbuf == 2 && j + pl.G < nTiles) {
-            issue_tile(j + pl.G, s ^ 1);
-            issued++;
-         }
-      }
-      // one thread polls; the barrier hands its observation (and the copied data) to the CTA
+   for (int ti = 0; ti < myTiles && ok; ti++) {
+      int b, mb, fh;
+      tile_of(ti, b, mb, fh);
       bool lok = true;
-      if (tid == 0) {
-         lok = mbar_wait(&vbar[s], par_of(i));
-         if (i == 0) lok = lok && mbar_wait(&wbar, 0);
-      }
+      if (tid == 0) lok = mbar_wait(&stbar, (uint32_t)(ti & 1));
       ok = __syncthreads_and(lok);
       if (!ok) break;
-      waited = i + 1;
+      rowsWaited = ti + 1;
 
-      // ---- residual window r = x - sum(partials), once per tile (FP32, zero outside the layer) ----
-      const int b = j / g.MB, mb = j % g.MB;
+      // ---- residual window (FP32) and its BF16 im2col, once per tile ----
       int ylo, yhi;
       tile_rows(mb, ylo, yhi);
       const int top = S * mb * g.rowsPerBlock - E;
-      const int RWC = rwin_cols(S, P, g.v1Nx);
       float *rwin = reinterpret_cast<float *>(smem + pl.offRW);
       {
-         const float *st = reinterpret_cast<const float *>(smem + pl.offST[s]);
+         const float *st = reinterpret_cast<const float *>(smem + pl.offST);
          const int stride = pl.stArrBytes / 4;
          const int n = RWR * RWC * C;
          for (int e = tid; e < n; e += 256) {
@@ -350,10 +348,14 @@ __global__ void __launch_bounds__(256, 1) post_tc_kernel(const __grid_constant__
          }
       }
       __syncthreads();
-      // ---- im2col: row ky of a position's receptive field is P*C contiguous window floats ----
+      // the staged rows are consumed: the next tile's rows can fly during this tile's blocks
+      if (tid == 0 && ti + 1 < myTiles) {
+         issue_rows(ti + 1);
+         rowsIssued++;
+      }
       {
-         constexpr int RUN = P * C;          // floats per patch row, a multiple of 8
-         constexpr int CPR = RUN / 8;        // 16-byte chunks per patch row
+         constexpr int RUN = P * C;
+         constexpr int CPR = RUN / 8;
          static_assert(RUN % 8 == 0, "patch rows must fill whole 16-byte chunks");
          const int p = tid & 127, half = tid >> 7;
          const int yl = p / g.v1Nx, x1 = p % g.v1Nx;
@@ -391,93 +393,115 @@ __global__ void __launch_bounds__(256, 1) post_tc_kernel(const __grid_constant__
       fence_proxy_async_smem();
       __syncthreads();
 
-      // ---- D[pos][f] on the tensor cores ----
-      if (tid == 0) {
-         tc_fence_after();
-         const uint32_t idesc = idesc_bf16(128, kPostNT);
-         const int npass = X3 ? 3 : 1;
-         for (int pass = 0; pass < npass; pass++) {
-            const uint32_t a0 = smem_u32(smem + ((X3 && pass == 2) ? pl.offIMlo : pl.offIM));
-            const uint32_t w0 = smem_u32(smem + ((X3 && pass == 1) ? pl.offWlo : pl.offW));
-            for (int kc = 0; kc < NKC; kc++)
+      // ---- the tile's feature blocks ----
+      for (int nb = 0; nb < nBlk; nb++) {
+         const int q = ti * nBlk + nb;
+         const int slot = q % pl.nslot;
+         const int f0 = fh * pl.FT + nb * kPostNT;
+         const int rowV = b * g.Npos + mb * 128;
+         lok = true;
+         if (tid == 0) {
+            if (pl.nslot == 2 && q + 1 < Q) {
+               bulk_wait_read_all();  // the previous block's V store has left the other slot
+               issue_block(q + 1);
+               blocksIssued++;
+            }
+            lok = mbar_wait(&ldbar[slot], (uint32_t)((q / pl.nslot) & 1));
+            if (lok) {
+               blocksWaited = q + 1;
+               tc_fence_after();
+               const uint32_t idesc = idesc_bf16(128, kPostNT);
+               const int npass = X3 ? 3 : 1;
+               for (int pass = 0; pass < npass; pass++) {
+                  const uint32_t a0 = smem_u32(smem + ((X3 && pass == 2) ? pl.offIMlo : pl.offIM));
+                  const uint32_t w0 = smem_u32(smem + ((X3 && pass == 1) ? pl.offWlo[slot] : pl.offW[slot]));
+                  for (int kc = 0; kc < NKC; kc++)
 #pragma unroll
-               for (int k = 0; k < 4; k++)
-                  mma_bf16(tmem, sdesc_sw128(a0 + kc * 16384 + k * 32), sdesc_sw128(w0 + kc * kPostNT * 128 + k * 32),
-                           idesc, (pass | kc | k) != 0);
-         }
-         mma_commit(&done);
-      }
-      ok = __syncthreads_and(tid != 0 || mbar_wait(&done, (uint32_t)(i & 1)));
-      if (!ok) break;
-      tc_fence_after();
-
-      // ---- epilogue: V update in place in the shared V tile, A staged for the store ----
-      {
-         const int q = warp & 3, h = warp >> 2;
-         const int p = 32 * q + lane;
-         float d[32], vo[32];
-         tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + 32 * h, d);
-         uint8_t *vt = smem + pl.offVT[s] + h * 16384 + p * 128;
-#pragma unroll
-         for (int qq = 0; qq < 8; qq++) {
-            const float4 t = *reinterpret_cast<const float4 *>(vt + ((qq ^ (p & 7)) << 4));
-            vo[4 * qq] = t.x;
-            vo[4 * qq + 1] = t.y;
-            vo[4 * qq + 2] = t.z;
-            vo[4 * qq + 3] = t.w;
-         }
-         float vn[32];
-         uint32_t ah[16], al[16];
-#pragma unroll
-         for (int jj = 0; jj < 32; jj++) vn[jj] = fmaf(g.e, vo[jj], (1.0f - g.e) * (d[jj] + g.si * thresh(vo[jj], g)));
-#pragma unroll
-         for (int jj = 0; jj < 32; jj += 2) {
-            const float a0 = thresh(vn[jj], g), a1 = thresh(vn[jj + 1], g);
-            __nv_bfloat162 hb = __floats2bfloat162_rn(a0, a1);
-            ah[jj / 2] = *reinterpret_cast<uint32_t *>(&hb);
-            if (X3) {
-               const float2 hf = __bfloat1622float2(hb);
-               al[jj / 2] = pack2(a0 - hf.x, a1 - hf.y);
+                     for (int k = 0; k < 4; k++)
+                        mma_bf16(tmem, sdesc_sw128(a0 + kc * 16384 + k * 32),
+                                 sdesc_sw128(w0 + kc * kPostNT * 128 + k * 32), idesc, (pass | kc | k) != 0);
+               }
+               mma_commit(&done);
+               lok = mbar_wait(&done, (uint32_t)(q & 1));
             }
          }
+         ok = __syncthreads_and(lok);
+         if (!ok) break;
+         tc_fence_after();
+
+         // ---- epilogue ----
+         {
+            const int qd = warp & 3, h = warp >> 2;
+            const int p = 32 * qd + lane;
+            float d[32], vo[32];
+            tmem_ld32(tmem + ((uint32_t)(32 * qd) << 16) + 32 * h, d);
+            uint8_t *vt = smem + pl.offVT[slot] + h * 16384 + p * 128;
 #pragma unroll
-         for (int qq = 0; qq < 8; qq++)
-            *reinterpret_cast<float4 *>(vt + ((qq ^ (p & 7)) << 4)) =
-                  make_float4(vn[4 * qq], vn[4 * qq + 1], vn[4 * qq + 2], vn[4 * qq + 3]);
+            for (int qq = 0; qq < 8; qq++) {
+               const float4 t = *reinterpret_cast<const float4 *>(vt + ((qq ^ (p & 7)) << 4));
+               vo[4 * qq] = t.x;
+               vo[4 * qq + 1] = t.y;
+               vo[4 * qq + 2] = t.z;
+               vo[4 * qq + 3] = t.w;
+            }
+            float vn[32], an[32];
+            const float om = 1.0f - g.e;
+            if (g.simple) {  // AMax = +inf, VWidth = 0: A = V < VThresh ? AMin : V - AShift
 #pragma unroll
-         for (int t = 0; t < 4; t++) {
-            const uint32_t off = p * 128 + ((((4 * h + t) ^ (p & 7))) << 4);
-            *reinterpret_cast<uint4 *>(smem + pl.offAST + off) =
-                  make_uint4(ah[4 * t], ah[4 * t + 1], ah[4 * t + 2], ah[4 * t + 3]);
-            if (X3)
-               *reinterpret_cast<uint4 *>(smem + pl.offASTlo + off) =
-                     make_uint4(al[4 * t], al[4 * t + 1], al[4 * t + 2], al[4 * t + 3]);
+               for (int jj = 0; jj < 32; jj++) {
+                  const float ao = vo[jj] < g.VThresh ? g.AMin : vo[jj] - g.AShift;
+                  vn[jj] = fmaf(g.e, vo[jj], om * (d[jj] + g.si * ao));
+                  an[jj] = vn[jj] < g.VThresh ? g.AMin : vn[jj] - g.AShift;
+               }
+            } else {
+#pragma unroll
+               for (int jj = 0; jj < 32; jj++) {
+                  vn[jj] = fmaf(g.e, vo[jj], om * (d[jj] + g.si * thresh(vo[jj], g)));
+                  an[jj] = thresh(vn[jj], g);
+               }
+            }
+#pragma unroll
+            for (int qq = 0; qq < 8; qq++)
+               *reinterpret_cast<float4 *>(vt + ((qq ^ (p & 7)) << 4)) =
+                     make_float4(vn[4 * qq], vn[4 * qq + 1], vn[4 * qq + 2], vn[4 * qq + 3]);
+            uint4 *ag = reinterpret_cast<uint4 *>(A + (size_t)(rowV + p) * g.F + f0 + 32 * h);
+#pragma unroll
+            for (int t = 0; t < 4; t++)
+               ag[t] = make_uint4(pack2(an[8 * t], an[8 * t + 1]), pack2(an[8 * t + 2], an[8 * t + 3]),
+                                  pack2(an[8 * t + 4], an[8 * t + 5]), pack2(an[8 * t + 6], an[8 * t + 7]));
+            if (X3) {
+               uint4 *lg = reinterpret_cast<uint4 *>(Alo + (size_t)(rowV + p) * g.F + f0 + 32 * h);
+#pragma unroll
+               for (int t = 0; t < 4; t++) {
+                  float l[8];
+#pragma unroll
+                  for (int u = 0; u < 8; u++) l[u] = an[8 * t + u] - __bfloat162float(__float2bfloat16_rn(an[8 * t + u]));
+                  lg[t] = make_uint4(pack2(l[0], l[1]), pack2(l[2], l[3]), pack2(l[4], l[5]), pack2(l[6], l[7]));
+               }
+            }
          }
-      }
-      fence_proxy_async_smem();
-      tc_fence_before();
-      __syncthreads();
-      if (tid == 0) {
-         const int rowV = b * g.Npos + mb * 128;
-         uint8_t *vt = smem + pl.offVT[s];
-         tma_store_2d(&tmV, vt, f0, rowV);
-         tma_store_2d(&tmV, vt + 16384, f0 + 32, rowV);
-         tma_store_2d(&tmA, smem + pl.offAST, f0, rowV);
-         if (X3) tma_store_2d(&tmAlo, smem + pl.offASTlo, f0, rowV);
-         bulk_commit();
-         if (pl.nbuf == 1 && j + pl.G < nTiles) {
-            bulk_wait_read_all();
-            issue_tile(j + pl.G, 0);
-            issued++;
+         fence_proxy_async_smem();
+         tc_fence_before();
+         __syncthreads();
+         if (tid == 0) {
+            uint8_t *vt = smem + pl.offVT[slot];
+            tma_store_2d(&tmV, vt, f0, rowV);
+            tma_store_2d(&tmV, vt + 16384, f0 + 32, rowV);
+            bulk_commit();
+            if (pl.nslot == 1 && q + 1 < Q) {
+               bulk_wait_read_all();
+               issue_block(q + 1);
+               blocksIssued++;
+            }
          }
       }
    }
    if (tid == 0) {
-      if (i == 0) mbar_wait(&wbar, 0);  // no tile ran: the weight copies still have to land
       bulk_wait_all();
       if (!ok) {
          // let copies still in flight land before shared memory goes away
-         for (int t = waited; t < issued; t++) mbar_wait(&vbar[buf_of(t)], par_of(t));
+         for (int t = rowsWaited; t < rowsIssued; t++) mbar_wait(&stbar, (uint32_t)(t & 1));
+         for (int t = blocksWaited; t < blocksIssued; t++) mbar_wait(&ldbar[t % pl.nslot], (uint32_t)((t / pl.nslot) & 1));
          atomicExch(err, 1);
       }
    }
@@ -603,52 +627,41 @@ PostPlan make_post_plan(const LcaGeom &g, int S, int P, int C, bool x3, int numS
    std::memset(&pl, 0, sizeof(pl));
    const uint32_t RWR = (uint32_t)rwin_rows(S, P, g.rowsPerBlock);
    pl.stArrBytes = ((RWR * g.inNx * C * 4) + 15u) & ~15u;
-   const uint32_t wB = NKC * kPostNT * 128, imB = NKC * 16384, astB = 16384, vtB = 2 * 16384;
+   const uint32_t wB = NKC * kPostNT * 128, imB = NKC * 16384, vtB = 2 * 16384;
    const uint32_t stB = (uint32_t)(g.MB + 1) * pl.stArrBytes;
-   // Two buffer sets (next-tile prefetch) when they fit; otherwise one, with the A staging
-   // tiles placed inside the staged-rows region, which is dead by the epilogue (the rows are
-   // consumed by the im2col build, and the next tile's copies are issued only after the
-   // stores have read the staging tiles).
-   for (int nbuf = 2; nbuf >= 1; nbuf--) {
+   const uint32_t rwB = RWR * (uint32_t)rwin_cols(S, P, g.v1Nx) * C * 4;
+   // two ring slots (the next block's copies fly during this block) when they fit, else one
+   for (int nslot = 2; nslot >= 1; nslot--) {
       uint32_t o = 0;
-      pl.offW = o;
-      o = al(o + wB);
-      pl.offWlo = o;
-      if (x3) o = al(o + wB);
       pl.offIM = o;
       o = al(o + imB);
       pl.offIMlo = o;
       if (x3) o = al(o + imB);
-      if (nbuf == 2) {
-         pl.offAST = o;
-         o = al(o + astB);
-         pl.offASTlo = o;
-         if (x3) o = al(o + astB);
+      for (int sl = 0; sl < 2; sl++) {
+         pl.offW[sl] = o;
+         pl.offWlo[sl] = o;
+         if (sl < nslot) {
+            o = al(o + wB);
+            pl.offWlo[sl] = o;
+            if (x3) o = al(o + wB);
+         }
       }
-      for (int b = 0; b < 2; b++) {
-         pl.offVT[b] = o;
-         if (b < nbuf) o = al(o + vtB);
+      for (int sl = 0; sl < 2; sl++) {
+         pl.offVT[sl] = o;
+         if (sl < nslot) o = al(o + vtB);
       }
-      const uint32_t stRegion = nbuf == 2 ? stB : std::max(stB, (x3 ? 2u : 1u) * astB);
-      for (int b = 0; b < 2; b++) {
-         pl.offST[b] = o;
-         if (b < nbuf) o = al(o + stRegion);
-      }
-      if (nbuf == 1) {
-         pl.offAST = pl.offST[0];
-         pl.offASTlo = pl.offST[0] + astB;
-      }
+      pl.offST = o;
+      o = al(o + stB);
       pl.offRW = o;
-      o = al(o + (uint32_t)(RWR * rwin_cols(S, P, g.v1Nx) * C * 4));
+      o = al(o + rwB);
       pl.total = o + 1024;
-      pl.nbuf = nbuf;
+      pl.nslot = nslot;
       if (pl.total <= 227u * 1024u) break;
    }
-   const int nTilesN = g.F / kPostNT;
-   int G = numSms / nTilesN;
-   if (G < 1) G = 1;
-   if (G > g.nb * g.MB) G = g.nb * g.MB;
-   pl.G = G;
+   pl.FT = g.F < 256 ? g.F : 256;
+   while (g.F % pl.FT) pl.FT -= 64;
+   const int nTiles = g.nb * g.MB * (g.F / pl.FT);
+   pl.G = numSms < nTiles ? numSms : nTiles;
    return pl;
 }
 
@@ -671,8 +684,7 @@ struct Launcher {
       auto pk = post_tc_kernel<S, P, C, X3>;
       e = cudaFuncSetAttribute(pk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.total);
       if (e != cudaSuccess) return pvgpu::record_cuda_error(e, "lca post attr");
-      pk<<<(s->g.F / kPostNT) * pl.G, 256, pl.total, st>>>(s->tmW, s->tmWlo, s->tmV, s->tmA, s->tmAlo, s->g, pl, x,
-                                                          s->partials, s->err);
+      pk<<<pl.G, 256, pl.total, st>>>(s->tmW, s->tmWlo, s->tmV, s->g, pl, x, s->partials, s->A, s->Alo, s->err);
       PVGPU_CHECK_LAUNCH("lca post");
       return PVGPU_OK;
    }
@@ -749,6 +761,7 @@ extern "C" pvgpu_status pvgpu_lca_solver_create(const pvgpu_lca_solver_desc *d, 
    g.VWidth = vw;
    g.e = (float)exp(-(double)d->dt / (double)d->tau);
    g.si = d->selfInteract ? 1.0f : 0.0f;
+   g.simple = (vw == 0.0f && !(d->AMax < FLT_MAX) && vt > -FLT_MAX) ? 1 : 0;
    const size_t nState = (size_t)g.nb * Npos * g.F;
    const size_t nPart = (size_t)g.nb * g.MB * d->inNx * d->inNy * C;
    const size_t nW = (size_t)g.F * KP;
