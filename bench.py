@@ -68,10 +68,10 @@ def dictionary(rng, nf, p, c):
 
 
 def make_inputs(cfg, nb=None, seed_offset=0):
-    rng = np.random.default_rng(cfg["seed"] + seed_offset)
+    """The dictionary (one model, the same on every rank) and an image shard (seed + 1 + offset)."""
     nb = cfg["nbatch"] if nb is None else nb
-    w = dictionary(rng, cfg["v1_shape"][2], cfg["nxp"], cfg["in_shape"][2])
-    x = one_over_f_images(rng, nb, *cfg["in_shape"])
+    w = dictionary(np.random.default_rng(cfg["seed"]), cfg["v1_shape"][2], cfg["nxp"], cfg["in_shape"][2])
+    x = one_over_f_images(np.random.default_rng(cfg["seed"] + 1 + seed_offset), nb, *cfg["in_shape"])
     return w, x
 
 
@@ -159,6 +159,29 @@ def fp64_energy(cfg, x, w, nimg, threads):
     _, _, _, e = O.lca_run(p, w.astype(np.float64), x[None, :nimg].astype(np.float64), cfg["timesteps"], v0,
                            f64=True, threads=threads, want_recon=False)
     return e[-1]
+
+
+# ---------------------------------------------------------------------------------------------
+# replicas over the batch: each rank solves its own shard; only timings cross ranks
+# ---------------------------------------------------------------------------------------------
+def shard_seed_offset(rank):
+    """Rank r solves its own 256-image shard, generated from seed + r."""
+    return rank
+
+
+def max_over_ranks(ms, dist, device):
+    """Slowest rank's time (the job finishes when the last replica does)."""
+    if dist is None:
+        return ms
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(world, nb, timesteps, ms):
+    """Whole-job images*timesteps per second: all ranks' images over the slowest rank's time."""
+    return world * nb * timesteps / (ms / 1000.0)
 
 
 # ---------------------------------------------------------------------------------------------
@@ -262,7 +285,7 @@ def run_ours(args, rank, world, local_rank):
         cfg["timesteps"] = args.timesteps
         cfg["x3_steps"] = min(cfg["x3_steps"], args.timesteps // 8)
     nb, T, X3 = cfg["nbatch"], cfg["timesteps"], cfg["x3_steps"]
-    w_np, x_np = make_inputs(cfg, seed_offset=rank)  # each rank solves its own batch shard
+    w_np, x_np = make_inputs(cfg, seed_offset=shard_seed_offset(rank))  # each rank solves its own batch shard
     vshape = (nb,) + cfg["v1_shape"]
     solver = capi.LcaSolver(nb, cfg["in_shape"], cfg["v1_shape"], cfg["nxp"], cfg["VThresh"], AMin=cfg["AMin"],
                             AShift=cfg["AShift"], VWidth=cfg["VWidth"], tau=cfg["tau"], dt=cfg["dt"])
@@ -296,12 +319,8 @@ def run_ours(args, rank, world, local_rank):
     recon_ms, post_ms, nprof = solver.profile_end()
     barrier()
     ms = e0.elapsed_time(e1) / args.steps
-    ms_all = ms
-    if dist is not None:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_all = float(t.item())
-    value = world * nb * T / (ms_all / 1000.0)
+    ms_all = max_over_ranks(ms, dist, dev)
+    value = job_value(world, nb, T, ms_all)
     assert solver.error_flag() == 0, "a bounded device wait timed out"
     e_gpu = energy.cpu().numpy().copy()
 
@@ -328,12 +347,8 @@ def run_ours(args, rank, world, local_rank):
         e2e_step()
     t1.record()
     torch.cuda.synchronize()
-    e2e_ms = t0.elapsed_time(t1) / args.steps
-    if dist is not None:
-        t = torch.tensor([e2e_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
-    e2e_value = world * nb * T / (e2e_ms / 1000.0)
+    e2e_ms = max_over_ranks(t0.elapsed_time(t1) / args.steps, dist, dev)
+    e2e_value = job_value(world, nb, T, e2e_ms)
     h2d = x_np.nbytes
     d2h = a_host.numel() * 4 + nb * 8
 
@@ -382,13 +397,13 @@ def run_ours(args, rank, world, local_rank):
     recon_avg_ms = recon_ms / nprof
     recon_flops_launch = 2 * npos * F * (cfg["nxp"] ** 2 * cfg["in_shape"][2]) * nb * (1 + 2 * x3_frac)
 
-    trafficf = os.path.join(ROOT, "profiles", "post_kernel_traffic.json")
+    # DRAM bytes per launch from the committed ncu summary of the same kernel and workload
     traffic = None
+    trafficf = os.path.join(ROOT, "profiles", "post_tc_kernel_batched_lca.md")
     if os.path.exists(trafficf):
-        try:
-            traffic = json.load(open(trafficf)).get("bytes_per_launch")
-        except (ValueError, OSError):
-            traffic = None
+        for line in open(trafficf):
+            if line.startswith("dram bytes per launch:"):
+                traffic = float(line.split(":")[1])
 
     cpu_val, cpu_dt = cpu_sample(cfg, cores, warm_steps=25, timed_steps=25)
     deliv = delivery_bench(torch, capi)
