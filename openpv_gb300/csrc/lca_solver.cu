@@ -18,13 +18,14 @@
 // its contributions in the same fixed group order -- deterministic, no atomics.  The
 // block's partial reconstruction goes to HBM.
 //
-// Kernel P ("post"): one CTA per (image, block of 128 positions, block of NT features).
+// Kernel P ("post"): persistent; tiles of (image, block of 128 positions, block of FT features).
 //   residual r = x - sum of the image's partial reconstructions (FP32, fixed order),
 //   staged for the block's receptive-field window in shared memory;
 //   im2col of r into a 128B-swizzled BF16 operand by the CTA's threads;
 //   D[pos][f] = sum_k r[pos][k] * W[f][k] on tcgen05 (TMEM accumulator);
 //   epilogue per (position, feature): A_old = T(V_old); V = e V_old + (1-e)(D + A_old);
-//   A = T(V) -> BF16 for the next step's kernel R.  V is prefetched by TMA at kernel start.
+//   A = T(V) -> BF16 for the next step's kernel R.  A load warp, an MMA warp and 8 epilogue
+//   warps hand tiles to one another through mbarriers (see the kernel's own header).
 // BF16x3 mode adds the hi*lo and lo*hi products (operands split as x = hi + lo).
 #include "lca_common.cuh"
 #include "tc_ptx.cuh"
@@ -199,28 +200,75 @@ __global__ void __launch_bounds__(128) recon_tc_kernel(const __grid_constant__ C
 }
 
 // -------------------------------------------------------------------------------------------
-// Kernel P: residual, post-perspective delivery and the LCA update (persistent)
+// Kernel D ("residual"): r = x - (sum of the image's partial reconstructions, in block order),
+// written with a zero border of E pixels on every side and rows padded to RP floats
+// (RP = (inNx + 2E) * C rounded up to a multiple of 4), so that the receptive-field window of
+// a 128-position block is one contiguous run of rows for a single bulk copy.  The zero border
+// is the restricted error layer's halo.
+// -------------------------------------------------------------------------------------------
+template <int C>
+__global__ void residual_kernel(LcaGeom g, int E, int RP, const float *__restrict__ x,
+                                const float *__restrict__ partials, float *__restrict__ rpad) {
+   const int rowsPad = g.inNy + 2 * E;
+   const size_t total = (size_t)g.nb * rowsPad * RP;
+   const int nPix = g.inNx * g.inNy * C;
+   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+      const int col = (int)(i % RP);
+      const size_t row = i / RP;
+      const int ye = (int)(row % rowsPad) - E;
+      const int b = (int)(row / rowsPad);
+      const int xe = col / C - E, c = col % C;
+      float v = 0.0f;
+      if (ye >= 0 && ye < g.inNy && xe >= 0 && xe < g.inNx) {
+         const size_t pi = ((size_t)ye * g.inNx + xe) * C + c;
+         const float *pb = partials + (size_t)b * g.MB * nPix;
+         float rec = pb[pi];
+         for (int m = 1; m < g.MB; m++) rec = __fadd_rn(rec, pb[(size_t)m * nPix + pi]);
+         v = __fadd_rn(x[(size_t)b * nPix + pi], -rec);
+      }
+      rpad[i] = v;
+   }
+}
+
+// -------------------------------------------------------------------------------------------
+// Kernel P: post-perspective delivery and the LCA update (persistent, warp-specialised)
 //
-// Tile: one image, 128 V1 positions, FT (<= 256) features, i.e. FT/64 MMA blocks of 64
-// features.  Grid: one CTA per SM walking tiles blockIdx.x, +G, ...  Per tile the 8 warps
-// build the residual window r = x - sum(partials) once (from input / partial rows bulk-copied
-// into shared memory during the previous tile) and its BF16 im2col operand; then, per block,
-// the block's weight tile and V tile arrive by TMA into a 2-slot ring (the next block's copies
-// fly during this block), one thread issues the tcgen05.mma chain (M=128, N=64, K=P*P*C) into
-// TMEM, and the epilogue (warp w: TMEM lanes 32*(w%4).., features 32*(w/4)..) updates V in
-// place in its shared tile (TMA-stored back) and writes A straight to global memory.
+// Tile: one image, 128 V1 positions, FT (<= 256) features, i.e. FT/64 blocks of 64 features.
+// Grid: one CTA per SM walking tiles blockIdx.x, +G, ...  Three roles:
+//   warp 8, lane 0 (loads):   the next tile's residual window (one bulk copy of RWR padded
+//                             rows), and each block's weight tile and V tile by TMA into rings
+//                             of nW / nV slots;
+//   warp 9, lane 0 (MMA):     per block one tcgen05.mma chain (M = 128, N = 64, K = P*P*C) into
+//                             one of two TMEM accumulators;
+//   warps 0-7 (epilogue):     per tile the BF16 im2col operand of the window (all 8 warps);
+//                             per block, each warp on its own: TMEM lanes 32*(w%4).., features
+//                             32*(w/4).., the LCA update of V in place in its 32 x 32 part of
+//                             the shared V tile (TMA-stored back by the warp), A to global memory.
+// Loads run up to nV blocks ahead of the epilogue, so several V tiles are in flight per SM.
+// Hand-offs are full/empty mbarriers:
+//   stFull / stEmpty   window landed / read by the im2col
+//   imFull / imEmpty   im2col built / all MMAs of the tile done (tcgen05.commit)
+//   wFull / wEmpty     weight slot landed / its MMAs done (tcgen05.commit)
+//   vFull / vEmpty     V slot landed / updated and read out by the 8 warps' stores
+//   accFull / accEmpty accumulator written (tcgen05.commit) / read by the 8 epilogue warps
+// A warp releases a V slot when its store of the next block has been issued and the slot's
+// own store has read shared memory (one store in flight per warp); with a single slot it
+// waits for the read at once.
+// Every wait is bounded; a timeout raises a shared abort flag that every role checks, the
+// roles drain their own copies and MMAs in flight, and the kernel reports through *err.
 // -------------------------------------------------------------------------------------------
 constexpr int kPostNT = 64;
+constexpr int kMaxVSlots = 3, kMaxWSlots = 2;
 
 struct PostPlan {
    int G;                             // persistent CTAs
    int FT;                            // features per tile (multiple of 64, <= 256)
-   int nslot;                         // ring slots for the per-block weight / V tiles (1 or 2)
+   int nV, nW;                        // ring slots for the per-block V tiles and weight tiles
+   int RP, rowsPad;                   // padded residual: floats per row, rows per image
    uint32_t offIM, offIMlo;
-   uint32_t offW[2], offWlo[2];
-   uint32_t offVT[2];
-   uint32_t offST, offRW;
-   uint32_t stArrBytes;               // one staged array (x or one partial), rounded to 16 B
+   uint32_t offW[kMaxWSlots], offWlo[kMaxWSlots];
+   uint32_t offVT[kMaxVSlots];
+   uint32_t offWin;                   // residual window, RWR rows x RP floats
    uint32_t total;                    // dynamic shared memory incl. alignment slack
 };
 
@@ -230,37 +278,55 @@ __device__ __forceinline__ uint32_t pack2(float lo, float hi) {
 }
 
 template <int S, int P, int C, bool X3>
-__global__ void __launch_bounds__(256, 1) post_tc_kernel(const __grid_constant__ CUtensorMap tmW,
+__global__ void __launch_bounds__(320, 1) post_tc_kernel(const __grid_constant__ CUtensorMap tmW,
                                                          const __grid_constant__ CUtensorMap tmWlo,
-                                                         const __grid_constant__ CUtensorMap tmV, LcaGeom g,
-                                                         PostPlan pl, const float *__restrict__ x,
-                                                         const float *__restrict__ partials, bf16 *__restrict__ A,
-                                                         bf16 *__restrict__ Alo, int *__restrict__ err) {
-   constexpr int KP = P * P * C, NKC = KP / 64, E = (P - S) / 2;
+                                                         const __grid_constant__ CUtensorMap tmV,
+                                                         const __grid_constant__ CUtensorMap tmVst, LcaGeom g,
+                                                         PostPlan pl, const float *__restrict__ rpad,
+                                                         bf16 *__restrict__ A, bf16 *__restrict__ Alo,
+                                                         int *__restrict__ err) {
+   constexpr int KP = P * P * C, NKC = KP / 64;
    constexpr uint32_t WBYTES = NKC * kPostNT * 128;
+   constexpr int EPI = 256;  // epilogue threads (warps 0-7)
+   static_assert((S * C) % 2 == 0, "window reads are 8-byte pairs");
    extern __shared__ uint8_t smem_raw[];
    uint8_t *smem = align1024(smem_raw);
-   __shared__ __align__(8) uint64_t stbar, ldbar[2], done;
+   __shared__ __align__(8) uint64_t stFull, stEmpty, imFull, imEmpty, wFull[kMaxWSlots], wEmpty[kMaxWSlots],
+         vFull[kMaxVSlots], vEmpty[kMaxVSlots], accFull[2], accEmpty[2];
    __shared__ uint32_t tmemBase;
+   __shared__ volatile int abortFlag;
 
    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
    const int nFH = g.F / pl.FT, nBlk = pl.FT / kPostNT;
    const int nTiles = g.nb * g.MB * nFH;
    const int myTiles = blockIdx.x < nTiles ? (nTiles - 1 - blockIdx.x) / pl.G + 1 : 0;
    const int Q = myTiles * nBlk;
+   const int nV = pl.nV, nW = pl.nW;
+   const int lagV = nV >= 2 ? nV - 1 : nV;  // blocks between a V slot's use and its release
    const int RWR = rwin_rows(S, P, g.rowsPerBlock);
-   const int RWC = rwin_cols(S, P, g.v1Nx);
-   const int rowElems = g.inNx * C;
-   const int nPix = g.inNy * rowElems;
+   const int RP = pl.RP;
 
    if (tid == 0) {
-      mbar_init(&stbar, 1);
-      mbar_init(&ldbar[0], 1);
-      mbar_init(&ldbar[1], 1);
-      mbar_init(&done, 1);
+      mbar_init(&stFull, 1);
+      mbar_init(&stEmpty, 1);
+      mbar_init(&imFull, 1);
+      mbar_init(&imEmpty, 1);
+      for (int i = 0; i < kMaxWSlots; i++) {
+         mbar_init(&wFull[i], 1);
+         mbar_init(&wEmpty[i], 1);
+      }
+      for (int i = 0; i < kMaxVSlots; i++) {
+         mbar_init(&vFull[i], 1);
+         mbar_init(&vEmpty[i], 8);  // one arrival per epilogue warp
+      }
+      for (int i = 0; i < 2; i++) {
+         mbar_init(&accFull[i], 1);
+         mbar_init(&accEmpty[i], 8);
+      }
+      abortFlag = 0;
       fence_mbar_init();
    }
-   if (warp == 0) tmem_alloc(&tmemBase, kPostNT);
+   if (warp == 0) tmem_alloc(&tmemBase, 2 * kPostNT);
    tc_fence_before();
    __syncthreads();
    tc_fence_after();
@@ -273,172 +339,191 @@ __global__ void __launch_bounds__(256, 1) post_tc_kernel(const __grid_constant__
       mb = r % g.MB;
       b = r / g.MB;
    };
-   auto tile_rows = [&](int mb, int &ylo, int &yhi) {
-      const int top = S * mb * g.rowsPerBlock - E;
-      ylo = top < 0 ? 0 : top;
-      yhi = top + RWR > g.inNy ? g.inNy : top + RWR;
+   auto wait_or_abort = [&](uint64_t *bar, uint32_t parity) {
+      if (abortFlag) return false;
+      if (mbar_wait(bar, parity)) return true;
+      abortFlag = 1;
+      return false;
    };
-   // thread 0 only: input / partial rows of tile ti
-   auto issue_rows = [&](int ti) {
-      int b, mb, fh;
-      tile_of(ti, b, mb, fh);
-      int ylo, yhi;
-      tile_rows(mb, ylo, yhi);
-      const uint32_t nbytes = (uint32_t)((yhi - ylo) * rowElems * 4);
-      mbar_arrive_expect_tx(&stbar, (uint32_t)(g.MB + 1) * nbytes);
-      uint8_t *st = smem + pl.offST;
-      bulk_load(st, x + (size_t)b * nPix + (size_t)ylo * rowElems, nbytes, &stbar);
-      for (int m = 0; m < g.MB; m++)
-         bulk_load(st + (size_t)(1 + m) * pl.stArrBytes,
-                   partials + ((size_t)b * g.MB + m) * nPix + (size_t)ylo * rowElems, nbytes, &stbar);
-   };
-   // thread 0 only: weight tile and V tile of block q into ring slot q % nslot
-   auto issue_block = [&](int q) {
-      const int ti = q / nBlk, nb = q % nBlk, slot = q % pl.nslot;
-      int b, mb, fh;
-      tile_of(ti, b, mb, fh);
-      const int f0 = fh * pl.FT + nb * kPostNT, rowV = b * g.Npos + mb * 128;
-      mbar_arrive_expect_tx(&ldbar[slot], (X3 ? 2 : 1) * WBYTES + 2 * 16384);
-      for (int kc = 0; kc < NKC; kc++) {
-         tma_load_2d(smem + pl.offW[slot] + kc * kPostNT * 128, &tmW, &ldbar[slot], kc * 64, f0);
-         if (X3) tma_load_2d(smem + pl.offWlo[slot] + kc * kPostNT * 128, &tmWlo, &ldbar[slot], kc * 64, f0);
-      }
-      uint8_t *vt = smem + pl.offVT[slot];
-      tma_load_2d(vt, &tmV, &ldbar[slot], f0, rowV);
-      tma_load_2d(vt + 16384, &tmV, &ldbar[slot], f0 + 32, rowV);
-   };
+   // last block (< n issued) that used ring slot sl of a ring of `slots`, or -1
+   auto last_use = [](int n, int sl, int slots) { return sl < n ? n - 1 - ((n - 1 - sl) % slots) : -1; };
 
-   int rowsIssued = 0, rowsWaited = 0, blocksIssued = 0, blocksWaited = 0;
-   if (tid == 0 && Q > 0) {
-      issue_rows(0);
-      rowsIssued = 1;
-      issue_block(0);
-      blocksIssued = 1;
-   }
-   bool ok = true;
-   for (int ti = 0; ti < myTiles && ok; ti++) {
-      int b, mb, fh;
-      tile_of(ti, b, mb, fh);
-      bool lok = true;
-      if (tid == 0) lok = mbar_wait(&stbar, (uint32_t)(ti & 1));
-      ok = __syncthreads_and(lok);
-      if (!ok) break;
-      rowsWaited = ti + 1;
-
-      // ---- residual window (FP32) and its BF16 im2col, once per tile ----
-      int ylo, yhi;
-      tile_rows(mb, ylo, yhi);
-      const int top = S * mb * g.rowsPerBlock - E;
-      float *rwin = reinterpret_cast<float *>(smem + pl.offRW);
-      {
-         const float *st = reinterpret_cast<const float *>(smem + pl.offST);
-         const int stride = pl.stArrBytes / 4;
-         const int n = RWR * RWC * C;
-         for (int e = tid; e < n; e += 256) {
-            const int c = e % C, xr = (e / C) % RWC, yr = e / (C * RWC);
-            const int ye = top + yr, xe = xr - E;
-            float v = 0.0f;
-            if (ye >= 0 && ye < g.inNy && xe >= 0 && xe < g.inNx) {
-               const int idx = ((ye - ylo) * g.inNx + xe) * C + c;
-               float rec = st[stride + idx];
-               for (int m = 1; m < g.MB; m++) rec = __fadd_rn(rec, st[(1 + m) * stride + idx]);
-               v = __fadd_rn(st[idx], -rec);
+   if (warp == 8) {
+      // ============================== loads ==============================
+      if (lane == 0 && Q > 0) {
+         int rowsIssued = 0, wIssued = 0, vIssued = 0;
+         const uint32_t winBytes = (uint32_t)(RWR * RP * 4);
+         auto issue_rows = [&](int ti) {
+            int b, mb, fh;
+            tile_of(ti, b, mb, fh);
+            // padded rows S*mb*rowsPerBlock .. +RWR hold error rows S*y0 - E .. +RWR
+            const float *src = rpad + ((size_t)b * pl.rowsPad + (size_t)S * mb * g.rowsPerBlock) * RP;
+            mbar_arrive_expect_tx(&stFull, winBytes);
+            bulk_load(smem + pl.offWin, src, winBytes, &stFull);
+            rowsIssued = ti + 1;
+         };
+         bool ok = true;
+         issue_rows(0);
+         for (int q = 0; ok && q < Q; q++) {
+            // tile t+1's window goes out once tile t's has been read, before the first load that
+            // waits for tile t's epilogue (V slot) or MMAs (weight slot): that load could not
+            // start earlier anyway, and a later issue would leave the epilogue without a window
+            while (ok && rowsIssued < myTiles && (rowsIssued - 1) * nBlk + (lagV < nW ? lagV : nW) <= q) {
+               ok = wait_or_abort(&stEmpty, (uint32_t)((rowsIssued - 1) & 1));
+               if (ok) issue_rows(rowsIssued);
             }
-            rwin[e] = v;
+            if (!ok) break;
+            const int ti = q / nBlk, nb = q % nBlk;
+            int b, mb, fh;
+            tile_of(ti, b, mb, fh);
+            const int f0 = fh * pl.FT + nb * kPostNT, rowV = b * g.Npos + mb * 128;
+            const int sw = q % nW, uw = q / nW;
+            if (uw > 0 && !(ok = wait_or_abort(&wEmpty[sw], (uint32_t)((uw - 1) & 1)))) break;
+            mbar_arrive_expect_tx(&wFull[sw], (X3 ? 2 : 1) * WBYTES);
+            for (int kc = 0; kc < NKC; kc++) {
+               tma_load_2d(smem + pl.offW[sw] + kc * kPostNT * 128, &tmW, &wFull[sw], kc * 64, f0);
+               if (X3) tma_load_2d(smem + pl.offWlo[sw] + kc * kPostNT * 128, &tmWlo, &wFull[sw], kc * 64, f0);
+            }
+            wIssued = q + 1;
+            const int sv = q % nV, uv = q / nV;
+            if (uv > 0 && !(ok = wait_or_abort(&vEmpty[sv], (uint32_t)((uv - 1) & 1)))) break;
+            mbar_arrive_expect_tx(&vFull[sv], 2 * 16384);
+            uint8_t *vt = smem + pl.offVT[sv];
+            tma_load_2d(vt, &tmV, &vFull[sv], f0, rowV);
+            tma_load_2d(vt + 16384, &tmV, &vFull[sv], f0 + 32, rowV);
+            vIssued = q + 1;
          }
-      }
-      __syncthreads();
-      // the staged rows are consumed: the next tile's rows can fly during this tile's blocks
-      if (tid == 0 && ti + 1 < myTiles) {
-         issue_rows(ti + 1);
-         rowsIssued++;
-      }
-      {
-         constexpr int RUN = P * C;
-         constexpr int CPR = RUN / 8;
-         static_assert(RUN % 8 == 0, "patch rows must fill whole 16-byte chunks");
-         const int p = tid & 127, half = tid >> 7;
-         const int yl = p / g.v1Nx, x1 = p % g.v1Nx;
-         const float *src0 = rwin + ((S * yl) * RWC + S * x1) * C;
-#pragma unroll 1
-         for (int ky = half * (P / 2); ky < (half + 1) * (P / 2); ky++) {
-            const float *src = src0 + ky * RWC * C;
-#pragma unroll
-            for (int cc = 0; cc < CPR; cc++) {
-               float vals[8];
-#pragma unroll
-               for (int jj = 0; jj < 8; jj++) vals[jj] = src[cc * 8 + jj];
-               uint4 hi;
-               hi.x = pack2(vals[0], vals[1]);
-               hi.y = pack2(vals[2], vals[3]);
-               hi.z = pack2(vals[4], vals[5]);
-               hi.w = pack2(vals[6], vals[7]);
-               const int c8 = ky * CPR + cc;
-               const uint32_t off = (c8 >> 3) * 16384 + sw128_offset(p, (c8 & 7) * 8);
-               *reinterpret_cast<uint4 *>(smem + pl.offIM + off) = hi;
-               if (X3) {
-                  const __nv_bfloat162 *h2 = reinterpret_cast<const __nv_bfloat162 *>(&hi);
-                  float2 f01 = __bfloat1622float2(h2[0]), f23 = __bfloat1622float2(h2[1]);
-                  float2 f45 = __bfloat1622float2(h2[2]), f67 = __bfloat1622float2(h2[3]);
-                  uint4 lo;
-                  lo.x = pack2(vals[0] - f01.x, vals[1] - f01.y);
-                  lo.y = pack2(vals[2] - f23.x, vals[3] - f23.y);
-                  lo.z = pack2(vals[4] - f45.x, vals[5] - f45.y);
-                  lo.w = pack2(vals[6] - f67.x, vals[7] - f67.y);
-                  *reinterpret_cast<uint4 *>(smem + pl.offIMlo + off) = lo;
-               }
+         while (ok && rowsIssued < myTiles) {
+            ok = wait_or_abort(&stEmpty, (uint32_t)((rowsIssued - 1) & 1));
+            if (ok) issue_rows(rowsIssued);
+         }
+         if (!ok) {
+            // the copies still in flight land before shared memory goes away
+            mbar_wait(&stFull, (uint32_t)((rowsIssued - 1) & 1));
+            for (int sl = 0; sl < nW; sl++) {
+               const int u = last_use(wIssued, sl, nW);
+               if (u >= 0) mbar_wait(&wFull[sl], (uint32_t)((u / nW) & 1));
+            }
+            for (int sl = 0; sl < nV; sl++) {
+               const int u = last_use(vIssued, sl, nV);
+               if (u >= 0) mbar_wait(&vFull[sl], (uint32_t)((u / nV) & 1));
             }
          }
       }
-      fence_proxy_async_smem();
-      __syncthreads();
-
-      // ---- the tile's feature blocks ----
-      for (int nb = 0; nb < nBlk; nb++) {
-         const int q = ti * nBlk + nb;
-         const int slot = q % pl.nslot;
-         const int f0 = fh * pl.FT + nb * kPostNT;
-         const int rowV = b * g.Npos + mb * 128;
-         lok = true;
-         if (tid == 0) {
-            if (pl.nslot == 2 && q + 1 < Q) {
-               bulk_wait_read_all();  // the previous block's V store has left the other slot
-               issue_block(q + 1);
-               blocksIssued++;
-            }
-            lok = mbar_wait(&ldbar[slot], (uint32_t)((q / pl.nslot) & 1));
-            if (lok) {
-               blocksWaited = q + 1;
-               tc_fence_after();
-               const uint32_t idesc = idesc_bf16(128, kPostNT);
-               const int npass = X3 ? 3 : 1;
-               for (int pass = 0; pass < npass; pass++) {
-                  const uint32_t a0 = smem_u32(smem + ((X3 && pass == 2) ? pl.offIMlo : pl.offIM));
-                  const uint32_t w0 = smem_u32(smem + ((X3 && pass == 1) ? pl.offWlo[slot] : pl.offW[slot]));
-                  for (int kc = 0; kc < NKC; kc++)
+   } else if (warp == 9) {
+      // ============================== MMA ==============================
+      if (lane == 0 && Q > 0) {
+         int mmaDone = 0;
+         bool ok = true;
+         for (int q = 0; ok && q < Q; q++) {
+            const int ti = q / nBlk, nb = q % nBlk, sw = q % nW, a = q & 1;
+            if (nb == 0 && !(ok = wait_or_abort(&imFull, (uint32_t)(ti & 1)))) break;
+            if (!(ok = wait_or_abort(&wFull[sw], (uint32_t)((q / nW) & 1)))) break;
+            if (q >= 2 && !(ok = wait_or_abort(&accEmpty[a], (uint32_t)(((q >> 1) - 1) & 1)))) break;
+            tc_fence_after();
+            const uint32_t idesc = idesc_bf16(128, kPostNT);
+            const uint32_t d = tmem + a * kPostNT;
+            const int npass = X3 ? 3 : 1;
+            for (int pass = 0; pass < npass; pass++) {
+               const uint32_t a0 = smem_u32(smem + ((X3 && pass == 2) ? pl.offIMlo : pl.offIM));
+               const uint32_t w0 = smem_u32(smem + ((X3 && pass == 1) ? pl.offWlo[sw] : pl.offW[sw]));
+               for (int kc = 0; kc < NKC; kc++)
 #pragma unroll
-                     for (int k = 0; k < 4; k++)
-                        mma_bf16(tmem, sdesc_sw128(a0 + kc * 16384 + k * 32),
-                                 sdesc_sw128(w0 + kc * kPostNT * 128 + k * 32), idesc, (pass | kc | k) != 0);
-               }
-               mma_commit(&done);
-               lok = mbar_wait(&done, (uint32_t)(q & 1));
+                  for (int k = 0; k < 4; k++)
+                     mma_bf16(d, sdesc_sw128(a0 + kc * 16384 + k * 32), sdesc_sw128(w0 + kc * kPostNT * 128 + k * 32),
+                              idesc, (pass | kc | k) != 0);
             }
+            mma_commit(&accFull[a]);
+            mma_commit(&wEmpty[sw]);
+            if (nb == nBlk - 1) mma_commit(&imEmpty);
+            mmaDone = q + 1;
          }
-         ok = __syncthreads_and(lok);
-         if (!ok) break;
-         tc_fence_after();
-
-         // ---- epilogue ----
+         // MMAs still in flight finish before shared memory and TMEM go away
+         if (!ok && mmaDone > 0) mbar_wait(&accFull[(mmaDone - 1) & 1], (uint32_t)(((mmaDone - 1) >> 1) & 1));
+      }
+   } else {
+      // ============================== epilogue (warps 0-7) ==============================
+      const float *win = reinterpret_cast<const float *>(smem + pl.offWin);
+      const int qd = warp & 3, h = warp >> 2;
+      const int pw = 32 * qd + lane;  // this thread's position (TMEM lane) in the epilogue
+      int pendingV = -1;              // V slot whose store this warp has in flight (lane 0)
+      // A warp whose wait failed leaves its block loop only; the next tile's barrier sees the
+      // abort flag in that warp and every warp leaves together (no warp skips a barrier).
+      for (int ti = 0; ti < myTiles; ti++) {
+         int b, mb, fh;
+         tile_of(ti, b, mb, fh);
+         if (tid == 0 && wait_or_abort(&stFull, (uint32_t)(ti & 1)) && ti > 0)
+            wait_or_abort(&imEmpty, (uint32_t)((ti - 1) & 1));  // the previous tile's MMAs are done
+         if (named_bar_or(1, EPI, abortFlag != 0)) break;
+         // ---- BF16 im2col of the window (row runs of P*C elements, read in pairs) ----
          {
-            const int qd = warp & 3, h = warp >> 2;
-            const int p = 32 * qd + lane;
+            constexpr int RUN = P * C;
+            constexpr int CPR = RUN / 8;
+            static_assert(RUN % 8 == 0, "patch rows must fill whole 16-byte chunks");
+            const int p = tid & 127, half = tid >> 7;
+            const int yl = p / g.v1Nx, x1 = p % g.v1Nx;
+            const float *src0 = win + (S * yl) * RP + S * x1 * C;
+#pragma unroll 1
+            for (int ky = half * (P / 2); ky < (half + 1) * (P / 2); ky++) {
+               const float2 *src = reinterpret_cast<const float2 *>(src0 + ky * RP);
+#pragma unroll
+               for (int cc = 0; cc < CPR; cc++) {
+                  float vals[8];
+#pragma unroll
+                  for (int jj = 0; jj < 4; jj++) {
+                     const float2 t = src[cc * 4 + jj];
+                     vals[2 * jj] = t.x;
+                     vals[2 * jj + 1] = t.y;
+                  }
+                  uint4 hi;
+                  hi.x = pack2(vals[0], vals[1]);
+                  hi.y = pack2(vals[2], vals[3]);
+                  hi.z = pack2(vals[4], vals[5]);
+                  hi.w = pack2(vals[6], vals[7]);
+                  const int c8 = ky * CPR + cc;
+                  const uint32_t off = (c8 >> 3) * 16384 + sw128_offset(p, (c8 & 7) * 8);
+                  *reinterpret_cast<uint4 *>(smem + pl.offIM + off) = hi;
+                  if (X3) {
+                     const __nv_bfloat162 *h2 = reinterpret_cast<const __nv_bfloat162 *>(&hi);
+                     float2 f01 = __bfloat1622float2(h2[0]), f23 = __bfloat1622float2(h2[1]);
+                     float2 f45 = __bfloat1622float2(h2[2]), f67 = __bfloat1622float2(h2[3]);
+                     uint4 lo;
+                     lo.x = pack2(vals[0] - f01.x, vals[1] - f01.y);
+                     lo.y = pack2(vals[2] - f23.x, vals[3] - f23.y);
+                     lo.z = pack2(vals[4] - f45.x, vals[5] - f45.y);
+                     lo.w = pack2(vals[6] - f67.x, vals[7] - f67.y);
+                     *reinterpret_cast<uint4 *>(smem + pl.offIMlo + off) = lo;
+                  }
+               }
+            }
+         }
+         fence_proxy_async_smem();
+         named_bar_sync(1, EPI);
+         if (tid == 0) {
+            mbar_arrive(&imFull);
+            mbar_arrive(&stEmpty);  // the window is read: the next tile's may land
+         }
+
+         // ---- the tile's feature blocks, each warp on its own ----
+         for (int nb = 0; nb < nBlk; nb++) {
+            const int q = ti * nBlk + nb, sv = q % nV, a = q & 1;
+            const int f0 = fh * pl.FT + nb * kPostNT, rowV = b * g.Npos + mb * 128;
+            int okw = 1;
+            if (lane == 0)
+               okw = wait_or_abort(&accFull[a], (uint32_t)((q >> 1) & 1)) &&
+                     wait_or_abort(&vFull[sv], (uint32_t)((q / nV) & 1));
+            okw = __shfl_sync(0xffffffffu, okw, 0);
+            if (!okw) break;
+            tc_fence_after();
             float d[32], vo[32];
-            tmem_ld32(tmem + ((uint32_t)(32 * qd) << 16) + 32 * h, d);
-            uint8_t *vt = smem + pl.offVT[slot] + h * 16384 + p * 128;
+            tmem_ld32(tmem + a * kPostNT + ((uint32_t)(32 * qd) << 16) + 32 * h, d);
+            tc_fence_before();
+            if (lane == 0) mbar_arrive(&accEmpty[a]);  // this warp is done with the accumulator
+            uint8_t *vsub = smem + pl.offVT[sv] + h * 16384 + 32 * qd * 128;  // this warp's 32 x 32 part
+            uint8_t *vt = vsub + lane * 128;
 #pragma unroll
             for (int qq = 0; qq < 8; qq++) {
-               const float4 t = *reinterpret_cast<const float4 *>(vt + ((qq ^ (p & 7)) << 4));
+               const float4 t = *reinterpret_cast<const float4 *>(vt + ((qq ^ (pw & 7)) << 4));
                vo[4 * qq] = t.x;
                vo[4 * qq + 1] = t.y;
                vo[4 * qq + 2] = t.z;
@@ -462,15 +547,19 @@ __global__ void __launch_bounds__(256, 1) post_tc_kernel(const __grid_constant__
             }
 #pragma unroll
             for (int qq = 0; qq < 8; qq++)
-               *reinterpret_cast<float4 *>(vt + ((qq ^ (p & 7)) << 4)) =
+               *reinterpret_cast<float4 *>(vt + ((qq ^ (pw & 7)) << 4)) =
                      make_float4(vn[4 * qq], vn[4 * qq + 1], vn[4 * qq + 2], vn[4 * qq + 3]);
-            uint4 *ag = reinterpret_cast<uint4 *>(A + (size_t)(rowV + p) * g.F + f0 + 32 * h);
+            bf16 *ag = A + (size_t)(rowV + pw) * g.F + f0 + 32 * h;
 #pragma unroll
-            for (int t = 0; t < 4; t++)
-               ag[t] = make_uint4(pack2(an[8 * t], an[8 * t + 1]), pack2(an[8 * t + 2], an[8 * t + 3]),
-                                  pack2(an[8 * t + 4], an[8 * t + 5]), pack2(an[8 * t + 6], an[8 * t + 7]));
+            for (int t = 0; t < 2; t++)
+               st_global_32B(ag + 16 * t,
+                             make_uint4(pack2(an[16 * t], an[16 * t + 1]), pack2(an[16 * t + 2], an[16 * t + 3]),
+                                        pack2(an[16 * t + 4], an[16 * t + 5]), pack2(an[16 * t + 6], an[16 * t + 7])),
+                             make_uint4(pack2(an[16 * t + 8], an[16 * t + 9]), pack2(an[16 * t + 10], an[16 * t + 11]),
+                                        pack2(an[16 * t + 12], an[16 * t + 13]),
+                                        pack2(an[16 * t + 14], an[16 * t + 15])));
             if (X3) {
-               uint4 *lg = reinterpret_cast<uint4 *>(Alo + (size_t)(rowV + p) * g.F + f0 + 32 * h);
+               uint4 *lg = reinterpret_cast<uint4 *>(Alo + (size_t)(rowV + pw) * g.F + f0 + 32 * h);
 #pragma unroll
                for (int t = 0; t < 4; t++) {
                   float l[8];
@@ -479,35 +568,31 @@ __global__ void __launch_bounds__(256, 1) post_tc_kernel(const __grid_constant__
                   lg[t] = make_uint4(pack2(l[0], l[1]), pack2(l[2], l[3]), pack2(l[4], l[5]), pack2(l[6], l[7]));
                }
             }
-         }
-         fence_proxy_async_smem();
-         tc_fence_before();
-         __syncthreads();
-         if (tid == 0) {
-            uint8_t *vt = smem + pl.offVT[slot];
-            tma_store_2d(&tmV, vt, f0, rowV);
-            tma_store_2d(&tmV, vt + 16384, f0 + 32, rowV);
-            bulk_commit();
-            if (pl.nslot == 1 && q + 1 < Q) {
-               bulk_wait_read_all();
-               issue_block(q + 1);
-               blocksIssued++;
+            fence_proxy_async_smem();
+            __syncwarp();
+            if (lane == 0) {
+               tma_store_2d(&tmVst, vsub, f0 + 32 * h, rowV + 32 * qd);
+               bulk_commit();
+               if (nV >= 2) {
+                  if (pendingV >= 0) {
+                     bulk_wait_read_1();  // the previous block's store has read its slot
+                     mbar_arrive(&vEmpty[pendingV]);
+                  }
+                  pendingV = sv;
+               } else {
+                  bulk_wait_read_all();
+                  mbar_arrive(&vEmpty[sv]);
+               }
             }
          }
       }
+      if (lane == 0) bulk_wait_all();
    }
-   if (tid == 0) {
-      bulk_wait_all();
-      if (!ok) {
-         // let copies still in flight land before shared memory goes away
-         for (int t = rowsWaited; t < rowsIssued; t++) mbar_wait(&stbar, (uint32_t)(t & 1));
-         for (int t = blocksWaited; t < blocksIssued; t++) mbar_wait(&ldbar[t % pl.nslot], (uint32_t)((t / pl.nslot) & 1));
-         atomicExch(err, 1);
-      }
-   }
+   __syncthreads();
+   if (tid == 0 && abortFlag) atomicExch(err, 1);
    tc_fence_before();
    __syncthreads();
-   if (warp == 0) tmem_dealloc(tmem, kPostNT);
+   if (warp == 0) tmem_dealloc(tmem, 2 * kPostNT);
 }
 
 // -------------------------------------------------------------------------------------------
@@ -605,9 +690,10 @@ struct pvgpu_lca_solver {
    int S, P, C, KP;
    int stepsRun;
    float *V = nullptr, *partials = nullptr, *A32 = nullptr, *W32 = nullptr, *Wt32 = nullptr;
+   float *rpad = nullptr;  // padded residual x - W^T a (kernel D -> kernel P)
    bf16 *A = nullptr, *Alo = nullptr, *W = nullptr, *Wlo = nullptr, *Wt = nullptr, *Wtlo = nullptr;
    int *err = nullptr;
-   CUtensorMap tmA, tmAlo, tmWt, tmWtlo, tmW, tmWlo, tmV;
+   CUtensorMap tmA, tmAlo, tmWt, tmWtlo, tmW, tmWlo, tmV, tmVst;
    PostPlan plan, planX3;
    bool weightsSet = false;
    // optional per-kernel timing: events before kernel R, between R and P, after P
@@ -621,42 +707,42 @@ namespace {
 int g_num_sms = 0;
 
 PostPlan make_post_plan(const LcaGeom &g, int S, int P, int C, bool x3, int numSms) {
-   const int KP = P * P * C, NKC = KP / 64;
+   const int KP = P * P * C, NKC = KP / 64, E = (P - S) / 2;
    auto al = [](uint32_t v) { return (v + 1023u) & ~1023u; };
    PostPlan pl;
    std::memset(&pl, 0, sizeof(pl));
+   pl.RP = ((g.inNx + 2 * E) * C + 3) & ~3;
+   pl.rowsPad = g.inNy + 2 * E;
    const uint32_t RWR = (uint32_t)rwin_rows(S, P, g.rowsPerBlock);
-   pl.stArrBytes = ((RWR * g.inNx * C * 4) + 15u) & ~15u;
    const uint32_t wB = NKC * kPostNT * 128, imB = NKC * 16384, vtB = 2 * 16384;
-   const uint32_t stB = (uint32_t)(g.MB + 1) * pl.stArrBytes;
-   const uint32_t rwB = RWR * (uint32_t)rwin_cols(S, P, g.v1Nx) * C * 4;
-   // two ring slots (the next block's copies fly during this block) when they fit, else one
-   for (int nslot = 2; nslot >= 1; nslot--) {
+   const uint32_t winB = RWR * (uint32_t)pl.RP * 4;
+   // deepest rings that fit: V tiles first (they come from HBM), then weight tiles (from L2)
+   static const int kRings[][2] = {{3, 2}, {3, 1}, {2, 2}, {2, 1}, {1, 1}};
+   for (const auto &r : kRings) {
+      const int nV = r[0], nW = r[1];
       uint32_t o = 0;
       pl.offIM = o;
       o = al(o + imB);
       pl.offIMlo = o;
       if (x3) o = al(o + imB);
-      for (int sl = 0; sl < 2; sl++) {
-         pl.offW[sl] = o;
-         pl.offWlo[sl] = o;
-         if (sl < nslot) {
+      for (int sl = 0; sl < kMaxWSlots; sl++) {
+         pl.offW[sl] = pl.offWlo[sl] = o;
+         if (sl < nW) {
             o = al(o + wB);
             pl.offWlo[sl] = o;
             if (x3) o = al(o + wB);
          }
       }
-      for (int sl = 0; sl < 2; sl++) {
+      for (int sl = 0; sl < kMaxVSlots; sl++) {
          pl.offVT[sl] = o;
-         if (sl < nslot) o = al(o + vtB);
+         if (sl < nV) o = al(o + vtB);
       }
-      pl.offST = o;
-      o = al(o + stB);
-      pl.offRW = o;
-      o = al(o + rwB);
+      pl.offWin = o;
+      o = al(o + winB);
       pl.total = o + 1024;
-      pl.nslot = nslot;
-      if (pl.total <= 227u * 1024u) break;
+      pl.nV = nV;
+      pl.nW = nW;
+      if (pl.total + 256u <= 227u * 1024u) break;  // static shared memory shares the budget
    }
    pl.FT = g.F < 256 ? g.F : 256;
    while (g.F % pl.FT) pl.FT -= 64;
@@ -679,12 +765,17 @@ struct Launcher {
       if (e != cudaSuccess) return pvgpu::record_cuda_error(e, "lca recon attr");
       rk<<<s->g.nb * s->g.MB, 128, rs, st>>>(s->tmA, s->tmAlo, s->tmWt, s->tmWtlo, s->g, s->partials, s->err);
       PVGPU_CHECK_LAUNCH("lca recon");
-      if (mid) cudaEventRecord(mid, st);
       const PostPlan &pl = X3 ? s->planX3 : s->plan;
+      {
+         constexpr int E = (P - S) / 2;
+         residual_kernel<C><<<g_num_sms * 4, 256, 0, st>>>(s->g, E, pl.RP, x, s->partials, s->rpad);
+         PVGPU_CHECK_LAUNCH("lca residual");
+      }
+      if (mid) cudaEventRecord(mid, st);
       auto pk = post_tc_kernel<S, P, C, X3>;
       e = cudaFuncSetAttribute(pk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.total);
       if (e != cudaSuccess) return pvgpu::record_cuda_error(e, "lca post attr");
-      pk<<<pl.G, 256, pl.total, st>>>(s->tmW, s->tmWlo, s->tmV, s->g, pl, x, s->partials, s->A, s->Alo, s->err);
+      pk<<<pl.G, 320, pl.total, st>>>(s->tmW, s->tmWlo, s->tmV, s->tmVst, s->g, pl, s->rpad, s->A, s->Alo, s->err);
       PVGPU_CHECK_LAUNCH("lca post");
       return PVGPU_OK;
    }
@@ -708,7 +799,7 @@ pvgpu_status dispatch(int S, int P, int C, Fn &&fn) {
 
 void free_solver(pvgpu_lca_solver *s) {
    for (cudaEvent_t e : s->ev) cudaEventDestroy(e);
-   void *ptrs[] = {s->V, s->partials, s->A32, s->W32, s->Wt32, s->A, s->Alo, s->W, s->Wlo, s->Wt, s->Wtlo, s->err};
+   void *ptrs[] = {s->V, s->partials, s->rpad, s->A32, s->W32, s->Wt32, s->A, s->Alo, s->W, s->Wlo, s->Wt, s->Wtlo, s->err};
    for (void *p : ptrs)
       if (p) cudaFree(p);
    delete s;
@@ -728,7 +819,6 @@ extern "C" pvgpu_status pvgpu_lca_solver_create(const pvgpu_lca_solver_desc *d, 
    const int P = d->nxp, C = d->inNf, KP = P * P * C;
    const int Npos = d->v1Nx * d->v1Ny;
    if (Npos % 128 || 128 % d->v1Nx || KP % 64 || KP > 256 || d->v1Nf % 64) return PVGPU_ERR_UNSUPPORTED_SHAPE;
-   if ((d->inNx * d->inNf) % 4) return PVGPU_ERR_UNSUPPORTED_SHAPE;  // input rows are bulk-copied (16-byte multiples)
    if (dispatch(S, P, C, [](auto) { return PVGPU_OK; }) != PVGPU_OK) return PVGPU_ERR_UNSUPPORTED_SHAPE;
    pvgpu_lca_solver *s = new (std::nothrow) pvgpu_lca_solver();
    if (!s) return PVGPU_ERR_OOM;
@@ -765,12 +855,15 @@ extern "C" pvgpu_status pvgpu_lca_solver_create(const pvgpu_lca_solver_desc *d, 
    const size_t nState = (size_t)g.nb * Npos * g.F;
    const size_t nPart = (size_t)g.nb * g.MB * d->inNx * d->inNy * C;
    const size_t nW = (size_t)g.F * KP;
+   const int E = (P - S) / 2;
+   const size_t nPad = (size_t)g.nb * (d->inNy + 2 * E) * (((d->inNx + 2 * E) * C + 3) & ~3);
    bool ok = cudaMalloc(&s->V, nState * 4) == cudaSuccess && cudaMalloc(&s->A32, nState * 4) == cudaSuccess &&
              cudaMalloc(&s->A, nState * 2) == cudaSuccess && cudaMalloc(&s->Alo, nState * 2) == cudaSuccess &&
              cudaMalloc(&s->partials, nPart * 4) == cudaSuccess && cudaMalloc(&s->W, nW * 2) == cudaSuccess &&
              cudaMalloc(&s->Wlo, nW * 2) == cudaSuccess && cudaMalloc(&s->Wt, nW * 2) == cudaSuccess &&
              cudaMalloc(&s->Wtlo, nW * 2) == cudaSuccess && cudaMalloc(&s->W32, nW * 4) == cudaSuccess &&
-             cudaMalloc(&s->Wt32, nW * 4) == cudaSuccess && cudaMalloc(&s->err, sizeof(int)) == cudaSuccess;
+             cudaMalloc(&s->Wt32, nW * 4) == cudaSuccess && cudaMalloc(&s->err, sizeof(int)) == cudaSuccess &&
+             cudaMalloc(&s->rpad, nPad * 4) == cudaSuccess;
    if (!ok) {
       cudaGetLastError();
       free_solver(s);
@@ -793,6 +886,10 @@ extern "C" pvgpu_status pvgpu_lca_solver_create(const pvgpu_lca_solver_desc *d, 
       ok = enc && enc(&s->tmV, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, s->V, dims, strides, box, estr,
                       CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                       CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+      cuuint32_t boxSt[2] = {32, 32};  // one epilogue warp's part of a V tile
+      ok = ok && enc(&s->tmVst, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, s->V, dims, strides, boxSt, estr,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
    }
    if (!ok) {
       free_solver(s);

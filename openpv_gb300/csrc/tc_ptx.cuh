@@ -180,8 +180,45 @@ __device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.comm
 // Wait until the bulk stores committed by this thread have finished reading shared memory.
 __device__ __forceinline__ void bulk_wait_read_all() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
 
+// Wait until all but the most recent bulk-store group of this thread have read shared memory.
+__device__ __forceinline__ void bulk_wait_read_1() { asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory"); }
+
 // Wait until the bulk stores committed by this thread have completed.
 __device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+
+}  // namespace tc
+}  // namespace pvgpu
+
+namespace pvgpu {
+namespace tc {
+
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// One 32-byte global store (address 32-byte aligned).
+__device__ __forceinline__ void st_global_32B(void *p, uint4 a, uint4 b) {
+   asm volatile("st.global.v8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"l"(p), "r"(a.x), "r"(a.y), "r"(a.z), "r"(a.w),
+                "r"(b.x), "r"(b.y), "r"(b.z), "r"(b.w)
+                : "memory");
+}
+
+// Barrier among `count` threads (a multiple of 32) on hardware barrier `id` (1..15).
+__device__ __forceinline__ void named_bar_sync(int id, int count) {
+   asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+
+// Barrier like named_bar_sync that also returns the OR of `pred` over the participating
+// threads, so a decision taken after it is the same in every thread.
+__device__ __forceinline__ bool named_bar_or(int id, int count, bool pred) {
+   uint32_t r;
+   asm volatile(
+         "{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n bar.red.or.pred q, %2, %3, p;\n selp.u32 %0, 1, 0, q;\n}\n"
+         : "=r"(r)
+         : "r"((uint32_t)pred), "r"(id), "r"(count)
+         : "memory");
+   return r != 0;
+}
 
 }  // namespace tc
 }  // namespace pvgpu
