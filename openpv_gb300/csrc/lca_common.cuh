@@ -22,6 +22,18 @@ struct LcaGeom {
    int simple;                  // AMax = +inf and VWidth = 0: A = V < VThresh ? AMin : V - AShift
 };
 
+// Device layout of the membrane potential V (solver-internal; the state and reset entry points
+// convert to and from the reference's [nb][ny][nx][nf]): one 32 KB chunk per (image, block of
+// 128 positions, block of 64 features), chunks in that order, so an image's chunks are
+// contiguous.  Inside a chunk: two halves of 32 features, each 128 rows (positions) of 128 B,
+// the 16-byte group j of row r stored at group j ^ (r % 8) -- the 128-byte swizzle, so that a
+// chunk copied linearly into 1024-byte aligned shared memory is conflict-free to read by rows.
+__host__ __device__ inline size_t v_index(const LcaGeom &g, int b, int pos, int f) {
+   const int mb = pos >> 7, r = pos & 127, fb = f >> 6, h = (f >> 5) & 1, j = (f >> 2) & 7, e = f & 3;
+   const size_t chunk = ((size_t)b * g.MB + mb) * (size_t)(g.F >> 6) + fb;
+   return chunk * 8192 + (size_t)h * 4096 + (size_t)r * 32 + (size_t)((j ^ (r & 7)) << 2) + e;
+}
+
 // ANNActivityBuffer::applyVThresh / applyAMax (components/ANNActivityBuffer.cpp:490-558)
 __device__ __forceinline__ float lca_thresh(float v, const LcaGeom &g) {
    float a = v;

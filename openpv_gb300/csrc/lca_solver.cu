@@ -48,6 +48,7 @@ using bf16 = __nv_bfloat16;
 using pvgpu::LcaGeom;
 using pvgpu::rwin_cols;
 using pvgpu::rwin_rows;
+using pvgpu::v_index;
 
 __device__ __forceinline__ uint8_t *align1024(uint8_t *p) {
    return reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(p) + 1023) & ~uintptr_t(1023));
@@ -207,26 +208,26 @@ __global__ void __launch_bounds__(128) recon_tc_kernel(const __grid_constant__ C
 // is the restricted error layer's halo.
 // -------------------------------------------------------------------------------------------
 template <int C>
-__global__ void residual_kernel(LcaGeom g, int E, int RP, const float *__restrict__ x,
-                                const float *__restrict__ partials, float *__restrict__ rpad) {
-   const int rowsPad = g.inNy + 2 * E;
-   const size_t total = (size_t)g.nb * rowsPad * RP;
-   const int nPix = g.inNx * g.inNy * C;
-   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
-      const int col = (int)(i % RP);
-      const size_t row = i / RP;
-      const int ye = (int)(row % rowsPad) - E;
-      const int b = (int)(row / rowsPad);
-      const int xe = col / C - E, c = col % C;
+__global__ void __launch_bounds__(128) residual_kernel(LcaGeom g, int E, int RP, const float *__restrict__ x,
+                                                       const float *__restrict__ partials, float *__restrict__ rpad) {
+   // grid: (padded row, image)
+   const int yp = blockIdx.x, b = blockIdx.y, ye = yp - E;
+   const int rowsPad = gridDim.x;
+   float *out = rpad + ((size_t)b * rowsPad + yp) * RP;
+   const bool inside = ye >= 0 && ye < g.inNy;
+   const int nPix = g.inNx * g.inNy * C, rowElems = g.inNx * C;
+   const int yc = inside ? ye : 0;
+   const float *pb = partials + (size_t)b * g.MB * nPix + (size_t)yc * rowElems;
+   const float *xb = x + (size_t)b * nPix + (size_t)yc * rowElems;
+   for (int col = threadIdx.x; col < RP; col += blockDim.x) {
+      const int j = col - E * C;  // element within the error row
       float v = 0.0f;
-      if (ye >= 0 && ye < g.inNy && xe >= 0 && xe < g.inNx) {
-         const size_t pi = ((size_t)ye * g.inNx + xe) * C + c;
-         const float *pb = partials + (size_t)b * g.MB * nPix;
-         float rec = pb[pi];
-         for (int m = 1; m < g.MB; m++) rec = __fadd_rn(rec, pb[(size_t)m * nPix + pi]);
-         v = __fadd_rn(x[(size_t)b * nPix + pi], -rec);
+      if (inside && j >= 0 && j < rowElems) {
+         float rec = pb[j];
+         for (int m = 1; m < g.MB; m++) rec = __fadd_rn(rec, pb[(size_t)m * nPix + j]);
+         v = __fadd_rn(xb[j], -rec);
       }
-      rpad[i] = v;
+      out[col] = v;
    }
 }
 
@@ -236,15 +237,18 @@ __global__ void residual_kernel(LcaGeom g, int E, int RP, const float *__restric
 // Tile: one image, 128 V1 positions, FT (<= 256) features, i.e. FT/64 blocks of 64 features.
 // Grid: one CTA per SM walking tiles blockIdx.x, +G, ...  Three roles:
 //   warp 8, lane 0 (loads):   the next tile's residual window (one bulk copy of RWR padded
-//                             rows), and each block's weight tile and V tile by TMA into rings
-//                             of nW / nV slots;
+//                             rows), each block's weight tile by TMA and its V chunk (32 KB,
+//                             contiguous in the device layout of V) by one bulk copy, into
+//                             rings of nW / nV slots;
 //   warp 9, lane 0 (MMA):     per block one tcgen05.mma chain (M = 128, N = 64, K = P*P*C) into
-//                             one of two TMEM accumulators;
-//   warps 0-7 (epilogue):     per tile the BF16 im2col operand of the window (all 8 warps);
-//                             per block, each warp on its own: TMEM lanes 32*(w%4).., features
-//                             32*(w/4).., the LCA update of V in place in its 32 x 32 part of
-//                             the shared V tile (TMA-stored back by the warp), A to global memory.
-// Loads run up to nV blocks ahead of the epilogue, so several V tiles are in flight per SM.
+//                             one of four TMEM accumulators;
+//   warps 0-7 (epilogue):     the BF16 im2col operand of each tile's window (all 8 warps, placed
+//                             inside the previous tile's blocks); per block, each warp on its
+//                             own: TMEM lanes 32*(w%4).., features 32*(w/4).., the LCA update of
+//                             V in place in its 32 x 32 part of the shared V chunk (a contiguous
+//                             4 KB, bulk-stored back by the warp), A staged in shared memory
+//                             and TMA-stored by the warp.
+// Loads run up to nV blocks ahead of the epilogue, so several V chunks are in flight per SM.
 // Hand-offs are full/empty mbarriers:
 //   stFull / stEmpty   window landed / read by the im2col
 //   imFull / imEmpty   im2col built / all MMAs of the tile done (tcgen05.commit)
@@ -259,6 +263,7 @@ __global__ void residual_kernel(LcaGeom g, int E, int RP, const float *__restric
 // -------------------------------------------------------------------------------------------
 constexpr int kPostNT = 64;
 constexpr int kMaxVSlots = 3, kMaxWSlots = 2;
+constexpr int kAcc = 4;  // TMEM accumulators (64 columns each): the MMAs run up to 4 blocks ahead
 
 struct PostPlan {
    int G;                             // persistent CTAs
@@ -269,6 +274,8 @@ struct PostPlan {
    uint32_t offW[kMaxWSlots], offWlo[kMaxWSlots];
    uint32_t offVT[kMaxVSlots];
    uint32_t offWin;                   // residual window, RWR rows x RP floats
+   uint32_t offA;                     // A staging, 2 KB per epilogue warp (when stageA)
+   int stageA;                        // A leaves through shared memory and TMA stores
    uint32_t total;                    // dynamic shared memory incl. alignment slack
 };
 
@@ -280,9 +287,9 @@ __device__ __forceinline__ uint32_t pack2(float lo, float hi) {
 template <int S, int P, int C, bool X3>
 __global__ void __launch_bounds__(320, 1) post_tc_kernel(const __grid_constant__ CUtensorMap tmW,
                                                          const __grid_constant__ CUtensorMap tmWlo,
-                                                         const __grid_constant__ CUtensorMap tmV,
-                                                         const __grid_constant__ CUtensorMap tmVst, LcaGeom g,
+                                                         const __grid_constant__ CUtensorMap tmAst, LcaGeom g,
                                                          PostPlan pl, const float *__restrict__ rpad,
+                                                         float *__restrict__ V,
                                                          bf16 *__restrict__ A, bf16 *__restrict__ Alo,
                                                          int *__restrict__ err) {
    constexpr int KP = P * P * C, NKC = KP / 64;
@@ -292,7 +299,7 @@ __global__ void __launch_bounds__(320, 1) post_tc_kernel(const __grid_constant__
    extern __shared__ uint8_t smem_raw[];
    uint8_t *smem = align1024(smem_raw);
    __shared__ __align__(8) uint64_t stFull, stEmpty, imFull, imEmpty, wFull[kMaxWSlots], wEmpty[kMaxWSlots],
-         vFull[kMaxVSlots], vEmpty[kMaxVSlots], accFull[2], accEmpty[2];
+         vFull[kMaxVSlots], vEmpty[kMaxVSlots], accFull[kAcc], accEmpty[kAcc];
    __shared__ uint32_t tmemBase;
    __shared__ volatile int abortFlag;
 
@@ -319,14 +326,14 @@ __global__ void __launch_bounds__(320, 1) post_tc_kernel(const __grid_constant__
          mbar_init(&vFull[i], 1);
          mbar_init(&vEmpty[i], 8);  // one arrival per epilogue warp
       }
-      for (int i = 0; i < 2; i++) {
+      for (int i = 0; i < kAcc; i++) {
          mbar_init(&accFull[i], 1);
          mbar_init(&accEmpty[i], 8);
       }
       abortFlag = 0;
       fence_mbar_init();
    }
-   if (warp == 0) tmem_alloc(&tmemBase, 2 * kPostNT);
+   if (warp == 0) tmem_alloc(&tmemBase, kAcc * kPostNT);
    tc_fence_before();
    __syncthreads();
    tc_fence_after();
@@ -362,6 +369,9 @@ __global__ void __launch_bounds__(320, 1) post_tc_kernel(const __grid_constant__
             bulk_load(smem + pl.offWin, src, winBytes, &stFull);
             rowsIssued = ti + 1;
          };
+         prefetch_tmap(&tmW);
+         if (X3) prefetch_tmap(&tmWlo);
+         if (pl.stageA) prefetch_tmap(&tmAst);
          bool ok = true;
          issue_rows(0);
          for (int q = 0; ok && q < Q; q++) {
@@ -387,10 +397,8 @@ __global__ void __launch_bounds__(320, 1) post_tc_kernel(const __grid_constant__
             wIssued = q + 1;
             const int sv = q % nV, uv = q / nV;
             if (uv > 0 && !(ok = wait_or_abort(&vEmpty[sv], (uint32_t)((uv - 1) & 1)))) break;
-            mbar_arrive_expect_tx(&vFull[sv], 2 * 16384);
-            uint8_t *vt = smem + pl.offVT[sv];
-            tma_load_2d(vt, &tmV, &vFull[sv], f0, rowV);
-            tma_load_2d(vt + 16384, &tmV, &vFull[sv], f0 + 32, rowV);
+            mbar_arrive_expect_tx(&vFull[sv], 32768);
+            bulk_load(smem + pl.offVT[sv], V + v_index(g, b, mb * 128, f0), 32768, &vFull[sv]);
             vIssued = q + 1;
          }
          while (ok && rowsIssued < myTiles) {
@@ -416,10 +424,10 @@ __global__ void __launch_bounds__(320, 1) post_tc_kernel(const __grid_constant__
          int mmaDone = 0;
          bool ok = true;
          for (int q = 0; ok && q < Q; q++) {
-            const int ti = q / nBlk, nb = q % nBlk, sw = q % nW, a = q & 1;
+            const int ti = q / nBlk, nb = q % nBlk, sw = q % nW, a = q % kAcc;
             if (nb == 0 && !(ok = wait_or_abort(&imFull, (uint32_t)(ti & 1)))) break;
             if (!(ok = wait_or_abort(&wFull[sw], (uint32_t)((q / nW) & 1)))) break;
-            if (q >= 2 && !(ok = wait_or_abort(&accEmpty[a], (uint32_t)(((q >> 1) - 1) & 1)))) break;
+            if (q >= kAcc && !(ok = wait_or_abort(&accEmpty[a], (uint32_t)((q / kAcc - 1) & 1)))) break;
             tc_fence_after();
             const uint32_t idesc = idesc_bf16(128, kPostNT);
             const uint32_t d = tmem + a * kPostNT;
@@ -439,81 +447,92 @@ __global__ void __launch_bounds__(320, 1) post_tc_kernel(const __grid_constant__
             mmaDone = q + 1;
          }
          // MMAs still in flight finish before shared memory and TMEM go away
-         if (!ok && mmaDone > 0) mbar_wait(&accFull[(mmaDone - 1) & 1], (uint32_t)(((mmaDone - 1) >> 1) & 1));
+         if (!ok && mmaDone > 0) mbar_wait(&accFull[(mmaDone - 1) % kAcc], (uint32_t)(((mmaDone - 1) / kAcc) & 1));
       }
    } else {
       // ============================== epilogue (warps 0-7) ==============================
       const float *win = reinterpret_cast<const float *>(smem + pl.offWin);
       const int qd = warp & 3, h = warp >> 2;
       const int pw = 32 * qd + lane;  // this thread's position (TMEM lane) in the epilogue
-      int pendingV = -1;              // V slot whose store this warp has in flight (lane 0)
-      // A warp whose wait failed leaves its block loop only; the next tile's barrier sees the
-      // abort flag in that warp and every warp leaves together (no warp skips a barrier).
-      for (int ti = 0; ti < myTiles; ti++) {
-         int b, mb, fh;
-         tile_of(ti, b, mb, fh);
-         if (tid == 0 && wait_or_abort(&stFull, (uint32_t)(ti & 1)) && ti > 0)
-            wait_or_abort(&imEmpty, (uint32_t)((ti - 1) & 1));  // the previous tile's MMAs are done
-         if (named_bar_or(1, EPI, abortFlag != 0)) break;
-         // ---- BF16 im2col of the window (row runs of P*C elements, read in pairs) ----
-         {
-            constexpr int RUN = P * C;
-            constexpr int CPR = RUN / 8;
-            static_assert(RUN % 8 == 0, "patch rows must fill whole 16-byte chunks");
-            const int p = tid & 127, half = tid >> 7;
-            const int yl = p / g.v1Nx, x1 = p % g.v1Nx;
-            const float *src0 = win + (S * yl) * RP + S * x1 * C;
-#pragma unroll 1
-            for (int ky = half * (P / 2); ky < (half + 1) * (P / 2); ky++) {
-               const float2 *src = reinterpret_cast<const float2 *>(src0 + ky * RP);
-#pragma unroll
-               for (int cc = 0; cc < CPR; cc++) {
-                  float vals[8];
-#pragma unroll
-                  for (int jj = 0; jj < 4; jj++) {
-                     const float2 t = src[cc * 4 + jj];
-                     vals[2 * jj] = t.x;
-                     vals[2 * jj + 1] = t.y;
-                  }
-                  uint4 hi;
-                  hi.x = pack2(vals[0], vals[1]);
-                  hi.y = pack2(vals[2], vals[3]);
-                  hi.z = pack2(vals[4], vals[5]);
-                  hi.w = pack2(vals[6], vals[7]);
-                  const int c8 = ky * CPR + cc;
-                  const uint32_t off = (c8 >> 3) * 16384 + sw128_offset(p, (c8 & 7) * 8);
-                  *reinterpret_cast<uint4 *>(smem + pl.offIM + off) = hi;
-                  if (X3) {
-                     const __nv_bfloat162 *h2 = reinterpret_cast<const __nv_bfloat162 *>(&hi);
-                     float2 f01 = __bfloat1622float2(h2[0]), f23 = __bfloat1622float2(h2[1]);
-                     float2 f45 = __bfloat1622float2(h2[2]), f67 = __bfloat1622float2(h2[3]);
-                     uint4 lo;
-                     lo.x = pack2(vals[0] - f01.x, vals[1] - f01.y);
-                     lo.y = pack2(vals[2] - f23.x, vals[3] - f23.y);
-                     lo.z = pack2(vals[4] - f45.x, vals[5] - f45.y);
-                     lo.w = pack2(vals[6] - f67.x, vals[7] - f67.y);
-                     *reinterpret_cast<uint4 *>(smem + pl.offIMlo + off) = lo;
+      int pendingV = -1;              // V slot whose store this warp has in flight
+      // im2col of tile t: all 8 warps, between two named barriers.  A warp whose own wait failed
+      // skips its block work until the next im2col, whose first barrier sees the abort flag in
+      // that warp, so that every warp leaves together (no warp skips a barrier).
+      auto im2col = [&](int t) {
+         if (tid == 0 && wait_or_abort(&stFull, (uint32_t)(t & 1)) && t > 0)
+            wait_or_abort(&imEmpty, (uint32_t)((t - 1) & 1));  // the previous tile's MMAs are done
+         if (named_bar_or(1, EPI, abortFlag != 0)) return false;
+            // ---- BF16 im2col of the window (row runs of P*C elements, read in pairs) ----
+            {
+               constexpr int RUN = P * C;
+               constexpr int CPR = RUN / 8;
+               static_assert(RUN % 8 == 0, "patch rows must fill whole 16-byte chunks");
+               const int p = tid & 127, half = tid >> 7;
+               const int yl = p / g.v1Nx, x1 = p % g.v1Nx;
+               const float *src0 = win + (S * yl) * RP + S * x1 * C;
+   #pragma unroll 1
+               for (int ky = half * (P / 2); ky < (half + 1) * (P / 2); ky++) {
+                  const float2 *src = reinterpret_cast<const float2 *>(src0 + ky * RP);
+   #pragma unroll
+                  for (int cc = 0; cc < CPR; cc++) {
+                     float vals[8];
+   #pragma unroll
+                     for (int jj = 0; jj < 4; jj++) {
+                        const float2 t = src[cc * 4 + jj];
+                        vals[2 * jj] = t.x;
+                        vals[2 * jj + 1] = t.y;
+                     }
+                     uint4 hi;
+                     hi.x = pack2(vals[0], vals[1]);
+                     hi.y = pack2(vals[2], vals[3]);
+                     hi.z = pack2(vals[4], vals[5]);
+                     hi.w = pack2(vals[6], vals[7]);
+                     const int c8 = ky * CPR + cc;
+                     const uint32_t off = (c8 >> 3) * 16384 + sw128_offset(p, (c8 & 7) * 8);
+                     *reinterpret_cast<uint4 *>(smem + pl.offIM + off) = hi;
+                     if (X3) {
+                        const __nv_bfloat162 *h2 = reinterpret_cast<const __nv_bfloat162 *>(&hi);
+                        float2 f01 = __bfloat1622float2(h2[0]), f23 = __bfloat1622float2(h2[1]);
+                        float2 f45 = __bfloat1622float2(h2[2]), f67 = __bfloat1622float2(h2[3]);
+                        uint4 lo;
+                        lo.x = pack2(vals[0] - f01.x, vals[1] - f01.y);
+                        lo.y = pack2(vals[2] - f23.x, vals[3] - f23.y);
+                        lo.z = pack2(vals[4] - f45.x, vals[5] - f45.y);
+                        lo.w = pack2(vals[6] - f67.x, vals[7] - f67.y);
+                        *reinterpret_cast<uint4 *>(smem + pl.offIMlo + off) = lo;
+                     }
                   }
                }
             }
-         }
          fence_proxy_async_smem();
          named_bar_sync(1, EPI);
          if (tid == 0) {
             mbar_arrive(&imFull);
             mbar_arrive(&stEmpty);  // the window is read: the next tile's may land
          }
-
-         // ---- the tile's feature blocks, each warp on its own ----
-         for (int nb = 0; nb < nBlk; nb++) {
-            const int q = ti * nBlk + nb, sv = q % nV, a = q & 1;
-            const int f0 = fh * pl.FT + nb * kPostNT, rowV = b * g.Npos + mb * 128;
-            int okw = 1;
-            if (lane == 0)
-               okw = wait_or_abort(&accFull[a], (uint32_t)((q >> 1) & 1)) &&
-                     wait_or_abort(&vFull[sv], (uint32_t)((q / nV) & 1));
-            okw = __shfl_sync(0xffffffffu, okw, 0);
-            if (!okw) break;
+         return true;
+      };
+      // The next tile's im2col goes in after block kIm of the current one: late enough that the
+      // loads of the current tile's remaining blocks are out and its MMAs (up to 4 blocks ahead)
+      // have released the operand, early enough that the next tile's MMAs run before its blocks.
+      int kIm = nBlk - 1 - lagV;
+      if (kIm < 1) kIm = 1;
+      if (kIm > nBlk - 1) kIm = nBlk - 1;
+      bool go = myTiles > 0 && im2col(0), dead = false;
+      for (int q = 0; go && q < Q; q++) {
+         const int ti = q / nBlk, nb = q % nBlk;
+         int b, mb, fh;
+         tile_of(ti, b, mb, fh);
+         // ---- block q, each warp on its own ----
+         const int sv = q % nV, a = q % kAcc;
+         const int f0 = fh * pl.FT + nb * kPostNT, rowV = b * g.Npos + mb * 128;
+         int okw = !dead;
+         if (lane == 0 && okw)
+            okw = wait_or_abort(&accFull[a], (uint32_t)((q / kAcc) & 1)) &&
+                  wait_or_abort(&vFull[sv], (uint32_t)((q / nV) & 1));
+         okw = __shfl_sync(0xffffffffu, okw, 0);
+         dead = !okw;
+         if (okw) {
             tc_fence_after();
             float d[32], vo[32];
             tmem_ld32(tmem + a * kPostNT + ((uint32_t)(32 * qd) << 16) + 32 * h, d);
@@ -545,19 +564,35 @@ __global__ void __launch_bounds__(320, 1) post_tc_kernel(const __grid_constant__
                   an[jj] = thresh(vn[jj], g);
                }
             }
+            // this warp's previous stores have read shared memory: their V slot goes back to the
+            // loads warp, and the A staging buffer may be rewritten
+            if (lane == 0 && pendingV >= 0) {
+               bulk_wait_read_all();
+               mbar_arrive(&vEmpty[pendingV]);
+            }
+            __syncwarp();
 #pragma unroll
             for (int qq = 0; qq < 8; qq++)
                *reinterpret_cast<float4 *>(vt + ((qq ^ (pw & 7)) << 4)) =
                      make_float4(vn[4 * qq], vn[4 * qq + 1], vn[4 * qq + 2], vn[4 * qq + 3]);
-            bf16 *ag = A + (size_t)(rowV + pw) * g.F + f0 + 32 * h;
+            uint8_t *abuf = smem + pl.offA + warp * 2048;  // 32 rows x 64 B, 64-byte swizzle
+            if (pl.stageA) {
 #pragma unroll
-            for (int t = 0; t < 2; t++)
-               st_global_32B(ag + 16 * t,
-                             make_uint4(pack2(an[16 * t], an[16 * t + 1]), pack2(an[16 * t + 2], an[16 * t + 3]),
-                                        pack2(an[16 * t + 4], an[16 * t + 5]), pack2(an[16 * t + 6], an[16 * t + 7])),
-                             make_uint4(pack2(an[16 * t + 8], an[16 * t + 9]), pack2(an[16 * t + 10], an[16 * t + 11]),
-                                        pack2(an[16 * t + 12], an[16 * t + 13]),
-                                        pack2(an[16 * t + 14], an[16 * t + 15])));
+               for (int c = 0; c < 4; c++)
+                  *reinterpret_cast<uint4 *>(abuf + lane * 64 + ((c ^ ((lane >> 1) & 3)) << 4)) =
+                        make_uint4(pack2(an[8 * c], an[8 * c + 1]), pack2(an[8 * c + 2], an[8 * c + 3]),
+                                   pack2(an[8 * c + 4], an[8 * c + 5]), pack2(an[8 * c + 6], an[8 * c + 7]));
+            } else {
+               bf16 *ag = A + (size_t)(rowV + pw) * g.F + f0 + 32 * h;
+#pragma unroll
+               for (int t = 0; t < 2; t++)
+                  st_global_32B(ag + 16 * t,
+                                make_uint4(pack2(an[16 * t], an[16 * t + 1]), pack2(an[16 * t + 2], an[16 * t + 3]),
+                                           pack2(an[16 * t + 4], an[16 * t + 5]), pack2(an[16 * t + 6], an[16 * t + 7])),
+                                make_uint4(pack2(an[16 * t + 8], an[16 * t + 9]), pack2(an[16 * t + 10], an[16 * t + 11]),
+                                           pack2(an[16 * t + 12], an[16 * t + 13]),
+                                           pack2(an[16 * t + 14], an[16 * t + 15])));
+            }
             if (X3) {
                uint4 *lg = reinterpret_cast<uint4 *>(Alo + (size_t)(rowV + pw) * g.F + f0 + 32 * h);
 #pragma unroll
@@ -571,20 +606,17 @@ __global__ void __launch_bounds__(320, 1) post_tc_kernel(const __grid_constant__
             fence_proxy_async_smem();
             __syncwarp();
             if (lane == 0) {
-               tma_store_2d(&tmVst, vsub, f0 + 32 * h, rowV + 32 * qd);
+               bulk_store(V + v_index(g, b, mb * 128 + 32 * qd, f0 + 32 * h), vsub, 4096);
+               if (pl.stageA) tma_store_2d(&tmAst, abuf, f0 + 32 * h, rowV + 32 * qd);
                bulk_commit();
-               if (nV >= 2) {
-                  if (pendingV >= 0) {
-                     bulk_wait_read_1();  // the previous block's store has read its slot
-                     mbar_arrive(&vEmpty[pendingV]);
-                  }
-                  pendingV = sv;
-               } else {
+               if (nV == 1) {  // the only slot: release it as soon as the store has read it
                   bulk_wait_read_all();
                   mbar_arrive(&vEmpty[sv]);
                }
             }
+            pendingV = nV == 1 ? -1 : sv;
          }
+         if (nb == kIm && ti + 1 < myTiles) go = im2col(ti + 1);
       }
       if (lane == 0) bulk_wait_all();
    }
@@ -592,7 +624,7 @@ __global__ void __launch_bounds__(320, 1) post_tc_kernel(const __grid_constant__
    if (tid == 0 && abortFlag) atomicExch(err, 1);
    tc_fence_before();
    __syncthreads();
-   if (warp == 0) tmem_dealloc(tmem, 2 * kPostNT);
+   if (warp == 0) tmem_dealloc(tmem, kAcc * kPostNT);
 }
 
 // -------------------------------------------------------------------------------------------
@@ -659,10 +691,17 @@ __global__ void prep_weights_kernel(const float *__restrict__ w, int F, int KP, 
 }
 
 // A = T(V) for the initial state, BF16 hi/lo and FP32
+// (i indexes the reference layout [nb][Npos][F]; V is in the device layout of v_index)
+__device__ __forceinline__ size_t v_of(const LcaGeom &g, size_t i) {
+   const int f = (int)(i % g.F);
+   const size_t bp = i / g.F;
+   return v_index(g, (int)(bp / g.Npos), (int)(bp % g.Npos), f);
+}
+
 __global__ void init_activity_kernel(LcaGeom g, const float *__restrict__ V, bf16 *A, bf16 *Alo, float *A32) {
    size_t n = (size_t)g.nb * g.Npos * g.F;
    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-      float a = thresh(V[i], g);
+      float a = thresh(V[v_of(g, i)], g);
       bf16 h = __float2bfloat16_rn(a);
       A[i] = h;
       Alo[i] = __float2bfloat16_rn(a - __bfloat162float(h));
@@ -673,7 +712,16 @@ __global__ void init_activity_kernel(LcaGeom g, const float *__restrict__ V, bf1
 __global__ void activity_out_kernel(LcaGeom g, const float *__restrict__ V, float *__restrict__ out) {
    size_t n = (size_t)g.nb * g.Npos * g.F;
    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-      out[i] = thresh(V[i], g);
+      out[i] = thresh(V[v_of(g, i)], g);
+}
+
+// V between the reference layout and the device layout
+__global__ void v_layout_kernel(LcaGeom g, const float *__restrict__ src, float *__restrict__ dst, int toDevice) {
+   size_t n = (size_t)g.nb * g.Npos * g.F;
+   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+      if (toDevice) dst[v_of(g, i)] = src[i];
+      else dst[i] = src[v_of(g, i)];
+   }
 }
 
 }  // namespace
@@ -693,7 +741,7 @@ struct pvgpu_lca_solver {
    float *rpad = nullptr;  // padded residual x - W^T a (kernel D -> kernel P)
    bf16 *A = nullptr, *Alo = nullptr, *W = nullptr, *Wlo = nullptr, *Wt = nullptr, *Wtlo = nullptr;
    int *err = nullptr;
-   CUtensorMap tmA, tmAlo, tmWt, tmWtlo, tmW, tmWlo, tmV, tmVst;
+   CUtensorMap tmA, tmAlo, tmWt, tmWtlo, tmW, tmWlo, tmAst;
    PostPlan plan, planX3;
    bool weightsSet = false;
    // optional per-kernel timing: events before kernel R, between R and P, after P
@@ -716,10 +764,14 @@ PostPlan make_post_plan(const LcaGeom &g, int S, int P, int C, bool x3, int numS
    const uint32_t RWR = (uint32_t)rwin_rows(S, P, g.rowsPerBlock);
    const uint32_t wB = NKC * kPostNT * 128, imB = NKC * 16384, vtB = 2 * 16384;
    const uint32_t winB = RWR * (uint32_t)pl.RP * 4;
-   // deepest rings that fit: V tiles first (they come from HBM), then weight tiles (from L2)
-   static const int kRings[][2] = {{3, 2}, {3, 1}, {2, 2}, {2, 1}, {1, 1}};
+   // deepest rings that fit, V tiles first (they come from HBM), then weight tiles (from L2);
+   // A staged for TMA stores where it fits with at least two V slots (not in BF16x3 steps,
+   // which also write the low halves)
+   static const int kRings[][3] = {{3, 2, 1}, {3, 1, 1}, {2, 2, 1}, {2, 1, 1}, {3, 2, 0},
+                                   {3, 1, 0}, {2, 2, 0}, {2, 1, 0}, {1, 1, 0}};
    for (const auto &r : kRings) {
-      const int nV = r[0], nW = r[1];
+      const int nV = r[0], nW = r[1], stA = r[2];
+      if (stA && x3) continue;
       uint32_t o = 0;
       pl.offIM = o;
       o = al(o + imB);
@@ -739,9 +791,12 @@ PostPlan make_post_plan(const LcaGeom &g, int S, int P, int C, bool x3, int numS
       }
       pl.offWin = o;
       o = al(o + winB);
+      pl.offA = o;
+      if (stA) o = al(o + 8 * 2048);
       pl.total = o + 1024;
       pl.nV = nV;
       pl.nW = nW;
+      pl.stageA = stA;
       if (pl.total + 256u <= 227u * 1024u) break;  // static shared memory shares the budget
    }
    pl.FT = g.F < 256 ? g.F : 256;
@@ -768,14 +823,14 @@ struct Launcher {
       const PostPlan &pl = X3 ? s->planX3 : s->plan;
       {
          constexpr int E = (P - S) / 2;
-         residual_kernel<C><<<g_num_sms * 4, 256, 0, st>>>(s->g, E, pl.RP, x, s->partials, s->rpad);
+         residual_kernel<C><<<dim3(pl.rowsPad, s->g.nb), 128, 0, st>>>(s->g, E, pl.RP, x, s->partials, s->rpad);
          PVGPU_CHECK_LAUNCH("lca residual");
       }
       if (mid) cudaEventRecord(mid, st);
       auto pk = post_tc_kernel<S, P, C, X3>;
       e = cudaFuncSetAttribute(pk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.total);
       if (e != cudaSuccess) return pvgpu::record_cuda_error(e, "lca post attr");
-      pk<<<pl.G, 320, pl.total, st>>>(s->tmW, s->tmWlo, s->tmV, s->tmVst, s->g, pl, s->rpad, s->A, s->Alo, s->err);
+      pk<<<pl.G, 320, pl.total, st>>>(s->tmW, s->tmWlo, s->tmAst, s->g, pl, s->rpad, s->V, s->A, s->Alo, s->err);
       PVGPU_CHECK_LAUNCH("lca post");
       return PVGPU_OK;
    }
@@ -877,19 +932,15 @@ extern "C" pvgpu_status pvgpu_lca_solver_create(const pvgpu_lca_solver_desc *d, 
         pvgpu::make_tmap_bf16_sw128(&s->tmWtlo, s->Wtlo, KP, g.F, g.F, KP) &&
         pvgpu::make_tmap_bf16_sw128(&s->tmW, s->W, g.F, KP, KP, g.NT) &&
         pvgpu::make_tmap_bf16_sw128(&s->tmWlo, s->Wlo, g.F, KP, KP, g.NT);
-   if (ok) {  // V tile: FP32 [rows][F], box 32 x 128, 128-byte swizzle
+   if (ok) {  // A: BF16 [rows][F], one epilogue warp's 32 x 32 part, 64-byte swizzle
       pvgpu::EncodeTiledFn enc = pvgpu::encode_tiled_fn();
       cuuint64_t dims[2] = {(cuuint64_t)g.F, rowsA};
-      cuuint64_t strides[1] = {(cuuint64_t)g.F * 4};
-      cuuint32_t box[2] = {32, 128};
+      cuuint64_t strides[1] = {(cuuint64_t)g.F * 2};
+      cuuint32_t box[2] = {32, 32};
       cuuint32_t estr[2] = {1, 1};
-      ok = enc && enc(&s->tmV, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, s->V, dims, strides, box, estr,
-                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+      ok = enc && enc(&s->tmAst, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, s->A, dims, strides, box, estr,
+                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                       CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
-      cuuint32_t boxSt[2] = {32, 32};  // one epilogue warp's part of a V tile
-      ok = ok && enc(&s->tmVst, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, s->V, dims, strides, boxSt, estr,
-                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
    }
    if (!ok) {
       free_solver(s);
@@ -936,8 +987,12 @@ extern "C" pvgpu_status pvgpu_lca_solver_reset(pvgpu_lca_solver *s, const float 
    if (!s) return PVGPU_ERR_BAD_ARG;
    cudaStream_t st = pvgpu::as_stream(stream);
    size_t n = (size_t)s->g.nb * s->g.Npos * s->g.F;
-   if (v0) PVGPU_CUDA(cudaMemcpyAsync(s->V, v0, n * 4, cudaMemcpyDeviceToDevice, st), "lca reset");
-   else PVGPU_CUDA(cudaMemsetAsync(s->V, 0, n * 4, st), "lca reset");
+   if (v0) {
+      v_layout_kernel<<<152 * 8, 256, 0, st>>>(s->g, v0, s->V, 1);
+      PVGPU_CHECK_LAUNCH("lca reset");
+   } else {
+      PVGPU_CUDA(cudaMemsetAsync(s->V, 0, n * 4, st), "lca reset");
+   }
    init_activity_kernel<<<152 * 8, 256, 0, st>>>(s->g, s->V, s->A, s->Alo, s->A32);
    PVGPU_CHECK_LAUNCH("lca reset");
    PVGPU_CUDA(cudaMemsetAsync(s->err, 0, sizeof(int), st), "lca reset");
@@ -1005,7 +1060,10 @@ extern "C" pvgpu_status pvgpu_lca_solver_state(pvgpu_lca_solver *s, float *v, fl
    if (!s) return PVGPU_ERR_BAD_ARG;
    cudaStream_t st = pvgpu::as_stream(stream);
    size_t n = (size_t)s->g.nb * s->g.Npos * s->g.F;
-   if (v) PVGPU_CUDA(cudaMemcpyAsync(v, s->V, n * 4, cudaMemcpyDeviceToDevice, st), "lca state");
+   if (v) {
+      v_layout_kernel<<<152 * 8, 256, 0, st>>>(s->g, s->V, v, 0);
+      PVGPU_CHECK_LAUNCH("lca state");
+   }
    if (a) {
       activity_out_kernel<<<152 * 8, 256, 0, st>>>(s->g, s->V, a);
       PVGPU_CHECK_LAUNCH("lca state");

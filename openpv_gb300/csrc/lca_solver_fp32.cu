@@ -161,14 +161,16 @@ __global__ void __launch_bounds__(kThreads) post32_kernel(LcaGeom g, const float
    const float e = g.e, om = __fadd_rn(1.0f, -g.e);
 #pragma unroll
    for (int i = 0; i < 8; i++) {
-      const size_t row = ((size_t)b * g.Npos + mb * 128 + tr + 16 * i) * g.F + f0;
+      const int pos = mb * 128 + tr + 16 * i;
+      const size_t row = ((size_t)b * g.Npos + pos) * g.F + f0;
 #pragma unroll
       for (int j = 0; j < TN; j++) {
          const int f = tc + 16 * j;
-         const float vo = V[row + f];
+         const size_t vi = pvgpu::v_index(g, b, pos, f0 + f);
+         const float vo = V[vi];
          const float ao = pvgpu::lca_thresh(vo, g);
          const float vn = __fadd_rn(__fmul_rn(e, vo), __fmul_rn(om, __fadd_rn(acc[i][j], __fmul_rn(g.si, ao))));
-         V[row + f] = vn;
+         V[vi] = vn;
          A32[row + f] = pvgpu::lca_thresh(vn, g);
       }
    }

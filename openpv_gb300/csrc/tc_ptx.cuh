@@ -168,6 +168,14 @@ __device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t b
                 : "memory");
 }
 
+// Contiguous shared -> global copy (16-byte aligned addresses, size a multiple of 16),
+// bulk-group completion.
+__device__ __forceinline__ void bulk_store(void *dst, const void *src, uint32_t bytes) {
+   asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(reinterpret_cast<uint64_t>(dst)),
+                "r"(smem_u32(src)), "r"(bytes)
+                : "memory");
+}
+
 // Tiled shared -> global store through a tensor map (bulk-group completion).
 __device__ __forceinline__ void tma_store_2d(const CUtensorMap *map, const void *src, int c0, int c1) {
    asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%2, %3}], [%1];"
