@@ -74,161 +74,251 @@ __device__ __forceinline__ void tmem_ld_cols(uint32_t taddr, float *v) {
 }
 
 // -------------------------------------------------------------------------------------------
-// Kernel R: reconstruction partials
+// Kernel R: reconstruction W^T a and the residual x - W^T a (persistent, warp-specialised)
+//
+// One CTA per SM walks images blockIdx.x, +G, ...  Per image and 128-position block mb:
+//   D[pos][k] = sum_f A[pos][f] * W[f][k],  k = (ky*P + kx)*C + c  (M = 128, N = P*P*C, K = F)
+// Roles:
+//   warp 4, lane 0 (loads): the image's x (bulk copy, two buffers) and, per block and chunk of
+//                           64 features, the A tile [128 x 64] and the W^T tile [P*P*C x 64] by
+//                           TMA into a ring of nStage stages;
+//   warp 5, lane 0 (MMA):   per block the tcgen05.mma chain over F into one of two TMEM
+//                           accumulators (256 columns apart);
+//   warps 0-3 (fold):       thread = position (TMEM lane).  The fold of D into the image (patch
+//                           (ky,kx) of position (y,x) lands on pixel (S*y - E + ky, S*x - E + kx))
+//                           runs in (P/S)^2 tap groups; one group holds one tap of each
+//                           pixel-parity class, so no two threads touch a pixel inside a group,
+//                           and every pixel sums its contributions in the same fixed order
+//                           (blocks in order, groups in order) -- deterministic, no atomics.
+//                           After the image's last block: the residual r = x - recon, written
+//                           with a zero border of E pixels and rows padded to RP floats (the
+//                           layout kernel P bulk-copies its windows from), then the image
+//                           buffer is cleared for the next image.
+// Hand-offs (full/empty mbarriers): full/empty per stage, accFull/accEmpty per accumulator,
+// xFull/xEmpty per x buffer.  Waits are bounded; a timeout raises the abort flag, the roles
+// drain their copies and MMAs in flight, and the kernel reports through *err.
 // -------------------------------------------------------------------------------------------
+struct ReconPlan {
+   int G;              // persistent CTAs
+   int nStage;         // A / W^T ring stages
+   int RP, rowsPad;    // padded residual rows
+   uint32_t stageBytes, offStage, offRec, offX[2];
+   uint32_t total;
+};
+
+constexpr int kMaxRStages = 4;
+
 template <int S, int P, int C, bool X3>
-__global__ void __launch_bounds__(128) recon_tc_kernel(const __grid_constant__ CUtensorMap tmA,
-                                                       const __grid_constant__ CUtensorMap tmAlo,
-                                                       const __grid_constant__ CUtensorMap tmWt,
-                                                       const __grid_constant__ CUtensorMap tmWtlo, LcaGeom g,
-                                                       float *__restrict__ partials, int *__restrict__ err) {
+__global__ void __launch_bounds__(192, 1) recon_tc_kernel(const __grid_constant__ CUtensorMap tmA,
+                                                          const __grid_constant__ CUtensorMap tmAlo,
+                                                          const __grid_constant__ CUtensorMap tmWt,
+                                                          const __grid_constant__ CUtensorMap tmWtlo, LcaGeom g,
+                                                          ReconPlan rp, const float *__restrict__ x,
+                                                          float *__restrict__ rpad, int *__restrict__ err) {
    constexpr int KP = P * P * C;
    constexpr int E = (P - S) / 2;
-   constexpr uint32_t NCOLS = KP <= 32 ? 32 : (KP <= 64 ? 64 : (KP <= 128 ? 128 : 256));
-   constexpr int BYTES_A = 128 * 64 * 2, BYTES_W = KP * 64 * 2, STAGE = BYTES_A + BYTES_W;
+   constexpr uint32_t BA = 128 * 64 * 2, BW = KP * 64 * 2;  // one A tile, one W^T tile
+   constexpr int FOLD = 128;                                // fold threads (warps 0-3)
+   static_assert(KP <= 256 && KP % 16 == 0, "one MMA N = P*P*C <= 256");
    extern __shared__ uint8_t smem_raw[];
    uint8_t *smem = align1024(smem_raw);
-   uint8_t *sA[2] = {smem, smem + STAGE};
-   uint8_t *sW[2] = {smem + BYTES_A, smem + STAGE + BYTES_A};
-   float *recon = reinterpret_cast<float *>(smem + 2 * STAGE);
-   __shared__ __align__(8) uint64_t full[2], empty[2], done;
+   __shared__ __align__(8) uint64_t full[kMaxRStages], empty[kMaxRStages], accFull[2], accEmpty[2], xFull[2],
+         xEmpty[2];
    __shared__ uint32_t tmemBase;
-   __shared__ int failed;
+   __shared__ volatile int abortFlag;
 
-   const int tid = threadIdx.x, warp = tid >> 5;
-   const int b = blockIdx.x / g.MB, mb = blockIdx.x % g.MB;
-   const int rowA = b * g.Npos + mb * 128;
+   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+   const int myImages = blockIdx.x < g.nb ? (g.nb - 1 - blockIdx.x) / rp.G + 1 : 0;
+   const int nkc = g.F / 64;
+   const int nStage = rp.nStage;
+   const int nPix = g.inNx * g.inNy * C;
+
    if (tid == 0) {
-      mbar_init(&full[0], 1);
-      mbar_init(&full[1], 1);
-      mbar_init(&empty[0], 1);
-      mbar_init(&empty[1], 1);
-      mbar_init(&done, 1);
+      for (int i = 0; i < kMaxRStages; i++) {
+         mbar_init(&full[i], 1);
+         mbar_init(&empty[i], 1);
+      }
+      for (int i = 0; i < 2; i++) {
+         mbar_init(&accFull[i], 1);
+         mbar_init(&accEmpty[i], 4);  // one arrival per fold warp
+         mbar_init(&xFull[i], 1);
+         mbar_init(&xEmpty[i], 1);
+      }
+      abortFlag = 0;
       fence_mbar_init();
-      failed = 0;
    }
-   if (warp == 0) tmem_alloc(&tmemBase, NCOLS);
+   if (warp == 0) tmem_alloc(&tmemBase, 512);
    tc_fence_before();
    __syncthreads();
    tc_fence_after();
    const uint32_t tmem = tmemBase;
 
-   if (tid == 0) {
-      const int nkc = g.F / 64;
-      const int total = (X3 ? 3 : 1) * nkc;
-      const uint32_t idesc = idesc_bf16(128, KP);
-      auto issue = [&](int j, int s) {
-         const int pass = j / nkc, kc = j % nkc;
-         const CUtensorMap *ma = (X3 && pass == 2) ? &tmAlo : &tmA;
-         const CUtensorMap *mw = (X3 && pass == 1) ? &tmWtlo : &tmWt;
-         mbar_arrive_expect_tx(&full[s], STAGE);
-         tma_load_2d(sA[s], ma, &full[s], kc * 64, rowA);
-         tma_load_2d(sW[s], mw, &full[s], kc * 64, 0);
-      };
-      int issued = 0, consumed = 0;
-      for (; issued < total && issued < 2; issued++) issue(issued, issued);
-      bool ok = true;
-      for (int j = 0; j < total; j++) {
-         const int s = j & 1;
-         const uint32_t ph = (j >> 1) & 1;
-         if (!mbar_wait(&full[s], ph)) {
-            ok = false;
-            break;
+   auto wait_or_abort = [&](uint64_t *bar, uint32_t parity) {
+      if (abortFlag) return false;
+      if (mbar_wait(bar, parity)) return true;
+      abortFlag = 1;
+      return false;
+   };
+   auto last_use = [](int n, int sl, int slots) { return sl < n ? n - 1 - ((n - 1 - sl) % slots) : -1; };
+
+   if (warp == 4) {
+      // ============================== loads ==============================
+      if (lane == 0 && myImages > 0) {
+         prefetch_tmap(&tmA);
+         prefetch_tmap(&tmWt);
+         if (X3) {
+            prefetch_tmap(&tmAlo);
+            prefetch_tmap(&tmWtlo);
          }
-         consumed++;
-         tc_fence_after();
-         const uint32_t a0 = smem_u32(sA[s]), w0 = smem_u32(sW[s]);
-#pragma unroll
-         for (int k = 0; k < 4; k++) mma_bf16(tmem, sdesc_sw128(a0 + k * 32), sdesc_sw128(w0 + k * 32), idesc, (j | k) != 0);
-         mma_commit(&empty[s]);
-         if (j + 2 < total) {
-            if (!mbar_wait(&empty[s], ph)) {
-               ok = false;
-               break;
-            }
-            issue(j + 2, s);
-            issued++;
-         }
-      }
-      mma_commit(&done);
-      if (!ok) {
-         failed = 1;
-         for (int i = consumed; i < issued; i++) mbar_wait(&full[i & 1], (i >> 1) & 1);
-      }
-   }
-   const int nPix = g.inNx * g.inNy * C;
-   for (int i = tid; i < nPix; i += 128) recon[i] = 0.0f;
-   __syncthreads();
-   const bool ok = __syncthreads_and(failed == 0 && mbar_wait(&done, 0));
-   tc_fence_after();
-   if (ok) {
-      // fold: thread = position (TMEM lane)
-      const uint32_t lanes = tmem + ((uint32_t)(warp * 32) << 16);
-      const int pos = mb * 128 + tid;
-      const int y1 = pos / g.v1Nx, x1 = pos % g.v1Nx;
-      const int py0 = S * y1 - E, px0 = S * x1 - E;
-#pragma unroll 1
-      for (int ty = 0; ty < P / S; ty++) {
-         float rowv[S][P * C];
-#pragma unroll
-         for (int dy = 0; dy < S; dy++) tmem_ld_cols<P * C>(lanes + (uint32_t)((S * ty + dy) * P * C), rowv[dy]);
-#pragma unroll
-         for (int tx = 0; tx < P / S; tx++) {
-#pragma unroll
-            for (int dy = 0; dy < S; dy++) {
-               const int py = py0 + S * ty + dy;
-#pragma unroll
-               for (int dx = 0; dx < S; dx++) {
-                  const int kx = S * tx + dx, px = px0 + kx;
-                  if (py >= 0 && py < g.inNy && px >= 0 && px < g.inNx) {
-                     float *rp = recon + (py * g.inNx + px) * C;
-#pragma unroll
-                     for (int c = 0; c < C; c++) rp[c] += rowv[dy][kx * C + c];
+         int issued = 0, xIssued = 0;
+         bool ok = true;
+         for (int ti = 0; ok && ti < myImages; ti++) {
+            const int b = blockIdx.x + ti * rp.G;
+            for (int mb = 0; ok && mb < g.MB; mb++) {
+               const int rowA = b * g.Npos + mb * 128;
+               for (int kc = 0; kc < nkc; kc++) {
+                  const int j = issued, st = j % nStage, u = j / nStage;
+                  if (u > 0 && !(ok = wait_or_abort(&empty[st], (uint32_t)((u - 1) & 1)))) break;
+                  uint8_t *base = smem + rp.offStage + st * rp.stageBytes;
+                  mbar_arrive_expect_tx(&full[st], (X3 ? 2 : 1) * (BA + BW));
+                  tma_load_2d(base, &tmA, &full[st], kc * 64, rowA);
+                  tma_load_2d(base + BA, &tmWt, &full[st], kc * 64, 0);
+                  if (X3) {
+                     tma_load_2d(base + BA + BW, &tmAlo, &full[st], kc * 64, rowA);
+                     tma_load_2d(base + 2 * BA + BW, &tmWtlo, &full[st], kc * 64, 0);
                   }
+                  issued++;
+               }
+               if (ok && mb == 0) {
+                  // the image's x, into buffer ti % 2 once image ti-2's residual has read it
+                  const int xb = ti & 1;
+                  if (ti >= 2 && !(ok = wait_or_abort(&xEmpty[xb], (uint32_t)(((ti >> 1) - 1) & 1)))) break;
+                  mbar_arrive_expect_tx(&xFull[xb], (uint32_t)nPix * 4);
+                  bulk_load(smem + rp.offX[xb], x + (size_t)b * nPix, (uint32_t)nPix * 4, &xFull[xb]);
+                  xIssued = ti + 1;
                }
             }
-            __syncthreads();
+         }
+         if (!ok) {
+            for (int sl = 0; sl < nStage; sl++) {
+               const int u = last_use(issued, sl, nStage);
+               if (u >= 0) mbar_wait(&full[sl], (uint32_t)((u / nStage) & 1));
+            }
+            for (int sl = 0; sl < 2; sl++) {
+               const int u = last_use(xIssued, sl, 2);
+               if (u >= 0) mbar_wait(&xFull[sl], (uint32_t)((u / 2) & 1));
+            }
          }
       }
-      float *out = partials + ((size_t)b * g.MB + mb) * nPix;
-      for (int i = tid; i < nPix; i += 128) out[i] = recon[i];
-   } else if (tid == 0) {
-      atomicExch(err, 1);
+   } else if (warp == 5) {
+      // ============================== MMA ==============================
+      if (lane == 0 && myImages > 0) {
+         const uint32_t idesc = idesc_bf16(128, KP);
+         int j = 0, blk = 0, mmaBlocks = 0;
+         bool ok = true;
+         for (int ti = 0; ok && ti < myImages; ti++) {
+            for (int mb = 0; ok && mb < g.MB; mb++, blk++) {
+               const int a = blk & 1;
+               if (blk >= 2 && !(ok = wait_or_abort(&accEmpty[a], (uint32_t)(((blk >> 1) - 1) & 1)))) break;
+               const uint32_t d = tmem + a * 256;
+               for (int kc = 0; kc < nkc; kc++, j++) {
+                  const int st = j % nStage;
+                  if (!(ok = wait_or_abort(&full[st], (uint32_t)((j / nStage) & 1)))) break;
+                  tc_fence_after();
+                  const uint32_t base = smem_u32(smem + rp.offStage + st * rp.stageBytes);
+                  const int npass = X3 ? 3 : 1;
+                  for (int pass = 0; pass < npass; pass++) {
+                     // hi x hi, then hi x lo(W), then lo(A) x hi
+                     const uint32_t a0 = base + ((X3 && pass == 2) ? BA + BW : 0);
+                     const uint32_t w0 = base + ((X3 && pass == 1) ? 2 * BA + BW : BA);
+#pragma unroll
+                     for (int k = 0; k < 4; k++)
+                        mma_bf16(d, sdesc_sw128(a0 + k * 32), sdesc_sw128(w0 + k * 32), idesc, (kc | pass | k) != 0);
+                  }
+                  mma_commit(&empty[st]);
+               }
+               if (!ok) break;
+               mma_commit(&accFull[a]);
+               mmaBlocks = blk + 1;
+            }
+         }
+         if (!ok && mmaBlocks > 0) mbar_wait(&accFull[(mmaBlocks - 1) & 1], (uint32_t)(((mmaBlocks - 1) >> 1) & 1));
+      }
+   } else {
+      // ============================== fold and residual (warps 0-3) ==============================
+      float *recon = reinterpret_cast<float *>(smem + rp.offRec);
+      for (int i = tid; i < nPix; i += FOLD) recon[i] = 0.0f;
+      named_bar_sync(1, FOLD);
+      int blk = 0;
+      for (int ti = 0; ti < myImages; ti++) {
+         const int b = blockIdx.x + ti * rp.G;
+         bool stop = false;
+         for (int mb = 0; mb < g.MB; mb++, blk++) {
+            const int a = blk & 1;
+            if (tid == 0) wait_or_abort(&accFull[a], (uint32_t)((blk >> 1) & 1));
+            if ((stop = named_bar_or(1, FOLD, abortFlag != 0))) break;
+            tc_fence_after();
+            const uint32_t lanes = tmem + a * 256 + ((uint32_t)(warp * 32) << 16);
+            const int pos = mb * 128 + tid;
+            const int y1 = pos / g.v1Nx, x1 = pos % g.v1Nx;
+            const int py0 = S * y1 - E, px0 = S * x1 - E;
+#pragma unroll 1
+            for (int ty = 0; ty < P / S; ty++) {
+               float rowv[S][P * C];
+#pragma unroll
+               for (int dy = 0; dy < S; dy++) tmem_ld_cols<P * C>(lanes + (uint32_t)((S * ty + dy) * P * C), rowv[dy]);
+               if (ty == P / S - 1) {
+                  tc_fence_before();
+                  if (lane == 0) mbar_arrive(&accEmpty[a]);  // this warp has read the accumulator
+               }
+#pragma unroll
+               for (int tx = 0; tx < P / S; tx++) {
+#pragma unroll
+                  for (int dy = 0; dy < S; dy++) {
+                     const int py = py0 + S * ty + dy;
+#pragma unroll
+                     for (int dx = 0; dx < S; dx++) {
+                        const int kx = S * tx + dx, px = px0 + kx;
+                        if (py >= 0 && py < g.inNy && px >= 0 && px < g.inNx) {
+                           float *rpx = recon + (py * g.inNx + px) * C;
+#pragma unroll
+                           for (int c = 0; c < C; c++) rpx[c] += rowv[dy][kx * C + c];
+                        }
+                     }
+                  }
+                  named_bar_sync(1, FOLD);
+               }
+            }
+         }
+         if (stop) break;
+         // ---- residual of image b into the padded layout ----
+         const int xb = ti & 1;
+         if (tid == 0) wait_or_abort(&xFull[xb], (uint32_t)((ti >> 1) & 1));
+         if (named_bar_or(1, FOLD, abortFlag != 0)) break;
+         const float *xs = reinterpret_cast<const float *>(smem + rp.offX[xb]);
+         float *out = rpad + (size_t)b * rp.rowsPad * rp.RP;
+         const int rowElems = g.inNx * C;
+         for (int i = tid; i < rp.rowsPad * rp.RP; i += FOLD) {
+            const int yp = i / rp.RP, col = i - yp * rp.RP;
+            const int ye = yp - E, j = col - E * C;
+            float v = 0.0f;
+            if (ye >= 0 && ye < g.inNy && j >= 0 && j < rowElems) {
+               const int pi = ye * rowElems + j;
+               v = __fadd_rn(xs[pi], -recon[pi]);
+            }
+            out[i] = v;
+         }
+         named_bar_sync(1, FOLD);
+         if (tid == 0) mbar_arrive(&xEmpty[xb]);  // x buffer free for image ti+2
+         for (int i = tid; i < nPix; i += FOLD) recon[i] = 0.0f;
+         named_bar_sync(1, FOLD);
+      }
    }
+   __syncthreads();
+   if (tid == 0 && abortFlag) atomicExch(err, 1);
    tc_fence_before();
    __syncthreads();
-   if (warp == 0) tmem_dealloc(tmem, NCOLS);
-}
-
-// -------------------------------------------------------------------------------------------
-// Kernel D ("residual"): r = x - (sum of the image's partial reconstructions, in block order),
-// written with a zero border of E pixels on every side and rows padded to RP floats
-// (RP = (inNx + 2E) * C rounded up to a multiple of 4), so that the receptive-field window of
-// a 128-position block is one contiguous run of rows for a single bulk copy.  The zero border
-// is the restricted error layer's halo.
-// -------------------------------------------------------------------------------------------
-template <int C>
-__global__ void __launch_bounds__(128) residual_kernel(LcaGeom g, int E, int RP, const float *__restrict__ x,
-                                                       const float *__restrict__ partials, float *__restrict__ rpad) {
-   // grid: (padded row, image)
-   const int yp = blockIdx.x, b = blockIdx.y, ye = yp - E;
-   const int rowsPad = gridDim.x;
-   float *out = rpad + ((size_t)b * rowsPad + yp) * RP;
-   const bool inside = ye >= 0 && ye < g.inNy;
-   const int nPix = g.inNx * g.inNy * C, rowElems = g.inNx * C;
-   const int yc = inside ? ye : 0;
-   const float *pb = partials + (size_t)b * g.MB * nPix + (size_t)yc * rowElems;
-   const float *xb = x + (size_t)b * nPix + (size_t)yc * rowElems;
-   for (int col = threadIdx.x; col < RP; col += blockDim.x) {
-      const int j = col - E * C;  // element within the error row
-      float v = 0.0f;
-      if (inside && j >= 0 && j < rowElems) {
-         float rec = pb[j];
-         for (int m = 1; m < g.MB; m++) rec = __fadd_rn(rec, pb[(size_t)m * nPix + j]);
-         v = __fadd_rn(xb[j], -rec);
-      }
-      out[col] = v;
-   }
+   if (warp == 0) tmem_dealloc(tmem, 512);
 }
 
 // -------------------------------------------------------------------------------------------
@@ -631,19 +721,31 @@ __global__ void __launch_bounds__(320, 1) post_tc_kernel(const __grid_constant__
 // Probe energy: l2Coeff * sum r^2 + costCoeff * sum cost(T(V)), per image, FP64
 // (ColumnEnergyProbe.cpp:60-70 over L2NormProbe and L1NormLCAProbe / FirmThresholdCostFnLCAProbe)
 // -------------------------------------------------------------------------------------------
+// The residual comes from the padded residual of kernel R (zero border) when rpad is given,
+// else from x and the partial reconstructions of the FP32 form.
 __global__ void __launch_bounds__(256) energy_kernel(LcaGeom g, int C, const float *__restrict__ x,
-                                                     const float *__restrict__ partials, const float *__restrict__ V,
-                                                     double l2Coeff, int costKind, double cp0, double cp1,
-                                                     double costCoeff, double *__restrict__ out) {
+                                                     const float *__restrict__ partials,
+                                                     const float *__restrict__ rpad, int padPerImage,
+                                                     const float *__restrict__ V, double l2Coeff, int costKind,
+                                                     double cp0, double cp1, double costCoeff,
+                                                     double *__restrict__ out) {
    const int b = blockIdx.x;
    const int nPix = g.inNx * g.inNy * C;
-   const float *pb = partials + (size_t)b * g.MB * nPix;
    double l2 = 0.0, cost = 0.0;
-   for (int i = threadIdx.x; i < nPix; i += 256) {
-      float rec = pb[i];
-      for (int m = 1; m < g.MB; m++) rec = __fadd_rn(rec, pb[(size_t)m * nPix + i]);
-      double r = (double)__fadd_rn(x[(size_t)b * nPix + i], -rec);
-      l2 += r * r;
+   if (rpad) {
+      const float *rb = rpad + (size_t)b * padPerImage;
+      for (int i = threadIdx.x; i < padPerImage; i += 256) {
+         double r = (double)rb[i];
+         l2 += r * r;
+      }
+   } else {
+      const float *pb = partials + (size_t)b * g.MB * nPix;
+      for (int i = threadIdx.x; i < nPix; i += 256) {
+         float rec = pb[i];
+         for (int m = 1; m < g.MB; m++) rec = __fadd_rn(rec, pb[(size_t)m * nPix + i]);
+         double r = (double)__fadd_rn(x[(size_t)b * nPix + i], -rec);
+         l2 += r * r;
+      }
    }
    const double tw = cp0 + cp1, maxc = 0.5 * tw, qc = 0.5 / tw;
    const float *vb = V + (size_t)b * g.Npos * g.F;
@@ -743,6 +845,8 @@ struct pvgpu_lca_solver {
    int *err = nullptr;
    CUtensorMap tmA, tmAlo, tmWt, tmWtlo, tmW, tmWlo, tmAst;
    PostPlan plan, planX3;
+   ReconPlan rplan, rplanX3;
+   bool padValid = false;  // rpad holds the residual of the last step (BF16 form) rather than partials
    bool weightsSet = false;
    // optional per-kernel timing: events before kernel R, between R and P, after P
    std::vector<cudaEvent_t> ev;
@@ -806,27 +910,44 @@ PostPlan make_post_plan(const LcaGeom &g, int S, int P, int C, bool x3, int numS
    return pl;
 }
 
+ReconPlan make_recon_plan(const LcaGeom &g, int S, int P, int C, bool x3, int numSms) {
+   const int KP = P * P * C, E = (P - S) / 2;
+   auto al = [](uint32_t v) { return (v + 1023u) & ~1023u; };
+   ReconPlan rp;
+   std::memset(&rp, 0, sizeof(rp));
+   rp.RP = ((g.inNx + 2 * E) * C + 3) & ~3;
+   rp.rowsPad = g.inNy + 2 * E;
+   rp.stageBytes = al((x3 ? 2u : 1u) * (128u * 64u * 2u + (uint32_t)KP * 64u * 2u));
+   const uint32_t imgB = al((uint32_t)(g.inNx * g.inNy * C) * 4u);
+   for (int n = kMaxRStages; n >= 2; n--) {
+      rp.nStage = n;
+      rp.offStage = 0;
+      uint32_t o = n * rp.stageBytes;
+      rp.offRec = o;
+      o += imgB;
+      rp.offX[0] = o;
+      o += imgB;
+      rp.offX[1] = o;
+      o += imgB;
+      rp.total = o + 1024;
+      if (rp.total + 512u <= 227u * 1024u) break;
+   }
+   rp.G = numSms < g.nb ? numSms : g.nb;
+   return rp;
+}
+
 template <int S, int P, int C>
 struct Launcher {
-   static size_t recon_smem(const pvgpu_lca_solver *s) {
-      constexpr int KP = P * P * C;
-      return 1024 + 2 * (size_t)(128 * 64 * 2 + KP * 64 * 2) + (size_t)s->g.inNx * s->g.inNy * C * 4;
-   }
    template <bool X3>
    static pvgpu_status step(pvgpu_lca_solver *s, const float *x, cudaStream_t st, cudaEvent_t mid) {
-      size_t rs = recon_smem(s);
+      const ReconPlan &rp = X3 ? s->rplanX3 : s->rplan;
       auto rk = recon_tc_kernel<S, P, C, X3>;
-      cudaError_t e = cudaFuncSetAttribute(rk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rs);
+      cudaError_t e = cudaFuncSetAttribute(rk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rp.total);
       if (e != cudaSuccess) return pvgpu::record_cuda_error(e, "lca recon attr");
-      rk<<<s->g.nb * s->g.MB, 128, rs, st>>>(s->tmA, s->tmAlo, s->tmWt, s->tmWtlo, s->g, s->partials, s->err);
+      rk<<<rp.G, 192, rp.total, st>>>(s->tmA, s->tmAlo, s->tmWt, s->tmWtlo, s->g, rp, x, s->rpad, s->err);
       PVGPU_CHECK_LAUNCH("lca recon");
-      const PostPlan &pl = X3 ? s->planX3 : s->plan;
-      {
-         constexpr int E = (P - S) / 2;
-         residual_kernel<C><<<dim3(pl.rowsPad, s->g.nb), 128, 0, st>>>(s->g, E, pl.RP, x, s->partials, s->rpad);
-         PVGPU_CHECK_LAUNCH("lca residual");
-      }
       if (mid) cudaEventRecord(mid, st);
+      const PostPlan &pl = X3 ? s->planX3 : s->plan;
       auto pk = post_tc_kernel<S, P, C, X3>;
       e = cudaFuncSetAttribute(pk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.total);
       if (e != cudaSuccess) return pvgpu::record_cuda_error(e, "lca post attr");
@@ -835,9 +956,8 @@ struct Launcher {
       return PVGPU_OK;
    }
    static bool fits(const pvgpu_lca_solver *s, bool x3) {
-      size_t lim = 227 * 1024;
-      if (recon_smem(s) > lim) return false;
-      return (x3 ? s->planX3.total : s->plan.total) <= lim;
+      const size_t lim = 227 * 1024 - 512;  // static shared memory shares the budget
+      return (x3 ? s->rplanX3.total : s->rplan.total) <= lim && (x3 ? s->planX3.total : s->plan.total) <= lim;
    }
    static pvgpu_status run_step(pvgpu_lca_solver *s, const float *x, bool x3, cudaStream_t st, cudaEvent_t mid) {
       return x3 ? step<true>(s, x, st, mid) : step<false>(s, x, st, mid);
@@ -874,6 +994,7 @@ extern "C" pvgpu_status pvgpu_lca_solver_create(const pvgpu_lca_solver_desc *d, 
    const int P = d->nxp, C = d->inNf, KP = P * P * C;
    const int Npos = d->v1Nx * d->v1Ny;
    if (Npos % 128 || 128 % d->v1Nx || KP % 64 || KP > 256 || d->v1Nf % 64) return PVGPU_ERR_UNSUPPORTED_SHAPE;
+   if ((d->inNx * d->inNy * d->inNf) % 4) return PVGPU_ERR_UNSUPPORTED_SHAPE;  // an image is bulk-copied (16-byte multiple)
    if (dispatch(S, P, C, [](auto) { return PVGPU_OK; }) != PVGPU_OK) return PVGPU_ERR_UNSUPPORTED_SHAPE;
    pvgpu_lca_solver *s = new (std::nothrow) pvgpu_lca_solver();
    if (!s) return PVGPU_ERR_OOM;
@@ -954,6 +1075,8 @@ extern "C" pvgpu_status pvgpu_lca_solver_create(const pvgpu_lca_solver_desc *d, 
    }
    s->plan = make_post_plan(g, S, P, C, false, g_num_sms);
    s->planX3 = make_post_plan(g, S, P, C, true, g_num_sms);
+   s->rplan = make_recon_plan(g, S, P, C, false, g_num_sms);
+   s->rplanX3 = make_recon_plan(g, S, P, C, true, g_num_sms);
    bool fits = true;
    dispatch(S, P, C, [&](auto L) {
       fits = L.fits(s, false);
@@ -997,6 +1120,7 @@ extern "C" pvgpu_status pvgpu_lca_solver_reset(pvgpu_lca_solver *s, const float 
    PVGPU_CHECK_LAUNCH("lca reset");
    PVGPU_CUDA(cudaMemsetAsync(s->err, 0, sizeof(int), st), "lca reset");
    s->stepsRun = 0;
+   s->padValid = false;
    return PVGPU_OK;
 }
 
@@ -1018,6 +1142,7 @@ extern "C" pvgpu_status pvgpu_lca_solver_run(pvgpu_lca_solver *s, const float *x
          }
       }
       s->stepsRun += numSteps;
+      if (numSteps > 0) s->padValid = false;
       return PVGPU_OK;
    }
    if (precision != PVGPU_LCA_BF16) return PVGPU_ERR_BAD_ARG;
@@ -1043,6 +1168,7 @@ extern "C" pvgpu_status pvgpu_lca_solver_run(pvgpu_lca_solver *s, const float *x
       }
    }
    s->stepsRun += numSteps;
+   if (numSteps > 0) s->padValid = true;
    return PVGPU_OK;
 }
 
@@ -1050,8 +1176,10 @@ extern "C" pvgpu_status pvgpu_lca_solver_energy(pvgpu_lca_solver *s, const float
                                                 double costThresh, double costWidth, double costCoeff,
                                                 double *energy, void *stream) {
    if (!s || !x || !energy || (costKind != 1 && costKind != 2)) return PVGPU_ERR_BAD_ARG;
-   energy_kernel<<<s->g.nb, 256, 0, pvgpu::as_stream(stream)>>>(s->g, s->C, x, s->partials, s->V, l2Coeff, costKind,
-                                                                costThresh, costWidth, costCoeff, energy);
+   energy_kernel<<<s->g.nb, 256, 0, pvgpu::as_stream(stream)>>>(s->g, s->C, x, s->partials,
+                                                                s->padValid ? s->rpad : nullptr, s->rplan.rowsPad * s->rplan.RP,
+                                                                s->V, l2Coeff, costKind, costThresh, costWidth,
+                                                                costCoeff, energy);
    PVGPU_CHECK_LAUNCH("lca energy");
    return PVGPU_OK;
 }
