@@ -50,8 +50,11 @@ using pvgpu::rwin_cols;
 using pvgpu::rwin_rows;
 using pvgpu::v_index;
 
+// Rounds a pointer into the dynamic shared array up to 1024 bytes by adding an offset to it
+// (not through an integer), so that accesses through the result stay shared-memory accesses.
 __device__ __forceinline__ uint8_t *align1024(uint8_t *p) {
-   return reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(p) + 1023) & ~uintptr_t(1023));
+   const uint32_t a = smem_u32(p);
+   return p + ((1024u - (a & 1023u)) & 1023u);
 }
 
 __device__ __forceinline__ float thresh(float v, const LcaGeom &g) { return pvgpu::lca_thresh(v, g); }
@@ -74,52 +77,62 @@ __device__ __forceinline__ void tmem_ld_cols(uint32_t taddr, float *v) {
 }
 
 // -------------------------------------------------------------------------------------------
-// Kernel R: reconstruction W^T a and the residual x - W^T a (persistent, warp-specialised)
+// Kernel R: reconstruction W^T a and the residual x - W^T a (persistent, warp-specialised,
+// clusters of two CTAs sharing the weight stream)
 //
-// One CTA per SM walks images blockIdx.x, +G, ...  Per image and 128-position block mb:
+// Each cluster (a pair of SMs) walks units of two images; CTA r of the pair takes image 2u + r
+// (the second CTA of an odd batch's last unit has no image and only takes part in the weight
+// stream).  Per image and 128-position block mb:
 //   D[pos][k] = sum_f A[pos][f] * W[f][k],  k = (ky*P + kx)*C + c  (M = 128, N = P*P*C, K = F)
 // Roles:
-//   warp 4, lane 0 (loads): the image's x (bulk copy, two buffers) and, per block and chunk of
-//                           64 features, the A tile [128 x 64] and the W^T tile [P*P*C x 64] by
-//                           TMA into a ring of nStage stages;
-//   warp 5, lane 0 (MMA):   per block the tcgen05.mma chain over F into one of two TMEM
-//                           accumulators (256 columns apart);
-//   warps 0-3 (fold):       thread = position (TMEM lane).  The fold of D into the image (patch
-//                           (ky,kx) of position (y,x) lands on pixel (S*y - E + ky, S*x - E + kx))
-//                           runs in (P/S)^2 tap groups; one group holds one tap of each
-//                           pixel-parity class, so no two threads touch a pixel inside a group,
-//                           and every pixel sums its contributions in the same fixed order
-//                           (blocks in order, groups in order) -- deterministic, no atomics.
-//                           After the image's last block: the residual r = x - recon, written
-//                           with a zero border of E pixels and rows padded to RP floats (the
-//                           layout kernel P bulk-copies its windows from), then the image
-//                           buffer is cleared for the next image.
-// Hand-offs (full/empty mbarriers): full/empty per stage, accFull/accEmpty per accumulator,
-// xFull/xEmpty per x buffer.  Waits are bounded; a timeout raises the abort flag, the roles
-// drain their copies and MMAs in flight, and the kernel reports through *err.
+//   warp 8, lane 0 (loads): per block and chunk of 64 features, into one stage of an nStage
+//                           ring: its own A tile [128 x 64] by TMA, and half of the W^T tile
+//                           [P*P*C x 64] by TMA multicast to both CTAs (each CTA fetches half and
+//                           receives the whole tile, so a weight byte crosses each SM's L2 port
+//                           once per pair); plus each image's x (bulk copy, two buffers);
+//   warp 9, lane 0 (MMA):   per block the tcgen05.mma chain over F into one of two TMEM
+//                           accumulators (256 columns apart); each stage is released by a
+//                           commit multicast to both CTAs, so a stage is refilled only when both
+//                           CTAs' MMAs are done with it;
+//   warps 0-7 (fold):       thread = position (TMEM lane) and half of the patch rows.  The fold
+//                           of D into the image (patch (ky,kx) of position (y,x) lands on pixel
+//                           (S*y - E + ky, S*x - E + kx)) runs in (P/S)^2 tap groups; one group
+//                           holds one tap of each pixel-parity class, so no two threads touch a
+//                           pixel inside a group, and every pixel sums its contributions in the
+//                           same fixed order (blocks in order, groups in order) -- deterministic,
+//                           no atomics.  After the image's last block: the residual
+//                           r = x - recon with a zero border of E pixels and rows padded to RP
+//                           floats (the layout kernel P bulk-copies its windows from); the image
+//                           buffer is then cleared.
+// Hand-offs (mbarriers): full (local, armed with the bytes the CTA receives) / empty (two
+// arrivals: both CTAs' commits) per stage, accFull / accEmpty per accumulator, xFull / xEmpty
+// per x buffer.  Waits are bounded; a timeout raises the abort flag, the roles drain their
+// copies and MMAs in flight, and the kernel reports through *err.  The pair meets at a cluster
+// barrier after the barriers are initialised and before either CTA exits.
 // -------------------------------------------------------------------------------------------
+constexpr int kMaxRStages = 4;
+
 struct ReconPlan {
-   int G;              // persistent CTAs
-   int nStage;         // A / W^T ring stages
+   int G;              // persistent CTAs (clusters of two)
+   int nStage;         // A + W^T ring stages
    int RP, rowsPad;    // padded residual rows
-   uint32_t stageBytes, offStage, offRec, offX[2];
+   uint32_t stageBytes, offRec, offX[2];
    uint32_t total;
 };
 
-constexpr int kMaxRStages = 4;
-
 template <int S, int P, int C, bool X3>
-__global__ void __launch_bounds__(192, 1) recon_tc_kernel(const __grid_constant__ CUtensorMap tmA,
-                                                          const __grid_constant__ CUtensorMap tmAlo,
-                                                          const __grid_constant__ CUtensorMap tmWt,
-                                                          const __grid_constant__ CUtensorMap tmWtlo, LcaGeom g,
-                                                          ReconPlan rp, const float *__restrict__ x,
-                                                          float *__restrict__ rpad, int *__restrict__ err) {
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(320, 1)
+      recon_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmAlo,
+                      const __grid_constant__ CUtensorMap tmWtH, const __grid_constant__ CUtensorMap tmWtloH,
+                      LcaGeom g, ReconPlan rp, const float *__restrict__ x, float *__restrict__ rpad,
+                      int *__restrict__ err) {
    constexpr int KP = P * P * C;
    constexpr int E = (P - S) / 2;
    constexpr uint32_t BA = 128 * 64 * 2, BW = KP * 64 * 2;  // one A tile, one W^T tile
-   constexpr int FOLD = 128;                                // fold threads (warps 0-3)
-   static_assert(KP <= 256 && KP % 16 == 0, "one MMA N = P*P*C <= 256");
+   constexpr uint32_t AB = (X3 ? 2 : 1) * BA;                 // A part of a stage (hi, lo)
+   constexpr int FOLD = 256;                                  // fold threads (warps 0-7)
+   static_assert(KP <= 256 && KP % 16 == 0, "one MMA N = P*P*C <= 256, halves of whole 8-row atoms");
+   static_assert(S % 2 == 0, "the fold splits the patch rows of a stride in two halves");
    extern __shared__ uint8_t smem_raw[];
    uint8_t *smem = align1024(smem_raw);
    __shared__ __align__(8) uint64_t full[kMaxRStages], empty[kMaxRStages], accFull[2], accEmpty[2], xFull[2],
@@ -128,19 +141,24 @@ __global__ void __launch_bounds__(192, 1) recon_tc_kernel(const __grid_constant_
    __shared__ volatile int abortFlag;
 
    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-   const int myImages = blockIdx.x < g.nb ? (g.nb - 1 - blockIdx.x) / rp.G + 1 : 0;
+   const uint32_t crank = cluster_ctarank();
+   constexpr uint16_t kPair = 3;
+   const int pairIdx = blockIdx.x >> 1, nPairs = gridDim.x >> 1;
+   const int nUnits = (g.nb + 1) >> 1;
+   const int myUnits = pairIdx < nUnits ? (nUnits - 1 - pairIdx) / nPairs + 1 : 0;
    const int nkc = g.F / 64;
    const int nStage = rp.nStage;
    const int nPix = g.inNx * g.inNy * C;
+   auto image_of = [&](int ui) { return 2 * (pairIdx + ui * nPairs) + (int)crank; };
 
    if (tid == 0) {
       for (int i = 0; i < kMaxRStages; i++) {
          mbar_init(&full[i], 1);
-         mbar_init(&empty[i], 1);
+         mbar_init(&empty[i], 2);  // both CTAs' MMA commits
       }
       for (int i = 0; i < 2; i++) {
          mbar_init(&accFull[i], 1);
-         mbar_init(&accEmpty[i], 4);  // one arrival per fold warp
+         mbar_init(&accEmpty[i], 8);  // one arrival per fold warp
          mbar_init(&xFull[i], 1);
          mbar_init(&xEmpty[i], 1);
       }
@@ -149,7 +167,7 @@ __global__ void __launch_bounds__(192, 1) recon_tc_kernel(const __grid_constant_
    }
    if (warp == 0) tmem_alloc(&tmemBase, 512);
    tc_fence_before();
-   __syncthreads();
+   cluster_sync();  // the peer multicasts into this CTA's stages and barriers from here on
    tc_fence_after();
    const uint32_t tmem = tmemBase;
 
@@ -161,41 +179,44 @@ __global__ void __launch_bounds__(192, 1) recon_tc_kernel(const __grid_constant_
    };
    auto last_use = [](int n, int sl, int slots) { return sl < n ? n - 1 - ((n - 1 - sl) % slots) : -1; };
 
-   if (warp == 4) {
+   if (warp == 8) {
       // ============================== loads ==============================
-      if (lane == 0 && myImages > 0) {
+      if (lane == 0 && myUnits > 0) {
          prefetch_tmap(&tmA);
-         prefetch_tmap(&tmWt);
+         prefetch_tmap(&tmWtH);
          if (X3) {
             prefetch_tmap(&tmAlo);
-            prefetch_tmap(&tmWtlo);
+            prefetch_tmap(&tmWtloH);
          }
          int issued = 0, xIssued = 0;
          bool ok = true;
-         for (int ti = 0; ok && ti < myImages; ti++) {
-            const int b = blockIdx.x + ti * rp.G;
+         for (int ui = 0; ok && ui < myUnits; ui++) {
+            const int b = image_of(ui);
+            const bool ghost = b >= g.nb;
             for (int mb = 0; ok && mb < g.MB; mb++) {
                const int rowA = b * g.Npos + mb * 128;
                for (int kc = 0; kc < nkc; kc++) {
                   const int j = issued, st = j % nStage, u = j / nStage;
                   if (u > 0 && !(ok = wait_or_abort(&empty[st], (uint32_t)((u - 1) & 1)))) break;
-                  uint8_t *base = smem + rp.offStage + st * rp.stageBytes;
-                  mbar_arrive_expect_tx(&full[st], (X3 ? 2 : 1) * (BA + BW));
-                  tma_load_2d(base, &tmA, &full[st], kc * 64, rowA);
-                  tma_load_2d(base + BA, &tmWt, &full[st], kc * 64, 0);
-                  if (X3) {
-                     tma_load_2d(base + BA + BW, &tmAlo, &full[st], kc * 64, rowA);
-                     tma_load_2d(base + 2 * BA + BW, &tmWtlo, &full[st], kc * 64, 0);
+                  uint8_t *base = smem + st * rp.stageBytes;
+                  mbar_arrive_expect_tx(&full[st], (ghost ? 0u : AB) + (X3 ? 2u : 1u) * BW);
+                  if (!ghost) {
+                     tma_load_2d(base, &tmA, &full[st], kc * 64, rowA);
+                     if (X3) tma_load_2d(base + BA, &tmAlo, &full[st], kc * 64, rowA);
                   }
+                  // this CTA's half of the W^T tile, to both CTAs
+                  const uint32_t hoff = crank * (BW / 2);
+                  tma_load_2d_mc(base + AB + hoff, &tmWtH, &full[st], kc * 64, (int)crank * (KP / 2), kPair);
+                  if (X3) tma_load_2d_mc(base + AB + BW + hoff, &tmWtloH, &full[st], kc * 64, (int)crank * (KP / 2), kPair);
                   issued++;
                }
-               if (ok && mb == 0) {
-                  // the image's x, into buffer ti % 2 once image ti-2's residual has read it
-                  const int xb = ti & 1;
-                  if (ti >= 2 && !(ok = wait_or_abort(&xEmpty[xb], (uint32_t)(((ti >> 1) - 1) & 1)))) break;
+               if (ok && mb == 0 && !ghost) {
+                  // the image's x, into buffer ui % 2 once the residual of unit ui-2 has read it
+                  const int xb = ui & 1;
+                  if (ui >= 2 && !(ok = wait_or_abort(&xEmpty[xb], (uint32_t)(((ui >> 1) - 1) & 1)))) break;
                   mbar_arrive_expect_tx(&xFull[xb], (uint32_t)nPix * 4);
                   bulk_load(smem + rp.offX[xb], x + (size_t)b * nPix, (uint32_t)nPix * 4, &xFull[xb]);
-                  xIssued = ti + 1;
+                  xIssued = ui + 1;
                }
             }
          }
@@ -210,79 +231,107 @@ __global__ void __launch_bounds__(192, 1) recon_tc_kernel(const __grid_constant_
             }
          }
       }
-   } else if (warp == 5) {
+   } else if (warp == 9) {
       // ============================== MMA ==============================
-      if (lane == 0 && myImages > 0) {
+      if (lane == 0 && myUnits > 0) {
          const uint32_t idesc = idesc_bf16(128, KP);
          int j = 0, blk = 0, mmaBlocks = 0;
          bool ok = true;
-         for (int ti = 0; ok && ti < myImages; ti++) {
-            for (int mb = 0; ok && mb < g.MB; mb++, blk++) {
+         for (int ui = 0; ok && ui < myUnits; ui++) {
+            const bool ghost = image_of(ui) >= g.nb;
+            for (int mb = 0; ok && mb < g.MB; mb++) {
                const int a = blk & 1;
-               if (blk >= 2 && !(ok = wait_or_abort(&accEmpty[a], (uint32_t)(((blk >> 1) - 1) & 1)))) break;
+               if (!ghost && blk >= 2 && !(ok = wait_or_abort(&accEmpty[a], (uint32_t)(((blk >> 1) - 1) & 1)))) break;
                const uint32_t d = tmem + a * 256;
                for (int kc = 0; kc < nkc; kc++, j++) {
                   const int st = j % nStage;
                   if (!(ok = wait_or_abort(&full[st], (uint32_t)((j / nStage) & 1)))) break;
-                  tc_fence_after();
-                  const uint32_t base = smem_u32(smem + rp.offStage + st * rp.stageBytes);
-                  const int npass = X3 ? 3 : 1;
-                  for (int pass = 0; pass < npass; pass++) {
-                     // hi x hi, then hi x lo(W), then lo(A) x hi
-                     const uint32_t a0 = base + ((X3 && pass == 2) ? BA + BW : 0);
-                     const uint32_t w0 = base + ((X3 && pass == 1) ? 2 * BA + BW : BA);
+                  if (!ghost) {
+                     tc_fence_after();
+                     const uint32_t base = smem_u32(smem + st * rp.stageBytes);
+                     const int npass = X3 ? 3 : 1;
+                     for (int pass = 0; pass < npass; pass++) {
+                        // hi x hi, then hi x lo(W), then lo(A) x hi
+                        const uint32_t a0 = base + ((X3 && pass == 2) ? BA : 0);
+                        const uint32_t w0 = base + AB + ((X3 && pass == 1) ? BW : 0);
 #pragma unroll
-                     for (int k = 0; k < 4; k++)
-                        mma_bf16(d, sdesc_sw128(a0 + k * 32), sdesc_sw128(w0 + k * 32), idesc, (kc | pass | k) != 0);
+                        for (int k = 0; k < 4; k++)
+                           mma_bf16(d, sdesc_sw128(a0 + k * 32), sdesc_sw128(w0 + k * 32), idesc, (kc | pass | k) != 0);
+                     }
                   }
-                  mma_commit(&empty[st]);
+                  mma_commit_mc(&empty[st], kPair);  // the stage is free here once both CTAs are done
                }
                if (!ok) break;
-               mma_commit(&accFull[a]);
-               mmaBlocks = blk + 1;
+               if (!ghost) {
+                  mma_commit(&accFull[a]);
+                  blk++;
+                  mmaBlocks = blk;
+               }
             }
          }
          if (!ok && mmaBlocks > 0) mbar_wait(&accFull[(mmaBlocks - 1) & 1], (uint32_t)(((mmaBlocks - 1) >> 1) & 1));
       }
-   } else {
-      // ============================== fold and residual (warps 0-3) ==============================
+   } else if (warp < 8) {
+      // ============================== fold and residual (warps 0-7) ==============================
+      // thread = (position p = tid % 128, row half hh = tid / 128): inside a tap group the
+      // thread adds the taps of its position whose patch row parity dy lies in its half, so the
+      // two halves touch different pixel rows and the pixels of a group stay disjoint.
+      constexpr int DH = S / 2;  // patch rows per half
       float *recon = reinterpret_cast<float *>(smem + rp.offRec);
       for (int i = tid; i < nPix; i += FOLD) recon[i] = 0.0f;
       named_bar_sync(1, FOLD);
+      const int p = tid & 127, hh = tid >> 7;
       int blk = 0;
-      for (int ti = 0; ti < myImages; ti++) {
-         const int b = blockIdx.x + ti * rp.G;
+      for (int ui = 0; ui < myUnits; ui++) {
+         const int b = image_of(ui);
+         if (b >= g.nb) break;  // only the last unit can lack an image
          bool stop = false;
          for (int mb = 0; mb < g.MB; mb++, blk++) {
             const int a = blk & 1;
             if (tid == 0) wait_or_abort(&accFull[a], (uint32_t)((blk >> 1) & 1));
             if ((stop = named_bar_or(1, FOLD, abortFlag != 0))) break;
             tc_fence_after();
-            const uint32_t lanes = tmem + a * 256 + ((uint32_t)(warp * 32) << 16);
-            const int pos = mb * 128 + tid;
+            const uint32_t lanes = tmem + a * 256 + ((uint32_t)((warp & 3) * 32) << 16);
+            const int pos = mb * 128 + p;
             const int y1 = pos / g.v1Nx, x1 = pos % g.v1Nx;
             const int py0 = S * y1 - E, px0 = S * x1 - E;
 #pragma unroll 1
             for (int ty = 0; ty < P / S; ty++) {
-               float rowv[S][P * C];
+               float rowv[DH][P * C];
 #pragma unroll
-               for (int dy = 0; dy < S; dy++) tmem_ld_cols<P * C>(lanes + (uint32_t)((S * ty + dy) * P * C), rowv[dy]);
+               for (int dd = 0; dd < DH; dd++)
+                  tmem_ld_cols<P * C>(lanes + (uint32_t)((S * ty + hh * DH + dd) * P * C), rowv[dd]);
                if (ty == P / S - 1) {
                   tc_fence_before();
                   if (lane == 0) mbar_arrive(&accEmpty[a]);  // this warp has read the accumulator
                }
 #pragma unroll
                for (int tx = 0; tx < P / S; tx++) {
+                  // the group's pixels of this thread: all loads, then all stores (they are
+                  // distinct, so the adds need not wait on one another)
+                  float old[DH][S][C];
+                  bool in[DH][S];
 #pragma unroll
-                  for (int dy = 0; dy < S; dy++) {
-                     const int py = py0 + S * ty + dy;
+                  for (int dd = 0; dd < DH; dd++) {
+                     const int py = py0 + S * ty + hh * DH + dd;
 #pragma unroll
                      for (int dx = 0; dx < S; dx++) {
-                        const int kx = S * tx + dx, px = px0 + kx;
-                        if (py >= 0 && py < g.inNy && px >= 0 && px < g.inNx) {
-                           float *rpx = recon + (py * g.inNx + px) * C;
+                        const int px = px0 + S * tx + dx;
+                        in[dd][dx] = py >= 0 && py < g.inNy && px >= 0 && px < g.inNx;
 #pragma unroll
-                           for (int c = 0; c < C; c++) rpx[c] += rowv[dy][kx * C + c];
+                        for (int c = 0; c < C; c++) old[dd][dx][c] = in[dd][dx] ? recon[(py * g.inNx + px) * C + c] : 0.0f;
+                     }
+                  }
+#pragma unroll
+                  for (int dd = 0; dd < DH; dd++) {
+                     const int py = py0 + S * ty + hh * DH + dd;
+#pragma unroll
+                     for (int dx = 0; dx < S; dx++) {
+                        const int px = px0 + S * tx + dx;
+                        if (in[dd][dx]) {
+#pragma unroll
+                           for (int c = 0; c < C; c++)
+                              recon[(py * g.inNx + px) * C + c] = old[dd][dx][c] + rowv[dd][(S * tx + dx) * C + c];
                         }
                      }
                   }
@@ -292,24 +341,28 @@ __global__ void __launch_bounds__(192, 1) recon_tc_kernel(const __grid_constant_
          }
          if (stop) break;
          // ---- residual of image b into the padded layout ----
-         const int xb = ti & 1;
-         if (tid == 0) wait_or_abort(&xFull[xb], (uint32_t)((ti >> 1) & 1));
+         const int xb = ui & 1;
+         if (tid == 0) wait_or_abort(&xFull[xb], (uint32_t)((ui >> 1) & 1));
          if (named_bar_or(1, FOLD, abortFlag != 0)) break;
          const float *xs = reinterpret_cast<const float *>(smem + rp.offX[xb]);
          float *out = rpad + (size_t)b * rp.rowsPad * rp.RP;
          const int rowElems = g.inNx * C;
-         for (int i = tid; i < rp.rowsPad * rp.RP; i += FOLD) {
-            const int yp = i / rp.RP, col = i - yp * rp.RP;
-            const int ye = yp - E, j = col - E * C;
-            float v = 0.0f;
-            if (ye >= 0 && ye < g.inNy && j >= 0 && j < rowElems) {
-               const int pi = ye * rowElems + j;
-               v = __fadd_rn(xs[pi], -recon[pi]);
+         // trip counts uniform across each warp (a divergent inner loop costs far more than
+         // the predicated body)
+         const int RPl = rp.RP, rowsPadl = rp.rowsPad, inNyl = g.inNy;
+         for (int c0 = 0; c0 < RPl; c0 += 128) {
+            const int col = c0 + p, j = col - E * C;
+            const bool colIn = col < RPl, colX = j >= 0 && j < rowElems;
+#pragma unroll 4
+            for (int yp = hh; yp < rowsPadl; yp += 2) {
+               const int ye = yp - E;
+               float v = 0.0f;
+               if (colX && ye >= 0 && ye < inNyl) v = __fadd_rn(xs[ye * rowElems + j], -recon[ye * rowElems + j]);
+               if (colIn) out[(size_t)yp * RPl + col] = v;
             }
-            out[i] = v;
          }
          named_bar_sync(1, FOLD);
-         if (tid == 0) mbar_arrive(&xEmpty[xb]);  // x buffer free for image ti+2
+         if (tid == 0) mbar_arrive(&xEmpty[xb]);  // x buffer free for unit ui+2
          for (int i = tid; i < nPix; i += FOLD) recon[i] = 0.0f;
          named_bar_sync(1, FOLD);
       }
@@ -317,7 +370,7 @@ __global__ void __launch_bounds__(192, 1) recon_tc_kernel(const __grid_constant_
    __syncthreads();
    if (tid == 0 && abortFlag) atomicExch(err, 1);
    tc_fence_before();
-   __syncthreads();
+   cluster_sync();  // neither CTA leaves while the other may still write into it
    if (warp == 0) tmem_dealloc(tmem, 512);
 }
 
@@ -843,7 +896,7 @@ struct pvgpu_lca_solver {
    float *rpad = nullptr;  // padded residual x - W^T a (kernel D -> kernel P)
    bf16 *A = nullptr, *Alo = nullptr, *W = nullptr, *Wlo = nullptr, *Wt = nullptr, *Wtlo = nullptr;
    int *err = nullptr;
-   CUtensorMap tmA, tmAlo, tmWt, tmWtlo, tmW, tmWlo, tmAst;
+   CUtensorMap tmA, tmAlo, tmWtH, tmWtloH, tmW, tmWlo, tmAst;  // tmWtH*: half-height W^T tiles
    PostPlan plan, planX3;
    ReconPlan rplan, rplanX3;
    bool padValid = false;  // rpad holds the residual of the last step (BF16 form) rather than partials
@@ -910,7 +963,7 @@ PostPlan make_post_plan(const LcaGeom &g, int S, int P, int C, bool x3, int numS
    return pl;
 }
 
-ReconPlan make_recon_plan(const LcaGeom &g, int S, int P, int C, bool x3, int numSms) {
+ReconPlan make_recon_plan(const LcaGeom &g, int S, int P, int C, bool x3, int maxPairs) {
    const int KP = P * P * C, E = (P - S) / 2;
    auto al = [](uint32_t v) { return (v + 1023u) & ~1023u; };
    ReconPlan rp;
@@ -921,7 +974,6 @@ ReconPlan make_recon_plan(const LcaGeom &g, int S, int P, int C, bool x3, int nu
    const uint32_t imgB = al((uint32_t)(g.inNx * g.inNy * C) * 4u);
    for (int n = kMaxRStages; n >= 2; n--) {
       rp.nStage = n;
-      rp.offStage = 0;
       uint32_t o = n * rp.stageBytes;
       rp.offRec = o;
       o += imgB;
@@ -932,7 +984,8 @@ ReconPlan make_recon_plan(const LcaGeom &g, int S, int P, int C, bool x3, int nu
       rp.total = o + 1024;
       if (rp.total + 512u <= 227u * 1024u) break;
    }
-   rp.G = numSms < g.nb ? numSms : g.nb;
+   const int units = (g.nb + 1) / 2;
+   rp.G = 2 * (maxPairs < units ? maxPairs : units);
    return rp;
 }
 
@@ -944,7 +997,7 @@ struct Launcher {
       auto rk = recon_tc_kernel<S, P, C, X3>;
       cudaError_t e = cudaFuncSetAttribute(rk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rp.total);
       if (e != cudaSuccess) return pvgpu::record_cuda_error(e, "lca recon attr");
-      rk<<<rp.G, 192, rp.total, st>>>(s->tmA, s->tmAlo, s->tmWt, s->tmWtlo, s->g, rp, x, s->rpad, s->err);
+      rk<<<rp.G, 320, rp.total, st>>>(s->tmA, s->tmAlo, s->tmWtH, s->tmWtloH, s->g, rp, x, s->rpad, s->err);
       PVGPU_CHECK_LAUNCH("lca recon");
       if (mid) cudaEventRecord(mid, st);
       const PostPlan &pl = X3 ? s->planX3 : s->plan;
@@ -954,6 +1007,25 @@ struct Launcher {
       pk<<<pl.G, 320, pl.total, st>>>(s->tmW, s->tmWlo, s->tmAst, s->g, pl, s->rpad, s->V, s->A, s->Alo, s->err);
       PVGPU_CHECK_LAUNCH("lca post");
       return PVGPU_OK;
+   }
+   // clusters of two recon CTAs that can be resident at once (one CTA per SM)
+   static int max_pairs(const ReconPlan &rp, bool x3) {
+      const void *fn = x3 ? reinterpret_cast<const void *>(recon_tc_kernel<S, P, C, true>)
+                          : reinterpret_cast<const void *>(recon_tc_kernel<S, P, C, false>);
+      if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rp.total) != cudaSuccess) {
+         cudaGetLastError();
+         return 0;
+      }
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(2 * 76, 1, 1);
+      cfg.blockDim = dim3(320, 1, 1);
+      cfg.dynamicSmemBytes = rp.total;
+      int n = 0;
+      if (cudaOccupancyMaxActiveClusters(&n, fn, &cfg) != cudaSuccess) {
+         cudaGetLastError();
+         return 0;
+      }
+      return n;
    }
    static bool fits(const pvgpu_lca_solver *s, bool x3) {
       const size_t lim = 227 * 1024 - 512;  // static shared memory shares the budget
@@ -1049,8 +1121,8 @@ extern "C" pvgpu_status pvgpu_lca_solver_create(const pvgpu_lca_solver_desc *d, 
    const uint64_t rowsA = (uint64_t)g.nb * Npos;
    ok = pvgpu::make_tmap_bf16_sw128(&s->tmA, s->A, rowsA, g.F, g.F, 128) &&
         pvgpu::make_tmap_bf16_sw128(&s->tmAlo, s->Alo, rowsA, g.F, g.F, 128) &&
-        pvgpu::make_tmap_bf16_sw128(&s->tmWt, s->Wt, KP, g.F, g.F, KP) &&
-        pvgpu::make_tmap_bf16_sw128(&s->tmWtlo, s->Wtlo, KP, g.F, g.F, KP) &&
+        pvgpu::make_tmap_bf16_sw128(&s->tmWtH, s->Wt, KP, g.F, g.F, KP / 2) &&
+        pvgpu::make_tmap_bf16_sw128(&s->tmWtloH, s->Wtlo, KP, g.F, g.F, KP / 2) &&
         pvgpu::make_tmap_bf16_sw128(&s->tmW, s->W, g.F, KP, KP, g.NT) &&
         pvgpu::make_tmap_bf16_sw128(&s->tmWlo, s->Wlo, g.F, KP, KP, g.NT);
    if (ok) {  // A: BF16 [rows][F], one epilogue warp's 32 x 32 part, 64-byte swizzle
@@ -1075,8 +1147,17 @@ extern "C" pvgpu_status pvgpu_lca_solver_create(const pvgpu_lca_solver_desc *d, 
    }
    s->plan = make_post_plan(g, S, P, C, false, g_num_sms);
    s->planX3 = make_post_plan(g, S, P, C, true, g_num_sms);
-   s->rplan = make_recon_plan(g, S, P, C, false, g_num_sms);
-   s->rplanX3 = make_recon_plan(g, S, P, C, true, g_num_sms);
+   s->rplan = make_recon_plan(g, S, P, C, false, g_num_sms / 2);
+   s->rplanX3 = make_recon_plan(g, S, P, C, true, g_num_sms / 2);
+   dispatch(S, P, C, [&](auto L) {
+      // as many pairs as can be resident together (the kernel is persistent)
+      for (int x3 = 0; x3 < 2; x3++) {
+         ReconPlan &rp = x3 ? s->rplanX3 : s->rplan;
+         const int n = L.max_pairs(rp, x3 != 0);
+         if (n > 0) rp = make_recon_plan(g, S, P, C, x3 != 0, std::min(n, g_num_sms / 2));
+      }
+      return PVGPU_OK;
+   });
    bool fits = true;
    dispatch(S, P, C, [&](auto L) {
       fits = L.fits(s, false);

@@ -211,6 +211,38 @@ __device__ __forceinline__ void st_global_32B(void *p, uint4 a, uint4 b) {
                 : "memory");
 }
 
+// ---- clusters ----------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t cluster_ctarank() {
+   uint32_t r;
+   asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+   return r;
+}
+
+// Every thread of every CTA of the cluster (release / acquire).
+__device__ __forceinline__ void cluster_sync() {
+   asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+// TMA tile load delivered to the same shared-memory offset in every CTA of `mask`, each CTA's
+// mbarrier at the offset of `bar` receiving the bytes it got.
+__device__ __forceinline__ void tma_load_2d_mc(void *dst, const CUtensorMap *map, uint64_t *bar, int c0, int c1,
+                                               uint16_t mask) {
+   asm volatile(
+         "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes.multicast::cluster"
+         " [%0], [%1, {%2, %3}], [%4], %5;" ::"r"(smem_u32(dst)),
+         "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(smem_u32(bar)), "h"(mask)
+         : "memory");
+}
+
+// Arrive on the mbarrier at the offset of `bar` in every CTA of `mask` once every tcgen05.mma
+// this thread issued so far has completed.
+__device__ __forceinline__ void mma_commit_mc(uint64_t *bar, uint16_t mask) {
+   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(
+                      smem_u32(bar)),
+                "h"(mask)
+                : "memory");
+}
+
 // Barrier among `count` threads (a multiple of 32) on hardware barrier `id` (1..15).
 __device__ __forceinline__ void named_bar_sync(int id, int count) {
    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
