@@ -387,13 +387,22 @@ def run_ours(args, rank, world, local_rank):
     npix = int(np.prod(cfg["in_shape"]))
     mb = npos // 128
     x3_frac = X3 / T
-    # per image-timestep: V read + write (FP32), A written (BF16; + BF16 lo in BF16x3 steps),
-    # the input and the partial reconstructions read once
-    post_bytes_unit = npos * F * (4 + 4 + 2 + 2 * x3_frac) + (mb + 1) * npix * 4
+    # per image-timestep, kernel P: V read + write (FP32), A written (BF16; + BF16 lo in BF16x3
+    # steps), and the padded residual window of each (128-position, feature-tile) tile read once
+    S = cfg["in_shape"][1] // cfg["v1_shape"][1]
+    P, C = cfg["nxp"], cfg["in_shape"][2]
+    E = (P - S) // 2
+    rows_per_block = 128 // cfg["v1_shape"][1]
+    RP = -(-(cfg["in_shape"][1] + 2 * E) * C // 4) * 4
+    rows_pad = cfg["in_shape"][0] + 2 * E
+    FT = min(F, 256)
+    window_bytes = (S * (rows_per_block - 1) + P) * RP * 4
+    post_bytes_unit = npos * F * (4 + 4 + 2 + 2 * x3_frac) + mb * (F // FT) * window_bytes
     post_bytes_launch = post_bytes_unit * nb
     post_avg_ms = post_ms / nprof
     achieved = post_bytes_launch / (post_avg_ms / 1000.0) / 1e9
-    recon_bytes_unit = npos * F * (2 + 2 * x3_frac) + mb * npix * 4
+    # kernel R: A read (BF16; + lo), x read, the padded residual written
+    recon_bytes_unit = npos * F * (2 + 2 * x3_frac) + npix * 4 + rows_pad * RP * 4
     recon_avg_ms = recon_ms / nprof
     recon_flops_launch = 2 * npos * F * (cfg["nxp"] ** 2 * cfg["in_shape"][2]) * nb * (1 + 2 * x3_frac)
 
@@ -428,7 +437,7 @@ def run_ours(args, rank, world, local_rank):
                    "l2": "state streamed each timestep (V 134 MB + activity 67 MB per step > 129 MB L2)"},
         "gpu_launches": args.steps * (2 * T + 2),
         "e2e": {"value": e2e_value, "unit": "images*steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-        "roofline": {"bound": "hbm", "kernel": "post_tc_kernel (residual + post delivery GEMM + LCA update)",
+        "roofline": {"bound": "hbm", "kernel": "post_tc_kernel (post delivery GEMM + LCA update, residual windows in)",
                      "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": achieved / pk["hbm_gbs"],
                      "peak_source": pk["source"], "traffic": traffic, "bytes_per_launch": post_bytes_launch,
                      "avg_launch_ms": post_avg_ms, "share_of_step": post_ms / (post_ms + recon_ms)},
