@@ -172,6 +172,198 @@ __global__ void __launch_bounds__(kWarps * 32) deliver_pre_kernel(PreGeom g, con
    }
 }
 
+// -------------------------------------------------------------------------------------------
+// FAST mode, one-to-one connections (pre and post of the same size): row-sliding kernel.
+//
+// A CTA owns 8 post columns (one per warp) x RS post rows x all nfp features (lane = FPL
+// consecutive features).  It walks the presynaptic extended rows that reach its rows in
+// ascending order -- the SparseList order -- and each warp keeps one register accumulator per
+// patch row in a circular buffer: presynaptic row ye adds to post rows ye - Hy + ky, slot
+// (ye - Hy + ky) mod NYP, and once row ye is done post row ye - Hy has all its contributions
+// and is added into GSyn (one read-modify-write per output, no atomics).  Unrolling the row
+// loop by NYP makes every slot index a compile-time constant.  Each active entry is read and
+// decoded once per warp and feeds NYP x FPL FMAs per lane; its weights W[f][ky][kx][*] come
+// through the read-only path (one coalesced 32*FPL-float row per ky).  The entry range of a
+// row inside the CTA's column window comes from a binary search per row, done in parallel by
+// the CTA's threads up front.  Order per output: presynaptic rows ascending, entries ascending
+// -- deterministic, not the reference's (that is what REFERENCE_ORDER mode is for).
+// -------------------------------------------------------------------------------------------
+constexpr int kRowsRS = 32;      // post rows per CTA
+constexpr int kRowsMax = 64;     // presynaptic rows a CTA may visit (RS + NYP - 1)
+
+template <int FPL>
+struct VecF;
+template <>
+struct VecF<1> {
+   using T = float;
+   __device__ static void ld(const float *p, float *v) { v[0] = __ldg(p); }
+   __device__ static void rmw(float *p, const float *v) { p[0] += v[0]; }
+};
+template <>
+struct VecF<2> {
+   __device__ static void ld(const float *p, float *v) {
+      const float2 t = __ldg(reinterpret_cast<const float2 *>(p));
+      v[0] = t.x;
+      v[1] = t.y;
+   }
+   __device__ static void rmw(float *p, const float *v) {
+      float2 t = *reinterpret_cast<float2 *>(p);
+      t.x += v[0];
+      t.y += v[1];
+      *reinterpret_cast<float2 *>(p) = t;
+   }
+};
+template <>
+struct VecF<4> {
+   __device__ static void ld(const float *p, float *v) {
+      const float4 t = __ldg(reinterpret_cast<const float4 *>(p));
+      v[0] = t.x;
+      v[1] = t.y;
+      v[2] = t.z;
+      v[3] = t.w;
+   }
+   __device__ static void rmw(float *p, const float *v) {
+      float4 t = *reinterpret_cast<float4 *>(p);
+      t.x += v[0];
+      t.y += v[1];
+      t.z += v[2];
+      t.w += v[3];
+      *reinterpret_cast<float4 *>(p) = t;
+   }
+};
+
+template <int FPL, int NYP, bool SPARSE>
+__global__ void __launch_bounds__(kWarps * 32) deliver_pre_rows_kernel(PreGeom g, const pvgpu_entry *__restrict__ entries,
+                                                                       const int64_t *__restrict__ numActive,
+                                                                       const float *__restrict__ aExt,
+                                                                       const float *__restrict__ W,
+                                                                       float *__restrict__ gsyn) {
+   __shared__ int64_t rowLo[kRowsMax], rowHi[kRowsMax];
+   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+   const int X0 = blockIdx.x * kWarps, X = X0 + warp;
+   const int P0 = blockIdx.y * kRowsRS, P1 = min(P0 + kRowsRS, g.post.ny);
+   const int b = blockIdx.z;
+   const int nxExt = g.pre.nxExt(), nyExt = g.pre.nyExt(), nf = g.pre.nf;
+   // one-to-one: patch start = index - H on both axes
+   const int Hy = -g.ay.start(0), Hx = -g.ax.start(0);
+   // presynaptic rows reaching post rows [P0, P1) and the columns reaching [X0, X0 + 8)
+   const int yeLo = max(0, P0 + Hy - NYP + 1), yeHi = min(nyExt - 1, P1 - 1 + Hy);
+   const int xlo = max(0, X0 + Hx - g.nxp + 1), xhi = min(nxExt - 1, X0 + kWarps - 1 + Hx);
+   const int nRows = yeHi - yeLo + 1;
+   auto key_lo = [&](int ye) { return ((int64_t)ye * nxExt + xlo) * nf; };
+   auto key_hi = [&](int ye) { return ((int64_t)ye * nxExt + xhi) * nf + nf; };  // one past
+   if (SPARSE) {
+      const pvgpu_entry *eb = entries + (size_t)b * g.pre.numExt();
+      const int64_t nAct = numActive[b];
+      for (int t = threadIdx.x; t < 2 * nRows && xlo <= xhi; t += blockDim.x) {
+         const int r = t >> 1;
+         const int64_t key = (t & 1) ? key_hi(yeLo + r) : key_lo(yeLo + r);
+         const int64_t v = lower_bound_entries(eb, nAct, (uint32_t)min(key, (int64_t)0xffffffffLL));
+         if (t & 1) rowHi[r] = key > 0xffffffffLL ? nAct : v;
+         else rowLo[r] = v;
+      }
+   }
+   __syncthreads();
+   if (X >= g.post.nx || xlo > xhi || nRows <= 0) return;  // no barrier below
+
+   const pvgpu_entry *eb = SPARSE ? entries + (size_t)b * g.pre.numExt() : nullptr;
+   const float *ab = SPARSE ? nullptr : aExt + (size_t)b * g.pre.numExt();
+   const int fo0 = lane * FPL;
+   const int rowStrideW = g.nxp * g.nfp;
+   float *gcol = gsyn + (size_t)b * g.post.numRes() + (size_t)X * g.nfp + fo0;
+   const size_t gRow = (size_t)g.post.nx * g.nfp;
+
+   float acc[NYP][FPL];
+#pragma unroll
+   for (int s = 0; s < NYP; s++)
+#pragma unroll
+      for (int q = 0; q < FPL; q++) acc[s][q] = 0.0f;
+
+   // first row with (ye - Hy) = 0 mod NYP, so that slots are static inside each group
+   const int yeStart = yeLo - (((yeLo - Hy) % NYP) + NYP) % NYP;
+   const int yeEnd = P1 - 1 + Hy;  // the row that completes post row P1 - 1
+   for (int ye0 = yeStart; ye0 <= yeEnd; ye0 += NYP) {
+#pragma unroll
+      for (int i = 0; i < NYP; i++) {
+         const int ye = ye0 + i;
+         if (ye >= yeLo && ye <= yeHi) {
+            const int64_t lo = SPARSE ? rowLo[ye - yeLo] : key_lo(ye);
+            const int64_t hi = SPARSE ? rowHi[ye - yeLo] : key_hi(ye);
+            const int64_t kRow = (int64_t)ye * nxExt * nf;
+            // patch rows of this presynaptic row that land inside [P0, P1)
+            const int kyMin = max(0, P0 - (ye - Hy)), kyMax = min(NYP - 1, P1 - 1 - (ye - Hy));
+            for (int64_t base = lo; base < hi; base += 32) {
+               int64_t k = 0;
+               float a = 0.0f;
+               const bool have = base + lane < hi;
+               if (have) {
+                  if (SPARSE) {
+                     const pvgpu_entry en = eb[base + lane];
+                     k = en.index;
+                     a = en.value;
+                  } else {
+                     k = base + lane;
+                     a = ab[base + lane];
+                  }
+               }
+               const int kr = (int)(k - kRow);
+               const int xe = kr / nf, f = kr - xe * nf;
+               const int kx = X - (xe - Hx);
+               const bool rel = have && a != 0.0f && kx >= 0 && kx < g.nxp;
+               unsigned m = __ballot_sync(0xffffffffu, rel);
+               const int woffMine = f * g.patchSize + kx * g.nfp;  // kernel index = f (one-to-one)
+               while (m) {
+                  const int j = __ffs(m) - 1;
+                  m &= m - 1;
+                  const float aj = __shfl_sync(0xffffffffu, a, j) * g.dtf;
+                  const float *wp = W + __shfl_sync(0xffffffffu, woffMine, j) + fo0;
+#pragma unroll
+                  for (int ky = 0; ky < NYP; ky++) {
+                     if (ky >= kyMin && ky <= kyMax) {
+                        float w[FPL];
+                        VecF<FPL>::ld(wp + ky * rowStrideW, w);
+                        const int s = (i + ky) % NYP;
+#pragma unroll
+                        for (int q = 0; q < FPL; q++) acc[s][q] = fmaf(aj, w[q], acc[s][q]);
+                     }
+                  }
+               }
+            }
+         }
+         // post row ye - Hy has all its contributions (slot i)
+         const int py = ye - Hy;
+         if (py >= P0 && py < P1) VecF<FPL>::rmw(gcol + (size_t)py * gRow, acc[i]);
+#pragma unroll
+         for (int q = 0; q < FPL; q++) acc[i][q] = 0.0f;
+      }
+   }
+}
+
+template <int FPL, int NYP>
+pvgpu_status launch_rows(const PreGeom &g, cudaStream_t s, const pvgpu_entry *entries, const int64_t *numActive,
+                         const float *aExt, const float *W, float *gsyn) {
+   dim3 grid((g.post.nx + kWarps - 1) / kWarps, (g.post.ny + kRowsRS - 1) / kRowsRS, g.post.nb);
+   if (entries)
+      deliver_pre_rows_kernel<FPL, NYP, true><<<grid, kWarps * 32, 0, s>>>(g, entries, numActive, nullptr, W, gsyn);
+   else
+      deliver_pre_rows_kernel<FPL, NYP, false><<<grid, kWarps * 32, 0, s>>>(g, nullptr, nullptr, aExt, W, gsyn);
+   PVGPU_CHECK_LAUNCH("deliver_pre rows");
+   return PVGPU_OK;
+}
+
+template <int FPL>
+pvgpu_status launch_rows_nyp(const PreGeom &g, cudaStream_t s, const pvgpu_entry *entries, const int64_t *numActive,
+                             const float *aExt, const float *W, float *gsyn) {
+   switch (g.nyp) {
+      case 1: return launch_rows<FPL, 1>(g, s, entries, numActive, aExt, W, gsyn);
+      case 3: return launch_rows<FPL, 3>(g, s, entries, numActive, aExt, W, gsyn);
+      case 5: return launch_rows<FPL, 5>(g, s, entries, numActive, aExt, W, gsyn);
+      case 7: return launch_rows<FPL, 7>(g, s, entries, numActive, aExt, W, gsyn);
+      case 9: return launch_rows<FPL, 9>(g, s, entries, numActive, aExt, W, gsyn);
+      default: return PVGPU_ERR_UNSUPPORTED_SHAPE;
+   }
+}
+
 template <bool SPARSE, bool EXACT>
 pvgpu_status launch(const PreGeom &g, int epl, dim3 grid, cudaStream_t s, const pvgpu_entry *entries,
                     const int64_t *numActive, const float *aExt, const float *W, float *gsyn) {
@@ -231,6 +423,17 @@ extern "C" pvgpu_status pvgpu_deliver_pre(const pvgpu_conn_desc *conn, const pvg
    dim3 grid((unsigned)gx, gy, pre.nbatch);
    cudaStream_t s = pvgpu::as_stream(stream);
    bool exact = mode == PVGPU_DELIVER_REFERENCE_ORDER;
+   // FAST mode, one-to-one, nfp a multiple of 32 up to 128, odd patch height up to 9: the
+   // row-sliding kernel
+   const int rowRange = kRowsRS + conn->nyp - 1;
+   if (!exact && pre.nx == post.nx && pre.ny == post.ny && post.nf % 32 == 0 && post.nf <= 128 &&
+       conn->nyp <= 9 && rowRange <= kRowsMax && (post.nf / 32) != 3) {
+      const int fpl = post.nf / 32;
+      pvgpu_status r = fpl == 1   ? launch_rows_nyp<1>(g, s, entries, numActive, aExt, weights, gsyn)
+                       : fpl == 2 ? launch_rows_nyp<2>(g, s, entries, numActive, aExt, weights, gsyn)
+                                  : launch_rows_nyp<4>(g, s, entries, numActive, aExt, weights, gsyn);
+      if (r != PVGPU_ERR_UNSUPPORTED_SHAPE) return r;
+   }
    if (entries)
       return exact ? launch<true, true>(g, p2, grid, s, entries, numActive, nullptr, weights, gsyn)
                    : launch<true, false>(g, p2, grid, s, entries, numActive, nullptr, weights, gsyn);

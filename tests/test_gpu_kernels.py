@@ -76,6 +76,13 @@ PRE_CASES = [
     ((1, 32, 32, 4, 6), (8, 8, 5, 0), 4, 4),        # many-to-one x4
     ((3, 12, 8, 3, 1), (24, 16, 2, 2), 6, 4),       # one-to-many, unequal axes
     ((1, 20, 20, 40, 0), (20, 20, 600, 0), 3, 3),   # post features above one tile
+    # one-to-one with 32 / 64 / 128 post features: the row-sliding kernel in FAST mode
+    ((2, 40, 70, 16, 3), (40, 70, 64, 0), 7, 7),    # several row segments, the last partial
+    ((1, 13, 37, 8, 2), (13, 37, 32, 0), 5, 5),     # columns not a multiple of 8
+    ((2, 24, 33, 4, 1), (24, 33, 128, 0), 3, 3),
+    ((1, 20, 40, 8, 4), (20, 40, 64, 1), 5, 5),     # pre halo above the margin, post halo
+    ((1, 16, 40, 8, 1), (16, 40, 32, 0), 7, 7),     # pre halo below the margin
+    ((2, 20, 36, 6, 4), (20, 36, 64, 0), 5, 9),     # unequal patch axes, tallest patch
 ]
 
 
