@@ -468,7 +468,16 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--timesteps", type=int, default=0, help="override the 400 LCA timesteps (profiling runs)")
     ap.add_argument("--quick", action="store_true", help="time the solve only (profiling runs; not a bench line)")
+    ap.add_argument("--delivery", action="store_true",
+                    help="run the presynaptic delivery microbenchmark only (profiling runs; not a bench line)")
     args = ap.parse_args()
+    if args.delivery:
+        import torch
+        from openpv_gb300 import build
+        build.build()
+        from openpv_gb300 import capi
+        print(json.dumps({"delivery": delivery_bench(torch, capi, reps=1)}))
+        return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", str(args.gpus if args.impl == "ours" else 1)))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))

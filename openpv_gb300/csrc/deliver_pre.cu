@@ -233,7 +233,7 @@ struct VecF<4> {
 };
 
 template <int FPL, int NYP, bool SPARSE>
-__global__ void __launch_bounds__(kWarps * 32) deliver_pre_rows_kernel(PreGeom g, const pvgpu_entry *__restrict__ entries,
+__global__ void __launch_bounds__(kWarps * 32, 4) deliver_pre_rows_kernel(PreGeom g, const pvgpu_entry *__restrict__ entries,
                                                                        const int64_t *__restrict__ numActive,
                                                                        const float *__restrict__ aExt,
                                                                        const float *__restrict__ W,
@@ -312,19 +312,35 @@ __global__ void __launch_bounds__(kWarps * 32) deliver_pre_rows_kernel(PreGeom g
                const bool rel = have && a != 0.0f && kx >= 0 && kx < g.nxp;
                unsigned m = __ballot_sync(0xffffffffu, rel);
                const int woffMine = f * g.patchSize + kx * g.nfp;  // kernel index = f (one-to-one)
+               // two entries per round: their weight loads are all in flight before the FMAs
                while (m) {
-                  const int j = __ffs(m) - 1;
+                  const int j1 = __ffs(m) - 1;
                   m &= m - 1;
-                  const float aj = __shfl_sync(0xffffffffu, a, j) * g.dtf;
-                  const float *wp = W + __shfl_sync(0xffffffffu, woffMine, j) + fo0;
+                  const bool two = m != 0;  // warp-uniform
+                  const int j2 = two ? __ffs(m) - 1 : j1;
+                  if (two) m &= m - 1;
+                  const float a1 = __shfl_sync(0xffffffffu, a, j1) * g.dtf;
+                  const float a2 = two ? __shfl_sync(0xffffffffu, a, j2) * g.dtf : 0.0f;
+                  const float *wp1 = W + __shfl_sync(0xffffffffu, woffMine, j1) + fo0;
+                  const float *wp2 = W + __shfl_sync(0xffffffffu, woffMine, j2) + fo0;
+                  float w1[NYP][FPL], w2[NYP][FPL];
 #pragma unroll
                   for (int ky = 0; ky < NYP; ky++) {
                      if (ky >= kyMin && ky <= kyMax) {
-                        float w[FPL];
-                        VecF<FPL>::ld(wp + ky * rowStrideW, w);
+                        VecF<FPL>::ld(wp1 + ky * rowStrideW, w1[ky]);
+                        if (two) VecF<FPL>::ld(wp2 + ky * rowStrideW, w2[ky]);
+                     }
+                  }
+#pragma unroll
+                  for (int ky = 0; ky < NYP; ky++) {
+                     if (ky >= kyMin && ky <= kyMax) {
                         const int s = (i + ky) % NYP;
 #pragma unroll
-                        for (int q = 0; q < FPL; q++) acc[s][q] = fmaf(aj, w[q], acc[s][q]);
+                        for (int q = 0; q < FPL; q++) acc[s][q] = fmaf(a1, w1[ky][q], acc[s][q]);
+                        if (two) {
+#pragma unroll
+                           for (int q = 0; q < FPL; q++) acc[s][q] = fmaf(a2, w2[ky][q], acc[s][q]);
+                        }
                      }
                   }
                }
