@@ -170,6 +170,10 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(320, 1)
    cluster_sync();  // the peer multicasts into this CTA's stages and barriers from here on
    tc_fence_after();
    const uint32_t tmem = tmemBase;
+   // Set-up above overlaps the previous kernel's tail; everything below reads A (written by the
+   // previous kernel P) or writes the residual (read by it).
+   griddep_launch_dependents();
+   griddep_wait();
 
    auto wait_or_abort = [&](uint64_t *bar, uint32_t parity) {
       if (abortFlag) return false;
@@ -481,6 +485,10 @@ __global__ void __launch_bounds__(320, 1) post_tc_kernel(const __grid_constant__
    __syncthreads();
    tc_fence_after();
    const uint32_t tmem = tmemBase;
+   // Set-up above overlaps the previous kernel's tail; everything below reads the residual
+   // (written by the previous kernel R) or V and A (which kernel R and the previous kernel P use).
+   griddep_launch_dependents();
+   griddep_wait();
 
    auto tile_of = [&](int ti, int &b, int &mb, int &fh) {
       const int j = blockIdx.x + ti * pl.G;
@@ -905,6 +913,12 @@ struct pvgpu_lca_solver {
    std::vector<cudaEvent_t> ev;
    size_t evNext = 0;
    bool profiling = false;
+   // the BF16 run as one CUDA graph: captured on capStream, replayed on the caller's stream;
+   // rebuilt when the input pointer or the step counts change
+   cudaStream_t capStream = nullptr;
+   cudaGraphExec_t graph = nullptr;
+   const float *graphX = nullptr;
+   int graphSteps = -1, graphX3 = -1;
 };
 
 namespace {
@@ -991,21 +1005,46 @@ ReconPlan make_recon_plan(const LcaGeom &g, int S, int P, int C, bool x3, int ma
 
 template <int S, int P, int C>
 struct Launcher {
+   // shared-memory limits of both kernels (once, at create: not inside a stream capture)
+   static pvgpu_status set_attrs(const pvgpu_lca_solver *s) {
+      const void *fns[4] = {reinterpret_cast<const void *>(recon_tc_kernel<S, P, C, false>),
+                            reinterpret_cast<const void *>(recon_tc_kernel<S, P, C, true>),
+                            reinterpret_cast<const void *>(post_tc_kernel<S, P, C, false>),
+                            reinterpret_cast<const void *>(post_tc_kernel<S, P, C, true>)};
+      const uint32_t bytes[4] = {s->rplan.total, s->rplanX3.total, s->plan.total, s->planX3.total};
+      for (int i = 0; i < 4; i++) {
+         if (bytes[i] > 227u * 1024u - 512u) continue;  // a form this shape cannot run (refused at run time)
+         cudaError_t e = cudaFuncSetAttribute(fns[i], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes[i]);
+         if (e != cudaSuccess) return pvgpu::record_cuda_error(e, "lca kernel attributes");
+      }
+      return PVGPU_OK;
+   }
+   // One LCA timestep: kernel R then kernel P, each launched with programmatic stream
+   // serialisation, so that its set-up overlaps the tail of the kernel before it.
    template <bool X3>
    static pvgpu_status step(pvgpu_lca_solver *s, const float *x, cudaStream_t st, cudaEvent_t mid) {
+      cudaLaunchAttribute attr[1];
+      attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+      attr[0].val.programmaticStreamSerializationAllowed = 1;
       const ReconPlan &rp = X3 ? s->rplanX3 : s->rplan;
-      auto rk = recon_tc_kernel<S, P, C, X3>;
-      cudaError_t e = cudaFuncSetAttribute(rk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rp.total);
-      if (e != cudaSuccess) return pvgpu::record_cuda_error(e, "lca recon attr");
-      rk<<<rp.G, 320, rp.total, st>>>(s->tmA, s->tmAlo, s->tmWtH, s->tmWtloH, s->g, rp, x, s->rpad, s->err);
-      PVGPU_CHECK_LAUNCH("lca recon");
+      cudaLaunchConfig_t cr = {};
+      cr.gridDim = dim3(rp.G);
+      cr.blockDim = dim3(320);
+      cr.dynamicSmemBytes = rp.total;
+      cr.stream = st;
+      cr.attrs = attr;
+      cr.numAttrs = mid ? 0 : 1;  // per-kernel timing keeps the kernels apart
+      cudaError_t e = cudaLaunchKernelEx(&cr, recon_tc_kernel<S, P, C, X3>, s->tmA, s->tmAlo, s->tmWtH, s->tmWtloH,
+                                         s->g, rp, x, s->rpad, s->err);
+      if (e != cudaSuccess) return pvgpu::record_cuda_error(e, "lca recon");
       if (mid) cudaEventRecord(mid, st);
       const PostPlan &pl = X3 ? s->planX3 : s->plan;
-      auto pk = post_tc_kernel<S, P, C, X3>;
-      e = cudaFuncSetAttribute(pk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.total);
-      if (e != cudaSuccess) return pvgpu::record_cuda_error(e, "lca post attr");
-      pk<<<pl.G, 320, pl.total, st>>>(s->tmW, s->tmWlo, s->tmAst, s->g, pl, s->rpad, s->V, s->A, s->Alo, s->err);
-      PVGPU_CHECK_LAUNCH("lca post");
+      cudaLaunchConfig_t cp = cr;
+      cp.gridDim = dim3(pl.G);
+      cp.dynamicSmemBytes = pl.total;
+      e = cudaLaunchKernelEx(&cp, post_tc_kernel<S, P, C, X3>, s->tmW, s->tmWlo, s->tmAst, s->g, pl,
+                             (const float *)s->rpad, s->V, s->A, s->Alo, s->err);
+      if (e != cudaSuccess) return pvgpu::record_cuda_error(e, "lca post");
       return PVGPU_OK;
    }
    // clusters of two recon CTAs that can be resident at once (one CTA per SM)
@@ -1046,6 +1085,8 @@ pvgpu_status dispatch(int S, int P, int C, Fn &&fn) {
 
 void free_solver(pvgpu_lca_solver *s) {
    for (cudaEvent_t e : s->ev) cudaEventDestroy(e);
+   if (s->graph) cudaGraphExecDestroy(s->graph);
+   if (s->capStream) cudaStreamDestroy(s->capStream);
    void *ptrs[] = {s->V, s->partials, s->rpad, s->A32, s->W32, s->Wt32, s->A, s->Alo, s->W, s->Wlo, s->Wt, s->Wtlo, s->err};
    for (void *p : ptrs)
       if (p) cudaFree(p);
@@ -1167,6 +1208,15 @@ extern "C" pvgpu_status pvgpu_lca_solver_create(const pvgpu_lca_solver_desc *d, 
       free_solver(s);
       return PVGPU_ERR_UNSUPPORTED_SHAPE;
    }
+   pvgpu_status ra = dispatch(S, P, C, [&](auto L) { return L.set_attrs(s); });
+   if (ra == PVGPU_OK && cudaStreamCreateWithFlags(&s->capStream, cudaStreamNonBlocking) != cudaSuccess) {
+      cudaGetLastError();
+      s->capStream = nullptr;  // runs then launch kernel by kernel
+   }
+   if (ra != PVGPU_OK) {
+      free_solver(s);
+      return ra;
+   }
    *out = s;
    return PVGPU_OK;
 }
@@ -1234,6 +1284,39 @@ extern "C" pvgpu_status pvgpu_lca_solver_run(pvgpu_lca_solver *s, const float *x
          return PVGPU_OK;
       });
       if (!x3ok) return PVGPU_ERR_UNSUPPORTED_SHAPE;
+   }
+   if (numSteps > 0 && !s->profiling && s->capStream) {
+      // the whole run as one graph of 2 x numSteps kernel nodes (programmatic edges between them)
+      if (!s->graph || s->graphX != x || s->graphSteps != numSteps || s->graphX3 != numX3Steps) {
+         if (s->graph) cudaGraphExecDestroy(s->graph);
+         s->graph = nullptr;
+         PVGPU_CUDA(cudaStreamBeginCapture(s->capStream, cudaStreamCaptureModeThreadLocal), "lca graph capture");
+         pvgpu_status r = PVGPU_OK;
+         for (int t = 0; t < numSteps && r == PVGPU_OK; t++) {
+            const bool x3 = t >= numSteps - numX3Steps;
+            r = dispatch(s->S, s->P, s->C, [&](auto L) { return L.run_step(s, x, x3, s->capStream, nullptr); });
+         }
+         cudaGraph_t g = nullptr;
+         cudaError_t ee = cudaStreamEndCapture(s->capStream, &g);
+         if (r != PVGPU_OK || ee != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            if (r == PVGPU_OK) r = pvgpu::record_cuda_error(ee, "lca graph capture");
+            return r;
+         }
+         cudaError_t ei = cudaGraphInstantiate(&s->graph, g, 0);
+         cudaGraphDestroy(g);
+         if (ei != cudaSuccess) {
+            s->graph = nullptr;
+            return pvgpu::record_cuda_error(ei, "lca graph instantiate");
+         }
+         s->graphX = x;
+         s->graphSteps = numSteps;
+         s->graphX3 = numX3Steps;
+      }
+      PVGPU_CUDA(cudaGraphLaunch(s->graph, st), "lca graph launch");
+      s->stepsRun += numSteps;
+      s->padValid = true;
+      return PVGPU_OK;
    }
    for (int t = 0; t < numSteps; t++) {
       const bool x3 = t >= numSteps - numX3Steps;

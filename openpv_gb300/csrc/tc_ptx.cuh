@@ -211,6 +211,14 @@ __device__ __forceinline__ void st_global_32B(void *p, uint4 a, uint4 b) {
                 : "memory");
 }
 
+// ---- programmatic dependent launch ---------------------------------------------------------
+// Let the next kernel in the stream be scheduled once every CTA of this grid has passed here
+// (or exited); its CTAs then occupy SMs as this grid's CTAs leave them.
+__device__ __forceinline__ void griddep_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+// Wait until the grids this one depends on have completed and their memory is visible.
+__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // ---- clusters ----------------------------------------------------------------------------
 __device__ __forceinline__ uint32_t cluster_ctarank() {
    uint32_t r;

@@ -126,3 +126,53 @@ def test_lca_bf16_x3_closer_than_bf16(torch, oracle):
         torch.cuda.synchronize()
         errs.append(np.abs(v.cpu().numpy() - v_ref).max())
     assert errs[1] < 0.25 * errs[0], errs
+
+
+def test_lca_bf16_graph_replay_equals_kernel_by_kernel(torch, oracle):
+    """A BF16 run is replayed as one CUDA graph with programmatic dependent launches between its
+    kernels; the state it leaves is bit-identical to the kernel-by-kernel run (per-kernel timing
+    mode), also after the graph is rebuilt for another input buffer and step count, and when run
+    on a side stream."""
+    from openpv_gb300 import capi
+    nb, ins, v1s, nxp, vth, steps, w, x, p = setup(oracle, "colour")
+    wd = torch.from_numpy(w).cuda()
+
+    def solve(xd, n, x3, direct, stream=None):
+        s = capi.LcaSolver(nb, ins, v1s, nxp, vth)
+        s.set_weights(wd)
+        s.reset()
+        if direct:
+            s.profile_begin(n)
+        s.run(xd, n, x3_steps=x3, precision=capi.LCA_BF16, stream=stream)
+        if direct:
+            s.profile_end()
+        v = torch.zeros((nb,) + v1s, device="cuda")
+        s.state(v, stream=stream)
+        torch.cuda.synchronize()
+        assert s.error_flag() == 0
+        return v.cpu().numpy()
+
+    xd = torch.from_numpy(x).cuda()
+    x2 = (xd * 0.5).contiguous()
+    for xi, n, x3 in ((xd, steps, 0), (x2, steps + 3, 4)):
+        ref = solve(xi, n, x3, direct=True)
+        assert np.array_equal(solve(xi, n, x3, direct=False).view(np.uint32), ref.view(np.uint32))
+    side = torch.cuda.Stream()
+    with torch.cuda.stream(side):
+        got = solve(x2, steps + 3, 4, direct=False, stream=side)
+    assert np.array_equal(got.view(np.uint32), ref.view(np.uint32))
+
+    # one solver, graph reused across runs and rebuilt when the input changes
+    s = capi.LcaSolver(nb, ins, v1s, nxp, vth)
+    s.set_weights(wd)
+    outs = []
+    for xi in (xd, xd, x2):
+        s.reset()
+        s.run(xi, steps, precision=capi.LCA_BF16)
+        v = torch.zeros((nb,) + v1s, device="cuda")
+        s.state(v)
+        torch.cuda.synchronize()
+        outs.append(v.cpu().numpy())
+    assert np.array_equal(outs[0], outs[1])
+    assert np.array_equal(outs[0], solve(xd, steps, 0, direct=True))
+    assert np.array_equal(outs[2], solve(x2, steps, 0, direct=True))
