@@ -299,6 +299,16 @@ pvgpu_status pvgpu_lca_solver_error_flag(pvgpu_lca_solver *s, int *hostFlag);
  * reconstruction kernel and of the post-delivery/update kernel over the recorded steps. */
 pvgpu_status pvgpu_lca_solver_profile_begin(pvgpu_lca_solver *s, int maxSteps);
 pvgpu_status pvgpu_lca_solver_profile_end(pvgpu_lca_solver *s, double *reconMs, double *postMs, int *steps);
+/* No counterpart in the reference (its CUDA kernels have fixed launch shapes).  Times every
+ * shape of the two BF16 kernels that fits in shared memory -- the post-delivery kernel's feature
+ * tile (64/128/256/512) and its V / weight ring depths and A staging, the reconstruction
+ * kernel's ring depth -- on trialSteps timesteps of x (BF16 and BF16x3 forms), keeps the fastest
+ * of each, and remembers them for every solver of the same geometry created later in the
+ * process.  Leaves V and A undefined: call pvgpu_lca_solver_reset before the next run. */
+pvgpu_status pvgpu_lca_solver_autotune(pvgpu_lca_solver *s, const float *x, int trialSteps, void *stream);
+/* The shapes in use: out[0..4] = {feature tile, V ring slots, weight ring slots, A staged (0/1),
+ * reconstruction ring stages} of the BF16 form, out[5..9] the same for BF16x3 steps. */
+pvgpu_status pvgpu_lca_solver_plan_info(const pvgpu_lca_solver *s, int *out);
 
 /* ---- diagnostics ----------------------------------------------------------------------------
  * No counterpart in the reference.  C[M][N] (FP32) = A[M][K] * B[N][K]^T with BF16 row-major

@@ -128,6 +128,8 @@ def _declare(L):
         "pvgpu_lca_solver_error_flag": (i, [vp, C.POINTER(i)]),
         "pvgpu_lca_solver_profile_begin": (i, [vp, i]),
         "pvgpu_lca_solver_profile_end": (i, [vp, C.POINTER(d), C.POINTER(d), C.POINTER(i)]),
+        "pvgpu_lca_solver_autotune": (i, [vp, vp, i, vp]),
+        "pvgpu_lca_solver_plan_info": (i, [vp, C.POINTER(i)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -290,6 +292,17 @@ class LcaSolver:
 
     def state(self, v=None, a=None, stream=None):
         check(lib().pvgpu_lca_solver_state(self.h, _ptr(v), _ptr(a), _stream(stream)), "lca_solver_state")
+
+    def autotune(self, x, trial_steps=6, stream=None):
+        """Pick the fastest kernel shapes for this geometry (state undefined afterwards: reset)."""
+        check(lib().pvgpu_lca_solver_autotune(self.h, _ptr(x), trial_steps, _stream(stream)), "lca_solver_autotune")
+
+    def plan_info(self):
+        """{"bf16"|"bf16x3": {FT, nV, nW, stageA, reconStages}} of the shapes in use."""
+        out = (C.c_int * 10)()
+        check(lib().pvgpu_lca_solver_plan_info(self.h, out), "lca_solver_plan_info")
+        keys = ("feature_tile", "v_slots", "w_slots", "a_staged", "recon_stages")
+        return {form: dict(zip(keys, out[5 * i:5 * i + 5])) for i, form in enumerate(("bf16", "bf16x3"))}
 
     def profile_begin(self, max_steps):
         check(lib().pvgpu_lca_solver_profile_begin(self.h, max_steps), "lca_solver_profile_begin")

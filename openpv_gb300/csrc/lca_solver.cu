@@ -38,6 +38,9 @@
 #include <cstdio>
 #include <cstring>
 #include <new>
+#include <array>
+#include <map>
+#include <mutex>
 #include <vector>
 
 namespace {
@@ -915,6 +918,7 @@ struct pvgpu_lca_solver {
    bool profiling = false;
    // the BF16 run as one CUDA graph: captured on capStream, replayed on the caller's stream;
    // rebuilt when the input pointer or the step counts change
+   int maxPairs[2] = {0, 0};  // co-resident kernel-R clusters (BF16, BF16x3)
    cudaStream_t capStream = nullptr;
    cudaGraphExec_t graph = nullptr;
    const float *graphX = nullptr;
@@ -925,59 +929,73 @@ namespace {
 
 int g_num_sms = 0;
 
-PostPlan make_post_plan(const LcaGeom &g, int S, int P, int C, bool x3, int numSms) {
+// Shared-memory layout of kernel P for a feature tile FT, ring depths nV / nW and A staging;
+// total = 0 when FT does not divide the features.
+PostPlan post_plan_for(const LcaGeom &g, int S, int P, int C, bool x3, int numSms, int FT, int nV, int nW, int stA) {
    const int KP = P * P * C, NKC = KP / 64, E = (P - S) / 2;
    auto al = [](uint32_t v) { return (v + 1023u) & ~1023u; };
    PostPlan pl;
    std::memset(&pl, 0, sizeof(pl));
+   if (FT <= 0 || FT % 64 || g.F % FT || (stA && x3)) return pl;
    pl.RP = ((g.inNx + 2 * E) * C + 3) & ~3;
    pl.rowsPad = g.inNy + 2 * E;
    const uint32_t RWR = (uint32_t)rwin_rows(S, P, g.rowsPerBlock);
    const uint32_t wB = NKC * kPostNT * 128, imB = NKC * 16384, vtB = 2 * 16384;
    const uint32_t winB = RWR * (uint32_t)pl.RP * 4;
-   // deepest rings that fit, V tiles first (they come from HBM), then weight tiles (from L2);
-   // A staged for TMA stores where it fits with at least two V slots (not in BF16x3 steps,
-   // which also write the low halves)
-   static const int kRings[][3] = {{3, 2, 1}, {3, 1, 1}, {2, 2, 1}, {2, 1, 1}, {3, 2, 0},
-                                   {3, 1, 0}, {2, 2, 0}, {2, 1, 0}, {1, 1, 0}};
-   for (const auto &r : kRings) {
-      const int nV = r[0], nW = r[1], stA = r[2];
-      if (stA && x3) continue;
-      uint32_t o = 0;
-      pl.offIM = o;
-      o = al(o + imB);
-      pl.offIMlo = o;
-      if (x3) o = al(o + imB);
-      for (int sl = 0; sl < kMaxWSlots; sl++) {
-         pl.offW[sl] = pl.offWlo[sl] = o;
-         if (sl < nW) {
-            o = al(o + wB);
-            pl.offWlo[sl] = o;
-            if (x3) o = al(o + wB);
-         }
+   uint32_t o = 0;
+   pl.offIM = o;
+   o = al(o + imB);
+   pl.offIMlo = o;
+   if (x3) o = al(o + imB);
+   for (int sl = 0; sl < kMaxWSlots; sl++) {
+      pl.offW[sl] = pl.offWlo[sl] = o;
+      if (sl < nW) {
+         o = al(o + wB);
+         pl.offWlo[sl] = o;
+         if (x3) o = al(o + wB);
       }
-      for (int sl = 0; sl < kMaxVSlots; sl++) {
-         pl.offVT[sl] = o;
-         if (sl < nV) o = al(o + vtB);
-      }
-      pl.offWin = o;
-      o = al(o + winB);
-      pl.offA = o;
-      if (stA) o = al(o + 8 * 2048);
-      pl.total = o + 1024;
-      pl.nV = nV;
-      pl.nW = nW;
-      pl.stageA = stA;
-      if (pl.total + 256u <= 227u * 1024u) break;  // static shared memory shares the budget
    }
-   pl.FT = g.F < 256 ? g.F : 256;
-   while (g.F % pl.FT) pl.FT -= 64;
+   for (int sl = 0; sl < kMaxVSlots; sl++) {
+      pl.offVT[sl] = o;
+      if (sl < nV) o = al(o + vtB);
+   }
+   pl.offWin = o;
+   o = al(o + winB);
+   pl.offA = o;
+   if (stA) o = al(o + 8 * 2048);
+   pl.total = o + 1024;
+   pl.nV = nV;
+   pl.nW = nW;
+   pl.stageA = stA;
+   pl.FT = FT;
    const int nTiles = g.nb * g.MB * (g.F / pl.FT);
    pl.G = numSms < nTiles ? numSms : nTiles;
    return pl;
 }
 
-ReconPlan make_recon_plan(const LcaGeom &g, int S, int P, int C, bool x3, int maxPairs) {
+constexpr uint32_t kSmemBudget = 227u * 1024u - 512u;  // dynamic shared memory; static shares the budget
+
+// ring shapes, best first: V tiles first (they come from HBM), then weight tiles (from L2); A
+// staged for TMA stores where it fits with at least two V slots (not in BF16x3 steps, which
+// also write the low halves)
+constexpr int kRings[][3] = {{3, 2, 1}, {3, 1, 1}, {2, 2, 1}, {2, 1, 1}, {3, 2, 0},
+                             {3, 1, 0}, {2, 2, 0}, {2, 1, 0}, {1, 1, 0}};
+
+// The default shape: 256-feature tiles (or the largest multiple of 64 dividing F) and the first
+// ring shape that fits.
+PostPlan make_post_plan(const LcaGeom &g, int S, int P, int C, bool x3, int numSms) {
+   int FT = g.F < 256 ? g.F : 256;
+   while (g.F % FT) FT -= 64;
+   PostPlan pl;
+   std::memset(&pl, 0, sizeof(pl));
+   for (const auto &r : kRings) {
+      pl = post_plan_for(g, S, P, C, x3, numSms, FT, r[0], r[1], r[2]);
+      if (pl.total && pl.total <= kSmemBudget) return pl;
+   }
+   return pl;
+}
+
+ReconPlan recon_plan_for(const LcaGeom &g, int S, int P, int C, bool x3, int maxPairs, int nStage) {
    const int KP = P * P * C, E = (P - S) / 2;
    auto al = [](uint32_t v) { return (v + 1023u) & ~1023u; };
    ReconPlan rp;
@@ -986,35 +1004,40 @@ ReconPlan make_recon_plan(const LcaGeom &g, int S, int P, int C, bool x3, int ma
    rp.rowsPad = g.inNy + 2 * E;
    rp.stageBytes = al((x3 ? 2u : 1u) * (128u * 64u * 2u + (uint32_t)KP * 64u * 2u));
    const uint32_t imgB = al((uint32_t)(g.inNx * g.inNy * C) * 4u);
-   for (int n = kMaxRStages; n >= 2; n--) {
-      rp.nStage = n;
-      uint32_t o = n * rp.stageBytes;
-      rp.offRec = o;
-      o += imgB;
-      rp.offX[0] = o;
-      o += imgB;
-      rp.offX[1] = o;
-      o += imgB;
-      rp.total = o + 1024;
-      if (rp.total + 512u <= 227u * 1024u) break;
-   }
+   rp.nStage = nStage;
+   uint32_t o = nStage * rp.stageBytes;
+   rp.offRec = o;
+   o += imgB;
+   rp.offX[0] = o;
+   o += imgB;
+   rp.offX[1] = o;
+   o += imgB;
+   rp.total = o + 1024;
    const int units = (g.nb + 1) / 2;
    rp.G = 2 * (maxPairs < units ? maxPairs : units);
+   return rp;
+}
+
+// The default shape: the deepest ring that fits.
+ReconPlan make_recon_plan(const LcaGeom &g, int S, int P, int C, bool x3, int maxPairs) {
+   ReconPlan rp = recon_plan_for(g, S, P, C, x3, maxPairs, 2);
+   for (int n = kMaxRStages; n >= 2; n--) {
+      rp = recon_plan_for(g, S, P, C, x3, maxPairs, n);
+      if (rp.total <= kSmemBudget) break;
+   }
    return rp;
 }
 
 template <int S, int P, int C>
 struct Launcher {
    // shared-memory limits of both kernels (once, at create: not inside a stream capture)
-   static pvgpu_status set_attrs(const pvgpu_lca_solver *s) {
+   static pvgpu_status set_attrs(const pvgpu_lca_solver *) {
       const void *fns[4] = {reinterpret_cast<const void *>(recon_tc_kernel<S, P, C, false>),
                             reinterpret_cast<const void *>(recon_tc_kernel<S, P, C, true>),
                             reinterpret_cast<const void *>(post_tc_kernel<S, P, C, false>),
                             reinterpret_cast<const void *>(post_tc_kernel<S, P, C, true>)};
-      const uint32_t bytes[4] = {s->rplan.total, s->rplanX3.total, s->plan.total, s->planX3.total};
       for (int i = 0; i < 4; i++) {
-         if (bytes[i] > 227u * 1024u - 512u) continue;  // a form this shape cannot run (refused at run time)
-         cudaError_t e = cudaFuncSetAttribute(fns[i], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes[i]);
+         cudaError_t e = cudaFuncSetAttribute(fns[i], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBudget);
          if (e != cudaSuccess) return pvgpu::record_cuda_error(e, "lca kernel attributes");
       }
       return PVGPU_OK;
@@ -1067,8 +1090,8 @@ struct Launcher {
       return n;
    }
    static bool fits(const pvgpu_lca_solver *s, bool x3) {
-      const size_t lim = 227 * 1024 - 512;  // static shared memory shares the budget
-      return (x3 ? s->rplanX3.total : s->rplan.total) <= lim && (x3 ? s->planX3.total : s->plan.total) <= lim;
+      const uint32_t pt = x3 ? s->planX3.total : s->plan.total;
+      return (x3 ? s->rplanX3.total : s->rplan.total) <= kSmemBudget && pt && pt <= kSmemBudget;
    }
    static pvgpu_status run_step(pvgpu_lca_solver *s, const float *x, bool x3, cudaStream_t st, cudaEvent_t mid) {
       return x3 ? step<true>(s, x, st, mid) : step<false>(s, x, st, mid);
@@ -1091,6 +1114,41 @@ void free_solver(pvgpu_lca_solver *s) {
    for (void *p : ptrs)
       if (p) cudaFree(p);
    delete s;
+}
+
+// ---- autotuning -------------------------------------------------------------------------
+// The shapes picked for one geometry: kernel P {FT, nV, nW, stageA} and kernel R {nStage}, for
+// the BF16 form [0] and the BF16x3 form [1].  Kept per process, keyed by the geometry and the
+// SM count, and applied to every solver created afterwards with the same geometry.
+struct TunedShapes {
+   int post[2][4];
+   int recon[2];
+};
+
+std::mutex g_tune_mu;
+std::map<std::array<int, 10>, TunedShapes> g_tuned;
+
+std::array<int, 10> tune_key(const pvgpu_lca_solver *s) {
+   const LcaGeom &g = s->g;
+   return {s->S, s->P, s->C, g.nb, g.inNx, g.inNy, g.v1Nx, g.v1Ny, g.F, g_num_sms};
+}
+
+void set_shapes(pvgpu_lca_solver *s, const TunedShapes &t) {
+   for (int x3 = 0; x3 < 2; x3++) {
+      const int *q = t.post[x3];
+      PostPlan pl = post_plan_for(s->g, s->S, s->P, s->C, x3 != 0, g_num_sms, q[0], q[1], q[2], q[3]);
+      if (pl.total && pl.total <= kSmemBudget) (x3 ? s->planX3 : s->plan) = pl;
+      ReconPlan rp = recon_plan_for(s->g, s->S, s->P, s->C, x3 != 0, s->maxPairs[x3], t.recon[x3]);
+      if (rp.total <= kSmemBudget) (x3 ? s->rplanX3 : s->rplan) = rp;
+   }
+   if (s->graph) cudaGraphExecDestroy(s->graph);
+   s->graph = nullptr;
+}
+
+void apply_tuned(pvgpu_lca_solver *s) {
+   std::lock_guard<std::mutex> lk(g_tune_mu);
+   auto it = g_tuned.find(tune_key(s));
+   if (it != g_tuned.end()) set_shapes(s, it->second);
 }
 
 }  // namespace
@@ -1190,15 +1248,20 @@ extern "C" pvgpu_status pvgpu_lca_solver_create(const pvgpu_lca_solver_desc *d, 
    s->planX3 = make_post_plan(g, S, P, C, true, g_num_sms);
    s->rplan = make_recon_plan(g, S, P, C, false, g_num_sms / 2);
    s->rplanX3 = make_recon_plan(g, S, P, C, true, g_num_sms / 2);
+   s->maxPairs[0] = s->maxPairs[1] = g_num_sms / 2;
    dispatch(S, P, C, [&](auto L) {
       // as many pairs as can be resident together (the kernel is persistent)
       for (int x3 = 0; x3 < 2; x3++) {
          ReconPlan &rp = x3 ? s->rplanX3 : s->rplan;
          const int n = L.max_pairs(rp, x3 != 0);
-         if (n > 0) rp = make_recon_plan(g, S, P, C, x3 != 0, std::min(n, g_num_sms / 2));
+         if (n > 0) {
+            s->maxPairs[x3] = std::min(n, g_num_sms / 2);
+            rp = make_recon_plan(g, S, P, C, x3 != 0, s->maxPairs[x3]);
+         }
       }
       return PVGPU_OK;
    });
+   apply_tuned(s);  // shapes an earlier autotune picked for this geometry, if any
    bool fits = true;
    dispatch(S, P, C, [&](auto L) {
       fits = L.fits(s, false);
@@ -1379,6 +1442,104 @@ extern "C" pvgpu_status pvgpu_lca_solver_profile_begin(pvgpu_lca_solver *s, int 
    }
    s->evNext = 0;
    s->profiling = true;
+   return PVGPU_OK;
+}
+
+namespace {
+
+// Kernel R and kernel P times summed over n timesteps of x, launched one by one with events.
+pvgpu_status time_steps(pvgpu_lca_solver *s, const float *x, int n, bool x3, void *stream, double *r, double *p) {
+   pvgpu_status st = pvgpu_lca_solver_profile_begin(s, n);
+   if (st != PVGPU_OK) return st;
+   st = pvgpu_lca_solver_run(s, x, n, x3 ? n : 0, PVGPU_LCA_BF16, stream);
+   int k = 0;
+   pvgpu_status st2 = pvgpu_lca_solver_profile_end(s, r, p, &k);
+   return st != PVGPU_OK ? st : st2;
+}
+
+}  // namespace
+
+extern "C" pvgpu_status pvgpu_lca_solver_autotune(pvgpu_lca_solver *s, const float *x, int trialSteps, void *stream) {
+   if (!s || !x || trialSteps <= 0 || !s->weightsSet) return PVGPU_ERR_BAD_ARG;
+   TunedShapes best;
+   const PostPlan keepP[2] = {s->plan, s->planX3};
+   const ReconPlan keepR[2] = {s->rplan, s->rplanX3};
+   for (int x3 = 0; x3 < 2; x3++) {
+      PostPlan &cur = x3 ? s->planX3 : s->plan;
+      ReconPlan &curR = x3 ? s->rplanX3 : s->rplan;
+      const PostPlan p0 = cur;
+      const ReconPlan r0 = curR;
+      best.post[x3][0] = p0.FT;
+      best.post[x3][1] = p0.nV;
+      best.post[x3][2] = p0.nW;
+      best.post[x3][3] = p0.stageA;
+      best.recon[x3] = r0.nStage;
+      if (!p0.total || p0.total > kSmemBudget || r0.total > kSmemBudget) continue;  // form not offered
+      // kernel P: every feature tile and ring shape that fits
+      double bestMs = 1e30;
+      for (int FT = 64; FT <= 512 && FT <= s->g.F; FT += 64) {
+         if (s->g.F % FT || (FT & (FT - 1))) continue;  // 64, 128, 256, 512 dividing F
+         for (const auto &rg : kRings) {
+            PostPlan pl = post_plan_for(s->g, s->S, s->P, s->C, x3 != 0, g_num_sms, FT, rg[0], rg[1], rg[2]);
+            if (!pl.total || pl.total > kSmemBudget) continue;
+            cur = pl;
+            double r = 0, p = 0;
+            pvgpu_status st = time_steps(s, x, 1, x3 != 0, stream, &r, &p);  // warm-up
+            if (st == PVGPU_OK) st = time_steps(s, x, trialSteps, x3 != 0, stream, &r, &p);
+            if (st != PVGPU_OK) {
+               s->plan = keepP[0];
+               s->planX3 = keepP[1];
+               return st;
+            }
+            if (p < bestMs) {
+               bestMs = p;
+               best.post[x3][0] = FT;
+               best.post[x3][1] = rg[0];
+               best.post[x3][2] = rg[1];
+               best.post[x3][3] = rg[2];
+            }
+         }
+      }
+      cur = post_plan_for(s->g, s->S, s->P, s->C, x3 != 0, g_num_sms, best.post[x3][0], best.post[x3][1],
+                          best.post[x3][2], best.post[x3][3]);
+      // kernel R: every ring depth that fits
+      bestMs = 1e30;
+      for (int n = 2; n <= kMaxRStages; n++) {
+         ReconPlan rp = recon_plan_for(s->g, s->S, s->P, s->C, x3 != 0, s->maxPairs[x3], n);
+         if (rp.total > kSmemBudget) continue;
+         curR = rp;
+         double r = 0, p = 0;
+         pvgpu_status st = time_steps(s, x, 1, x3 != 0, stream, &r, &p);
+         if (st == PVGPU_OK) st = time_steps(s, x, trialSteps, x3 != 0, stream, &r, &p);
+         if (st != PVGPU_OK) {
+            s->rplan = keepR[0];
+            s->rplanX3 = keepR[1];
+            return st;
+         }
+         if (r < bestMs) {
+            bestMs = r;
+            best.recon[x3] = n;
+         }
+      }
+   }
+   set_shapes(s, best);
+   std::lock_guard<std::mutex> lk(g_tune_mu);
+   g_tuned[tune_key(s)] = best;
+   return PVGPU_OK;
+}
+
+extern "C" pvgpu_status pvgpu_lca_solver_plan_info(const pvgpu_lca_solver *s, int *out) {
+   if (!s || !out) return PVGPU_ERR_BAD_ARG;
+   for (int x3 = 0; x3 < 2; x3++) {
+      const PostPlan &pl = x3 ? s->planX3 : s->plan;
+      const ReconPlan &rp = x3 ? s->rplanX3 : s->rplan;
+      int *o = out + 5 * x3;
+      o[0] = pl.FT;
+      o[1] = pl.nV;
+      o[2] = pl.nW;
+      o[3] = pl.stageA;
+      o[4] = rp.nStage;
+   }
    return PVGPU_OK;
 }
 

@@ -176,3 +176,35 @@ def test_lca_bf16_graph_replay_equals_kernel_by_kernel(torch, oracle):
     assert np.array_equal(outs[0], outs[1])
     assert np.array_equal(outs[0], solve(xd, steps, 0, direct=True))
     assert np.array_equal(outs[2], solve(x2, steps, 0, direct=True))
+
+
+def test_lca_autotune_picks_valid_shapes_and_keeps_parity(torch, oracle):
+    """The autotuner times every kernel shape that fits, keeps the fastest (reported by
+    plan_info), hands it to later solvers of the same geometry, and the tuned solver still meets
+    the 1e-3 energy bar against the FP64 oracle."""
+    from openpv_gb300 import capi
+    nb, ins, v1s, nxp, vth, steps, w, x, p = setup(oracle, "colour")
+    v0 = np.zeros((nb,) + v1s)
+    _, _, _, e64 = oracle.lca_run(p, w.astype(np.float64), x[None].astype(np.float64), steps, v0, f64=True,
+                                  want_recon=False)
+    s = capi.LcaSolver(nb, ins, v1s, nxp, vth)
+    s.set_weights(torch.from_numpy(w).cuda())
+    xd = torch.from_numpy(x).cuda()
+    s.autotune(xd, trial_steps=2)
+    info = s.plan_info()
+    for form in ("bf16", "bf16x3"):
+        q = info[form]
+        assert q["feature_tile"] in (64, 128) and v1s[2] % q["feature_tile"] == 0, info
+        assert 1 <= q["v_slots"] <= 3 and 1 <= q["w_slots"] <= 2 and 2 <= q["recon_stages"] <= 4, info
+    assert info["bf16x3"]["a_staged"] == 0
+    s2 = capi.LcaSolver(nb, ins, v1s, nxp, vth)
+    assert s2.plan_info() == info
+    e = torch.zeros(nb, dtype=torch.float64, device="cuda")
+    for x3 in (0, 5):
+        s.reset()
+        s.run(xd, steps, x3_steps=x3, precision=capi.LCA_BF16)
+        s.energy(xd, e)
+        torch.cuda.synchronize()
+        assert s.error_flag() == 0
+        rel = np.abs(e.cpu().numpy() - e64[-1]) / np.abs(e64[-1])
+        assert rel.max() < 1e-3, (x3, rel, info)
