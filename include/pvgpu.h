@@ -155,6 +155,17 @@ pvgpu_status pvgpu_deliver_post(
  * on the device, for WeightsPair::finalizeUpdate (components/WeightsPair.cpp:261-277). */
 pvgpu_status pvgpu_transpose_weights(const pvgpu_conn_desc *conn, const float *preWeights, float *postWeights, void *stream);
 
+/* IdentDelivery::deliver (delivery/IdentDelivery.cpp:99-180): GSyn[b][k] += A_ext[b][kex(k)] for
+ * every restricted neuron k of an IdentConn (pre and post of the same size).  Sparse form when
+ * entries != NULL (halo entries skipped), dense form from aExt otherwise; gsyn is the channel's
+ * [nbatch][ny][nx][nf] buffer. */
+pvgpu_status pvgpu_deliver_ident(const pvgpu_loc *pre, const pvgpu_loc *post, const pvgpu_entry *entries,
+                                 const int64_t *numActive, const float *aExt, float *gsyn, void *stream);
+/* ErrScaleInternalStateBuffer::updateBufferCPU (components/ErrScaleInternalStateBuffer.cpp:41-53):
+ * V[k] *= errScale for the n neurons across the batch (after V = accumulated GSyn). */
+pvgpu_status pvgpu_err_scale(int64_t n, float errScale, float *v, void *stream);
+
+
 /* ---- a6..a9: layer update ------------------------------------------------------------- */
 /* updateGSynAccumulatorOnGPU (components/GSynAccumulator.kpp:16-44): G = sum_ch coeff[ch]*GSyn[ch].
  * coeffs is a host array of numChannels floats. */

@@ -1,0 +1,64 @@
+/* pvhost.h -- C API of libpvhost.so, the C++ host side of the LCA hot path above libpvgpu.so.
+ *
+ * A column is built from the text of an OpenPV params file (HyPerCol, ImageLayer / PvpLayer
+ * inputs, HyPerLayer, ANNLayer, ANNErrorLayer, HyPerLCALayer, HyPerConn, TransposeConn,
+ * IdentConn) with the reference's meaning of every parameter it reads; each connection's
+ * delivery is the class HyPerDeliveryCreator (delivery/HyPerDeliveryCreator.cpp:105-126) names
+ * from receiveGpu / pvpatchAccumulateType / updateGSynFromPostPerspective, all of them on the
+ * GPU ("...ConvolveDelivery" = the reference CPU loop's order, bit for bit).  Weights and input
+ * frames come from the host (the reference reads them from files through weightInitType and
+ * the input layer's inputPath).  Every call returns a pvgpu_status; pvhost_last_error() tells
+ * what went wrong.  Not thread-safe per column. */
+#ifndef PVHOST_H
+#define PVHOST_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "pvgpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct pvhost_column pvhost_column;
+
+/* The message of the last failed call on this thread. */
+const char *pvhost_last_error(void);
+
+/* Parses params text (the grammar of io/parser/params.y) and writes a canonical listing (one
+ * parameter per line) into buf; PVGPU_ERR_BAD_ARG with the line of the error otherwise.  No
+ * GPU needed. */
+pvgpu_status pvhost_params_dump(const char *paramsText, char *buf, size_t bufSize);
+
+/* HyPerCol construction from params text: layers sized from nx, ny, nxScale, nyScale, nf;
+ * halos from the margins the connections need (requiredConvolveMargin); device buffers
+ * allocated; initial V per InitVType (ZeroV, ConstantV) and A = T(V) published. */
+pvgpu_status pvhost_column_create(const char *paramsText, pvhost_column **out);
+pvgpu_status pvhost_column_destroy(pvhost_column *c);
+
+/* Shared weights of a HyPerConn, host FP32 [kernel][nyp][nxp][nfp]; the post weights of a
+ * post-perspective delivery and the weights of every TransposeConn of it follow on the device
+ * (TransposeWeights). */
+pvgpu_status pvhost_set_weights(pvhost_column *c, const char *connName, const float *hostW, int64_t n);
+/* Frames of an input layer, host FP32 [numFrames][nbatch][ny][nx][nf]; frame
+ * ((t - 1) / displayPeriod) % numFrames is shown at timestep t (frame 0 when displayPeriod = 0). */
+pvgpu_status pvhost_set_input(pvhost_column *c, const char *layerName, const float *hostFrames, int numFrames);
+/* V of a non-input layer, host FP32 [nbatch][ny][nx][nf]; A = T(V) is published. */
+pvgpu_status pvhost_set_state(pvhost_column *c, const char *layerName, const float *hostV);
+/* HyPerCol::advanceTime numSteps times (phase order: per phase, every layer of the phase
+ * receives its synaptic input, then updates and publishes); returns when the device is done. */
+pvgpu_status pvhost_advance(pvhost_column *c, int numSteps);
+/* V (which = 0) or the restricted activity A (which = 1) of a layer into host FP32
+ * [nbatch][ny][nx][nf]; n must be that size. */
+pvgpu_status pvhost_read_layer(pvhost_column *c, const char *layerName, int which, float *host, int64_t n);
+/* {nbatch, nx, ny, nf, halo, phase} of a layer. */
+pvgpu_status pvhost_layer_info(pvhost_column *c, const char *layerName, int *out6);
+/* The delivery class a connection got, e.g. "PostsynapticPerspectiveConvolveDelivery". */
+pvgpu_status pvhost_delivery_keyword(pvhost_column *c, const char *connName, char *buf, size_t bufSize);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PVHOST_H */

@@ -17,6 +17,8 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libpvgpu.so")
+HOST = os.path.join(HERE, "host")
+HOST_LIB = os.path.join(HERE, "libpvhost.so")
 INCLUDE = os.path.join(ROOT, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -34,7 +36,7 @@ def nvcc():
 
 def _headers_mtime():
     hs = glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(CSRC, "*.h")) + \
-        glob.glob(os.path.join(INCLUDE, "*.h"))
+        glob.glob(os.path.join(INCLUDE, "*.h")) + glob.glob(os.path.join(HOST, "*.hpp"))
     return max((os.path.getmtime(h) for h in hs), default=0.0)
 
 
@@ -71,7 +73,35 @@ def build(verbose=False, extra=()):
             raise RuntimeError(f"libpvgpu link failed:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
     if verbose:
         print("built", LIB)
+    build_host(verbose)
     return LIB
+
+
+def build_host(verbose=False):
+    """libpvhost.so: the C++ host side (params reader, column, delivery classes) over libpvgpu.so."""
+    srcs = sorted(glob.glob(os.path.join(HOST, "*.cpp")))
+    if not srcs:
+        return None
+    hm = _headers_mtime()
+    flags = ["-I", HOST]
+    with cf.ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 4)) as ex:
+        jobs = [ex.submit(_compile, s, os.path.join(OBJ, "host_" + os.path.splitext(os.path.basename(s))[0] + ".o"),
+                          hm, flags) for s in srcs]
+        results = [j.result() for j in jobs]
+    errs = [e for _, e in results if e]
+    if errs:
+        raise RuntimeError("libpvhost build failed:\n" + "\n".join(errs))
+    objs = [o for o, _ in results]
+    if not os.path.exists(HOST_LIB) or any(os.path.getmtime(o) > os.path.getmtime(HOST_LIB) for o in objs) or \
+            os.path.getmtime(LIB) > os.path.getmtime(HOST_LIB):
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", HOST_LIB] + objs + ["-L", HERE, "-lpvgpu", "-Xlinker",
+                                                                       "-rpath,$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"libpvhost link failed:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    if verbose:
+        print("built", HOST_LIB)
+    return HOST_LIB
 
 
 if __name__ == "__main__":

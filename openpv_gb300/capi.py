@@ -130,6 +130,8 @@ def _declare(L):
         "pvgpu_lca_solver_profile_end": (i, [vp, C.POINTER(d), C.POINTER(d), C.POINTER(i)]),
         "pvgpu_lca_solver_autotune": (i, [vp, vp, i, vp]),
         "pvgpu_lca_solver_plan_info": (i, [vp, C.POINTER(i)]),
+        "pvgpu_deliver_ident": (i, [lp, lp, vp, vp, vp, vp, vp]),
+        "pvgpu_err_scale": (i, [i64, f, vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -137,12 +139,12 @@ def _declare(L):
         fn.argtypes = args
 
 
-def exported_symbols():
-    """Names of the pvgpu_* functions declared in include/pvgpu.h."""
+def exported_symbols(header="pvgpu.h", prefix="pvgpu"):
+    """Names of the <prefix>_* functions declared in include/<header>."""
     import re
-    hdr = os.path.join(os.path.dirname(HERE), "include", "pvgpu.h")
+    hdr = os.path.join(os.path.dirname(HERE), "include", header)
     txt = open(hdr).read()
-    return sorted(set(re.findall(r"\b(pvgpu_[a-z0-9_]+)\s*\(", txt)))
+    return sorted(set(re.findall(r"\b(" + prefix + r"_[a-z0-9_]+)\s*\(", txt)))
 
 
 def version():
@@ -317,3 +319,102 @@ class LcaSolver:
         f = C.c_int(0)
         check(lib().pvgpu_lca_solver_error_flag(self.h, C.byref(f)), "lca_solver_error_flag")
         return f.value
+
+
+# ---- libpvhost.so: the C++ host side (params file -> column of layers and connections) ----------
+
+HOST_LIB_PATH = os.path.join(HERE, "libpvhost.so")
+_host = None
+
+
+def host_lib():
+    global _host
+    if _host is None:
+        lib()  # libpvgpu.so first (libpvhost.so links it)
+        if not os.path.exists(HOST_LIB_PATH):
+            raise RuntimeError(f"{HOST_LIB_PATH} is missing: build it with openpv_gb300.build.build()")
+        _host = C.CDLL(HOST_LIB_PATH)
+        vp, i, i64, sz, cs = C.c_void_p, C.c_int, C.c_int64, C.c_size_t, C.c_char_p
+        sig = {
+            "pvhost_last_error": (cs, []),
+            "pvhost_params_dump": (i, [cs, C.c_char_p, sz]),
+            "pvhost_column_create": (i, [cs, C.POINTER(vp)]),
+            "pvhost_column_destroy": (i, [vp]),
+            "pvhost_set_weights": (i, [vp, cs, vp, i64]),
+            "pvhost_set_input": (i, [vp, cs, vp, i]),
+            "pvhost_set_state": (i, [vp, cs, vp]),
+            "pvhost_advance": (i, [vp, i]),
+            "pvhost_read_layer": (i, [vp, cs, i, vp, i64]),
+            "pvhost_layer_info": (i, [vp, cs, C.POINTER(i)]),
+            "pvhost_delivery_keyword": (i, [vp, cs, C.c_char_p, sz]),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(_host, name)
+            fn.restype = res
+            fn.argtypes = args
+    return _host
+
+
+class PvhostError(RuntimeError):
+    def __init__(self, status, what):
+        self.status = status
+        super().__init__(f"{what}: {status_string(status)} ({host_lib().pvhost_last_error().decode()})")
+
+
+def host_check(status, what):
+    if status != PVGPU_OK:
+        raise PvhostError(status, what)
+
+
+def params_dump(text):
+    """Canonical listing of a params file's groups and parameters (no GPU needed)."""
+    buf = C.create_string_buffer(1 << 20)
+    host_check(host_lib().pvhost_params_dump(text.encode(), buf, len(buf)), "params_dump")
+    return buf.value.decode()
+
+
+class Column:
+    """An OpenPV column built from params text by libpvhost.so; host numpy arrays in and out."""
+
+    def __init__(self, params_text):
+        self.h = C.c_void_p()
+        host_check(host_lib().pvhost_column_create(params_text.encode(), C.byref(self.h)), "column_create")
+
+    def __del__(self):
+        if getattr(self, "h", None) and _host is not None:
+            _host.pvhost_column_destroy(self.h)
+            self.h = None
+
+    def layer_info(self, name):
+        out = (C.c_int * 6)()
+        host_check(host_lib().pvhost_layer_info(self.h, name.encode(), out), "layer_info")
+        return dict(zip(("nbatch", "nx", "ny", "nf", "halo", "phase"), out))
+
+    def delivery(self, conn):
+        buf = C.create_string_buffer(128)
+        host_check(host_lib().pvhost_delivery_keyword(self.h, conn.encode(), buf, len(buf)), "delivery_keyword")
+        return buf.value.decode()
+
+    def set_weights(self, conn, w):
+        w = np.ascontiguousarray(w, dtype=np.float32)
+        host_check(host_lib().pvhost_set_weights(self.h, conn.encode(), w.ctypes.data_as(C.c_void_p), w.size),
+                   "set_weights")
+
+    def set_input(self, layer, frames):
+        f = np.ascontiguousarray(frames, dtype=np.float32)
+        host_check(host_lib().pvhost_set_input(self.h, layer.encode(), f.ctypes.data_as(C.c_void_p), f.shape[0]),
+                   "set_input")
+
+    def set_state(self, layer, v):
+        v = np.ascontiguousarray(v, dtype=np.float32)
+        host_check(host_lib().pvhost_set_state(self.h, layer.encode(), v.ctypes.data_as(C.c_void_p)), "set_state")
+
+    def advance(self, steps):
+        host_check(host_lib().pvhost_advance(self.h, steps), "advance")
+
+    def read(self, layer, which):
+        i = self.layer_info(layer)
+        out = np.zeros((i["nbatch"], i["ny"], i["nx"], i["nf"]), np.float32)
+        host_check(host_lib().pvhost_read_layer(self.h, layer.encode(), 0 if which == "V" else 1,
+                                                out.ctypes.data_as(C.c_void_p), out.size), "read_layer")
+        return out

@@ -48,3 +48,13 @@ def test_bad_arguments_rejected_without_gpu(built):
     assert L.pvgpu_deliver_pre(C.byref(illegal), None, None, dummy, dummy, dummy, 0, None) == 6
     assert L.pvgpu_compact_active(None, 1, 10, None, None, None, 0, None) == 1
     assert L.pvgpu_cost_sum(None, None, 0, 0.0, 0.0, None, None) == 1
+
+
+def test_host_library_exports_every_declared_symbol(built):
+    """libpvhost.so (the C++ host side over the C ABI) loads and exports include/pvhost.h."""
+    from openpv_gb300 import build, capi
+    lib = C.CDLL(build.HOST_LIB)
+    declared = capi.exported_symbols("pvhost.h", "pvhost")
+    assert len(declared) >= 8
+    missing = [s for s in declared if not hasattr(lib, s)]
+    assert not missing, f"declared in include/pvhost.h but not exported: {missing}"

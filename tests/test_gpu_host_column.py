@@ -1,0 +1,110 @@
+"""The C++ host side (libpvhost.so) runs the LCA module from an OpenPV params file on the GPU:
+IdentConn input -> residual, HyPerConn V1 -> residual (presynaptic perspective), TransposeConn
+residual -> V1 (postsynaptic perspective), ANNErrorLayer and HyPerLCALayer updates in phase order.
+
+With receiveGpu = false every delivery is the reference's "...ConvolveDelivery" keyword, run by
+the REFERENCE_ORDER kernels: V and A of V1 equal the FP32 oracle's LCA (the reference CPU loops
+restated and pinned bit for bit) exactly, whether V1 publishes a SparseList or dense activity.
+With receiveGpu = true the "...GPUDelivery" keywords run the FAST kernels: within 1e-5 relative
+(V) of the same oracle after the same steps."""
+import numpy as np
+import pytest
+
+from tests.lca_params import lca_params
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def capi():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from openpv_gb300 import build
+    build.build()
+    from openpv_gb300 import capi
+    return capi
+
+
+def inputs(nb, n, c, nf, nxp, seed=11):
+    rng = np.random.default_rng(seed)
+    x = rng.normal(size=(nb, n, n, c)).astype(np.float32)
+    x = (x - x.mean(axis=(1, 2, 3), keepdims=True)) / x.std(axis=(1, 2, 3), keepdims=True)
+    w = rng.normal(size=(nf, nxp, nxp, c))
+    w = (w / np.sqrt((w ** 2).sum(axis=(1, 2, 3), keepdims=True))).astype(np.float32)
+    return x, w
+
+
+def oracle_lca(oracle, x, w, steps, nb, n, c, nf, nxp, vthresh=0.1, tau=100.0, err_scale=1.0):
+    p = oracle.lca_params(nbatch=nb, inNx=n, inNy=n, inNf=c, v1Nx=n // 2, v1Ny=n // 2, v1Nf=nf, nxp=nxp, nyp=nxp,
+                          VThresh=vthresh, AShift=vthresh, AMin=0.0, VWidth=0.0, tau=tau, errScale=err_scale,
+                          dtFixed=1.0)
+    v0 = np.zeros((nb, n // 2, n // 2, nf), np.float32)
+    v, a, _, _ = oracle.lca_run(p, w, x[None], steps, v0, want_recon=False)
+    return v, a
+
+
+def run_column(capi, text, x, w, steps):
+    col = capi.Column(text)
+    col.set_weights("V1ToResidual", w)
+    col.set_input("Input", x[None])
+    col.advance(steps)
+    return col, col.read("V1", "V"), col.read("V1", "A")
+
+
+@pytest.mark.parametrize("sparse", [True, False])
+def test_convolve_deliveries_equal_the_reference_cpu_path(capi, oracle, sparse):
+    nb, n, c, nf, nxp, steps = 2, 32, 1, 16, 8, 12
+    x, w = inputs(nb, n, c, nf, nxp)
+    col, v, a = run_column(capi, lca_params(nb=nb, n=n, c=c, nf=nf, nxp=nxp, receive_gpu=False, sparse=sparse), x, w,
+                           steps)
+    assert col.delivery("V1ToResidual") == "PresynapticPerspectiveConvolveDelivery"
+    assert col.delivery("ResidualToV1") == "PostsynapticPerspectiveConvolveDelivery"
+    assert col.delivery("InputToResidual") == "IdentDelivery"
+    # halos from the connections' margins (requiredConvolveMargin), as the reference sizes them
+    assert col.layer_info("V1")["halo"] == 2 and col.layer_info("Residual")["halo"] == 3
+    v_ref, a_ref = oracle_lca(oracle, x, w, steps, nb, n, c, nf, nxp)
+    assert (a_ref > 0).any() and (a_ref == 0).any()  # a sparse, nontrivial code
+    assert np.array_equal(v.view(np.uint32), v_ref.view(np.uint32))
+    assert np.array_equal(a.view(np.uint32), a_ref.view(np.uint32))
+
+
+def test_colour_and_err_scale(capi, oracle):
+    nb, n, c, nf, nxp, steps = 1, 32, 3, 32, 8, 8
+    x, w = inputs(nb, n, c, nf, nxp, seed=5)
+    text = lca_params(nb=nb, n=n, c=c, nf=nf, nxp=nxp, receive_gpu=False, err_scale=0.75)
+    _, v, a = run_column(capi, text, x, w, steps)
+    v_ref, a_ref = oracle_lca(oracle, x, w, steps, nb, n, c, nf, nxp, err_scale=0.75)
+    assert np.array_equal(v.view(np.uint32), v_ref.view(np.uint32))
+    assert np.array_equal(a.view(np.uint32), a_ref.view(np.uint32))
+
+
+def test_gpu_deliveries_within_fp32_tolerance(capi, oracle):
+    nb, n, c, nf, nxp, steps = 2, 32, 1, 16, 8, 12
+    x, w = inputs(nb, n, c, nf, nxp)
+    col, v, a = run_column(capi, lca_params(nb=nb, n=n, c=c, nf=nf, nxp=nxp, receive_gpu=True), x, w, steps)
+    assert col.delivery("V1ToResidual") == "PresynapticPerspectiveGPUDelivery"
+    assert col.delivery("ResidualToV1") == "PostsynapticPerspectiveGPUDelivery"
+    v_ref, a_ref = oracle_lca(oracle, x, w, steps, nb, n, c, nf, nxp)
+    vs = np.abs(v_ref).max()
+    np.testing.assert_allclose(v, v_ref, rtol=1e-5, atol=1e-5 * vs)
+    np.testing.assert_allclose(a, a_ref, rtol=1e-5, atol=1e-5 * vs)
+
+
+def test_presynaptic_transpose_and_errors(capi, oracle):
+    """The transpose delivered from the presynaptic perspective (its weights transposed on the
+    device) gives the same V1 within FP32 summation-order tolerance; unsupported switches are
+    refused with the reference's wording."""
+    nb, n, c, nf, nxp, steps = 1, 32, 1, 16, 8, 6
+    x, w = inputs(nb, n, c, nf, nxp)
+    col, v, _ = run_column(capi, lca_params(nb=nb, n=n, c=c, nf=nf, nxp=nxp, post_perspective=False), x, w, steps)
+    assert col.delivery("ResidualToV1") == "PresynapticPerspectiveConvolveDelivery"
+    v_ref, _ = oracle_lca(oracle, x, w, steps, nb, n, c, nf, nxp)
+    np.testing.assert_allclose(v, v_ref, rtol=1e-5, atol=1e-5 * np.abs(v_ref).max())
+    bad = lca_params().replace('pvpatchAccumulateType = "convolve";\n};\n\nTransposeConn',
+                               'pvpatchAccumulateType = "stochastic";\n};\n\nTransposeConn')
+    assert "stochastic" in bad
+    with pytest.raises(RuntimeError, match="PresynapticPerspectiveStochasticDelivery"):
+        capi.Column(bad)
+    with pytest.raises(RuntimeError, match="pvpatchAccumulateType"):
+        capi.Column(lca_params().replace('"convolve"', '"maxpooling"', 1))
