@@ -2,6 +2,8 @@
 the C ABI (libpvgpu.so).  Integer work (compaction, geometry) and the update kernels are
 compared bit for bit; FP32 delivery sums within 1e-5 relative in FAST mode and bit for
 bit in REFERENCE_ORDER mode (the reference's single-thread order)."""
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -289,3 +291,35 @@ def test_tc_gemm_bf16(cuda, M, N, K):
     torch.cuda.synchronize()
     assert int(err.item()) == 0, "a bounded device wait timed out"
     np.testing.assert_allclose(C.cpu().numpy(), ref.numpy(), rtol=1e-4, atol=1e-3)
+
+
+def test_deliver_ident_matches_reference_rule(cuda, oracle):
+    """IdentDelivery (delivery/IdentDelivery.cpp:99-180): GSyn += the restricted activity, from the
+    dense extended buffer or from the SparseList (entries in the halo skipped); one contribution
+    per element, so bit-exact."""
+    torch = cuda
+    from openpv_gb300 import capi
+    pre = capi.Loc.make(3, 20, 12, 5, 2)
+    post = capi.Loc.make(3, 20, 12, 5, 0)
+    rng = np.random.default_rng(21)
+    a = sparse_activity(rng, pre, 0.3, zero_halo=False)  # halo entries present: must be skipped
+    g0 = rng.normal(size=post.res_shape()).astype(np.float32)
+    ref = g0 + a[:, 2:14, 2:22, :]
+    ent, num = oracle.compact(a.reshape(3, -1))
+    L = capi.lib()
+    for sparse in (False, True):
+        g = T(torch, g0)
+        if sparse:
+            ent_d = T(torch, ent.view(np.uint8))
+            st = L.pvgpu_deliver_ident(C.byref(pre), C.byref(post), capi._ptr(ent_d), capi._ptr(T(torch, num)), None,
+                                       capi._ptr(g), capi._stream())
+        else:
+            st = L.pvgpu_deliver_ident(C.byref(pre), C.byref(post), None, None, capi._ptr(T(torch, a)), capi._ptr(g),
+                                       capi._stream())
+        assert st == 0
+        assert np.array_equal(H(g).view(np.uint32), ref.view(np.uint32)), sparse
+    # errScale: V *= s, elementwise in FP32
+    v = rng.normal(size=1000).astype(np.float32)
+    vd = T(torch, v)
+    assert L.pvgpu_err_scale(v.size, C.c_float(0.3), capi._ptr(vd), capi._stream()) == 0
+    assert np.array_equal(H(vd), v * np.float32(0.3))
