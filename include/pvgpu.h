@@ -190,6 +190,20 @@ pvgpu_status pvgpu_lca_update(
       float *v,
       void *stream);
 
+/* MomentumLCAInternalStateBuffer::updateBufferGPU / updateMomentumLCAOnGPU
+ * (components/MomentumLCAInternalStateBuffer.kpp:18-69): drive = (1 - e)(G + selfInteract A),
+ * V = e V + drive + momentumRate prevDrive, prevDrive = drive; e = (float)exp(-dtAdapt[b]/tau).
+ * Bit-identical to the reference CPU update. */
+pvgpu_status pvgpu_momentum_lca_update(const pvgpu_loc *loc, int selfInteract, float momentumRate,
+                                       const double *dtAdapt, float tau, const float *g, const float *aExt,
+                                       float *prevDrive, float *v, void *stream);
+/* ISTAInternalStateBuffer::updateBufferGPU / updateISTAInternalStateBufferOnGPU
+ * (components/ISTAInternalStateBuffer.kpp:16-63): V += ((float)dtAdapt[b] / tau)(G - VThresh sign(A)).
+ * Bit-identical to the reference CPU update. */
+pvgpu_status pvgpu_ista_update(const pvgpu_loc *loc, float VThresh, const double *dtAdapt, float tau, const float *g,
+                               const float *aExt, float *v, void *stream);
+
+
 /* ANNActivityBuffer threshold, CPU form (components/ANNActivityBuffer.cpp:432-558; the
  * reference GPU runs the vertex form of ANNActivityBuffer.kpp:16-77 instead): A_ext = T(V) on
  * the restricted region; the halo is left untouched. */

@@ -131,6 +131,8 @@ def _declare(L):
         "pvgpu_lca_solver_autotune": (i, [vp, vp, i, vp]),
         "pvgpu_lca_solver_plan_info": (i, [vp, C.POINTER(i)]),
         "pvgpu_deliver_ident": (i, [lp, lp, vp, vp, vp, vp, vp]),
+        "pvgpu_momentum_lca_update": (i, [lp, i, f, vp, f, vp, vp, vp, vp, vp]),
+        "pvgpu_ista_update": (i, [lp, f, vp, f, vp, vp, vp, vp]),
         "pvgpu_err_scale": (i, [i64, f, vp, vp]),
     }
     for name, (res, args) in sig.items():
@@ -221,6 +223,17 @@ def gsyn_accumulate(n, coeffs, gsyn, g, stream=None):
 def lca_update(loc, self_interact, dt_adapt, tau, g, a_ext, v, stream=None):
     check(lib().pvgpu_lca_update(C.byref(loc), int(self_interact), _ptr(dt_adapt), tau, _ptr(g), _ptr(a_ext), _ptr(v),
                                  _stream(stream)), "lca_update")
+
+
+def momentum_lca_update(loc, self_interact, momentum_rate, dt_adapt, tau, g, a_ext, prev_drive, v, stream=None):
+    check(lib().pvgpu_momentum_lca_update(C.byref(loc), int(self_interact), momentum_rate, _ptr(dt_adapt), tau,
+                                          _ptr(g), _ptr(a_ext), _ptr(prev_drive), _ptr(v), _stream(stream)),
+          "momentum_lca_update")
+
+
+def ista_update(loc, vthresh, dt_adapt, tau, g, a_ext, v, stream=None):
+    check(lib().pvgpu_ista_update(C.byref(loc), vthresh, _ptr(dt_adapt), tau, _ptr(g), _ptr(a_ext), _ptr(v),
+                                  _stream(stream)), "ista_update")
 
 
 def ann_activity(loc, v, VThresh, AMin, AMax, AShift, VWidth, a_ext, stream=None):

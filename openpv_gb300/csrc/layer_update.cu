@@ -87,6 +87,49 @@ __global__ void __launch_bounds__(kThreads) lca_update_kernel(Loc loc, float si,
    }
 }
 
+// MomentumLCAInternalStateBuffer.kpp:51-66, rounded as the reference's C++ evaluates it:
+// drive = (1 - e)(G + si A); V = (e V + drive) + rate * prevDrive; prevDrive = drive.
+__global__ void __launch_bounds__(kThreads) momentum_lca_kernel(Loc loc, float si, float rate,
+                                                                const double *__restrict__ dtAdapt, float tau,
+                                                                const float *__restrict__ g,
+                                                                const float *__restrict__ aExt,
+                                                                float *__restrict__ prevDrive, float *__restrict__ v) {
+   const int64_t numNeurons = loc.numRes(), total = numNeurons * loc.nb;
+   const int64_t first = (int64_t)blockIdx.x * kThreads * kItems;
+   __shared__ float eS[kMaxB];
+   block_decay(dtAdapt, tau, first, numNeurons, loc.nb, eS);
+   __syncthreads();
+   const int b0 = (int)(first / numNeurons);
+#pragma unroll
+   for (int it = 0; it < kItems; it++) {
+      int64_t i = first + it * kThreads + threadIdx.x;
+      if (i >= total) break;
+      int b = (int)(i / numNeurons);
+      int64_t k = i - (int64_t)b * numNeurons;
+      const float e = eS[b - b0];
+      const float a = aExt[(size_t)b * loc.numExt() + loc.kex(k)];
+      const float drive = __fmul_rn(__fadd_rn(1.0f, -e), __fadd_rn(g[i], __fmul_rn(si, a)));
+      v[i] = __fadd_rn(__fadd_rn(__fmul_rn(e, v[i]), drive), __fmul_rn(rate, prevDrive[i]));
+      prevDrive[i] = drive;
+   }
+}
+
+// ISTAInternalStateBuffer.kpp:46-60: V += ((float)dt / tau)(G - VThresh sign(A)).
+__global__ void __launch_bounds__(kThreads) ista_kernel(Loc loc, float VThresh, const double *__restrict__ dtAdapt,
+                                                        float tau, const float *__restrict__ g,
+                                                        const float *__restrict__ aExt, float *__restrict__ v) {
+   const int64_t numNeurons = loc.numRes(), total = numNeurons * loc.nb;
+   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+      int b = (int)(i / numNeurons);
+      int64_t k = i - (int64_t)b * numNeurons;
+      const float a = aExt[(size_t)b * loc.numExt() + loc.kex(k)];
+      float sign = 0.0f;
+      if (a != 0.0f) sign = __fdiv_rn(a, fabsf(a));
+      const float q = __fdiv_rn((float)dtAdapt[b], tau);
+      v[i] = __fadd_rn(v[i], __fmul_rn(q, __fadd_rn(g[i], -__fmul_rn(VThresh, sign))));
+   }
+}
+
 __global__ void __launch_bounds__(kThreads) ann_kernel(Loc loc, Thresh t, const float *__restrict__ v,
                                                        float *__restrict__ aExt) {
    const int64_t numNeurons = loc.numRes(), total = numNeurons * loc.nb;
@@ -157,6 +200,32 @@ extern "C" pvgpu_status pvgpu_lca_update(const pvgpu_loc *loc, int selfInteract,
    lca_update_kernel<<<(unsigned)blocks, kThreads, 0, pvgpu::as_stream(stream)>>>(l, selfInteract ? 1.0f : 0.0f,
                                                                                   dtAdapt, tau, g, aExt, v);
    PVGPU_CHECK_LAUNCH("lca_update");
+   return PVGPU_OK;
+}
+
+extern "C" pvgpu_status pvgpu_momentum_lca_update(const pvgpu_loc *loc, int selfInteract, float momentumRate,
+                                                  const double *dtAdapt, float tau, const float *g, const float *aExt,
+                                                  float *prevDrive, float *v, void *stream) {
+   if (!loc || !pvgpu::loc_valid(*loc) || !dtAdapt || !g || !aExt || !prevDrive || !v) return PVGPU_ERR_BAD_ARG;
+   Loc l = pvgpu::to_loc(*loc);
+   if (!blocks_fit_batch(l)) return PVGPU_ERR_UNSUPPORTED_SHAPE;
+   int64_t total = l.numRes() * l.nb;
+   int64_t blocks = (total + kThreads * kItems - 1) / (kThreads * kItems);
+   momentum_lca_kernel<<<(unsigned)blocks, kThreads, 0, pvgpu::as_stream(stream)>>>(
+         l, selfInteract ? 1.0f : 0.0f, momentumRate, dtAdapt, tau, g, aExt, prevDrive, v);
+   PVGPU_CHECK_LAUNCH("momentum_lca_update");
+   return PVGPU_OK;
+}
+
+extern "C" pvgpu_status pvgpu_ista_update(const pvgpu_loc *loc, float VThresh, const double *dtAdapt, float tau,
+                                          const float *g, const float *aExt, float *v, void *stream) {
+   if (!loc || !pvgpu::loc_valid(*loc) || !dtAdapt || !g || !aExt || !v) return PVGPU_ERR_BAD_ARG;
+   Loc l = pvgpu::to_loc(*loc);
+   int64_t total = l.numRes() * l.nb;
+   int64_t blocks = (total + kThreads - 1) / kThreads;
+   if (blocks > 152 * 64) blocks = 152 * 64;
+   ista_kernel<<<(unsigned)blocks, kThreads, 0, pvgpu::as_stream(stream)>>>(l, VThresh, dtAdapt, tau, g, aExt, v);
+   PVGPU_CHECK_LAUNCH("ista_update");
    return PVGPU_OK;
 }
 

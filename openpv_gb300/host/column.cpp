@@ -131,12 +131,13 @@ bool Column::build(const std::string &text, std::string &err) {
    for (const auto &g : params_.groups) {
       static const std::map<std::string, Layer::Kind> kinds = {
             {"ImageLayer", Layer::Input}, {"PvpLayer", Layer::Input},     {"HyPerLayer", Layer::HyPer},
-            {"ANNLayer", Layer::ANN},     {"ANNErrorLayer", Layer::ANNError}, {"HyPerLCALayer", Layer::LCA}};
+            {"ANNLayer", Layer::ANN},     {"ANNErrorLayer", Layer::ANNError}, {"HyPerLCALayer", Layer::LCA},
+            {"MomentumLCALayer", Layer::MomentumLCA}, {"ISTALayer", Layer::ISTA}};
       auto k = kinds.find(g.keyword);
       if (k == kinds.end()) {
          if (g.keyword.size() > 5 && g.keyword.compare(g.keyword.size() - 5, 5, "Layer") == 0) {
             err = fmt("layer type ", g.keyword, " is outside this drop-in (inputs, HyPerLayer, ANNLayer, "
-                                                "ANNErrorLayer, HyPerLCALayer)");
+                                                "ANNErrorLayer, HyPerLCALayer, MomentumLCALayer, ISTALayer)");
             return false;
          }
          continue;
@@ -180,6 +181,7 @@ bool Column::build(const std::string &text, std::string &err) {
       }
       L->errScale = (float)g.number("errScale", 1.0);
       L->tau = (float)g.number("timeConstantTau", 1.0);
+      L->momentumRate = (float)g.number("LCAMomentumRate", 0.0);
       L->selfInteract = g.flag("selfInteract", true);
       L->displayPeriod = (int)g.number("displayPeriod", 0);
       if (g.has("adaptiveTimeScaleProbe") && !g.string("adaptiveTimeScaleProbe", "").empty()) {
@@ -334,7 +336,12 @@ bool Column::allocate(std::string &err) {
          L->numChannels = std::max(L->numChannels, 1);
          L->gsyn = (float *)dalloc(L->numRes() * nb * L->numChannels * 4);
          L->G = (float *)dalloc(L->numRes() * nb * 4);
-         L->V = L->kind == Layer::LCA ? (float *)dalloc(L->numRes() * nb * 4) : L->G;
+         const bool ownV = L->kind == Layer::LCA || L->kind == Layer::MomentumLCA || L->kind == Layer::ISTA;
+         L->V = ownV ? (float *)dalloc(L->numRes() * nb * 4) : L->G;
+         if (L->kind == Layer::MomentumLCA) {
+            L->prevDrive = (float *)dalloc(L->numRes() * nb * 4);
+            if (!L->prevDrive) break;
+         }
          L->dtAdapt = (double *)dalloc(nb * sizeof(double));
          if (!L->A || !L->gsyn || !L->G || !L->V || !L->dtAdapt) break;
          std::vector<double> dts(nb, dt_);
@@ -499,6 +506,11 @@ pvgpu_status Column::update(Layer &L, std::string &err) {
       if (s == PVGPU_OK && L.kind == Layer::ANNError && L.errScale != 1.0f) s = pvgpu_err_scale(n, L.errScale, L.V, stream_);
       if (s == PVGPU_OK && L.kind == Layer::LCA)
          s = pvgpu_lca_update(&L.loc, L.selfInteract ? 1 : 0, L.dtAdapt, (float)(L.tau / dt_), L.G, L.A, L.V, stream_);
+      if (s == PVGPU_OK && L.kind == Layer::MomentumLCA)
+         s = pvgpu_momentum_lca_update(&L.loc, L.selfInteract ? 1 : 0, L.momentumRate, L.dtAdapt, (float)(L.tau / dt_),
+                                       L.G, L.A, L.prevDrive, L.V, stream_);
+      if (s == PVGPU_OK && L.kind == Layer::ISTA)
+         s = pvgpu_ista_update(&L.loc, L.VThresh, L.dtAdapt, (float)(L.tau / dt_), L.G, L.A, L.V, stream_);
       if (s == PVGPU_OK)
          s = pvgpu_ann_activity(&L.loc, L.V, L.VThresh, L.AMin, L.AMax, L.AShift, L.VWidth, L.A, stream_);
    }

@@ -7,6 +7,8 @@
 //   ANNLayer            V = G, A = T(V)                 (components/ANNActivityBuffer.cpp)
 //   ANNErrorLayer       V = errScale * G, A = T(V)      (ErrScaleInternalStateBuffer.cpp)
 //   HyPerLCALayer       LCA update, A = T(V)            (HyPerLCAInternalStateBuffer.kpp)
+//   MomentumLCALayer    LCA update with momentum        (MomentumLCAInternalStateBuffer.kpp)
+//   ISTALayer           ISTA update                     (ISTAInternalStateBuffer.kpp)
 //   HyPerConn / TransposeConn / IdentConn               (connections/*.cpp)
 //
 // and selects each connection's delivery by the keyword HyPerDeliveryCreator builds
@@ -37,7 +39,7 @@ class Column;
 struct Conn;
 
 struct Layer {
-   enum Kind { Input, HyPer, ANN, ANNError, LCA } kind = HyPer;
+   enum Kind { Input, HyPer, ANN, ANNError, LCA, MomentumLCA, ISTA } kind = HyPer;
    std::string name, keyword;
    int phase = 0;
    pvgpu_loc loc{};  // halo = the largest margin its outgoing connections need
@@ -47,12 +49,13 @@ struct Layer {
    // activity threshold (ANNActivityBuffer::applyVThresh / applyAMax)
    float VThresh = 0, AMin = 0, AMax = 0, AShift = 0, VWidth = 0;
    float errScale = 1.0f;                // ANNErrorLayer
-   float tau = 1.0f;                     // HyPerLCALayer timeConstantTau
+   float tau = 1.0f;                     // HyPerLCALayer / MomentumLCALayer / ISTALayer timeConstantTau
+   float momentumRate = 0.0f;            // MomentumLCALayer LCAMomentumRate
    bool selfInteract = true;             // HyPerLCALayer
    int displayPeriod = 0;                // input layers
    double initV = 0.0;                   // ConstantV initial state
    // device buffers
-   float *gsyn = nullptr, *G = nullptr, *V = nullptr, *A = nullptr, *frames = nullptr;
+   float *gsyn = nullptr, *G = nullptr, *V = nullptr, *A = nullptr, *frames = nullptr, *prevDrive = nullptr;
    double *dtAdapt = nullptr;
    int numFrames = 0;
    pvgpu_entry *entries = nullptr;

@@ -124,6 +124,8 @@ def _declare(L):
         "pvo_deliver_post_f64": (i, [lp, lp, i, i, vp, vp, d, vp]),
         "pvo_gsyn_accumulate": (None, [i, i, vp, vp, vp]),
         "pvo_lca_update": (None, [lp, i, vp, f, vp, vp, vp]),
+        "pvo_momentum_lca_update": (None, [lp, i, f, vp, f, vp, vp, vp, vp]),
+        "pvo_ista_update": (None, [lp, f, vp, f, vp, vp, vp]),
         "pvo_lca_update_f64": (None, [lp, i, vp, d, vp, vp, vp]),
         "pvo_ann_activity": (None, [lp, vp, f, f, f, f, f, vp]),
         "pvo_ann_activity_f64": (None, [lp, vp, d, d, d, d, d, vp]),
@@ -249,6 +251,23 @@ def lca_update(loc, g, a_ext, v, dt_adapt, tau, self_interact=True):
     v = _c(v, np.float32).copy()
     lib().pvo_lca_update(C.byref(loc), int(self_interact), _p(_c(dt_adapt, np.float64)), tau,
                          _p(_c(g, np.float32)), _p(_c(a_ext, np.float32)), _p(v))
+    return v
+
+
+def momentum_lca_update(loc, g, a_ext, prev_drive, v, dt_adapt, tau, momentum_rate, self_interact=True):
+    """MomentumLCAInternalStateBuffer.kpp:18-69; returns (v, prev_drive)."""
+    v = _c(v, np.float32).copy()
+    pd = _c(prev_drive, np.float32).copy()
+    lib().pvo_momentum_lca_update(C.byref(loc), int(self_interact), momentum_rate, _p(_c(dt_adapt, np.float64)), tau,
+                                  _p(_c(g, np.float32)), _p(_c(a_ext, np.float32)), _p(pd), _p(v))
+    return v, pd
+
+
+def ista_update(loc, g, a_ext, v, dt_adapt, tau, vthresh):
+    """ISTAInternalStateBuffer.kpp:16-63."""
+    v = _c(v, np.float32).copy()
+    lib().pvo_ista_update(C.byref(loc), vthresh, _p(_c(dt_adapt, np.float64)), tau, _p(_c(g, np.float32)),
+                          _p(_c(a_ext, np.float32)), _p(v))
     return v
 
 

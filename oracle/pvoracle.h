@@ -145,6 +145,16 @@ int pvo_deliver_post_f64(
 /* ---- a6..a9: layer update ------------------------------------------------ */
 /* GSynAccumulator.kpp:16-44 */
 void pvo_gsyn_accumulate(int numNeuronsAcrossBatch, int numChannels, const float *coeffs, const float *gsyn, float *g);
+/* MomentumLCAInternalStateBuffer.kpp:18-69 */
+void pvo_momentum_lca_update(const pvo_loc *loc, int selfInteract, float momentumRate, const double *dtAdapt, float tau,
+                             const float *g, const float *aExt, float *prevDrive, float *v);
+void pvo_momentum_lca_update_f64(const pvo_loc *loc, int selfInteract, double momentumRate, const double *dtAdapt,
+                                 double tau, const double *g, const double *aExt, double *prevDrive, double *v);
+/* ISTAInternalStateBuffer.kpp:16-63 */
+void pvo_ista_update(const pvo_loc *loc, float VThresh, const double *dtAdapt, float tau, const float *g,
+                     const float *aExt, float *v);
+void pvo_ista_update_f64(const pvo_loc *loc, double VThresh, const double *dtAdapt, double tau, const double *g,
+                         const double *aExt, double *v);
 /* HyPerLCAInternalStateBuffer.kpp:18-63 */
 void pvo_lca_update(
       const pvo_loc *loc,

@@ -5,6 +5,8 @@
 // Compiled from the reference, unmodified, where they lie:
 //   components/PatchGeometry.cpp            (PV::PatchGeometry)
 //   components/HyPerLCAInternalStateBuffer.kpp  (PV::updateHyPerLCAOnCPU)
+//   components/MomentumLCAInternalStateBuffer.kpp  (PV::updateMomentumLCAOnCPU)
+//   components/ISTAInternalStateBuffer.kpp  (PV::updateISTAInternalStateBufferOnCPU)
 //   components/GSynAccumulator.kpp          (PV::updateGSynAccumulatorOnCPU)
 //   components/ANNActivityBuffer.kpp        (PV::applyVerticesANNActivityBufferOnCPU)
 //   probes/CostFunctions.hpp                (L2/L1/firm-threshold cost functions)
@@ -13,6 +15,8 @@
 
 #include "components/PatchGeometry.hpp"
 #include "components/HyPerLCAInternalStateBuffer.kpp"
+#include "components/ISTAInternalStateBuffer.kpp"
+#include "components/MomentumLCAInternalStateBuffer.kpp"
 #include "components/GSynAccumulator.kpp"
 #include "components/ANNActivityBuffer.kpp"
 #include "probes/CostFunctions.hpp"
@@ -81,6 +85,19 @@ void pvr_lca_update(
       float *v) {
    PV::updateHyPerLCAOnCPU(l->nbatch, l->nx * l->ny * l->nf, l->nx, l->ny, l->nf, l->lt, l->rt, l->dn, l->up,
                            selfInteract != 0, dtAdapt, tau, g, aExt, v);
+}
+
+void pvr_momentum_lca_update(
+      pvr_loc const *l, int selfInteract, float momentumRate, double const *dtAdapt, float tau, float const *g,
+      float const *aExt, float *prevDrive, float *v) {
+   PV::updateMomentumLCAOnCPU(l->nbatch, l->nx * l->ny * l->nf, l->nx, l->ny, l->nf, l->lt, l->rt, l->dn, l->up,
+                              selfInteract != 0, momentumRate, dtAdapt, tau, g, aExt, prevDrive, v);
+}
+
+void pvr_ista_update(
+      pvr_loc const *l, float VThresh, double const *dtAdapt, float tau, float const *g, float const *aExt, float *v) {
+   PV::updateISTAInternalStateBufferOnCPU(l->nbatch, l->nx * l->ny * l->nf, l->nx, l->ny, l->nf, l->lt, l->rt, l->dn,
+                                          l->up, VThresh, dtAdapt, tau, g, aExt, v);
 }
 
 void pvr_gsyn_accumulate(int n, int numChannels, float const *coeffs, float const *gsyn, float *out) {

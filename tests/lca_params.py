@@ -5,7 +5,7 @@ V1 -> residual (channel 1, presynaptic perspective, V1 sparse), TransposeConn re
 
 
 def lca_params(nb=2, n=32, c=1, v1_scale=0.5, nf=16, nxp=8, vthresh=0.1, tau=100.0, receive_gpu=False,
-               sparse=True, post_perspective=True, err_scale=1.0):
+               sparse=True, post_perspective=True, err_scale=1.0, v1_keyword="HyPerLCALayer", momentum=0.0):
     rg = "true" if receive_gpu else "false"
     return f"""
 // LCA module: input -> residual <-> V1
@@ -39,7 +39,8 @@ ANNErrorLayer "Residual" = {{
    sparseLayer = false;
 }};
 
-HyPerLCALayer "V1" = {{
+{v1_keyword} "V1" = {{
+   LCAMomentumRate = {momentum};
    nxScale = {v1_scale};
    nyScale = {v1_scale};
    nf = {nf};

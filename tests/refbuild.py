@@ -42,6 +42,10 @@ def lib():
         _lib.pvr_patch_geometry.argtypes = [lp, lp, C.c_int, C.c_int] + [vp] * 7
         _lib.pvr_lca_update.restype = None
         _lib.pvr_lca_update.argtypes = [lp, C.c_int, vp, C.c_float, vp, vp, vp]
+        _lib.pvr_momentum_lca_update.restype = None
+        _lib.pvr_momentum_lca_update.argtypes = [lp, C.c_int, C.c_float, vp, C.c_float, vp, vp, vp, vp]
+        _lib.pvr_ista_update.restype = None
+        _lib.pvr_ista_update.argtypes = [lp, C.c_float, vp, C.c_float, vp, vp, vp]
         _lib.pvr_gsyn_accumulate.restype = None
         _lib.pvr_gsyn_accumulate.argtypes = [C.c_int, C.c_int, vp, vp, vp]
         _lib.pvr_apply_vertices.restype = None
@@ -82,6 +86,23 @@ def lca_update(loc, g, a_ext, v, dt_adapt, tau, self_interact=True):
     lib().pvr_lca_update(C.byref(RefLoc.of(loc)), int(self_interact),
                          _p(np.ascontiguousarray(dt_adapt, np.float64)), tau,
                          _p(np.ascontiguousarray(g, np.float32)), _p(np.ascontiguousarray(a_ext, np.float32)), _p(v))
+    return v
+
+
+def momentum_lca_update(loc, g, a_ext, prev_drive, v, dt_adapt, tau, momentum_rate, self_interact=True):
+    v = np.ascontiguousarray(v, np.float32).copy()
+    pd = np.ascontiguousarray(prev_drive, np.float32).copy()
+    lib().pvr_momentum_lca_update(C.byref(RefLoc.of(loc)), int(self_interact), momentum_rate,
+                                  _p(np.ascontiguousarray(dt_adapt, np.float64)), tau,
+                                  _p(np.ascontiguousarray(g, np.float32)), _p(np.ascontiguousarray(a_ext, np.float32)),
+                                  _p(pd), _p(v))
+    return v, pd
+
+
+def ista_update(loc, g, a_ext, v, dt_adapt, tau, vthresh):
+    v = np.ascontiguousarray(v, np.float32).copy()
+    lib().pvr_ista_update(C.byref(RefLoc.of(loc)), vthresh, _p(np.ascontiguousarray(dt_adapt, np.float64)), tau,
+                          _p(np.ascontiguousarray(g, np.float32)), _p(np.ascontiguousarray(a_ext, np.float32)), _p(v))
     return v
 
 

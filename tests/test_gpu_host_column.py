@@ -108,3 +108,47 @@ def test_presynaptic_transpose_and_errors(capi, oracle):
         capi.Column(bad)
     with pytest.raises(RuntimeError, match="pvpatchAccumulateType"):
         capi.Column(lca_params().replace('"convolve"', '"maxpooling"', 1))
+
+
+def module_oracle(oracle, x, w, steps, nb, n, c, nf, nxp, kind, vthresh=0.1, tau=100.0, rate=0.0):
+    """The LCA module composed from the oracle's pinned pieces in the reference's phase order,
+    with the V1 membrane update of HyPerLCALayer, MomentumLCALayer or ISTALayer."""
+    v1n = n // 2
+    v1 = oracle.Loc.make(nb, v1n, v1n, nf, 2)
+    er = oracle.Loc.make(nb, n, n, c, 3)
+    fmax = np.float32(3.4028234663852886e38)
+    v = np.zeros(v1.res_shape(), np.float32)
+    prev = np.zeros_like(v)
+    a1 = oracle.ann_activity(v1, v, vthresh, 0.0, fmax, vthresh, 0.0)
+    dt = np.ones(nb, np.float64)
+    for _ in range(steps):
+        ch1 = oracle.deliver_pre(v1, er, nxp, nxp, w, a_ext=a1)
+        g = oracle.gsyn_accumulate(np.stack([x + np.float32(0), ch1]), np.array([1.0, -1.0], np.float32))
+        ae = oracle.ann_activity(er, g, -fmax, -fmax, fmax, 0.0, 0.0)
+        g1 = oracle.gsyn_accumulate(oracle.deliver_post(er, v1, nxp, nxp, w, ae)[None], np.array([1.0, -1.0], np.float32))
+        if kind == "HyPerLCALayer":
+            v = oracle.lca_update(v1, g1, a1, v, dt, tau)
+        elif kind == "MomentumLCALayer":
+            v, prev = oracle.momentum_lca_update(v1, g1, a1, prev, v, dt, tau, rate)
+        else:
+            v = oracle.ista_update(v1, g1, a1, v, dt, tau, vthresh)
+        a1 = oracle.ann_activity(v1, v, vthresh, 0.0, fmax, vthresh, 0.0)
+    return v, a1[:, 2:-2, 2:-2, :]
+
+
+@pytest.mark.parametrize("kind, rate", [("HyPerLCALayer", 0.0), ("MomentumLCALayer", 0.5), ("ISTALayer", 0.0)])
+def test_lca_variants_equal_the_reference_composition(capi, oracle, kind, rate):
+    """MomentumLCALayer (MomentumLCAInternalStateBuffer.kpp) and ISTALayer
+    (ISTAInternalStateBuffer.kpp) in the params-built column, Convolve deliveries: V and A equal
+    the oracle pieces composed in phase order, bit for bit (HyPerLCALayer as the control)."""
+    nb, n, c, nf, nxp, steps = 2, 32, 1, 16, 8, 10
+    x, w = inputs(nb, n, c, nf, nxp, seed=3)
+    tau = 100.0 if kind != "ISTALayer" else 20.0
+    text = lca_params(nb=nb, n=n, c=c, nf=nf, nxp=nxp, tau=tau, v1_keyword=kind, momentum=rate)
+    _, v, a = run_column(capi, text, x, w, steps)
+    v_ref, a_ref = module_oracle(oracle, x, w, steps, nb, n, c, nf, nxp, kind, tau=tau, rate=rate)
+    assert np.array_equal(v.view(np.uint32), v_ref.view(np.uint32)), kind
+    assert np.array_equal(a.view(np.uint32), a_ref.view(np.uint32)), kind
+    if kind == "HyPerLCALayer":  # the composition is the oracle's LCA module itself
+        v2, _ = oracle_lca(oracle, x, w, steps, nb, n, c, nf, nxp)
+        assert np.array_equal(v_ref.view(np.uint32), v2.view(np.uint32))

@@ -238,6 +238,31 @@ def test_update_kernels_bitexact(cuda, oracle):
     assert np.array_equal(H(ad2).view(np.uint32), a2_ref.view(np.uint32))
 
 
+def test_momentum_and_ista_updates_bitexact(cuda, oracle):
+    """MomentumLCAInternalStateBuffer.kpp and ISTAInternalStateBuffer.kpp on the GPU equal the
+    oracle (itself pinned to the reference .kpp code) bit for bit, over several steps."""
+    torch = cuda
+    from openpv_gb300 import capi
+    rng = np.random.default_rng(23)
+    loc = capi.Loc.make(4, 12, 10, 32, 2)
+    ol = OL(oracle, loc)
+    dt = np.array([1.0, 0.5, 0.25, 2.0], np.float64)
+    v = rng.normal(0, 0.3, loc.res_shape()).astype(np.float32)
+    pd = np.zeros_like(v)
+    vd, pdd = T(torch, v), T(torch, pd)
+    vi, vid = v.copy(), T(torch, v)
+    for step in range(4):
+        g = rng.normal(0, 0.3, loc.res_shape()).astype(np.float32)
+        a = oracle.ann_activity(ol, rng.normal(0, 0.3, loc.res_shape()).astype(np.float32), 0.1, 0.0, np.inf, 0.1, 0.0)
+        v, pd = oracle.momentum_lca_update(ol, g, a, pd, v, dt, 50.0, 0.6, step % 2 == 0)
+        capi.momentum_lca_update(loc, step % 2 == 0, 0.6, T(torch, dt), 50.0, T(torch, g), T(torch, a), pdd, vd)
+        assert np.array_equal(H(vd).view(np.uint32), v.view(np.uint32))
+        assert np.array_equal(H(pdd).view(np.uint32), pd.view(np.uint32))
+        vi = oracle.ista_update(ol, g, a, vi, dt, 20.0, 0.1)
+        capi.ista_update(loc, 0.1, T(torch, dt), 20.0, T(torch, g), T(torch, a), vid)
+        assert np.array_equal(H(vid).view(np.uint32), vi.view(np.uint32))
+
+
 # ---- a11: energy ---------------------------------------------------------------------------
 
 @pytest.mark.parametrize("kind,p0,p1", [(0, 0.0, 0.0), (1, 0.0, 0.0), (2, 0.025, 0.025)])

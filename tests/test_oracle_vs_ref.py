@@ -69,6 +69,38 @@ def test_lca_update_bitexact(oracle, halo, self_interact):
     assert np.array_equal(mine.view(np.uint32), ref.view(np.uint32))
 
 
+@pytest.mark.parametrize("halo", [(0, 0), (2, 2)])
+@pytest.mark.parametrize("self_interact", [True, False])
+def test_momentum_lca_update_bitexact(oracle, halo, self_interact):
+    rng = np.random.default_rng(17)
+    loc = L(oracle, 2, 9, 6, 4, *halo)
+    v = rng.normal(size=loc.res_shape()).astype(np.float32)
+    g = rng.normal(size=loc.res_shape()).astype(np.float32)
+    a = rng.normal(size=loc.ext_shape()).astype(np.float32)
+    pd = rng.normal(size=loc.res_shape()).astype(np.float32)
+    dt = np.array([1.0, 0.3], np.float64)
+    for _ in range(3):  # a few steps: the momentum buffer carries over
+        mv, mp = oracle.momentum_lca_update(loc, g, a, pd, v, dt, 50.0, 0.7, self_interact)
+        rv, rp = refbuild.momentum_lca_update(loc, g, a, pd, v, dt, 50.0, 0.7, self_interact)
+        assert np.array_equal(mv.view(np.uint32), rv.view(np.uint32))
+        assert np.array_equal(mp.view(np.uint32), rp.view(np.uint32))
+        v, pd = mv, mp
+
+
+@pytest.mark.parametrize("halo", [(0, 0), (3, 1)])
+def test_ista_update_bitexact(oracle, halo):
+    rng = np.random.default_rng(19)
+    loc = L(oracle, 3, 8, 7, 3, *halo)
+    v = rng.normal(size=loc.res_shape()).astype(np.float32)
+    g = rng.normal(size=loc.res_shape()).astype(np.float32)
+    a = rng.normal(size=loc.ext_shape()).astype(np.float32)
+    a[rng.random(a.shape) < 0.4] = 0.0  # sign(0) = 0
+    dt = np.array([1.0, 0.25, 2.0], np.float64)
+    mine = oracle.ista_update(loc, g, a, v, dt, 20.0, 0.15)
+    ref = refbuild.ista_update(loc, g, a, v, dt, 20.0, 0.15)
+    assert np.array_equal(mine.view(np.uint32), ref.view(np.uint32))
+
+
 @pytest.mark.parametrize("nch", [1, 2, 3])
 def test_gsyn_accumulate_bitexact(oracle, nch):
     rng = np.random.default_rng(nch)
