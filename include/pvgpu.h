@@ -151,6 +151,41 @@ pvgpu_status pvgpu_deliver_post(
       int mode,
       void *stream);
 
+/* ---- a4 / a5 on the tensor cores ---------------------------------------------------------
+ * The same deliveries for a one-to-one connection (pre and post of equal nx, ny; pre.nf and
+ * post.nf multiples of 32; nxp <= 9; equal halo on all sides, at least the connection's
+ * margin), computed as an implicit GEMM on the tcgen05 tensor cores with each FP32 operand
+ * split into two TF32 parts and three TF32 products per term, accumulated in short tensor-core
+ * chains that are summed in FP32 with round-to-nearest: the FAST mode's accuracy class.  Reads the dense
+ * extended presynaptic activity (the layer's activity buffer, which the reference's GPU
+ * deliveries also receive: recv_pre_params.preData, cudakernels/CudaRecvPre.hpp:19-45), so the
+ * cost does not depend on the activity's density.  GSyn of the channel is accumulated into.
+ * `workspace` (device, 16-byte aligned, >= pvgpu_deliver_tc_workspace_bytes) holds the split
+ * (and, for the presynaptic entry, transposed) weights; calls that overlap on the GPU need
+ * separate workspaces.  Other shapes return PVGPU_ERR_UNSUPPORTED_SHAPE: use
+ * pvgpu_deliver_pre / pvgpu_deliver_post.  No reference counterpart as an entry point; it
+ * replaces the same calls as those two. */
+size_t pvgpu_deliver_tc_workspace_bytes(const pvgpu_conn_desc *conn);
+pvgpu_status pvgpu_deliver_post_tc(
+      const pvgpu_conn_desc *conn,
+      const float *aExt,
+      const float *postWeights,
+      float *gsyn,
+      void *workspace,
+      size_t workspaceBytes,
+      void *stream);
+pvgpu_status pvgpu_deliver_pre_tc(
+      const pvgpu_conn_desc *conn,
+      const float *aExt,
+      const float *weights,
+      float *gsyn,
+      void *workspace,
+      size_t workspaceBytes,
+      void *stream);
+/* 1 if a bounded device-side wait of a tensor-core delivery gave up since the last call (and
+ * clears the flag); synchronises the device. */
+int pvgpu_deliver_tc_check_error(void);
+
 /* Post weights from pre weights: TransposeWeights::transposeShared (utils/TransposeWeights.cpp:56-115)
  * on the device, for WeightsPair::finalizeUpdate (components/WeightsPair.cpp:261-277). */
 pvgpu_status pvgpu_transpose_weights(const pvgpu_conn_desc *conn, const float *preWeights, float *postWeights, void *stream);

@@ -17,6 +17,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libpvgpu.so")
 
 PVGPU_OK = 0
+PVGPU_ERR_BAD_ARG = 1
+PVGPU_ERR_UNSUPPORTED_SHAPE = 5
 DELIVER_FAST = 0
 DELIVER_REFERENCE_ORDER = 1
 COST_L2, COST_L1, COST_FIRM = 0, 1, 2
@@ -134,6 +136,10 @@ def _declare(L):
         "pvgpu_momentum_lca_update": (i, [lp, i, f, vp, f, vp, vp, vp, vp, vp]),
         "pvgpu_ista_update": (i, [lp, f, vp, f, vp, vp, vp, vp]),
         "pvgpu_err_scale": (i, [i64, f, vp, vp]),
+        "pvgpu_deliver_tc_workspace_bytes": (sz, [cp]),
+        "pvgpu_deliver_post_tc": (i, [cp, vp, vp, vp, vp, sz, vp]),
+        "pvgpu_deliver_pre_tc": (i, [cp, vp, vp, vp, vp, sz, vp]),
+        "pvgpu_deliver_tc_check_error": (i, []),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -209,6 +215,30 @@ def deliver_pre(conn, weights, gsyn, entries=None, num_active=None, a_ext=None, 
 def deliver_post(conn, a_ext, post_weights, gsyn, mode=DELIVER_FAST, stream=None):
     check(lib().pvgpu_deliver_post(C.byref(conn), _ptr(a_ext), _ptr(post_weights), _ptr(gsyn), mode,
                                    _stream(stream)), "deliver_post")
+
+
+def deliver_tc_workspace_bytes(conn):
+    return int(lib().pvgpu_deliver_tc_workspace_bytes(C.byref(conn)))
+
+
+def _ws_nbytes(workspace):
+    return workspace.numel() * workspace.element_size()
+
+
+def deliver_post_tc(conn, a_ext, post_weights, gsyn, workspace, stream=None):
+    """Post-perspective delivery on the tensor cores (split-TF32); see include/pvgpu.h."""
+    check(lib().pvgpu_deliver_post_tc(C.byref(conn), _ptr(a_ext), _ptr(post_weights), _ptr(gsyn), _ptr(workspace),
+                                      _ws_nbytes(workspace), _stream(stream)), "deliver_post_tc")
+
+
+def deliver_pre_tc(conn, a_ext, weights, gsyn, workspace, stream=None):
+    """Pre-perspective delivery from the dense activity on the tensor cores (split-TF32)."""
+    check(lib().pvgpu_deliver_pre_tc(C.byref(conn), _ptr(a_ext), _ptr(weights), _ptr(gsyn), _ptr(workspace),
+                                     _ws_nbytes(workspace), _stream(stream)), "deliver_pre_tc")
+
+
+def deliver_tc_check_error():
+    return int(lib().pvgpu_deliver_tc_check_error())
 
 
 def transpose_weights(conn, w_pre, w_post, stream=None):

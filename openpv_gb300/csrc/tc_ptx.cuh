@@ -270,3 +270,57 @@ __device__ __forceinline__ bool named_bar_or(int id, int count, bool pred) {
 
 }  // namespace tc
 }  // namespace pvgpu
+
+namespace pvgpu {
+namespace tc {
+
+// ---- TF32 operands (kind::tf32) ------------------------------------------------------------
+// 3-D TMA tile load (coordinates innermost first) completing on an mbarrier.
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, uint64_t *bar, int c0, int c1, int c2) {
+   asm volatile(
+         "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+         ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
+         : "memory");
+}
+
+// FP32 -> TF32 (round to nearest, ties away from zero), returned as an FP32 whose low 13
+// mantissa bits are zero.
+__device__ __forceinline__ float to_tf32(float x) {
+   uint32_t r;
+   asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+   return __uint_as_float(r);
+}
+
+// K-major descriptor without swizzle: 8-row x 16-byte core matrices, `lbo` bytes between core
+// matrices along K, `sbo` bytes between 8-row groups along M/N.  With sbo = 128 the rows of a
+// 16-byte K chunk sit 16 B apart, so an operand may start at any row of such a column.
+__device__ __forceinline__ uint64_t sdesc_noswizzle(uint32_t smem_addr, uint32_t lbo, uint32_t sbo) {
+   uint64_t d = 0;
+   d |= (uint64_t)((smem_addr >> 4) & 0x3FFFu);
+   d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+   d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+   d |= (uint64_t)1 << 46;
+   return d;  // swizzle mode 0
+}
+
+// Instruction descriptor, kind::tf32: D = FP32, A = B = TF32, both K-major, M x N.
+__host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
+   return (1u << 4)                        // D format F32
+          | (2u << 7)                      // A format TF32
+          | (2u << 10)                     // B format TF32
+          | ((uint32_t)(N >> 3) << 17)     // N / 8
+          | ((uint32_t)(M >> 4) << 24);    // M / 16
+}
+
+// D[tmem] (+)= A[smem] * B[smem]^T, one instruction (M x N x 8, TF32), issued by one thread.
+__device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accumulate) {
+   asm volatile(
+         "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+         " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+         "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+         : "memory");
+}
+
+}  // namespace tc
+}  // namespace pvgpu
