@@ -1,9 +1,8 @@
 // deliver_tc.cu -- a4 / a5 on the tensor cores: FP32 one-to-one delivery as an implicit GEMM
 // whose FP32 operands are each split into two TF32 parts (hi = tf32(x), lo = tf32(x - hi)),
-// three TF32 products per term (hi*hi + hi*lo + lo*hi) accumulated in FP32 in TMEM.  The
-// dropped lo*lo term and the split's rounding leave a relative error of about 2^-21 per
-// product, the size of FP32 rounding in a long sum, so the result stands in for the FP32
-// deliveries:
+// three TF32 products per term (hi*hi + hi*lo + lo*hi) accumulated in FP32 in TMEM.  The dropped
+// lo*lo term and the split's rounding leave a relative error of about 2^-21 per product, the size
+// of FP32 rounding in a long sum, so the result stands in for the FP32 deliveries:
 //
 //   GSyn[b][y][x][n] += dt_factor * sum_{ky, kx, f} A_ext[b][y + ky + sy0][x + kx + sx0][f]
 //                                                  * Wpost[n][ky][kx][f]
@@ -22,17 +21,25 @@
 // rows, rows 16 B apart.  In that layout an operand may start at any row, so one split row
 // serves all KX shifts kx (the descriptor starts kx rows down) and all (ky, r) with r + ky = its
 // row.  (A 128-byte-swizzled tile cannot be read from a row that is not a multiple of 8: the
-// MMA applies the swizzle phase from the first row it reads.)  The weight tiles (hi and lo,
-// NT x 32 TF32 each, pre-split in the workspace, 128-byte swizzle) stream through a ring, each
-// used by the R rows of a unit.
+// MMA applies the swizzle phase from the first row it reads.)  The weight tiles (hi rows then
+// lo rows, NT x 32 TF32 each, pre-split in the workspace, 128-byte swizzle) stream through a
+// ring, each used by the R rows of a unit.
+//
+// MMA shape.  One tcgen05.mma costs about 117 cycles for N <= 128 and 171 for N = 256 (TF32,
+// M = 128, same accumulator), against 32 for N = 64 at the tensor pipe's peak, and switching
+// accumulators between consecutive MMAs costs more still.  So the hi and lo weight tiles are
+// one N = 2*NT operand: per K step, MMA 1 = A_hi x [W_hi; W_lo] (N = 2*NT) and MMA 2 =
+// A_lo x W_hi (N = NT) into the same accumulator (columns n: W_hi parts, NT + n: A_hi x W_lo),
+// two MMAs where three N = NT products would take three; the dropped A_lo x W_lo is below 2^-22
+// of each product.
 //
 // Accumulation order.  The tensor core adds each MMA's products into the FP32 accumulator
 // rounding toward zero, so a long chain of MMAs into one accumulator drifts toward zero in
 // proportion to its length (measured: 1e-4 of max|GSyn| at K = 12,544).  The MMAs therefore
 // accumulate short chains -- a run of patch rows of one 32-feature chunk, at least 7 weight
 // tiles (28 K steps) long -- into one of two TMEM chain buffers, and the epilogue warps add each
-// chain into FP32 registers with round-to-nearest, then add dt_factor * sum into GSyn once per
-// unit.  Each chain's drift is small and its sign follows the chain's own partial sum, so the
+// chain's two column halves and then the chain into FP32 registers with round-to-nearest, and
+// add dt_factor * sum into GSyn once per unit.  Each chain's drift is small and its sign follows the chain's own partial sum, so the
 // drifts of the chains cancel like rounding errors.
 //
 #include "pvgpu_internal.cuh"
@@ -70,7 +77,8 @@ __device__ __forceinline__ uint8_t *align1024(uint8_t *p) {
    return reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(p) + 1023) & ~static_cast<uintptr_t>(1023));
 }
 
-// NCH = R * NT / 32: 32-column chunks of one chain buffer, summed in registers by the epilogue.
+// NCH = R * NT / 32: 32-column chunks of the result, summed in registers by the epilogue (a
+// chain buffer holds 2 * NCH chunks: hi-weight and lo-weight columns).
 template <int NCH>
 __global__ void __launch_bounds__(kThreads, 1) conv_tf32x3_kernel(const __grid_constant__ CUtensorMap tmA,
                                                                   const __grid_constant__ CUtensorMap tmB, TcGeom g,
@@ -185,8 +193,16 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tf32x3_kernel(const __grid_c
    } else if (warp == 1) {
       // ================================ MMA issuer ================================
       if (lane == 0) {
-         const uint32_t idesc = idesc_tf32(128, g.NT);
+         const uint32_t idesc = idesc_tf32(128, 2 * g.NT), idescHi = idesc_tf32(128, g.NT);
+         // Descriptors are built once; an operand at byte offset o from its base is the base
+         // descriptor plus o >> 4 (the start-address field, which cannot carry: shared-memory
+         // addresses are below 2^18).
+         const uint64_t aD0 = sdesc_noswizzle(smem_u32(smem), kColA, 128);
+         const uint64_t bD0 = sdesc_sw128(smem_u32(smem + g.offB));
+         constexpr uint64_t kLoA = kHalfA >> 4, kStepA = (2 * kColA) >> 4;
          uint32_t cbase = 0, cb = 0, cc = 0;  // split rows, weight tiles, chains so far
+         int slotBase = 0;                    // cbase % NS
+         int d = 0;                           // cb % NB
          bool ok = true;
          for (int u = blockIdx.x; u < g.units && ok; u += gridDim.x) {
             int grp = 0;
@@ -197,7 +213,7 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tf32x3_kernel(const __grid_c
                   if (chainStart) {
                      const int buf = cc & 1;
                      if (cc >= 2 && !(ok = wait_or_abort(&chainEmpty[buf], ((cc >> 1) - 1) & 1))) break;
-                     tacc = tmem + (uint32_t)(buf * NCH * 32);
+                     tacc = tmem + (uint32_t)(buf * 2 * NCH * 32);
                   }
                   // source rows ky .. ky+R-1 of this chunk must be split
                   for (int j = ky == 0 ? 0 : ky + g.R - 1; j < ky + g.R && ok; j++) {
@@ -206,39 +222,39 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tf32x3_kernel(const __grid_c
                   }
                   if (!ok) break;
                   tc_fence_after();
+                  const int slotKy = (slotBase + ky) % g.NS;
                   for (int kx = 0; kx < g.KX && ok; kx++) {
-                     const int d = (int)(cb % g.NB);
                      if (!(ok = wait_or_abort(&bFull[d], (cb / g.NB) & 1))) break;
                      tc_fence_after();
-                     const uint32_t bHi = smem_u32(smem + g.offB + d * 2 * bBytes), bLo = bHi + bBytes;
+                     const uint64_t bd = bD0 + (uint64_t)((d * 2 * bBytes) >> 4);
                      const bool fresh = chainStart && kx == 0;
+                     int slot = slotKy;
                      for (int r = 0; r < g.R; r++) {
-                        const uint32_t c = cbase + ky + r;
-                        const uint32_t aHi = smem_u32(smem + (c % g.NS) * kSlotA) + kx * 16, aLo = aHi + kHalfA;
-                        const uint32_t dt = tacc + (uint32_t)(r * g.NT);
+                        const uint64_t ad = aD0 + (uint64_t)((slot * kSlotA + kx * 16) >> 4);
+                        const uint32_t dt = tacc + (uint32_t)(r * 2 * g.NT);
 #pragma unroll
                         for (int k = 0; k < 4; k++) {  // K step of 8 TF32 = two chunk columns
-                           const uint64_t ah = sdesc_noswizzle(aHi + k * 2 * kColA, kColA, 128);
-                           const uint64_t al = sdesc_noswizzle(aLo + k * 2 * kColA, kColA, 128);
-                           const uint64_t bh = sdesc_sw128(bHi + k * 32), bl = sdesc_sw128(bLo + k * 32);
-                           mma_tf32(dt, ah, bh, idesc, !(fresh && k == 0));
-                           mma_tf32(dt, ah, bl, idesc, 1);
-                           mma_tf32(dt, al, bh, idesc, 1);
+                           const uint64_t ah = ad + k * kStepA, bhl = bd + 2 * k;
+                           mma_tf32(dt, ah, bhl, idesc, !(fresh && k == 0));  // A_hi x [W_hi; W_lo]
+                           mma_tf32(dt, ah + kLoA, bhl, idescHi, 1);           // A_lo x W_hi
                         }
+                        if (++slot == g.NS) slot = 0;
                      }
                      mma_commit(&bEmpty[d]);
                      cb++;
+                     if (++d == g.NB) d = 0;
                   }
                   if (!ok) break;
-                  mma_commit(&aEmpty[(cbase + ky) % g.NS]);  // row ky has no later use
+                  mma_commit(&aEmpty[slotKy]);  // row ky has no later use
                   if ((grp + 1) % g.groupsPerChain == 0 || grp + 1 == groupsPerUnit) {
                      mma_commit(&chainFull[cc & 1]);
                      cc++;
                   }
                }
                if (!ok) break;
-               for (int j = g.KY; j < rowsPerFC; j++) mma_commit(&aEmpty[(cbase + j) % g.NS]);
+               for (int j = g.KY; j < rowsPerFC; j++) mma_commit(&aEmpty[(slotBase + j) % g.NS]);
                cbase += rowsPerFC;
+               slotBase = (slotBase + rowsPerFC) % g.NS;
             }
          }
          // every MMA issued has completed before TMEM is released
@@ -302,10 +318,19 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tf32x3_kernel(const __grid_c
             tc_fence_after();
 #pragma unroll
             for (int c = 0; c < NCH; c++) {
-               float v[32];
-               tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)((buf * NCH + c) * 32), v);
+               // chunk c = (row r, feature columns h*32 ..): hi-weight part at r*2NT + h*32,
+               // lo-weight part NT columns further
+               const int r = c / chunksPerRow, h = c - r * chunksPerRow;
+               const uint32_t col = (uint32_t)(buf * 2 * NCH * 32 + r * 2 * g.NT + h * 32);
 #pragma unroll
-               for (int i = 0; i < 32; i++) acc[c * 32 + i] = __fadd_rn(acc[c * 32 + i], v[i]);
+               for (int half = 0; half < 2; half++) {
+                  float vh[16], vl[16];
+                  tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + col + 16 * half, vh);
+                  tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + col + 16 * half + g.NT, vl);
+#pragma unroll
+                  for (int i = 0; i < 16; i++)
+                     acc[c * 32 + 16 * half + i] = __fadd_rn(acc[c * 32 + 16 * half + i], __fadd_rn(vh[i], vl[i]));
+               }
             }
             tc_fence_before();
             __syncwarp();
@@ -435,7 +460,7 @@ pvgpu_status plan(const pvgpu_conn_desc *conn, TcGeom &g, int numSms) {
    g.offRaw = (uint32_t)g.NS * kSlotA;
    g.offB = g.offRaw + (uint32_t)g.NR * kHalfA;
    uint32_t cols = 32;
-   while (cols < (uint32_t)(2 * g.R * g.NT)) cols <<= 1;
+   while (cols < (uint32_t)(4 * g.R * g.NT)) cols <<= 1;  // two chain buffers of R x 2NT
    g.tmemCols = cols;
    return PVGPU_OK;
 }
