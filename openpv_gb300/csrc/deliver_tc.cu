@@ -77,9 +77,12 @@ __device__ __forceinline__ uint8_t *align1024(uint8_t *p) {
    return reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(p) + 1023) & ~static_cast<uintptr_t>(1023));
 }
 
-// NCH = R * NT / 32: 32-column chunks of the result, summed in registers by the epilogue (a
-// chain buffer holds 2 * NCH chunks: hi-weight and lo-weight columns).
-template <int NCH>
+// R = target rows per unit (g.R); NCH = R * NT / 32: 32-column chunks of the result, summed in
+// registers by the epilogue (a chain buffer holds 2 * NCH chunks: hi-weight and lo-weight
+// columns).  R is a template parameter so that the 8R MMAs of one weight tile issue as one
+// branch-free sequence: a branch between consecutive tcgen05.mma instructions costs the issuing
+// thread tens of cycles, as much as an N = 64 MMA itself.
+template <int R, int NCH>
 __global__ void __launch_bounds__(kThreads, 1) conv_tf32x3_kernel(const __grid_constant__ CUtensorMap tmA,
                                                                   const __grid_constant__ CUtensorMap tmB, TcGeom g,
                                                                   float *__restrict__ gsyn, int *__restrict__ err) {
@@ -135,6 +138,7 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tf32x3_kernel(const __grid_c
       if (!all && lane == 0) abortFlag = 1;
       return all;
    };
+   auto fresh0 = [](bool fresh) { return fresh ? 0u : 1u; };
    auto unit_of = [&](int u, int &b, int &y0, int &x0, int &n0) {
       n0 = (u % g.nNT) * g.NT;
       const int t0 = u / g.nNT;
@@ -203,6 +207,7 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tf32x3_kernel(const __grid_c
          uint32_t cbase = 0, cb = 0, cc = 0;  // split rows, weight tiles, chains so far
          int slotBase = 0;                    // cbase % NS
          int d = 0;                           // cb % NB
+         uint32_t bPar = 0;                   // (cb / NB) & 1
          bool ok = true;
          for (int u = blockIdx.x; u < g.units && ok; u += gridDim.x) {
             int grp = 0;
@@ -213,6 +218,7 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tf32x3_kernel(const __grid_c
                   if (chainStart) {
                      const int buf = cc & 1;
                      if (cc >= 2 && !(ok = wait_or_abort(&chainEmpty[buf], ((cc >> 1) - 1) & 1))) break;
+                     tc_fence_after();  // the epilogue's TMEM reads of this buffer precede the MMAs
                      tacc = tmem + (uint32_t)(buf * 2 * NCH * 32);
                   }
                   // source rows ky .. ky+R-1 of this chunk must be split
@@ -221,28 +227,34 @@ __global__ void __launch_bounds__(kThreads, 1) conv_tf32x3_kernel(const __grid_c
                      ok = wait_or_abort(&aReady[c % g.NS], (c / g.NS) & 1);
                   }
                   if (!ok) break;
-                  tc_fence_after();
+                  // operands written by TMA or by proxy-fenced stores need no tcgen05 fence
                   const int slotKy = (slotBase + ky) % g.NS;
                   for (int kx = 0; kx < g.KX && ok; kx++) {
-                     if (!(ok = wait_or_abort(&bFull[d], (cb / g.NB) & 1))) break;
-                     tc_fence_after();
+                     if (!(ok = wait_or_abort(&bFull[d], bPar))) break;
                      const uint64_t bd = bD0 + (uint64_t)((d * 2 * bBytes) >> 4);
-                     const bool fresh = chainStart && kx == 0;
-                     int slot = slotKy;
-                     for (int r = 0; r < g.R; r++) {
-                        const uint64_t ad = aD0 + (uint64_t)((slot * kSlotA + kx * 16) >> 4);
+                     const uint32_t acc0 = fresh0(chainStart && kx == 0);
+                     uint64_t adr[R];
+#pragma unroll
+                     for (int r = 0; r < R; r++) {
+                        const int slot = slotKy + r >= g.NS ? slotKy + r - g.NS : slotKy + r;
+                        adr[r] = aD0 + (uint64_t)((slot * kSlotA + kx * 16) >> 4);
+                     }
+#pragma unroll
+                     for (int r = 0; r < R; r++) {
                         const uint32_t dt = tacc + (uint32_t)(r * 2 * g.NT);
 #pragma unroll
                         for (int k = 0; k < 4; k++) {  // K step of 8 TF32 = two chunk columns
-                           const uint64_t ah = ad + k * kStepA, bhl = bd + 2 * k;
-                           mma_tf32(dt, ah, bhl, idesc, !(fresh && k == 0));  // A_hi x [W_hi; W_lo]
+                           const uint64_t ah = adr[r] + k * kStepA, bhl = bd + 2 * k;
+                           mma_tf32(dt, ah, bhl, idesc, k == 0 ? acc0 : 1u);  // A_hi x [W_hi; W_lo]
                            mma_tf32(dt, ah + kLoA, bhl, idescHi, 1);           // A_lo x W_hi
                         }
-                        if (++slot == g.NS) slot = 0;
                      }
                      mma_commit(&bEmpty[d]);
                      cb++;
-                     if (++d == g.NB) d = 0;
+                     if (++d == g.NB) {
+                        d = 0;
+                        bPar ^= 1u;
+                     }
                   }
                   if (!ok) break;
                   mma_commit(&aEmpty[slotKy]);  // row ky has no later use
@@ -441,12 +453,13 @@ pvgpu_status plan(const pvgpu_conn_desc *conn, TcGeom &g, int numSms) {
       const int groups = g.nFC * g.KY;
       g.chainsPerUnit = (groups + g.groupsPerChain - 1) / g.groupsPerChain;
    }
-   // shared memory: split rows (R+1 at least, R+2 preferred), raw rows (2 preferred), weight
-   // tiles (5 preferred: a kx step is short next to a TMA round trip); relax in that order
+   // shared memory: weight tiles first (6 preferred: a slot frees only when its MMAs retire, and
+   // a tile's MMAs are short next to an L2 round trip), then split rows (R+2 preferred, R+1 at
+   // least), then raw rows (2 preferred; one suffices, a source row is needed once per patch row)
    const int64_t bTile = 2 * (int64_t)g.NT * 128;
    const int64_t budget = kSmemLimit - 1024 - 512;
    g.NS = 0;
-   for (int want = 5; want >= 2 && g.NS == 0; want--)
+   for (int want = 6; want >= 2 && g.NS == 0; want--)
       for (int nr = kMaxNR; nr >= 1 && g.NS == 0; nr--)
          for (int ns = std::min(kMaxNS, g.R + 2); ns >= g.R + 1 && g.NS == 0; ns--) {
             const int64_t nbFit = (budget - (int64_t)ns * kSlotA - (int64_t)nr * kHalfA) / bTile;
@@ -523,7 +536,7 @@ pvgpu_status run(const pvgpu_conn_desc *conn, const float *aExt, const float *po
    const int nch = g.R * g.NT / 32;
    using Kern = void (*)(CUtensorMap, CUtensorMap, TcGeom, float *, int *);
    auto launch = [&](Kern kern, int idx) -> pvgpu_status {
-      static bool attrSet[4] = {false, false, false, false};  // one flag per instantiation
+      static bool attrSet[8] = {false, false, false, false, false, false, false, false};  // per instantiation
       if (!attrSet[idx]) {
          PVGPU_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemLimit - 512),
                     "deliver_tc smem attribute");
@@ -533,11 +546,15 @@ pvgpu_status run(const pvgpu_conn_desc *conn, const float *aExt, const float *po
       return PVGPU_OK;
    };
    pvgpu_status ls = PVGPU_ERR_UNSUPPORTED_SHAPE;
-   switch (nch) {
-      case 1: ls = launch(conv_tf32x3_kernel<1>, 0); break;
-      case 2: ls = launch(conv_tf32x3_kernel<2>, 1); break;
-      case 3: ls = launch(conv_tf32x3_kernel<3>, 2); break;
-      case 4: ls = launch(conv_tf32x3_kernel<4>, 3); break;
+   switch (g.R * 8 + nch) {
+      case 1 * 8 + 1: ls = launch(conv_tf32x3_kernel<1, 1>, 0); break;
+      case 1 * 8 + 2: ls = launch(conv_tf32x3_kernel<1, 2>, 1); break;
+      case 1 * 8 + 3: ls = launch(conv_tf32x3_kernel<1, 3>, 2); break;
+      case 1 * 8 + 4: ls = launch(conv_tf32x3_kernel<1, 4>, 3); break;
+      case 2 * 8 + 2: ls = launch(conv_tf32x3_kernel<2, 2>, 4); break;
+      case 2 * 8 + 4: ls = launch(conv_tf32x3_kernel<2, 4>, 5); break;
+      case 3 * 8 + 3: ls = launch(conv_tf32x3_kernel<3, 3>, 6); break;
+      case 4 * 8 + 4: ls = launch(conv_tf32x3_kernel<4, 4>, 7); break;
       default: break;
    }
    if (ls != PVGPU_OK) return ls;
