@@ -222,6 +222,10 @@ def run_reference(args, rank, world):
 # delivery microbenchmark (presynaptic sparse delivery, 128x128x256 -> 128x128x64, 7x7, batch 16)
 # ---------------------------------------------------------------------------------------------
 def delivery_bench(torch, capi, reps=5):
+    """Presynaptic delivery of the 16 x (128x128x256 -> 128x128x64), 7x7 workload at three
+    densities: the sparse kernel from the SparseList, the tensor-core kernel from the dense
+    activity (split-TF32, density-independent), and the faster of the two; then the
+    postsynaptic delivery of the same connection, FP32 SIMT and tensor-core."""
     nb = 16
     pre = capi.Loc.make(nb, 128, 128, 256, 3)
     post = capi.Loc.make(nb, 128, 128, 64, 0)
@@ -229,8 +233,22 @@ def delivery_bench(torch, capi, reps=5):
     g = torch.Generator(device="cuda").manual_seed(1234 + 2)
     w = (torch.randn(256 * 7 * 7 * 64, device="cuda", generator=g) * 0.05).contiguous()
     gsyn = torch.zeros(post.res_shape(), device="cuda")
+    gtc = torch.zeros(post.res_shape(), device="cuda")
     entries = torch.empty((nb, pre.num_ext, 2), dtype=torch.int32, device="cuda")
     num = torch.zeros(nb, dtype=torch.int64, device="cuda")
+    ws = torch.empty(capi.deliver_tc_workspace_bytes(conn), dtype=torch.uint8, device="cuda")
+
+    def timed(fn, n):
+        fn()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(n):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / n
+
+    dense_flops = 2 * nb * 128 * 128 * 64 * 49 * 256
     out = {}
     for p in (0.01, 0.05, 0.2):
         a = torch.zeros(pre.ext_shape(), device="cuda")
@@ -240,29 +258,34 @@ def delivery_bench(torch, capi, reps=5):
         capi.compact_active(a, nb, pre.num_ext, entries, num)
         torch.cuda.synchronize()
         nnz = int(num.sum().item())
-        # warm-up, then reps timed with events
-        capi.deliver_pre(conn, w, gsyn, entries=entries, num_active=num)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        for _ in range(reps):
-            capi.deliver_pre(conn, w, gsyn, entries=entries, num_active=num)
-        e1.record()
-        torch.cuda.synchronize()
-        ms = e0.elapsed_time(e1) / reps
+        ms = timed(lambda: capi.deliver_pre(conn, w, gsyn, entries=entries, num_active=num), reps)
         # algorithmic bytes: entries read, GSyn read+write, weights once
         byts = 8 * nnz + 8 * post.num_res * nb + 4 * w.numel()
         flops = 2 * nnz * 7 * 7 * 64
-        # compaction of the dense activity (HBM-bound integer work)
-        c0, c1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        c0.record()
-        for _ in range(reps):
-            capi.compact_active(a, nb, pre.num_ext, entries, num)
-        c1.record()
-        torch.cuda.synchronize()
-        cms = c0.elapsed_time(c1) / reps
+        cms = timed(lambda: capi.compact_active(a, nb, pre.num_ext, entries, num), reps)
         cbytes = 2 * 4 * pre.num_ext * nb + 8 * nnz  # two passes over the activity + entries written
+        tms = timed(lambda: capi.deliver_pre_tc(conn, a, w, gtc, ws), reps)
+        # size-independent check at full size: both kernels from zero give the same GSyn
+        gsyn.zero_()
+        gtc.zero_()
+        capi.deliver_pre(conn, w, gsyn, entries=entries, num_active=num)
+        capi.deliver_pre_tc(conn, a, w, gtc, ws)
+        torch.cuda.synchronize()
+        rel = float((gsyn - gtc).abs().max().item() / max(gsyn.abs().max().item(), 1e-30))
         out[str(p)] = {"nnz_per_image": nnz / nb, "ms": ms, "GB_s": byts / ms / 1e6, "GFLOP_s": flops / ms / 1e6,
-                       "compaction_ms": cms, "compaction_GB_s": cbytes / cms / 1e6}
+                       "compaction_ms": cms, "compaction_GB_s": cbytes / cms / 1e6,
+                       "tc_ms": tms, "tc_dense_TFLOP_s": dense_flops / tms / 1e9,
+                       "best_ms": min(ms, tms), "best": "sparse" if ms <= tms else "tensor-core",
+                       "sparse_vs_tc_max_rel_diff": rel}
+    capi.deliver_tc_check_error()
+    # postsynaptic perspective, dense activity (p = 0.2 from above), post weights on the device
+    wpost = torch.zeros_like(w)
+    capi.transpose_weights(conn, w, wpost)
+    fp32_ms = timed(lambda: capi.deliver_post(conn, a, wpost, gsyn), 1)
+    tc_ms = timed(lambda: capi.deliver_post_tc(conn, a, wpost, gtc, ws), reps)
+    out["post"] = {"fp32_ms": fp32_ms, "tc_ms": tc_ms, "fp32_TFLOP_s": dense_flops / fp32_ms / 1e9,
+                   "tc_TFLOP_s": dense_flops / tc_ms / 1e9, "speedup_tc_over_fp32": fp32_ms / tc_ms,
+                   "tc_tf32_products_per_term": 3}
     return out
 
 
@@ -458,8 +481,11 @@ def run_ours(args, rank, world, local_rank):
         "cpu_baseline": {"value": cpu_val, "unit": "images*steps/s", "cores": cores, "kind": "port",
                          "sample": f"oracle FP32 LCA, {cores} images (one per thread) x 25 timesteps after 25 "
                                    f"warm-up timesteps, same layer sizes ({cpu_dt:.1f} s)"},
-        "delivery": {"workload": "presynaptic sparse delivery 16 x (128x128x256 -> 128x128x64), 7x7 shared weights",
-                     "by_density": deliv, "hbm_peak_gbs": pk["hbm_gbs"]},
+        "delivery": {"workload": "delivery 16 x (128x128x256 -> 128x128x64), 7x7 shared weights: presynaptic "
+                                 "sparse (SparseList) and tensor-core (dense activity, split-TF32) at three "
+                                 "densities; postsynaptic FP32 SIMT and tensor-core",
+                     "by_density": {k: v for k, v in deliv.items() if k != "post"}, "post": deliv["post"],
+                     "hbm_peak_gbs": pk["hbm_gbs"], "tf32_tensor_peak_tflops": pk["bf16_tflops"] / 2},
         "clocks": clocks,
     }
     print(json.dumps(line), flush=True)
