@@ -56,6 +56,10 @@ pvgpu_status pvhost_read_layer(pvhost_column *c, const char *layerName, int whic
 pvgpu_status pvhost_layer_info(pvhost_column *c, const char *layerName, int *out6);
 /* The delivery class a connection got, e.g. "PostsynapticPerspectiveConvolveDelivery". */
 pvgpu_status pvhost_delivery_keyword(pvhost_column *c, const char *connName, char *buf, size_t bufSize);
+/* Which kernel family ran the connection's last delivery: "tensor-core" (split-TF32 tcgen05),
+ * "simt" (FP32 FAST kernels), "reference-order" (the Convolve keywords), "ident", or "none"
+ * before the first step.  No reference counterpart (diagnostics). */
+pvgpu_status pvhost_delivery_engine(pvhost_column *c, const char *connName, char *buf, size_t bufSize);
 
 #ifdef __cplusplus
 }

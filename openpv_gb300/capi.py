@@ -390,6 +390,7 @@ def host_lib():
             "pvhost_read_layer": (i, [vp, cs, i, vp, i64]),
             "pvhost_layer_info": (i, [vp, cs, C.POINTER(i)]),
             "pvhost_delivery_keyword": (i, [vp, cs, C.c_char_p, sz]),
+            "pvhost_delivery_engine": (i, [vp, cs, C.c_char_p, sz]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(_host, name)
@@ -436,6 +437,11 @@ class Column:
     def delivery(self, conn):
         buf = C.create_string_buffer(128)
         host_check(host_lib().pvhost_delivery_keyword(self.h, conn.encode(), buf, len(buf)), "delivery_keyword")
+        return buf.value.decode()
+
+    def delivery_engine(self, conn):
+        buf = C.create_string_buffer(64)
+        host_check(host_lib().pvhost_delivery_engine(self.h, conn.encode(), buf, len(buf)), "delivery_engine")
         return buf.value.decode()
 
     def set_weights(self, conn, w):

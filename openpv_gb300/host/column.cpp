@@ -40,6 +40,7 @@ class PreDelivery : public Delivery {
    const char *keyword() const override { return kw_; }
    pvgpu_status deliver(float *channel, cudaStream_t s) override {
       const Layer &pre = *c_->pre;
+      engine_ = mode_ == PVGPU_DELIVER_FAST ? "simt" : "reference-order";
       if (pre.sparse)
          return pvgpu_deliver_pre(&c_->desc, pre.entries, pre.numActive, nullptr, c_->W, channel, mode_, s);
       return pvgpu_deliver_pre(&c_->desc, nullptr, nullptr, pre.A, c_->W, channel, mode_, s);
@@ -50,17 +51,44 @@ class PreDelivery : public Delivery {
    const char *kw_;
 };
 
+// The GPU keyword tries the tensor-core form first (one-to-one connections with 32-multiple
+// feature counts) and keeps the SIMT kernel for every other shape; the Convolve keyword always
+// runs the reference-order kernel.
 class PostDelivery : public Delivery {
  public:
    PostDelivery(Conn *c, int mode, const char *kw) : Delivery(c), mode_(mode), kw_(kw) {}
+   ~PostDelivery() override {
+      if (ws_) cudaFree(ws_);
+   }
    const char *keyword() const override { return kw_; }
    pvgpu_status deliver(float *channel, cudaStream_t s) override {
+      if (mode_ == PVGPU_DELIVER_FAST && tc_) {
+         if (!ws_) {
+            wsBytes_ = pvgpu_deliver_tc_workspace_bytes(&c_->desc);
+            if (cudaMalloc(&ws_, wsBytes_) != cudaSuccess) {
+               ws_ = nullptr;
+               return PVGPU_ERR_OOM;
+            }
+         }
+         const pvgpu_status st = pvgpu_deliver_post_tc(&c_->desc, c_->pre->A, c_->Wpost, channel, ws_, wsBytes_, s);
+         if (st != PVGPU_ERR_UNSUPPORTED_SHAPE) {
+            engine_ = "tensor-core";
+            return st;
+         }
+         tc_ = false;  // this geometry stays on the SIMT kernel
+         cudaFree(ws_);
+         ws_ = nullptr;
+      }
+      engine_ = mode_ == PVGPU_DELIVER_FAST ? "simt" : "reference-order";
       return pvgpu_deliver_post(&c_->desc, c_->pre->A, c_->Wpost, channel, mode_, s);
    }
 
  private:
    int mode_;
    const char *kw_;
+   bool tc_ = true;
+   void *ws_ = nullptr;
+   size_t wsBytes_ = 0;
 };
 
 class IdentDeliveryImpl : public Delivery {
@@ -69,6 +97,7 @@ class IdentDeliveryImpl : public Delivery {
    const char *keyword() const override { return "IdentDelivery"; }
    pvgpu_status deliver(float *channel, cudaStream_t s) override {
       const Layer &pre = *c_->pre;
+      engine_ = "ident";
       return pvgpu_deliver_ident(&c_->desc.pre, &c_->desc.post, pre.sparse ? pre.entries : nullptr,
                                  pre.sparse ? pre.numActive : nullptr, pre.sparse ? nullptr : pre.A, channel, s);
    }

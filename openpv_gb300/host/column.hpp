@@ -76,10 +76,13 @@ class Delivery {
    explicit Delivery(Conn *c) : c_(c) {}
    virtual ~Delivery() = default;
    virtual const char *keyword() const = 0;
+   // kernel family of the last deliver() (see pvhost_delivery_engine)
+   virtual const char *engine() const { return engine_; }
    virtual pvgpu_status deliver(float *channel, cudaStream_t s) = 0;
 
  protected:
    Conn *c_;
+   const char *engine_ = "none";
 };
 
 struct Conn {

@@ -101,6 +101,14 @@ extern "C" pvgpu_status pvhost_layer_info(pvhost_column *c, const char *name, in
    return PVGPU_OK;
 }
 
+extern "C" pvgpu_status pvhost_delivery_engine(pvhost_column *c, const char *name, char *buf, size_t n) {
+   if (!c || !name) return fail(PVGPU_ERR_BAD_ARG, "null argument");
+   pvhost::Conn *k = c->col.conn(name);
+   if (!k) return fail(PVGPU_ERR_BAD_ARG, std::string("no connection \"") + name + "\"");
+   if (!copy_out(k->delivery->engine(), buf, n)) return fail(PVGPU_ERR_BAD_ARG, "buffer too small");
+   return PVGPU_OK;
+}
+
 extern "C" pvgpu_status pvhost_delivery_keyword(pvhost_column *c, const char *name, char *buf, size_t n) {
    if (!c || !name) return fail(PVGPU_ERR_BAD_ARG, "null argument");
    pvhost::Conn *k = c->col.conn(name);

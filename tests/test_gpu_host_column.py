@@ -61,6 +61,7 @@ def test_convolve_deliveries_equal_the_reference_cpu_path(capi, oracle, sparse):
     assert col.delivery("V1ToResidual") == "PresynapticPerspectiveConvolveDelivery"
     assert col.delivery("ResidualToV1") == "PostsynapticPerspectiveConvolveDelivery"
     assert col.delivery("InputToResidual") == "IdentDelivery"
+    assert col.delivery_engine("ResidualToV1") == "reference-order"
     # halos from the connections' margins (requiredConvolveMargin), as the reference sizes them
     assert col.layer_info("V1")["halo"] == 2 and col.layer_info("Residual")["halo"] == 3
     v_ref, a_ref = oracle_lca(oracle, x, w, steps, nb, n, c, nf, nxp)
@@ -152,3 +153,44 @@ def test_lca_variants_equal_the_reference_composition(capi, oracle, kind, rate):
     if kind == "HyPerLCALayer":  # the composition is the oracle's LCA module itself
         v2, _ = oracle_lca(oracle, x, w, steps, nb, n, c, nf, nxp)
         assert np.array_equal(v_ref.view(np.uint32), v2.view(np.uint32))
+
+
+def one_to_one_params(nb, nx, ny, cin, cout, p, perspective_post):
+    return f"""
+HyPerCol "column" = {{ nx = {nx}; ny = {ny}; nbatch = {nb}; dt = 1.0; stopTime = 10; }};
+ImageLayer "Input" = {{ nxScale = 1; nyScale = 1; nf = {cin}; phase = 0; displayPeriod = 0; inputPath = "in.txt"; }};
+HyPerLayer "Out" = {{ nxScale = 1; nyScale = 1; nf = {cout}; phase = 1; InitVType = "ZeroV"; sparseLayer = false; }};
+HyPerConn "InToOut" = {{
+   preLayerName = "Input"; postLayerName = "Out"; channelCode = 0;
+   nxp = {p}; nyp = {p}; nfp = {cout}; sharedWeights = true; weightInitType = "FileWeight";
+   initWeightsFile = "w.pvp"; plasticityFlag = false; receiveGpu = true;
+   updateGSynFromPostPerspective = {"true" if perspective_post else "false"}; pvpatchAccumulateType = "convolve";
+}};
+"""
+
+
+@pytest.mark.parametrize("post", [True, False])
+def test_one_to_one_gpu_delivery_in_the_column(capi, oracle, post):
+    """A one-to-one HyPerConn with 32 / 64 features: the postsynaptic GPU keyword runs the
+    tensor-core delivery, the presynaptic one the sparse kernel; both within 1e-5 of the oracle's
+    FP32 delivery of the input frame (HyPerLayer: V = GSyn)."""
+    from tests.test_gpu_kernels import OL
+    nb, nx, ny, cin, cout, p = 2, 40, 12, 32, 64, 5
+    rng = np.random.default_rng(17)
+    x = ((rng.random((nb, ny, nx, cin)) < 0.3) * rng.uniform(0, 1, (nb, ny, nx, cin))).astype(np.float32)
+    w = rng.normal(0, 0.05, (cin, p, p, cout)).astype(np.float32)
+    col = capi.Column(one_to_one_params(nb, nx, ny, cin, cout, p, post))
+    assert col.delivery("InToOut") == ("PostsynapticPerspectiveGPUDelivery" if post else
+                                       "PresynapticPerspectiveGPUDelivery")
+    col.set_weights("InToOut", w)
+    col.set_input("Input", x[None])
+    col.advance(1)
+    assert col.delivery_engine("InToOut") == ("tensor-core" if post else "simt")
+    v = col.read("Out", "V")
+    h = col.layer_info("Input")["halo"]
+    pre = oracle.Loc.make(nb, nx, ny, cin, h, h)
+    postl = oracle.Loc.make(nb, nx, ny, cout, 0, 0)
+    a = np.zeros(pre.ext_shape(), np.float32)
+    a[:, h:h + ny, h:h + nx, :] = x
+    ref = oracle.deliver_pre(pre, postl, p, p, w, a_ext=a)
+    np.testing.assert_allclose(v, ref, rtol=1e-5, atol=1e-5 * np.abs(ref).max())
