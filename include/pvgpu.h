@@ -151,6 +151,44 @@ pvgpu_status pvgpu_deliver_post(
       int mode,
       void *stream);
 
+/* ---- LIF layer update ----------------------------------------------------------------------
+ * LIFActivityComponent::updateActivity (components/LIFActivityComponent.cpp:332-942; CPU-only in
+ * the reference) on the device, one step for every restricted neuron: noise on the EXC, INH and
+ * INHB GSyn channels (gsynHead holds the three, each nbatch * nx*ny*nf), the conductance and
+ * membrane update of `method` ('a' arma, the reference default; 'b' Heun; 'o' exponential Euler),
+ * the threshold relaxation and the spike (A = 1 at the extended index, V = Vrest,
+ * Vth += deltaVth, G_IB += deltaGIB).  rnd, V, Vth, GE, GI, GIB are restricted and updated in
+ * place; aExt's halo is not written.  'b' equals the reference bit for bit; 'a' and 'o' differ
+ * only by the device's expf / powf / logf in their per-neuron filter coefficients. */
+typedef struct {
+   uint32_t s0, s1, s2, s3; /* taus_uint4 (include/pv_types.h:54-59): last output, generator words */
+} pvgpu_taus;
+
+typedef struct { /* LIFParams (components/LIFActivityComponent.hpp:22-45), same fields and order */
+   float Vrest, Vexc, Vinh, VinhB;
+   float VthRest, tau, tauVth, deltaVth, deltaGIB;
+   float noiseAmpE, noiseAmpI, noiseAmpIB, noiseFreqE, noiseFreqI, noiseFreqIB;
+   float tauE, tauI, tauIB;
+} pvgpu_lif_params;
+
+pvgpu_status pvgpu_lif_update(
+      const pvgpu_loc *loc,
+      char method,
+      const pvgpu_lif_params *params,
+      float dt,
+      pvgpu_taus *rnd,
+      float *V,
+      float *Vth,
+      float *GE,
+      float *GI,
+      float *GIB,
+      const float *gsynHead,
+      float *aExt,
+      void *stream);
+
+/* cl_random_init (utils/cl_random.c) on the device: element i seeded with i + seed. */
+pvgpu_status pvgpu_taus_init(pvgpu_taus *state, int64_t count, uint32_t seed, void *stream);
+
 /* ---- a4 / a5 on the tensor cores ---------------------------------------------------------
  * The same deliveries for a one-to-one connection (pre and post of equal nx, ny; pre.nf and
  * post.nf multiples of 32; nxp <= 9; equal halo on all sides, at least the connection's

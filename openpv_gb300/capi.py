@@ -140,6 +140,8 @@ def _declare(L):
         "pvgpu_deliver_post_tc": (i, [cp, vp, vp, vp, vp, sz, vp]),
         "pvgpu_deliver_pre_tc": (i, [cp, vp, vp, vp, vp, sz, vp]),
         "pvgpu_deliver_tc_check_error": (i, []),
+        "pvgpu_lif_update": (i, [lp, C.c_char, vp, f, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
+        "pvgpu_taus_init": (i, [vp, i64, C.c_uint32, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -235,6 +237,34 @@ def deliver_pre_tc(conn, a_ext, weights, gsyn, workspace, stream=None):
     """Pre-perspective delivery from the dense activity on the tensor cores (split-TF32)."""
     check(lib().pvgpu_deliver_pre_tc(C.byref(conn), _ptr(a_ext), _ptr(weights), _ptr(gsyn), _ptr(workspace),
                                      _ws_nbytes(workspace), _stream(stream)), "deliver_pre_tc")
+
+
+LIF_FIELDS = ("Vrest", "Vexc", "Vinh", "VinhB", "VthRest", "tau", "tauVth", "deltaVth", "deltaGIB",
+              "noiseAmpE", "noiseAmpI", "noiseAmpIB", "noiseFreqE", "noiseFreqI", "noiseFreqIB", "tauE", "tauI", "tauIB")
+
+
+class LifParams(C.Structure):
+    """pvgpu_lif_params (LIFParams, components/LIFActivityComponent.hpp:22-45)."""
+    _fields_ = [(n, C.c_float) for n in LIF_FIELDS]
+    DEFAULTS = dict(Vrest=-70.0, Vexc=0.0, Vinh=-75.0, VinhB=-90.0, VthRest=-55.0, tau=20.0, tauVth=10.0,
+                    deltaVth=5.0, deltaGIB=1.0, noiseAmpE=0.0, noiseAmpI=0.0, noiseAmpIB=0.0, noiseFreqE=250.0,
+                    noiseFreqI=250.0, noiseFreqIB=250.0, tauE=1.0, tauI=5.0, tauIB=10.0)
+
+    @staticmethod
+    def make(**kw):
+        d = dict(LifParams.DEFAULTS, **kw)
+        return LifParams(*[d[n] for n in LIF_FIELDS])
+
+
+def lif_update(loc, method, params, dt, rnd, v, vth, ge, gi, gib, gsyn_head, a_ext, stream=None):
+    """LIF step on the device; rnd is a [n, 4] uint32 (or int32) tensor of {s0, s1, s2, s3}."""
+    check(lib().pvgpu_lif_update(C.byref(loc), method.encode()[:1], C.byref(params), dt, _ptr(rnd), _ptr(v),
+                                 _ptr(vth), _ptr(ge), _ptr(gi), _ptr(gib), _ptr(gsyn_head), _ptr(a_ext),
+                                 _stream(stream)), "lif_update")
+
+
+def taus_init(state, count, seed, stream=None):
+    check(lib().pvgpu_taus_init(_ptr(state), count, seed, _stream(stream)), "taus_init")
 
 
 def deliver_tc_check_error():

@@ -125,6 +125,9 @@ def _declare(L):
         "pvo_gsyn_accumulate": (None, [i, i, vp, vp, vp]),
         "pvo_lca_update": (None, [lp, i, vp, f, vp, vp, vp]),
         "pvo_momentum_lca_update": (None, [lp, i, f, vp, f, vp, vp, vp, vp]),
+        "pvo_taus_init": (None, [vp, C.c_size_t, C.c_uint32]),
+        "pvo_taus_next": (None, [vp, C.c_size_t]),
+        "pvo_lif_update": (i, [C.c_char, lp, vp, f, vp, vp, vp, vp, vp, vp, vp, vp]),
         "pvo_ista_update": (None, [lp, f, vp, f, vp, vp, vp]),
         "pvo_lca_update_f64": (None, [lp, i, vp, d, vp, vp, vp]),
         "pvo_ann_activity": (None, [lp, vp, f, f, f, f, f, vp]),
@@ -261,6 +264,49 @@ def momentum_lca_update(loc, g, a_ext, prev_drive, v, dt_adapt, tau, momentum_ra
     lib().pvo_momentum_lca_update(C.byref(loc), int(self_interact), momentum_rate, _p(_c(dt_adapt, np.float64)), tau,
                                   _p(_c(g, np.float32)), _p(_c(a_ext, np.float32)), _p(pd), _p(v))
     return v, pd
+
+
+# LIFParams (components/LIFActivityComponent.hpp:22-45) field order and defaults
+# (include/default_params.h: V_REST -70, V_EXC 0, V_INH -75, V_INHB -90, VTH_REST -55, TAU_VMEM 20,
+# TAU_VTH 10, DELTA_VTH 5, DELTA_G_INHB 1, TAU_EXC 1, TAU_INH 5, TAU_INHB 10; noise amplitudes 0,
+# noise frequencies 250 Hz).
+LIF_FIELDS = ("Vrest", "Vexc", "Vinh", "VinhB", "VthRest", "tau", "tauVth", "deltaVth", "deltaGIB",
+              "noiseAmpE", "noiseAmpI", "noiseAmpIB", "noiseFreqE", "noiseFreqI", "noiseFreqIB", "tauE", "tauI", "tauIB")
+LIF_DEFAULTS = dict(Vrest=-70.0, Vexc=0.0, Vinh=-75.0, VinhB=-90.0, VthRest=-55.0, tau=20.0, tauVth=10.0, deltaVth=5.0,
+                    deltaGIB=1.0, noiseAmpE=0.0, noiseAmpI=0.0, noiseAmpIB=0.0, noiseFreqE=250.0, noiseFreqI=250.0,
+                    noiseFreqIB=250.0, tauE=1.0, tauI=5.0, tauIB=10.0)
+TAUS_DTYPE = np.dtype([("s0", "<u4"), ("s1", "<u4"), ("s2", "<u4"), ("s3", "<u4")])
+
+
+def lif_params_array(**kw):
+    d = dict(LIF_DEFAULTS, **kw)
+    return np.array([d[k] for k in LIF_FIELDS], np.float32)
+
+
+def taus_init(count, seed):
+    """cl_random_init (utils/cl_random.c): structured array of {s0, s1, s2, s3}."""
+    st = np.zeros(count, TAUS_DTYPE)
+    lib().pvo_taus_init(_p(st), count, seed)
+    return st
+
+
+def taus_next(st):
+    st = st.copy()
+    lib().pvo_taus_next(_p(st), st.size)
+    return st
+
+
+def lif_update(method, loc, params, dt, state, gsyn_head, a_ext):
+    """One LIF step (LIFActivityComponent.cpp:332-942).  state: dict of rnd, V, Vth, GE, GI, GIB
+    (updated copies returned); gsyn_head: [3][nbatch*nx*ny*nf] EXC, INH, INHB; returns
+    (state, a_ext)."""
+    st = {k: (v.copy() if k == "rnd" else _c(v, np.float32).copy()) for k, v in state.items()}
+    a = _c(a_ext, np.float32).copy()
+    rc = lib().pvo_lif_update(method.encode()[:1], C.byref(loc), _p(_c(params, np.float32)), dt, _p(st["rnd"]),
+                              _p(st["V"]), _p(st["Vth"]), _p(st["GE"]), _p(st["GI"]), _p(st["GIB"]),
+                              _p(_c(gsyn_head, np.float32)), _p(a))
+    _check(rc, "lif_update")
+    return st, a
 
 
 def ista_update(loc, g, a_ext, v, dt_adapt, tau, vthresh):

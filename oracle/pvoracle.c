@@ -406,3 +406,146 @@ void pvo_gsyn_accumulate(int numNeuronsAcrossBatch, int numChannels, const float
       g[index] = value;
    }
 }
+
+/* ---- LIF (components/LIFActivityComponent.cpp:332-942) ------------------------------------ */
+
+/* Tausworthe generator of utils/cl_random.c (after GSL rng/taus.c): three shift-register
+ * components; s0 holds the last output s1 ^ s2 ^ s3. */
+static uint32_t taus_component(uint32_t s, int a, int b, uint32_t mask, int d) {
+   return ((s & mask) << d) ^ (((s << a) ^ s) >> b);
+}
+
+static pvo_taus taus_next(pvo_taus t) {
+   t.s1 = taus_component(t.s1, 13, 19, 4294967294u, 12);
+   t.s2 = taus_component(t.s2, 2, 25, 4294967288u, 4);
+   t.s3 = taus_component(t.s3, 3, 11, 4294967280u, 17);
+   t.s0 = t.s1 ^ t.s2 ^ t.s3;
+   return t;
+}
+
+/* cl_random_prob: the last output scaled to [0, 1) in float. */
+static float taus_uniform(pvo_taus t) { return (float)t.s0 / 4294967296.0f; }
+
+/* cl_random_init (utils/cl_random.c): element i is seeded with i + seed (0 counts as 1) through
+ * three LCG steps, then warmed up by six generator steps; s0 = s1 ^ s2 ^ s3. */
+void pvo_taus_init(pvo_taus *state, size_t count, uint32_t seed) {
+   if (seed == 0) seed = 1;
+   for (size_t i = 0; i < count; i++) {
+      uint32_t s = (uint32_t)i + seed;
+      if (s == 0) s = 1;
+      pvo_taus t;
+      t.s1 = 69069u * s;
+      t.s2 = 69069u * t.s1;
+      t.s3 = 69069u * t.s2;
+      for (int w = 0; w < 6; w++) t = taus_next(t);
+      t.s0 = t.s1 ^ t.s2 ^ t.s3;
+      state[i] = t;
+   }
+}
+
+void pvo_taus_next(pvo_taus *state, size_t count) {
+   for (size_t i = 0; i < count; i++) state[i] = taus_next(state[i]);
+}
+
+/* Noise on one conductance input: one draw decides whether an event happens this step (rate
+ * freq in Hz over dt in seconds), a second draw scales its amplitude. */
+static float lif_noise(pvo_taus *r, float gsyn, float dtSec, float freq, float amp) {
+   *r = taus_next(*r);
+   if (taus_uniform(*r) < dtSec * freq) {
+      *r = taus_next(*r);
+      gsyn = gsyn + amp * taus_uniform(*r);
+   }
+   return gsyn;
+}
+
+/* dV/dt of the conductance-based membrane (LIF_Vmem_derivative). */
+static float lif_dvdt(float v, float ge, float gi, float gib, const pvo_lif_params *p) {
+   float g = 1.0f + ge + gi + gib;
+   float vinf = (p->Vrest + p->Vexc * ge + p->Vinh * gi + p->VinhB * gib) / g;
+   return g * (vinf - v) / p->tau;
+}
+
+/* One LIF timestep for every restricted neuron (index k across the batch), in the reference's
+ * float arithmetic: noise on the three GSyn channels (EXC, INH, INHB at channel offsets
+ * c * nbatch * numNeurons), the conductance and membrane update of the method ('a' arma filter,
+ * 'b' Heun with conductances at both ends of the step, 'o' exponential Euler with end-of-step
+ * conductances), the threshold relaxation, and the spike (A = 1 at the extended index, V reset to
+ * Vrest, Vth += deltaVth, G_IB += deltaGIB).  GMAX = 10 caps each conductance. */
+int pvo_lif_update(char method, const pvo_loc *loc, const pvo_lif_params *p, float dt, pvo_taus *rnd, float *V,
+                   float *Vth, float *GE, float *GI, float *GIB, const float *gsynHead, float *aExt) {
+   if (method != 'a' && method != 'b' && method != 'o') return -1;
+   const float GMAX = 10.0f;
+   const int numNeurons = loc_num_res(loc);
+   const int numExt = loc_num_ext(loc);
+   const int total = numNeurons * loc->nbatch;
+   const float eE = expf(-dt / p->tauE), eI = expf(-dt / p->tauI), eIB = expf(-dt / p->tauIB);
+   const float eVth = expf(-dt / p->tauVth);
+   const float dtSec = 0.001f * dt;
+   const float *gsE = gsynHead, *gsI = gsynHead + total, *gsIB = gsynHead + 2 * (size_t)total;
+   for (int k = 0; k < total; k++) {
+      const int b = k / numNeurons, kr = k % numNeurons;
+      const int kex = b * numExt + kIndexExtended(kr, loc->nx, loc->ny, loc->nf, loc->halo.lt, loc->halo.rt,
+                                                  loc->halo.dn, loc->halo.up);
+      pvo_taus r = rnd[k];
+      float v = V[k], vth = Vth[k], ge = GE[k], gi = GI[k], gib = GIB[k];
+      float inE = lif_noise(&r, gsE[k], dtSec, p->noiseFreqE, p->noiseAmpE);
+      float inI = lif_noise(&r, gsI[k], dtSec, p->noiseFreqI, p->noiseAmpI);
+      float inIB = lif_noise(&r, gsIB[k], dtSec, p->noiseFreqIB, p->noiseAmpIB);
+      if (method == 'o') {
+         ge = inE + ge * eE;
+         gi = inI + gi * eI;
+         gib = inIB + gib * eIB;
+         ge = ge > GMAX ? GMAX : ge;
+         gi = gi > GMAX ? GMAX : gi;
+         gib = gib > GMAX ? GMAX : gib;
+         float tauInf = (dt / p->tau) * (1.0f + ge + gi + gib);
+         float vInf = (p->Vrest + ge * p->Vexc + gi * p->Vinh + gib * p->VinhB) / (1.0f + ge + gi + gib);
+         v = vInf + (v - vInf) * expf(-tauInf);
+      } else {
+         float ge0 = ge + inE, gi0 = gi + inI, gib0 = gib + inIB;
+         float tauInf0 = 0.0f, vInf0 = 0.0f;
+         if (method == 'a') {  /* before the cap */
+            tauInf0 = p->tau / (1 + ge0 + gi0 + gib0);
+            vInf0 = (p->Vrest + p->Vexc * ge0 + p->Vinh * gi0 + p->VinhB * gib0) / (1 + ge0 + gi0 + gib0);
+         }
+         ge0 = ge0 > GMAX ? GMAX : ge0;
+         gi0 = gi0 > GMAX ? GMAX : gi0;
+         gib0 = gib0 > GMAX ? GMAX : gib0;
+         float ge1 = ge0 * eE, gi1 = gi0 * eI, gib1 = gib0 * eIB;
+         if (method == 'b') {
+            float d1 = lif_dvdt(v, ge0, gi0, gib0, p);
+            float d2 = lif_dvdt(v + dt * d1, ge1, gi1, gib1, p);
+            float d = (d1 + d2) * 0.5f;
+            v = v + dt * d;
+         } else {
+            /* the end-of-step time constant takes the start-of-step G_IB, as the reference does */
+            float tauInf1 = p->tau / (1 + ge1 + gi1 + gib0);
+            float vInf1 = (p->Vrest + p->Vexc * ge1 + p->Vinh * gi1 + p->VinhB * gib1) / (1 + ge1 + gi1 + gib1);
+            float slope = (tauInf1 - tauInf0) / dt;
+            float f1 = slope == 0.0f ? expf(-dt / tauInf0) : powf(tauInf1 / tauInf0, -1 / slope);
+            float f2 = slope == -1.0f ? tauInf0 / dt * logf(tauInf1 / tauInf0 + 1.0f)
+                                      : (1 - tauInf0 / dt * (1 - f1)) / (1 + slope);
+            float f3 = 1.0f - f1 - f2;
+            v = f1 * v + f2 * vInf0 + f3 * vInf1;
+         }
+         ge = ge1;
+         gi = gi1;
+         gib = gib1;
+      }
+      vth = p->VthRest + (vth - p->VthRest) * eVth;
+      const int fired = v > vth;
+      aExt[kex] = fired ? 1.0f : 0.0f;
+      if (fired) {
+         v = p->Vrest;
+         vth = vth + p->deltaVth;
+         gib = gib + p->deltaGIB;
+      }
+      rnd[k] = r;
+      V[k] = v;
+      Vth[k] = vth;
+      GE[k] = ge;
+      GI[k] = gi;
+      GIB[k] = gib;
+   }
+   return 0;
+}

@@ -24,6 +24,7 @@
 #ifndef PVORACLE_H_
 #define PVORACLE_H_
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -305,6 +306,28 @@ int pvo_lca_run_f64(
       double *energy,
       double *aFinal,
       int numThreads);
+
+
+/* ---- LIF (components/LIFActivityComponent.cpp:332-942) ---- */
+/* taus_uint4 (include/pv_types.h:54-59): last output, then the three generator words. */
+typedef struct {
+   uint32_t s0, s1, s2, s3;
+} pvo_taus;
+
+/* LIFParams (components/LIFActivityComponent.hpp:22-45), same order; defaults from
+ * include/default_params.h. */
+typedef struct {
+   float Vrest, Vexc, Vinh, VinhB;
+   float VthRest, tau, tauVth, deltaVth, deltaGIB;
+   float noiseAmpE, noiseAmpI, noiseAmpIB, noiseFreqE, noiseFreqI, noiseFreqIB;
+   float tauE, tauI, tauIB;
+} pvo_lif_params;
+
+void pvo_taus_init(pvo_taus *state, size_t count, uint32_t seed);
+void pvo_taus_next(pvo_taus *state, size_t count);
+/* method 'a' (arma), 'b' (beginning: Heun), 'o' (original: Euler); returns -1 otherwise. */
+int pvo_lif_update(char method, const pvo_loc *loc, const pvo_lif_params *p, float dt, pvo_taus *rnd, float *V,
+                   float *Vth, float *GE, float *GI, float *GIB, const float *gsynHead, float *aExt);
 
 #ifdef __cplusplus
 }

@@ -54,6 +54,12 @@ def lib():
         _lib.pvr_deliver_pre.argtypes = [lp, lp, C.c_int, C.c_int, vp, vp, vp, vp, vp]
         _lib.pvr_deliver_post.restype = C.c_int
         _lib.pvr_deliver_post.argtypes = [lp, lp, C.c_int, C.c_int, vp, vp, vp]
+        _lib.pvr_lif_update.restype = C.c_int
+        _lib.pvr_lif_update.argtypes = [C.c_char, lp, vp, C.c_float, C.c_float] + [vp] * 8
+        _lib.pvr_taus_init.restype = None
+        _lib.pvr_taus_init.argtypes = [vp, C.c_size_t, C.c_uint]
+        _lib.pvr_taus_next.restype = None
+        _lib.pvr_taus_next.argtypes = [vp, C.c_size_t]
         _lib.pvr_cost.restype = C.c_double
         _lib.pvr_cost.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double]
     return _lib
@@ -152,3 +158,26 @@ def deliver_post(src, tgt, nxp_post, nyp_post, w_post, a_ext, gsyn=None):
     if rc != 0:
         raise ValueError("reference rejected geometry")
     return g
+
+
+def taus_init(count, seed, dtype):
+    st = np.zeros(count, dtype)
+    lib().pvr_taus_init(_p(st), count, seed)
+    return st
+
+
+def taus_next(st):
+    st = st.copy()
+    lib().pvr_taus_next(_p(st), st.size)
+    return st
+
+
+def lif_update(method, loc, params, dt, state, gsyn_head, a_ext, sim_time=0.0):
+    """The reference's LIFActivityComponent::updateActivity{Arma,Beginning,Original}."""
+    st = {k: v.copy() for k, v in state.items()}
+    a = np.ascontiguousarray(a_ext, dtype=np.float32).copy()
+    rc = lib().pvr_lif_update(method.encode()[:1], C.byref(RefLoc.of(loc)), _p(np.ascontiguousarray(params, np.float32)),
+                              sim_time, dt, _p(st["rnd"]), _p(st["V"]), _p(st["Vth"]), _p(st["GE"]), _p(st["GI"]),
+                              _p(st["GIB"]), _p(np.ascontiguousarray(gsyn_head, np.float32)), _p(a))
+    assert rc == 0
+    return st, a

@@ -1,0 +1,153 @@
+"""LIF on the device (pvgpu_lif_update, pvgpu_taus_init) against the oracle's restatement of
+LIFActivityComponent.cpp, itself pinned bit for bit to the reference's own update loops
+(tests/test_oracle_vs_ref.py).  Method 'b' and the generator are compared bit for bit; 'a' and
+'o' bit for bit in everything but V, which carries the device's expf / powf / logf in the filter
+coefficients (within 2e-6 relative).  A spiking network step -- Poisson spikes as a SparseList,
+presynaptic delivery into the EXC channel, the LIF update, compaction of the spikes -- is checked
+against the oracle composed the same way."""
+import numpy as np
+import pytest
+
+from tests.test_gpu_kernels import OL, H, T
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def cuda():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from openpv_gb300 import build
+    build.build()
+    from openpv_gb300 import capi
+    capi.lib()
+    return torch
+
+
+def state(oracle, n, rng, seed):
+    return {"rnd": oracle.taus_init(n, seed),
+            "V": rng.uniform(-75.0, -50.0, n).astype(np.float32),
+            "Vth": rng.uniform(-57.0, -48.0, n).astype(np.float32),
+            "GE": rng.uniform(0.0, 2.0, n).astype(np.float32),
+            "GI": rng.uniform(0.0, 1.0, n).astype(np.float32),
+            "GIB": rng.uniform(0.0, 0.5, n).astype(np.float32)}
+
+
+def to_dev(torch, st):
+    return {k: T(torch, v.view(np.uint32).reshape(-1, 4).view(np.int32) if k == "rnd" else v) for k, v in st.items()}
+
+
+def from_dev(d, dtype):
+    return {k: (H(v).view(np.uint32).reshape(-1).view(dtype) if k == "rnd" else H(v)) for k, v in d.items()}
+
+
+def test_taus_init_bitexact(cuda, oracle):
+    torch = cuda
+    from openpv_gb300 import capi
+    for n, seed in [(1, 0), (1000, 17), (70000, 123456)]:
+        d = torch.zeros((n, 4), dtype=torch.int32, device="cuda")
+        capi.taus_init(d, n, seed)
+        ref = oracle.taus_init(n, seed)
+        assert np.array_equal(H(d).view(np.uint32).reshape(-1), ref.view(np.uint32))
+
+
+@pytest.mark.parametrize("method", ["b", "a", "o"])
+@pytest.mark.parametrize("noise", [False, True])
+def test_lif_update_matches_oracle(cuda, oracle, method, noise):
+    torch = cuda
+    from openpv_gb300 import capi
+    loc = capi.Loc.make(3, 40, 17, 8, 2)
+    ol = OL(oracle, loc)
+    n = loc.nbatch * loc.nx * loc.ny * loc.nf
+    rng = np.random.default_rng(ord(method) * 3 + noise)
+    kw = dict(noiseAmpE=0.5, noiseAmpI=0.3, noiseAmpIB=0.2, noiseFreqE=300.0) if noise else {}
+    p_o, p_d = oracle.lif_params_array(**kw), capi.LifParams.make(**kw)
+    st = state(oracle, n, rng, seed=5)
+    dev = to_dev(torch, st)
+    a_o = np.zeros(loc.ext_shape(), np.float32)
+    a_d = T(torch, a_o)
+    fired = 0
+    for step in range(5):
+        gs = np.stack([rng.uniform(0, 1.5, n), rng.uniform(0, 0.8, n), rng.uniform(0, 0.3, n)]).astype(np.float32)
+        st, a_o = oracle.lif_update(method, ol, p_o, 1.0, st, gs, a_o)
+        capi.lif_update(loc, method, p_d, 1.0, dev["rnd"], dev["V"], dev["Vth"], dev["GE"], dev["GI"], dev["GIB"],
+                        T(torch, gs), a_d)
+        got = from_dev(dev, oracle.TAUS_DTYPE)
+        assert np.array_equal(H(a_d), a_o), step
+        fired += int(a_o.sum())
+        for k in ("rnd", "Vth", "GE", "GI", "GIB") + (("V",) if method == "b" else ()):
+            assert np.array_equal(got[k].view(np.uint32), st[k].view(np.uint32)), (k, step)
+        if method != "b":
+            np.testing.assert_allclose(got["V"], st["V"], rtol=2e-6, atol=0)
+            st["V"] = got["V"].copy()  # continue both from the same state
+    assert fired > 0
+
+
+def test_lif_rejects_unknown_method(cuda):
+    torch = cuda
+    from openpv_gb300 import capi
+    loc = capi.Loc.make(1, 4, 4, 1, 0)
+    z = torch.zeros(64, device="cuda")
+    with pytest.raises(capi.PvgpuError):
+        capi.lif_update(loc, "x", capi.LifParams.make(), 1.0, z, z, z, z, z, z, z, z)
+
+
+@pytest.mark.parametrize("method, mode", [("b", "reference"), ("a", "fast")])
+def test_spiking_network_steps(cuda, oracle, method, mode):
+    """Poisson input spikes (pre-generated, 64x64x1, rate 30 Hz at dt = 1 ms) -> 11x11 Gauss2D-like
+    weights -> excitatory LIF layer 64x64x8 over 8 steps: the input SparseList is delivered into
+    the EXC channel, the layer updates and its spikes are compacted each step.  Reference-order
+    delivery with method 'b' is bit for bit; FAST delivery with 'a' within tolerance and the same
+    spikes."""
+    torch = cuda
+    from openpv_gb300 import capi
+    nb, n, nfo, p, steps = 2, 64, 8, 11, 8
+    pre = capi.Loc.make(nb, n, n, 1, 5)
+    post = capi.Loc.make(nb, n, n, nfo, 0)
+    rng = np.random.default_rng(29)
+    yy, xx = np.mgrid[-5:6, -5:6]
+    gauss = np.exp(-(xx ** 2 + yy ** 2) / (2 * 2.5 ** 2))
+    w = (0.4 * gauss[None, :, :, None] * rng.uniform(0.5, 1.5, (1, p, p, nfo))).astype(np.float32)
+    nres = nb * n * n * nfo
+    st = state(oracle, nres, rng, seed=9)
+    st["V"][:] = -70.0
+    st["Vth"][:] = -55.0
+    st["GE"][:] = 0
+    st["GI"][:] = 0
+    st["GIB"][:] = 0
+    dev = to_dev(torch, st)
+    a_o = np.zeros(post.ext_shape(), np.float32)
+    a_d = T(torch, a_o)
+    conn = capi.conn_desc(pre, post, p, p)
+    dmode = capi.DELIVER_REFERENCE_ORDER if mode == "reference" else capi.DELIVER_FAST
+    gs_d = torch.zeros((3, nres), device="cuda")
+    ent = torch.zeros((nb, pre.num_ext, 2), dtype=torch.int32, device="cuda")
+    num = torch.zeros(nb, dtype=torch.int64, device="cuda")
+    total_spikes = 0
+    p_o, p_d = oracle.lif_params_array(), capi.LifParams.make()
+    for step in range(steps):
+        x = np.zeros(pre.ext_shape(), np.float32)
+        x[:, 5:5 + n, 5:5 + n, :] = (rng.random((nb, n, n, 1)) < 0.03).astype(np.float32)
+        # oracle: SparseList of the input, delivery, update
+        e_o, c_o = oracle.compact(x.reshape(nb, -1))
+        g_exc = oracle.deliver_pre(OL(oracle, pre), OL(oracle, post), p, p, w, entries=e_o, num_active=c_o)
+        gs = np.stack([g_exc.reshape(-1), np.zeros(nres, np.float32), np.zeros(nres, np.float32)])
+        st, a_o = oracle.lif_update(method, OL(oracle, post), p_o, 1.0, st, gs, a_o)
+        # device: compaction, delivery into the EXC channel, update
+        capi.compact_active(T(torch, x), nb, pre.num_ext, ent, num)
+        gs_d.zero_()
+        capi.deliver_pre(conn, T(torch, w), gs_d[0], entries=ent, num_active=num, mode=dmode)
+        capi.lif_update(post, method, p_d, 1.0, dev["rnd"], dev["V"], dev["Vth"], dev["GE"], dev["GI"], dev["GIB"],
+                        gs_d, a_d)
+        got = from_dev(dev, oracle.TAUS_DTYPE)
+        assert np.array_equal(H(a_d), a_o), step
+        total_spikes += int(a_o.sum())
+        if method == "b":
+            for k in st:
+                assert np.array_equal(got[k].view(np.uint32), st[k].view(np.uint32)), (k, step)
+        else:
+            for k in ("V", "GE"):
+                np.testing.assert_allclose(got[k], st[k], rtol=1e-5, atol=1e-5)
+            st = {k: (v.copy() if k == "rnd" else got[k].copy()) for k, v in st.items()}
+    assert total_spikes > 0

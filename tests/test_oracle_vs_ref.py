@@ -207,3 +207,51 @@ def test_deliver_post_bitexact_vs_reference(oracle, case):
     mine = oracle.deliver_post(pre, post, nxpP, nypP, w_post, a, gsyn=g0.copy())
     ref = refbuild.deliver_post(pre, post, nxpP, nypP, w_post, a, gsyn=g0.copy())
     assert np.array_equal(mine.view(np.uint32), ref.view(np.uint32))
+
+
+def lif_state(oracle, loc, rng, seed):
+    n = loc.nbatch * loc.nx * loc.ny * loc.nf
+    return {"rnd": oracle.taus_init(n, seed),
+            "V": rng.uniform(-75.0, -50.0, n).astype(np.float32),
+            "Vth": rng.uniform(-57.0, -48.0, n).astype(np.float32),
+            "GE": rng.uniform(0.0, 2.0, n).astype(np.float32),
+            "GI": rng.uniform(0.0, 1.0, n).astype(np.float32),
+            "GIB": rng.uniform(0.0, 0.5, n).astype(np.float32)}
+
+
+def test_taus_generator_matches_reference(oracle):
+    """cl_random_init / cl_random_get (utils/cl_random.c) restated: identical states."""
+    st = oracle.taus_init(1000, 17)
+    rs = refbuild.taus_init(1000, 17, oracle.TAUS_DTYPE)
+    assert np.array_equal(st.view(np.uint32), rs.view(np.uint32))
+    for _ in range(5):
+        st, rs = oracle.taus_next(st), refbuild.taus_next(rs)
+    assert np.array_equal(st.view(np.uint32), rs.view(np.uint32))
+    assert np.array_equal(oracle.taus_init(8, 0).view(np.uint32), refbuild.taus_init(8, 0, oracle.TAUS_DTYPE).view(np.uint32))
+
+
+@pytest.mark.parametrize("method", ["a", "b", "o"])
+@pytest.mark.parametrize("noise", [False, True])
+def test_lif_update_matches_reference(oracle, method, noise):
+    """LIFActivityComponent::updateActivity{Arma,Beginning,Original} (compiled from the reference
+    tree) and the oracle's restatement agree bit for bit over several steps: V, Vth, the three
+    conductances, the generator states and the extended activity."""
+    loc = oracle.Loc.make(2, 12, 9, 4, 1, 1)
+    rng = np.random.default_rng(ord(method) + 7 * noise)
+    kw = dict(noiseAmpE=0.5, noiseAmpI=0.3, noiseAmpIB=0.2, noiseFreqE=300.0) if noise else {}
+    p = oracle.lif_params_array(**kw)
+    st_o = lif_state(oracle, loc, rng, seed=3)
+    st_r = {k: v.copy() for k, v in st_o.items()}
+    a_o = np.zeros(loc.ext_shape(), np.float32)
+    a_r = a_o.copy()
+    n = loc.nbatch * loc.nx * loc.ny * loc.nf
+    spikes = 0
+    for step in range(6):
+        gs = np.stack([rng.uniform(0, 1.5, n), rng.uniform(0, 0.8, n), rng.uniform(0, 0.3, n)]).astype(np.float32)
+        st_o, a_o = oracle.lif_update(method, loc, p, 1.0, st_o, gs, a_o)
+        st_r, a_r = refbuild.lif_update(method, loc, p, 1.0, st_r, gs, a_r, sim_time=float(step))
+        for k in st_o:
+            assert np.array_equal(st_o[k].view(np.uint32), st_r[k].view(np.uint32)), (k, step)
+        assert np.array_equal(a_o.view(np.uint32), a_r.view(np.uint32)), step
+        spikes += int(a_o.sum())
+    assert spikes > 0  # the inputs drive some neurons over threshold
