@@ -290,6 +290,128 @@ def delivery_bench(torch, capi, reps=5):
 
 
 # ---------------------------------------------------------------------------------------------
+# LIF network step (Poisson input -> excitatory LIF layer), 16 images
+# ---------------------------------------------------------------------------------------------
+def lif_bench(torch, capi, steps=40, cpu_sample=True):
+    """One timestep of the spiking path on 16 images: input spikes 256x256x1 (Poisson, rates
+    U[5, 50] Hz at dt = 1 ms, pre-generated as SparseLists, 8 frames cycled) delivered
+    presynaptically through 11x11x32 Gaussian weights into the EXC channel of a 256x256x32 LIF
+    layer (arma method), the LIF update, and the compaction of its spikes into a SparseList."""
+    nb, n, nf, p = 16, 256, 32, 11
+    pre = capi.Loc.make(nb, n, n, 1, 5)
+    post = capi.Loc.make(nb, n, n, nf, 0)
+    conn = capi.conn_desc(pre, post, p, p)
+    g = torch.Generator(device="cuda").manual_seed(1234 + 5)
+    yy, xx = torch.meshgrid(torch.arange(-5, 6, device="cuda"), torch.arange(-5, 6, device="cuda"), indexing="ij")
+    gauss = torch.exp(-(xx ** 2 + yy ** 2).float() / (2 * 2.5 ** 2))
+    w = (0.5 * gauss[None, :, :, None] * (0.5 + torch.rand((1, p, p, nf), device="cuda", generator=g))).contiguous()
+    rates = 5.0 + 45.0 * torch.rand((nb, n, n, 1), device="cuda", generator=g)
+    frames, ents, nums = 8, [], []
+    for _ in range(frames):
+        x = torch.zeros(pre.ext_shape(), device="cuda")
+        x[:, 5:5 + n, 5:5 + n, :] = (torch.rand((nb, n, n, 1), device="cuda", generator=g) < rates * 1e-3).float()
+        e = torch.zeros((nb, pre.num_ext, 2), dtype=torch.int32, device="cuda")
+        c = torch.zeros(nb, dtype=torch.int64, device="cuda")
+        capi.compact_active(x, nb, pre.num_ext, e, c)
+        ents.append(e)
+        nums.append(c)
+    torch.cuda.synchronize()
+    spikes_in = float(torch.stack(nums).float().mean().item())
+    nres = nb * n * n * nf
+    rnd = torch.zeros((nres, 4), dtype=torch.int32, device="cuda")
+    capi.taus_init(rnd, nres, 17)
+    V = torch.full((nres,), -70.0, device="cuda")
+    Vth = torch.full((nres,), -55.0, device="cuda")
+    GE, GI, GIB = (torch.zeros(nres, device="cuda") for _ in range(3))
+    gs = torch.zeros((3, nres), device="cuda")
+    a = torch.zeros(post.ext_shape(), device="cuda")
+    out_e = torch.zeros((nb, post.num_ext, 2), dtype=torch.int32, device="cuda")
+    out_n = torch.zeros(nb, dtype=torch.int64, device="cuda")
+    scratch = torch.empty(max(1, capi.lib().pvgpu_compact_scratch_bytes(nb, post.num_ext)), dtype=torch.uint8, device="cuda")
+    prm = capi.LifParams.make()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    t_deliv = t_lif = t_comp = 0.0
+
+    def step(i, split=False):
+        nonlocal t_deliv, t_lif, t_comp
+        if split:
+            ev[0].record()
+        gs[0].zero_()
+        capi.deliver_pre(conn, w, gs[0], entries=ents[i % frames], num_active=nums[i % frames])
+        if split:
+            ev[1].record()
+        capi.lif_update(post, "a", prm, 1.0, rnd, V, Vth, GE, GI, GIB, gs, a)
+        if split:
+            ev[2].record()
+        capi.compact_active(a, nb, post.num_ext, out_e, out_n, scratch=scratch)
+        if split:
+            ev[3].record()
+            torch.cuda.synchronize()
+            t_deliv += ev[0].elapsed_time(ev[1])
+            t_lif += ev[1].elapsed_time(ev[2])
+            t_comp += ev[2].elapsed_time(ev[3])
+
+    for i in range(5):
+        step(i)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for i in range(steps):
+        step(i)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    ksplit = 10
+    for i in range(ksplit):
+        step(i, split=True)
+    spikes_out = float(out_n.float().mean().item())
+    mac = spikes_in * p * p * nf
+    lif_bytes = nres * (12 + 40 + 32 + 4)
+    out = {"workload": "16 images: Poisson input 256x256x1 (rates U[5,50] Hz, dt 1 ms) -> 11x11x32 Gaussian "
+                       "weights -> LIF 256x256x32 (arma) -> spike compaction; input SparseLists pre-generated",
+           "ms_per_step": ms, "image_steps_per_s": nb / (ms / 1e3),
+           "input_spikes_per_image": spikes_in, "output_spikes_per_image": spikes_out,
+           "delivery_ms": t_deliv / ksplit, "delivery_GFLOP_s": 2 * mac * nb / (t_deliv / ksplit) / 1e6,
+           "lif_update_ms": t_lif / ksplit, "lif_update_GB_s": lif_bytes / (t_lif / ksplit) / 1e6,
+           "compaction_ms": t_comp / ksplit}
+    if cpu_sample:
+        out["cpu_oracle"] = lif_cpu_sample()
+    return out
+
+
+def lif_cpu_sample():
+    """The same step for one image on one host core through the oracle (pinned to the reference's
+    own LIF loops and delivery): delivery from the SparseList, LIF update; 3 steps."""
+    from oracle import oracle as O
+    O.build()
+    rng = np.random.default_rng(1234 + 5)
+    n, nf, p = 256, 32, 11
+    pre = O.Loc.make(1, n, n, 1, 5, 5)
+    post = O.Loc.make(1, n, n, nf, 0, 0)
+    yy, xx = np.mgrid[-5:6, -5:6]
+    w = (0.5 * np.exp(-(xx ** 2 + yy ** 2) / (2 * 2.5 ** 2))[None, :, :, None] *
+         rng.uniform(0.5, 1.5, (1, p, p, nf))).astype(np.float32)
+    nres = n * n * nf
+    st = {"rnd": O.taus_init(nres, 17), "V": np.full(nres, -70.0, np.float32), "Vth": np.full(nres, -55.0, np.float32),
+          "GE": np.zeros(nres, np.float32), "GI": np.zeros(nres, np.float32), "GIB": np.zeros(nres, np.float32)}
+    a = np.zeros(post.ext_shape(), np.float32)
+    prm = O.lif_params_array()
+    rates = rng.uniform(5, 50, (1, n, n, 1))
+    reps = 3
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        x = np.zeros(pre.ext_shape(), np.float32)
+        x[:, 5:5 + n, 5:5 + n, :] = (rng.random((1, n, n, 1)) < rates * 1e-3).astype(np.float32)
+        e, c = O.compact(x.reshape(1, -1))
+        g = O.deliver_pre(pre, post, p, p, w, entries=e, num_active=c)
+        gs = np.stack([g.reshape(-1), np.zeros(nres, np.float32), np.zeros(nres, np.float32)])
+        st, a = O.lif_update("a", post, prm, 1.0, st, gs, a)
+    dt = time.perf_counter() - t0
+    return {"value": reps / dt, "unit": "image-steps/s", "cores": 1, "kind": "port",
+            "sample": f"oracle, 1 image x {reps} steps ({dt:.2f} s)"}
+
+
+# ---------------------------------------------------------------------------------------------
 # our arm
 # ---------------------------------------------------------------------------------------------
 def run_ours(args, rank, world, local_rank):
@@ -446,6 +568,7 @@ def run_ours(args, rank, world, local_rank):
 
     cpu_val, cpu_dt = cpu_sample(cfg, cores, warm_steps=25, timed_steps=25)
     deliv = delivery_bench(torch, capi)
+    lifb = lif_bench(torch, capi)
     clocks = clk.summary()
 
     line = {
@@ -486,6 +609,7 @@ def run_ours(args, rank, world, local_rank):
                                  "densities; postsynaptic FP32 SIMT and tensor-core",
                      "by_density": {k: v for k, v in deliv.items() if k != "post"}, "post": deliv["post"],
                      "hbm_peak_gbs": pk["hbm_gbs"], "tf32_tensor_peak_tflops": pk["bf16_tflops"] / 2},
+        "lif_network": lifb,
         "clocks": clocks,
     }
     print(json.dumps(line), flush=True)
@@ -504,7 +628,16 @@ def main():
     ap.add_argument("--quick", action="store_true", help="time the solve only (profiling runs; not a bench line)")
     ap.add_argument("--delivery", action="store_true",
                     help="run the presynaptic delivery microbenchmark only (profiling runs; not a bench line)")
+    ap.add_argument("--lif", action="store_true",
+                    help="run the LIF network step only (profiling runs; not a bench line)")
     args = ap.parse_args()
+    if args.lif:
+        import torch
+        from openpv_gb300 import build
+        build.build()
+        from openpv_gb300 import capi
+        print(json.dumps({"lif_network": lif_bench(torch, capi, steps=10, cpu_sample=False)}))
+        return
     if args.delivery:
         import torch
         from openpv_gb300 import build

@@ -178,10 +178,12 @@ __global__ void __launch_bounds__(kWarps * 32) deliver_pre_kernel(PreGeom g, con
 // A CTA owns 8 post columns (one per warp) x RS post rows x all nfp features (lane = FPL
 // consecutive features).  It walks the presynaptic extended rows that reach its rows in
 // ascending order -- the SparseList order -- and each warp keeps one register accumulator per
-// patch row in a circular buffer: presynaptic row ye adds to post rows ye - Hy + ky, slot
-// (ye - Hy + ky) mod NYP, and once row ye is done post row ye - Hy has all its contributions
-// and is added into GSyn (one read-modify-write per output, no atomics).  Unrolling the row
-// loop by NYP makes every slot index a compile-time constant.  Each active entry is read and
+// patch row in a sliding window: presynaptic row ye adds its patch row ky to post row
+// ye - Hy + ky, held in acc[ky]; once row ye is done post row ye - Hy (acc[0]) has all its
+// contributions and is added into GSyn (one read-modify-write per output, no atomics), and the
+// window shifts by one row (NYP x FPL register moves, so every index stays a compile-time
+// constant without unrolling the row loop -- an unrolled loop outgrows the instruction cache at
+// 11 and 13 patch rows).  Each active entry is read and
 // decoded once per warp and feeds NYP x FPL FMAs per lane; its weights W[f][ky][kx][*] come
 // through the read-only path (one coalesced 32*FPL-float row per ky).  The entry range of a
 // row inside the CTA's column window comes from a binary search per row, done in parallel by
@@ -232,8 +234,10 @@ struct VecF<4> {
    }
 };
 
+// More than 16 accumulators per lane (NYP x FPL) do not fit the 64 registers of four CTAs per SM
+// next to the entry pipeline; those instantiations take two CTAs per SM (128 registers) instead.
 template <int FPL, int NYP, bool SPARSE>
-__global__ void __launch_bounds__(kWarps * 32, 4) deliver_pre_rows_kernel(PreGeom g, const pvgpu_entry *__restrict__ entries,
+__global__ void __launch_bounds__(kWarps * 32, (FPL * NYP > 16) ? 2 : 4) deliver_pre_rows_kernel(PreGeom g, const pvgpu_entry *__restrict__ entries,
                                                                        const int64_t *__restrict__ numActive,
                                                                        const float *__restrict__ aExt,
                                                                        const float *__restrict__ W,
@@ -279,79 +283,81 @@ __global__ void __launch_bounds__(kWarps * 32, 4) deliver_pre_rows_kernel(PreGeo
 #pragma unroll
       for (int q = 0; q < FPL; q++) acc[s][q] = 0.0f;
 
-   // first row with (ye - Hy) = 0 mod NYP, so that slots are static inside each group
-   const int yeStart = yeLo - (((yeLo - Hy) % NYP) + NYP) % NYP;
+   // Window of NYP post rows: while presynaptic row ye is processed, acc[j] holds post row
+   // ye - Hy + j, so patch row ky of an entry of row ye always adds into acc[ky] (a static index).
+   // After row ye, post row ye - Hy (acc[0]) has all its contributions: it is added into GSyn and
+   // the window shifts by one row.  The first row visited puts post row P0 in acc[NYP - 1].
+   const int yeFirst = P0 + Hy - (NYP - 1);
    const int yeEnd = P1 - 1 + Hy;  // the row that completes post row P1 - 1
-   for (int ye0 = yeStart; ye0 <= yeEnd; ye0 += NYP) {
+   for (int ye = yeFirst; ye <= yeEnd; ye++) {
+      if (ye >= yeLo && ye <= yeHi) {
+         const int64_t lo = SPARSE ? rowLo[ye - yeLo] : key_lo(ye);
+         const int64_t hi = SPARSE ? rowHi[ye - yeLo] : key_hi(ye);
+         const int64_t kRow = (int64_t)ye * nxExt * nf;
+         // patch rows of this presynaptic row that land inside [P0, P1)
+         const int kyMin = max(0, P0 - (ye - Hy)), kyMax = min(NYP - 1, P1 - 1 - (ye - Hy));
+         for (int64_t base = lo; base < hi; base += 32) {
+            int64_t k = 0;
+            float a = 0.0f;
+            const bool have = base + lane < hi;
+            if (have) {
+               if (SPARSE) {
+                  const pvgpu_entry en = eb[base + lane];
+                  k = en.index;
+                  a = en.value;
+               } else {
+                  k = base + lane;
+                  a = ab[base + lane];
+               }
+            }
+            const int kr = (int)(k - kRow);
+            const int xe = kr / nf, f = kr - xe * nf;
+            const int kx = X - (xe - Hx);
+            const bool rel = have && a != 0.0f && kx >= 0 && kx < g.nxp;
+            unsigned m = __ballot_sync(0xffffffffu, rel);
+            const int woffMine = f * g.patchSize + kx * g.nfp;  // kernel index = f (one-to-one)
+            // two entries per round: their weight loads are all in flight before the FMAs
+            while (m) {
+               const int j1 = __ffs(m) - 1;
+               m &= m - 1;
+               const bool two = m != 0;  // warp-uniform
+               const int j2 = two ? __ffs(m) - 1 : j1;
+               if (two) m &= m - 1;
+               const float a1 = __shfl_sync(0xffffffffu, a, j1) * g.dtf;
+               const float a2 = two ? __shfl_sync(0xffffffffu, a, j2) * g.dtf : 0.0f;
+               const float *wp1 = W + __shfl_sync(0xffffffffu, woffMine, j1) + fo0;
+               const float *wp2 = W + __shfl_sync(0xffffffffu, woffMine, j2) + fo0;
+               float w1[NYP][FPL], w2[NYP][FPL];
 #pragma unroll
-      for (int i = 0; i < NYP; i++) {
-         const int ye = ye0 + i;
-         if (ye >= yeLo && ye <= yeHi) {
-            const int64_t lo = SPARSE ? rowLo[ye - yeLo] : key_lo(ye);
-            const int64_t hi = SPARSE ? rowHi[ye - yeLo] : key_hi(ye);
-            const int64_t kRow = (int64_t)ye * nxExt * nf;
-            // patch rows of this presynaptic row that land inside [P0, P1)
-            const int kyMin = max(0, P0 - (ye - Hy)), kyMax = min(NYP - 1, P1 - 1 - (ye - Hy));
-            for (int64_t base = lo; base < hi; base += 32) {
-               int64_t k = 0;
-               float a = 0.0f;
-               const bool have = base + lane < hi;
-               if (have) {
-                  if (SPARSE) {
-                     const pvgpu_entry en = eb[base + lane];
-                     k = en.index;
-                     a = en.value;
-                  } else {
-                     k = base + lane;
-                     a = ab[base + lane];
+               for (int ky = 0; ky < NYP; ky++) {
+                  if (ky >= kyMin && ky <= kyMax) {
+                     VecF<FPL>::ld(wp1 + ky * rowStrideW, w1[ky]);
+                     if (two) VecF<FPL>::ld(wp2 + ky * rowStrideW, w2[ky]);
                   }
                }
-               const int kr = (int)(k - kRow);
-               const int xe = kr / nf, f = kr - xe * nf;
-               const int kx = X - (xe - Hx);
-               const bool rel = have && a != 0.0f && kx >= 0 && kx < g.nxp;
-               unsigned m = __ballot_sync(0xffffffffu, rel);
-               const int woffMine = f * g.patchSize + kx * g.nfp;  // kernel index = f (one-to-one)
-               // two entries per round: their weight loads are all in flight before the FMAs
-               while (m) {
-                  const int j1 = __ffs(m) - 1;
-                  m &= m - 1;
-                  const bool two = m != 0;  // warp-uniform
-                  const int j2 = two ? __ffs(m) - 1 : j1;
-                  if (two) m &= m - 1;
-                  const float a1 = __shfl_sync(0xffffffffu, a, j1) * g.dtf;
-                  const float a2 = two ? __shfl_sync(0xffffffffu, a, j2) * g.dtf : 0.0f;
-                  const float *wp1 = W + __shfl_sync(0xffffffffu, woffMine, j1) + fo0;
-                  const float *wp2 = W + __shfl_sync(0xffffffffu, woffMine, j2) + fo0;
-                  float w1[NYP][FPL], w2[NYP][FPL];
 #pragma unroll
-                  for (int ky = 0; ky < NYP; ky++) {
-                     if (ky >= kyMin && ky <= kyMax) {
-                        VecF<FPL>::ld(wp1 + ky * rowStrideW, w1[ky]);
-                        if (two) VecF<FPL>::ld(wp2 + ky * rowStrideW, w2[ky]);
-                     }
-                  }
+               for (int ky = 0; ky < NYP; ky++) {
+                  if (ky >= kyMin && ky <= kyMax) {
 #pragma unroll
-                  for (int ky = 0; ky < NYP; ky++) {
-                     if (ky >= kyMin && ky <= kyMax) {
-                        const int s = (i + ky) % NYP;
+                     for (int q = 0; q < FPL; q++) acc[ky][q] = fmaf(a1, w1[ky][q], acc[ky][q]);
+                     if (two) {
 #pragma unroll
-                        for (int q = 0; q < FPL; q++) acc[s][q] = fmaf(a1, w1[ky][q], acc[s][q]);
-                        if (two) {
-#pragma unroll
-                           for (int q = 0; q < FPL; q++) acc[s][q] = fmaf(a2, w2[ky][q], acc[s][q]);
-                        }
+                        for (int q = 0; q < FPL; q++) acc[ky][q] = fmaf(a2, w2[ky][q], acc[ky][q]);
                      }
                   }
                }
             }
          }
-         // post row ye - Hy has all its contributions (slot i)
-         const int py = ye - Hy;
-         if (py >= P0 && py < P1) VecF<FPL>::rmw(gcol + (size_t)py * gRow, acc[i]);
-#pragma unroll
-         for (int q = 0; q < FPL; q++) acc[i][q] = 0.0f;
       }
+      // post row ye - Hy has all its contributions
+      const int py = ye - Hy;
+      if (py >= P0 && py < P1) VecF<FPL>::rmw(gcol + (size_t)py * gRow, acc[0]);
+#pragma unroll
+      for (int j = 0; j + 1 < NYP; j++)
+#pragma unroll
+         for (int q = 0; q < FPL; q++) acc[j][q] = acc[j + 1][q];
+#pragma unroll
+      for (int q = 0; q < FPL; q++) acc[NYP - 1][q] = 0.0f;
    }
 }
 
@@ -376,6 +382,11 @@ pvgpu_status launch_rows_nyp(const PreGeom &g, cudaStream_t s, const pvgpu_entry
       case 5: return launch_rows<FPL, 5>(g, s, entries, numActive, aExt, W, gsyn);
       case 7: return launch_rows<FPL, 7>(g, s, entries, numActive, aExt, W, gsyn);
       case 9: return launch_rows<FPL, 9>(g, s, entries, numActive, aExt, W, gsyn);
+      // taller patches keep NYP x FPL accumulators per lane: 32 and 64 post features only
+      case 11: return FPL <= 2 ? launch_rows<FPL <= 2 ? FPL : 1, 11>(g, s, entries, numActive, aExt, W, gsyn)
+                               : PVGPU_ERR_UNSUPPORTED_SHAPE;
+      case 13: return FPL <= 2 ? launch_rows<FPL <= 2 ? FPL : 1, 13>(g, s, entries, numActive, aExt, W, gsyn)
+                               : PVGPU_ERR_UNSUPPORTED_SHAPE;
       default: return PVGPU_ERR_UNSUPPORTED_SHAPE;
    }
 }
@@ -439,11 +450,11 @@ extern "C" pvgpu_status pvgpu_deliver_pre(const pvgpu_conn_desc *conn, const pvg
    dim3 grid((unsigned)gx, gy, pre.nbatch);
    cudaStream_t s = pvgpu::as_stream(stream);
    bool exact = mode == PVGPU_DELIVER_REFERENCE_ORDER;
-   // FAST mode, one-to-one, nfp a multiple of 32 up to 128, odd patch height up to 9: the
-   // row-sliding kernel
+   // FAST mode, one-to-one, nfp a multiple of 32 up to 128, odd patch height up to 9 (up to 13
+   // for 32 or 64 post features): the row-sliding kernel
    const int rowRange = kRowsRS + conn->nyp - 1;
    if (!exact && pre.nx == post.nx && pre.ny == post.ny && post.nf % 32 == 0 && post.nf <= 128 &&
-       conn->nyp <= 9 && rowRange <= kRowsMax && (post.nf / 32) != 3) {
+       conn->nyp <= 13 && rowRange <= kRowsMax && (post.nf / 32) != 3) {
       const int fpl = post.nf / 32;
       pvgpu_status r = fpl == 1   ? launch_rows_nyp<1>(g, s, entries, numActive, aExt, weights, gsyn)
                        : fpl == 2 ? launch_rows_nyp<2>(g, s, entries, numActive, aExt, weights, gsyn)

@@ -84,7 +84,9 @@ PRE_CASES = [
     ((2, 24, 33, 4, 1), (24, 33, 128, 0), 3, 3),
     ((1, 20, 40, 8, 4), (20, 40, 64, 1), 5, 5),     # pre halo above the margin, post halo
     ((1, 16, 40, 8, 1), (16, 40, 32, 0), 7, 7),     # pre halo below the margin
-    ((2, 20, 36, 6, 4), (20, 36, 64, 0), 5, 9),     # unequal patch axes, tallest patch
+    ((2, 20, 36, 6, 4), (20, 36, 64, 0), 5, 9),     # unequal patch axes
+    ((1, 30, 40, 1, 5), (30, 40, 32, 0), 11, 11),   # 11x11 (Gauss2D-style LIF input), 32 features
+    ((2, 20, 36, 4, 6), (20, 36, 64, 0), 13, 13),   # tallest patch of the row-sliding kernel
 ]
 
 
