@@ -381,7 +381,7 @@ def lif_bench(torch, capi, steps=40, cpu_sample=True):
 
 def lif_cpu_sample():
     """The same step for one image on one host core through the oracle (pinned to the reference's
-    own LIF loops and delivery): delivery from the SparseList, LIF update; 3 steps."""
+    own LIF loops and delivery): delivery from the SparseList, LIF update; 20 steps (about 2 s)."""
     from oracle import oracle as O
     O.build()
     rng = np.random.default_rng(1234 + 5)
@@ -397,7 +397,7 @@ def lif_cpu_sample():
     a = np.zeros(post.ext_shape(), np.float32)
     prm = O.lif_params_array()
     rates = rng.uniform(5, 50, (1, n, n, 1))
-    reps = 3
+    reps = 20
     t0 = time.perf_counter()
     for _ in range(reps):
         x = np.zeros(pre.ext_shape(), np.float32)
