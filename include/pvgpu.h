@@ -189,6 +189,34 @@ pvgpu_status pvgpu_lif_update(
 /* cl_random_init (utils/cl_random.c) on the device: element i seeded with i + seed. */
 pvgpu_status pvgpu_taus_init(pvgpu_taus *state, int64_t count, uint32_t seed, void *stream);
 
+/* ---- .pvp activity frames, built on the device -------------------------------------------
+ * Sparse frame payloads for PVP_ACT_SPARSEVALUES_FILE_TYPE files: each batch element's SparseList
+ * (extended indices, stride numExt) as the file stores it -- halo entries dropped, indices made
+ * restricted, order kept (SparseLayerBatchGatherScatter::gather then SparseList::crop,
+ * io/SparseLayerBatchGatherScatter.cpp:24-80, structures/SparseList.hpp:76-110).  out has
+ * capacity nx*ny*nf entries per batch element (stride nx*ny*nf); counts[b] receives the number
+ * kept. */
+pvgpu_status pvgpu_pvp_sparse_frames(
+      const pvgpu_loc *loc,
+      const pvgpu_entry *entries,
+      const int64_t *numActive,
+      pvgpu_entry *out,
+      int32_t *counts,
+      void *stream);
+/* Dense frame payloads (PVP_NONSPIKING_ACT_FILE_TYPE): the restricted activity of each batch
+ * element, [nbatch][ny][nx][nf]. */
+pvgpu_status pvgpu_pvp_dense_frames(const pvgpu_loc *loc, const float *aExt, float *out, void *stream);
+/* A file's sparse frames (restricted entries, stride nx*ny*nf, counts[b]) into the extended
+ * activity, which is zeroed first; an index outside the layer sets *badIndex (device int) to 1
+ * and is skipped. */
+pvgpu_status pvgpu_pvp_scatter_sparse(
+      const pvgpu_loc *loc,
+      const pvgpu_entry *fileEntries,
+      const int32_t *counts,
+      float *aExt,
+      int32_t *badIndex,
+      void *stream);
+
 /* ---- a4 / a5 on the tensor cores ---------------------------------------------------------
  * The same deliveries for a one-to-one connection (pre and post of equal nx, ny; pre.nf and
  * post.nf multiples of 32; nxp <= 9; equal halo on all sides, at least the connection's

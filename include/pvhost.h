@@ -61,6 +61,43 @@ pvgpu_status pvhost_delivery_keyword(pvhost_column *c, const char *connName, cha
  * before the first step.  No reference counterpart (diagnostics). */
 pvgpu_status pvhost_delivery_engine(pvhost_column *c, const char *connName, char *buf, size_t bufSize);
 
+
+/* ---- .pvp activity files (utils/BufferUtilsPvp.hpp, io/LayerIO.cpp, io/SparseLayerIO.cpp) ----
+ * Writer: header as LayerIO / SparseLayerIO::writeHeader (nBands = 0, timestamp 0), frames
+ * appended, nBands rewritten after each frame.  One frame per batch element per call, in batch
+ * order, as LayerOutputComponent writes them. */
+typedef struct pvhost_pvp_writer pvhost_pvp_writer;
+pvgpu_status pvhost_pvp_writer_open(const char *path, int nx, int ny, int nf, int sparse, pvhost_pvp_writer **out);
+/* From the device: a sparse layer's SparseList (pvgpu_pvp_sparse_frames on the device, then one
+ * copy of the kept entries per batch element), or a dense layer's extended activity
+ * (pvgpu_pvp_dense_frames, then one copy).  Synchronises the stream. */
+pvgpu_status pvhost_pvp_write_sparse_device(pvhost_pvp_writer *w, const pvgpu_loc *loc, const pvgpu_entry *entries,
+                                            const int64_t *numActive, double timestamp, void *stream);
+pvgpu_status pvhost_pvp_write_dense_device(pvhost_pvp_writer *w, const pvgpu_loc *loc, const float *aExt,
+                                           double timestamp, void *stream);
+/* From host buffers: one frame. */
+pvgpu_status pvhost_pvp_write_sparse_host(pvhost_pvp_writer *w, const pvgpu_entry *entries, int32_t count,
+                                          double timestamp);
+pvgpu_status pvhost_pvp_write_dense_host(pvhost_pvp_writer *w, const float *restricted, double timestamp);
+pvgpu_status pvhost_pvp_writer_close(pvhost_pvp_writer *w);
+
+/* Reader: activity files of type 4 (dense), 6 (sparse values) and 2 (binary spikes). */
+typedef struct pvhost_pvp_reader pvhost_pvp_reader;
+pvgpu_status pvhost_pvp_reader_open(const char *path, pvhost_pvp_reader **out);
+/* The 18 header ints (headerSize ... nBands) and the header timestamp; *numFrames = frames in
+ * the file (from its length, as SparseLayerIO counts them). */
+pvgpu_status pvhost_pvp_reader_info(pvhost_pvp_reader *r, int32_t *out18, double *timestamp, int *numFrames);
+/* Frame as the restricted activity [ny][nx][nf] (n = nx*ny*nf floats). */
+pvgpu_status pvhost_pvp_read_dense(pvhost_pvp_reader *r, int frame, float *host, int64_t n, double *timestamp);
+/* Frame as {restricted index, value} entries (capacity entries; *count receives how many). */
+pvgpu_status pvhost_pvp_read_sparse(pvhost_pvp_reader *r, int frame, pvgpu_entry *host, int64_t capacity,
+                                    int32_t *count, double *timestamp);
+/* Frames first .. first+nbatch-1 into a device extended activity (sparse frames scattered on the
+ * device; dense frames copied into the restricted part); the halo is zeroed. */
+pvgpu_status pvhost_pvp_read_to_device(pvhost_pvp_reader *r, int firstFrame, const pvgpu_loc *loc, float *aExt,
+                                       void *stream);
+pvgpu_status pvhost_pvp_reader_close(pvhost_pvp_reader *r);
+
 #ifdef __cplusplus
 }
 #endif

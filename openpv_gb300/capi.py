@@ -141,6 +141,9 @@ def _declare(L):
         "pvgpu_deliver_pre_tc": (i, [cp, vp, vp, vp, vp, sz, vp]),
         "pvgpu_deliver_tc_check_error": (i, []),
         "pvgpu_lif_update": (i, [lp, C.c_char, vp, f, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
+        "pvgpu_pvp_sparse_frames": (i, [lp, vp, vp, vp, vp, vp]),
+        "pvgpu_pvp_dense_frames": (i, [lp, vp, vp, vp]),
+        "pvgpu_pvp_scatter_sparse": (i, [lp, vp, vp, vp, vp, vp]),
         "pvgpu_taus_init": (i, [vp, i64, C.c_uint32, vp]),
     }
     for name, (res, args) in sig.items():
@@ -421,6 +424,18 @@ def host_lib():
             "pvhost_layer_info": (i, [vp, cs, C.POINTER(i)]),
             "pvhost_delivery_keyword": (i, [vp, cs, C.c_char_p, sz]),
             "pvhost_delivery_engine": (i, [vp, cs, C.c_char_p, sz]),
+            "pvhost_pvp_writer_open": (i, [cs, i, i, i, i, C.POINTER(vp)]),
+            "pvhost_pvp_write_sparse_device": (i, [vp, C.POINTER(Loc), vp, vp, C.c_double, vp]),
+            "pvhost_pvp_write_dense_device": (i, [vp, C.POINTER(Loc), vp, C.c_double, vp]),
+            "pvhost_pvp_write_sparse_host": (i, [vp, vp, C.c_int32, C.c_double]),
+            "pvhost_pvp_write_dense_host": (i, [vp, vp, C.c_double]),
+            "pvhost_pvp_writer_close": (i, [vp]),
+            "pvhost_pvp_reader_open": (i, [cs, C.POINTER(vp)]),
+            "pvhost_pvp_reader_info": (i, [vp, vp, C.POINTER(C.c_double), C.POINTER(i)]),
+            "pvhost_pvp_read_dense": (i, [vp, i, vp, C.c_int64, C.POINTER(C.c_double)]),
+            "pvhost_pvp_read_sparse": (i, [vp, i, vp, C.c_int64, C.POINTER(C.c_int32), C.POINTER(C.c_double)]),
+            "pvhost_pvp_read_to_device": (i, [vp, i, C.POINTER(Loc), vp, vp]),
+            "pvhost_pvp_reader_close": (i, [vp]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(_host, name)
@@ -445,6 +460,113 @@ def params_dump(text):
     buf = C.create_string_buffer(1 << 20)
     host_check(host_lib().pvhost_params_dump(text.encode(), buf, len(buf)), "params_dump")
     return buf.value.decode()
+
+
+PVP_HEADER_FIELDS = ("headerSize", "numParams", "fileType", "nx", "ny", "nf", "numRecords", "recordSize", "dataSize",
+                     "dataType", "nxProcs", "nyProcs", "nxExtended", "nyExtended", "kx0", "ky0", "nBatch", "nBands")
+
+
+def pvp_sparse_frames(loc, entries, num_active, out, counts, stream=None):
+    check(lib().pvgpu_pvp_sparse_frames(C.byref(loc), _ptr(entries), _ptr(num_active), _ptr(out), _ptr(counts),
+                                        _stream(stream)), "pvp_sparse_frames")
+
+
+def pvp_dense_frames(loc, a_ext, out, stream=None):
+    check(lib().pvgpu_pvp_dense_frames(C.byref(loc), _ptr(a_ext), _ptr(out), _stream(stream)), "pvp_dense_frames")
+
+
+def pvp_scatter_sparse(loc, file_entries, counts, a_ext, bad, stream=None):
+    check(lib().pvgpu_pvp_scatter_sparse(C.byref(loc), _ptr(file_entries), _ptr(counts), _ptr(a_ext), _ptr(bad),
+                                         _stream(stream)), "pvp_scatter_sparse")
+
+
+class PvpWriter:
+    """A .pvp activity file being written (libpvhost.so)."""
+
+    def __init__(self, path, nx, ny, nf, sparse):
+        h = C.c_void_p()
+        host_check(host_lib().pvhost_pvp_writer_open(str(path).encode(), nx, ny, nf, int(sparse), C.byref(h)),
+                   "pvp_writer_open")
+        self.h = h
+
+    def write_sparse_device(self, loc, entries, num_active, t, stream=None):
+        host_check(host_lib().pvhost_pvp_write_sparse_device(self.h, C.byref(loc), _ptr(entries), _ptr(num_active),
+                                                             float(t), _stream(stream)), "pvp_write_sparse_device")
+
+    def write_dense_device(self, loc, a_ext, t, stream=None):
+        host_check(host_lib().pvhost_pvp_write_dense_device(self.h, C.byref(loc), _ptr(a_ext), float(t),
+                                                            _stream(stream)), "pvp_write_dense_device")
+
+    def write_sparse(self, indices, values, t):
+        e = np.zeros(len(indices), ENTRY_DTYPE)
+        e["index"] = indices
+        e["value"] = values
+        host_check(host_lib().pvhost_pvp_write_sparse_host(self.h, e.ctypes.data_as(C.c_void_p) if len(e) else None,
+                                                           len(e), float(t)), "pvp_write_sparse_host")
+
+    def write_dense(self, values, t):
+        v = np.ascontiguousarray(values, dtype=np.float32)
+        host_check(host_lib().pvhost_pvp_write_dense_host(self.h, v.ctypes.data_as(C.c_void_p), float(t)),
+                   "pvp_write_dense_host")
+
+    def close(self):
+        if self.h:
+            host_check(host_lib().pvhost_pvp_writer_close(self.h), "pvp_writer_close")
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+class PvpReader:
+    """A .pvp activity file (types 2, 4, 6) read by libpvhost.so."""
+
+    def __init__(self, path):
+        h = C.c_void_p()
+        host_check(host_lib().pvhost_pvp_reader_open(str(path).encode(), C.byref(h)), "pvp_reader_open")
+        self.h = h
+        v = (C.c_int32 * 18)()
+        t = C.c_double()
+        n = C.c_int()
+        host_check(host_lib().pvhost_pvp_reader_info(self.h, v, C.byref(t), C.byref(n)), "pvp_reader_info")
+        self.header = dict(zip(PVP_HEADER_FIELDS, list(v)))
+        self.header["timestamp"] = t.value
+        self.num_frames = n.value
+        self.shape = (self.header["ny"], self.header["nx"], self.header["nf"])
+
+    def read_dense(self, frame):
+        out = np.zeros(self.shape, np.float32)
+        t = C.c_double()
+        host_check(host_lib().pvhost_pvp_read_dense(self.h, frame, out.ctypes.data_as(C.c_void_p), out.size,
+                                                    C.byref(t)), "pvp_read_dense")
+        return out, t.value
+
+    def read_sparse(self, frame):
+        cap = int(np.prod(self.shape))
+        e = np.zeros(cap, ENTRY_DTYPE)
+        n = C.c_int32()
+        t = C.c_double()
+        host_check(host_lib().pvhost_pvp_read_sparse(self.h, frame, e.ctypes.data_as(C.c_void_p), cap, C.byref(n),
+                                                     C.byref(t)), "pvp_read_sparse")
+        return e[:n.value].copy(), t.value
+
+    def read_to_device(self, first_frame, loc, a_ext, stream=None):
+        host_check(host_lib().pvhost_pvp_read_to_device(self.h, first_frame, C.byref(loc), _ptr(a_ext),
+                                                        _stream(stream)), "pvp_read_to_device")
+
+    def close(self):
+        if self.h:
+            host_lib().pvhost_pvp_reader_close(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
 
 
 class Column:

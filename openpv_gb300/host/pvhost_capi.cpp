@@ -13,13 +13,18 @@ struct pvhost_column {
 };
 
 namespace {
-
 thread_local std::string g_err;
+}  // namespace
 
+namespace pvhost_capi {
 pvgpu_status fail(pvgpu_status s, const std::string &msg) {
    g_err = msg;
    return s;
 }
+}  // namespace pvhost_capi
+using pvhost_capi::fail;
+
+namespace {
 
 bool copy_out(const std::string &s, char *buf, size_t n) {
    if (!buf || n == 0 || s.size() + 1 > n) return false;
