@@ -1,5 +1,6 @@
 // column.cpp -- see column.hpp.
 #include "column.hpp"
+#include "pvp.hpp"
 
 #include <algorithm>
 #include <cfloat>
@@ -123,6 +124,8 @@ std::unique_ptr<Delivery> create_delivery(const std::string &kw, Conn *c) {
 
 Column::~Column() {
    if (stream_) cudaStreamSynchronize(stream_);
+   for (auto &L : layers_)
+      if (L->out) pvhost_pvp_writer_close(L->out);
    for (void *p : allocs_) cudaFree(p);
    if (stream_) cudaStreamDestroy(stream_);
 }
@@ -152,6 +155,8 @@ bool Column::build(const std::string &text, std::string &err) {
    ny_ = (int)col->number("ny", 0);
    nbatch_ = (int)col->number("nbatch", 1);
    dt_ = col->number("dt", 1.0);
+   outputPath_ = col->string("outputPath", "");
+   randomSeed_ = (uint32_t)col->number("randomSeed", 1.0);
    if (nx_ <= 0 || ny_ <= 0 || nbatch_ <= 0 || dt_ <= 0) {
       err = fmt("HyPerCol \"", col->name, "\": nx, ny, nbatch and dt must be positive");
       return false;
@@ -161,12 +166,12 @@ bool Column::build(const std::string &text, std::string &err) {
       static const std::map<std::string, Layer::Kind> kinds = {
             {"ImageLayer", Layer::Input}, {"PvpLayer", Layer::Input},     {"HyPerLayer", Layer::HyPer},
             {"ANNLayer", Layer::ANN},     {"ANNErrorLayer", Layer::ANNError}, {"HyPerLCALayer", Layer::LCA},
-            {"MomentumLCALayer", Layer::MomentumLCA}, {"ISTALayer", Layer::ISTA}};
+            {"MomentumLCALayer", Layer::MomentumLCA}, {"ISTALayer", Layer::ISTA}, {"LIFLayer", Layer::LIF}};
       auto k = kinds.find(g.keyword);
       if (k == kinds.end()) {
          if (g.keyword.size() > 5 && g.keyword.compare(g.keyword.size() - 5, 5, "Layer") == 0) {
             err = fmt("layer type ", g.keyword, " is outside this drop-in (inputs, HyPerLayer, ANNLayer, "
-                                                "ANNErrorLayer, HyPerLCALayer, MomentumLCALayer, ISTALayer)");
+                                                "ANNErrorLayer, HyPerLCALayer, MomentumLCALayer, ISTALayer, LIFLayer)");
             return false;
          }
          continue;
@@ -213,6 +218,41 @@ bool Column::build(const std::string &text, std::string &err) {
       L->momentumRate = (float)g.number("LCAMomentumRate", 0.0);
       L->selfInteract = g.flag("selfInteract", true);
       L->displayPeriod = (int)g.number("displayPeriod", 0);
+      L->inputPath = g.string("inputPath", "");
+      // LayerOutputComponent: writeStep defaults to dt when absent, initialWriteTime to 0
+      L->writeStep = g.number("writeStep", dt_);
+      L->writeTime = g.number("initialWriteTime", 0.0);
+      if (L->kind == Layer::LIF) {
+         // LIFParams (components/LIFActivityComponent.hpp:22-45) with default_params.h defaults
+         pvgpu_lif_params &q = L->lif;
+         q.Vrest = (float)g.number("Vrest", -70.0);
+         q.Vexc = (float)g.number("Vexc", 0.0);
+         q.Vinh = (float)g.number("Vinh", -75.0);
+         q.VinhB = (float)g.number("VinhB", -90.0);
+         q.VthRest = (float)g.number("VthRest", -55.0);
+         q.tau = (float)g.number("tau", 20.0);
+         q.tauVth = (float)g.number("tauVth", 10.0);
+         q.deltaVth = (float)g.number("deltaVth", 5.0);
+         q.deltaGIB = (float)g.number("deltaGIB", 1.0);
+         q.noiseAmpE = (float)g.number("noiseAmpE", 0.0);
+         q.noiseAmpI = (float)g.number("noiseAmpI", 0.0);
+         q.noiseAmpIB = (float)g.number("noiseAmpIB", 0.0);
+         // noise frequencies are capped at one event per step (LIFActivityComponent::initializeState)
+         const float maxFreq = (float)(1000.0 / dt_);
+         q.noiseFreqE = std::min((float)g.number("noiseFreqE", 250.0), maxFreq);
+         q.noiseFreqI = std::min((float)g.number("noiseFreqI", 250.0), maxFreq);
+         q.noiseFreqIB = std::min((float)g.number("noiseFreqIB", 250.0), maxFreq);
+         q.tauE = (float)g.number("tauE", 1.0);
+         q.tauI = (float)g.number("tauI", 5.0);
+         q.tauIB = (float)g.number("tauIB", 10.0);
+         const std::string method = g.string("method", "arma");
+         L->lifMethod = method.empty() ? 'a' : method[0];
+         if (L->lifMethod != 'a' && L->lifMethod != 'b' && L->lifMethod != 'o') {
+            err = fmt("layer \"", g.name, "\": method \"", method, "\" (arma, beginning or original)");
+            return false;
+         }
+         L->numChannels = 3;  // EXC, INH, INHB
+      }
       if (g.has("adaptiveTimeScaleProbe") && !g.string("adaptiveTimeScaleProbe", "").empty()) {
          err = fmt("layer \"", g.name, "\": the adaptive time-scale probe is outside this drop-in (fixed dt)");
          return false;
@@ -371,6 +411,15 @@ bool Column::allocate(std::string &err) {
             L->prevDrive = (float *)dalloc(L->numRes() * nb * 4);
             if (!L->prevDrive) break;
          }
+         if (L->kind == Layer::LIF) {
+            L->V = (float *)dalloc(L->numRes() * nb * 4);
+            L->Vth = (float *)dalloc(L->numRes() * nb * 4);
+            L->GE = (float *)dalloc(L->numRes() * nb * 4);
+            L->GI = (float *)dalloc(L->numRes() * nb * 4);
+            L->GIB = (float *)dalloc(L->numRes() * nb * 4);
+            L->rnd = (pvgpu_taus *)dalloc(L->numRes() * nb * sizeof(pvgpu_taus));
+            if (!L->V || !L->Vth || !L->GE || !L->GI || !L->GIB || !L->rnd) break;
+         }
          L->dtAdapt = (double *)dalloc(nb * sizeof(double));
          if (!L->A || !L->gsyn || !L->G || !L->V || !L->dtAdapt) break;
          std::vector<double> dts(nb, dt_);
@@ -394,6 +443,26 @@ bool Column::allocate(std::string &err) {
    // initial state: V from InitVType, A = T(V), published (HyPerActivityBuffer::initializeState)
    for (auto &L : layers_) {
       if (L->kind == Layer::Input) continue;
+      if (L->kind == Layer::LIF) {
+         // LIFActivityComponent::initializeState: conductances 0, Vth = VthRest; V from InitVType;
+         // generator states seeded from the column's randomSeed (cl_random_init layout); A = 0
+         const size_t n = (size_t)L->numRes() * nbatch_;
+         std::vector<float> v(n, (float)L->initV), vth(n, L->lif.VthRest);
+         pvgpu_status s = pvgpu_taus_init(L->rnd, (int64_t)n, randomSeed_, stream_);
+         if (s != PVGPU_OK || cudaMemcpyAsync(L->V, v.data(), n * 4, cudaMemcpyHostToDevice, stream_) != cudaSuccess ||
+             cudaMemcpyAsync(L->Vth, vth.data(), n * 4, cudaMemcpyHostToDevice, stream_) != cudaSuccess ||
+             cudaStreamSynchronize(stream_) != cudaSuccess) {
+            err = "LIF initial state failed";
+            return false;
+         }
+         if (L->sparse &&
+             pvgpu_compact_active(L->A, nbatch_, L->numExt(), L->entries, L->numActive, L->scratch, L->scratchBytes,
+                                  stream_) != PVGPU_OK) {
+            err = std::string("initial state: ") + pvgpu_last_error();
+            return false;
+         }
+         continue;
+      }
       if (L->initV != 0.0) {
          std::vector<float> v((size_t)L->numRes() * nbatch_, (float)L->initV);
          std::string e2;
@@ -418,7 +487,57 @@ bool Column::allocate(std::string &err) {
       err = "initialisation failed on the device";
       return false;
    }
+   for (auto &L : layers_) {
+      if (L->keyword == "PvpLayer" && !L->inputPath.empty() && !load_pvp_frames(*L, err)) return false;
+      if (!outputPath_.empty() && L->writeStep >= 0) {
+         const std::string path = outputPath_ + "/" + L->name + ".pvp";
+         if (pvhost_pvp_writer_open(path.c_str(), L->loc.nx, L->loc.ny, L->loc.nf, L->sparse ? 1 : 0, &L->out) !=
+             PVGPU_OK) {
+            err = fmt("layer \"", L->name, "\": ") + pvhost_last_error();
+            return false;
+         }
+      }
+   }
    return true;
+}
+
+// PvpLayer frames (InputActivityBuffer with batchMethod byFile, components/BatchIndexer.cpp:60-83):
+// batch element b in display period d shows file frame (b + d * nbatch) mod F; the frame sequence
+// repeats after F / gcd(F, nbatch) display periods, which are loaded here.
+bool Column::load_pvp_frames(Layer &L, std::string &err) {
+   PvpReader r;
+   if (!r.open(L.inputPath, err)) return false;
+   const PvpHeader &h = r.header();
+   if (h.nx != L.loc.nx || h.ny != L.loc.ny || h.nf != L.loc.nf || r.num_frames() <= 0) {
+      err = fmt("layer \"", L.name, "\": ", L.inputPath, " holds ", h.nx, "x", h.ny, "x", h.nf, " frames (",
+                r.num_frames(), ")");
+      return false;
+   }
+   const int F = r.num_frames();
+   int a = F, b = nbatch_;
+   while (b) {
+      const int t = a % b;
+      a = b;
+      b = t;
+   }
+   const int D = F / a;
+   const size_t n = (size_t)L.numRes();
+   std::vector<float> frames((size_t)D * nbatch_ * n);
+   for (int d = 0; d < D; d++)
+      for (int bb = 0; bb < nbatch_; bb++)
+         if (!r.read_dense((bb + d * nbatch_) % F, frames.data() + ((size_t)d * nbatch_ + bb) * n, nullptr, err))
+            return false;
+   return set_input(L.name, frames.data(), D, err) == PVGPU_OK;
+}
+
+// LayerOutputComponent::outputState (components/LayerOutputComponent.cpp:183-197).
+pvgpu_status Column::output(Layer &L, double simTime, std::string &err) {
+   if (!L.out || L.writeStep < 0 || simTime < L.writeTime - dt_ / 2) return PVGPU_OK;
+   L.writeTime += L.writeStep;
+   pvgpu_status s = L.sparse ? pvhost_pvp_write_sparse_device(L.out, &L.loc, L.entries, L.numActive, simTime, stream_)
+                             : pvhost_pvp_write_dense_device(L.out, &L.loc, L.A, simTime, stream_);
+   if (s != PVGPU_OK) err = fmt("layer \"", L.name, "\" output: ") + pvhost_last_error();
+   return s;
 }
 
 pvgpu_status Column::refresh_weights(Conn &c, std::string &err) {
@@ -529,6 +648,10 @@ pvgpu_status Column::update(Layer &L, std::string &err) {
       const int frame = L.displayPeriod > 0 ? ((t_ - 1) / L.displayPeriod) % L.numFrames : 0;
       const float *src = L.frames + (size_t)frame * n;
       s = pvgpu_ann_activity(&L.loc, src, -FLT_MAX, -FLT_MAX, FLT_MAX, 0.0f, 0.0f, L.A, stream_);
+   } else if (L.kind == Layer::LIF) {
+      // the three channels as LIFActivityComponent reads them (GSynHead, channel-major)
+      s = pvgpu_lif_update(&L.loc, L.lifMethod, &L.lif, (float)dt_, L.rnd, L.V, L.Vth, L.GE, L.GI, L.GIB, L.gsyn, L.A,
+                           stream_);
    } else {
       const int nch = std::min(L.numChannels, (int)L.coeffs.size());
       s = pvgpu_gsyn_accumulate(n, nch, L.coeffs.data(), L.gsyn, L.G, stream_);
@@ -579,12 +702,29 @@ pvgpu_status Column::step(std::string &err) {
          pvgpu_status s = update(*L, err);
          if (s != PVGPU_OK) return s;
       }
+      for (Layer *L : now) {
+         pvgpu_status s = output(*L, t_ * dt_, err);
+         if (s != PVGPU_OK) return s;
+      }
    }
    return PVGPU_OK;
 }
 
 pvgpu_status Column::advance(int numSteps, std::string &err) {
    if (numSteps < 0) return PVGPU_ERR_BAD_ARG;
+   if (t_ == 0 && !initialOutputDone_ && !outputPath_.empty()) {
+      // the initial conditions (HyPerCol::allocateDataStructures, columns/HyPerCol.cpp:400-415)
+      initialOutputDone_ = true;
+      for (auto &L : layers_) {
+         if (L->kind == Layer::Input && !L->frames) continue;
+         if (L->kind == Layer::Input) {
+            pvgpu_status s = update(*L, err);  // the frame shown at time 0
+            if (s != PVGPU_OK) return s;
+         }
+         pvgpu_status s = output(*L, 0.0, err);
+         if (s != PVGPU_OK) return s;
+      }
+   }
    for (int i = 0; i < numSteps; i++) {
       pvgpu_status s = step(err);
       if (s != PVGPU_OK) return s;

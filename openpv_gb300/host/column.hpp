@@ -9,6 +9,7 @@
 //   HyPerLCALayer       LCA update, A = T(V)            (HyPerLCAInternalStateBuffer.kpp)
 //   MomentumLCALayer    LCA update with momentum        (MomentumLCAInternalStateBuffer.kpp)
 //   ISTALayer           ISTA update                     (ISTAInternalStateBuffer.kpp)
+//   LIFLayer            LIF update on channels EXC / INH / INHB (LIFActivityComponent.cpp)
 //   HyPerConn / TransposeConn / IdentConn               (connections/*.cpp)
 //
 // and selects each connection's delivery by the keyword HyPerDeliveryCreator builds
@@ -19,12 +20,19 @@
 // channels, the GSyn accumulator (channelCoefficients, default +1, -1) and sparse publication
 // (sparseLayer: the SparseList built on the device) follow the reference components.
 //
+// Layer output (LayerOutputComponent.cpp): when the HyPerCol group names an outputPath, every
+// layer with writeStep >= 0 (default dt) writes <outputPath>/<layer>.pvp -- sparse-values frames
+// for sparse layers, packed on the device -- at initialWriteTime (default 0) and every writeStep
+// after its phase publishes.  PvpLayer reads its frames from inputPath (.pvp) with the byFile
+// batching of BatchIndexer (batch element b, display period d: frame (b + d * nbatch) mod F).
+//
 // Out of this drop-in (refused with a message): plasticity, delays, stochastic release, the
 // adaptive time-scale probe, random initial V, layer types outside the list above.
 #pragma once
 
 #include "params.hpp"
 #include "pvgpu.h"
+#include "pvhost.h"
 
 #include <cuda_runtime.h>
 
@@ -39,7 +47,7 @@ class Column;
 struct Conn;
 
 struct Layer {
-   enum Kind { Input, HyPer, ANN, ANNError, LCA, MomentumLCA, ISTA } kind = HyPer;
+   enum Kind { Input, HyPer, ANN, ANNError, LCA, MomentumLCA, ISTA, LIF } kind = HyPer;
    std::string name, keyword;
    int phase = 0;
    pvgpu_loc loc{};  // halo = the largest margin its outgoing connections need
@@ -53,9 +61,16 @@ struct Layer {
    float momentumRate = 0.0f;            // MomentumLCALayer LCAMomentumRate
    bool selfInteract = true;             // HyPerLCALayer
    int displayPeriod = 0;                // input layers
+   std::string inputPath;                // PvpLayer
    double initV = 0.0;                   // ConstantV initial state
+   pvgpu_lif_params lif{};               // LIFLayer
+   char lifMethod = 'a';
+   double writeStep = -1.0, writeTime = 0.0;  // layer output
+   pvhost_pvp_writer *out = nullptr;
    // device buffers
    float *gsyn = nullptr, *G = nullptr, *V = nullptr, *A = nullptr, *frames = nullptr, *prevDrive = nullptr;
+   float *Vth = nullptr, *GE = nullptr, *GI = nullptr, *GIB = nullptr;  // LIF
+   pvgpu_taus *rnd = nullptr;
    double *dtAdapt = nullptr;
    int numFrames = 0;
    pvgpu_entry *entries = nullptr;
@@ -119,12 +134,17 @@ class Column {
  private:
    pvgpu_status step(std::string &err);
    pvgpu_status update(Layer &L, std::string &err);
+   pvgpu_status output(Layer &L, double simTime, std::string &err);
+   bool load_pvp_frames(Layer &L, std::string &err);
    pvgpu_status refresh_weights(Conn &c, std::string &err);
    bool allocate(std::string &err);
 
    Params params_;
    int nx_ = 0, ny_ = 0, nbatch_ = 1;
    double dt_ = 1.0;
+   std::string outputPath_;
+   uint32_t randomSeed_ = 1;
+   bool initialOutputDone_ = false;
    int t_ = 0;
    int maxPhase_ = 0;
    cudaStream_t stream_ = nullptr;

@@ -194,3 +194,74 @@ def test_one_to_one_gpu_delivery_in_the_column(capi, oracle, post):
     a[:, h:h + ny, h:h + nx, :] = x
     ref = oracle.deliver_pre(pre, postl, p, p, w, a_ext=a)
     np.testing.assert_allclose(v, ref, rtol=1e-5, atol=1e-5 * np.abs(ref).max())
+
+
+def lif_network_params(nb, n, p, outdir, inpath, method):
+    return f"""
+HyPerCol "column" = {{ nx = {n}; ny = {n}; nbatch = {nb}; dt = 1.0; stopTime = 10; randomSeed = 5;
+   outputPath = "{outdir}"; }};
+PvpLayer "Spikes" = {{ nxScale = 1; nyScale = 1; nf = 1; phase = 0; displayPeriod = 1; inputPath = "{inpath}";
+   sparseLayer = true; writeStep = 1; }};
+LIFLayer "Exc" = {{ nxScale = 1; nyScale = 1; nf = 4; phase = 1; InitVType = "ConstantV"; valueV = -70;
+   method = "{method}"; sparseLayer = true; writeStep = 1; }};
+HyPerConn "SpikesToExc" = {{ preLayerName = "Spikes"; postLayerName = "Exc"; channelCode = 0;
+   nxp = {p}; nyp = {p}; nfp = 4; sharedWeights = true; weightInitType = "FileWeight"; initWeightsFile = "w.pvp";
+   plasticityFlag = false; receiveGpu = false; updateGSynFromPostPerspective = false;
+   pvpatchAccumulateType = "convolve"; }};
+"""
+
+
+def test_lif_network_from_params_with_pvp_input_and_output(capi, oracle, tmp_path):
+    """A spiking network from an OpenPV params file: a PvpLayer replays Poisson spike frames from
+    a .pvp file (byFile batching), a HyPerConn delivers them (Convolve keyword: reference order)
+    into the EXC channel of a LIFLayer (Heun method), and both layers write their activity to
+    <outputPath>/<layer>.pvp every step from t = 0.  The written frames equal the oracle's network
+    composed from the pinned pieces, bit for bit."""
+    from tests.test_gpu_kernels import OL
+    nb, n, p, steps, F = 2, 24, 5, 5, 6
+    rng = np.random.default_rng(41)
+    frames = (rng.random((F, n, n, 1)) < 0.08).astype(np.float32)
+    inpath = tmp_path / "spikes.pvp"
+    with capi.PvpWriter(inpath, n, n, 1, True) as w:
+        for f in range(F):
+            idx = np.nonzero(frames[f].reshape(-1))[0]
+            w.write_sparse(idx, np.ones(len(idx), np.float32), float(f))
+    w = (0.8 * rng.uniform(0.5, 1.5, (1, p, p, 4))).astype(np.float32)
+    col = capi.Column(lif_network_params(nb, n, p, tmp_path, inpath, "beginning"))
+    col.set_weights("SpikesToExc", w)
+    col.advance(steps)
+    del col  # closes the files
+    # oracle
+    h = 2
+    pre = oracle.Loc.make(nb, n, n, 1, h, h)
+    post = oracle.Loc.make(nb, n, n, 4, 0, 0)
+    nres = nb * n * n * 4
+    st = {"rnd": oracle.taus_init(nres, 5), "V": np.full(nres, -70.0, np.float32),
+          "Vth": np.full(nres, -55.0, np.float32), "GE": np.zeros(nres, np.float32),
+          "GI": np.zeros(nres, np.float32), "GIB": np.zeros(nres, np.float32)}
+    a = np.zeros(post.ext_shape(), np.float32)
+    prm = oracle.lif_params_array()
+    want_exc, want_in = [a[:, :, :, :].copy()], []
+    for t in range(1, steps + 1):
+        x = np.zeros(pre.ext_shape(), np.float32)
+        for b in range(nb):
+            x[b, h:h + n, h:h + n, :] = frames[(b + (t - 1) * nb) % F]
+        want_in.append(x[:, h:h + n, h:h + n, :].copy())
+        e, c = oracle.compact(x.reshape(nb, -1))
+        g = oracle.deliver_pre(pre, post, p, p, w, entries=e, num_active=c)
+        gs = np.stack([g.reshape(-1), np.zeros(nres, np.float32), np.zeros(nres, np.float32)])
+        st, a = oracle.lif_update("b", post, prm, 1.0, st, gs, a)
+        want_exc.append(a.copy())
+    assert sum(float(x.sum()) for x in want_exc) > 0
+    with capi.PvpReader(tmp_path / "Exc.pvp") as r:
+        assert r.header["fileType"] == 6 and r.num_frames == (steps + 1) * nb
+        for t in range(steps + 1):
+            for b in range(nb):
+                v, ts = r.read_dense(t * nb + b)
+                assert ts == float(t)
+                assert np.array_equal(v, want_exc[t][b]), (t, b)
+    with capi.PvpReader(tmp_path / "Spikes.pvp") as r:
+        assert r.num_frames == (steps + 1) * nb
+        for t in range(1, steps + 1):
+            for b in range(nb):
+                assert np.array_equal(r.read_dense(t * nb + b)[0], want_in[t - 1][b])
