@@ -365,6 +365,17 @@ pvgpu_status pvgpu_hebbian_dw(
       float *dw,
       void *stream);
 
+/* ---- MomentumUpdater (weightupdaters/MomentumUpdater.cpp:291-345) --------------------------
+ * The momentum factors of MomentumUpdater::applyMomentum for momentumMethod 'v' (viscosity:
+ * dwFactor = exp(-1/tau), 0 for tau 0), 's' (simple: tau) and 'a' (alex: tau, wFactor scaled by
+ * dWMax); wFactor = momentumDecay.  Host function. */
+pvgpu_status pvgpu_momentum_factors(char method, float tau, float decay, float dWMax, float *dwFactor, float *wFactor);
+/* One MomentumUpdater::updateWeights on the device, weight by weight: dW = dW*(1 - dwFactor)
+ * + dwFactor*prev_dW - wFactor*W, then prev_dW = dW and W += dW (HebbianUpdater::updateWeights).
+ * dw holds the Hebbian dW of this update (pvgpu_hebbian_dw) on entry. */
+pvgpu_status pvgpu_momentum_update_weights(int64_t n, float dwFactor, float wFactor, float *dw, float *prevDw,
+                                           float *w, void *stream);
+
 /* ---- the batched LCA module ------------------------------------------------------------------
  * The per-timestep layer sequence of an LCA module (input -> error <-> V1; the LCA-CIFAR
  * topology of tutorials/LCA-CIFAR and tests/GPULCATest), replacing, per step, the reference's

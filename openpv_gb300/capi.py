@@ -142,6 +142,8 @@ def _declare(L):
         "pvgpu_deliver_tc_check_error": (i, []),
         "pvgpu_lif_update": (i, [lp, C.c_char, vp, f, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
         "pvgpu_pvp_sparse_frames": (i, [lp, vp, vp, vp, vp, vp]),
+        "pvgpu_momentum_factors": (i, [C.c_char, f, f, f, C.POINTER(f), C.POINTER(f)]),
+        "pvgpu_momentum_update_weights": (i, [i64, f, f, vp, vp, vp, vp]),
         "pvgpu_pvp_dense_frames": (i, [lp, vp, vp, vp]),
         "pvgpu_pvp_scatter_sparse": (i, [lp, vp, vp, vp, vp, vp]),
         "pvgpu_taus_init": (i, [vp, i64, C.c_uint32, vp]),
@@ -268,6 +270,18 @@ def lif_update(loc, method, params, dt, rnd, v, vth, ge, gi, gib, gsyn_head, a_e
 
 def taus_init(state, count, seed, stream=None):
     check(lib().pvgpu_taus_init(_ptr(state), count, seed, _stream(stream)), "taus_init")
+
+
+def momentum_factors(method, tau, decay=0.0, dw_max=1.0):
+    a, b = C.c_float(), C.c_float()
+    check(lib().pvgpu_momentum_factors(method.encode()[:1], tau, decay, dw_max, C.byref(a), C.byref(b)),
+          "momentum_factors")
+    return a.value, b.value
+
+
+def momentum_update_weights(dw, prev_dw, w, dw_factor, w_factor, stream=None):
+    check(lib().pvgpu_momentum_update_weights(dw.numel(), dw_factor, w_factor, _ptr(dw), _ptr(prev_dw), _ptr(w),
+                                              _stream(stream)), "momentum_update_weights")
 
 
 def deliver_tc_check_error():

@@ -149,3 +149,53 @@ extern "C" pvgpu_status pvgpu_hebbian_dw(const pvgpu_conn_desc *conn, float dWMa
    PVGPU_CHECK_LAUNCH("hebbian_dw");
    return PVGPU_OK;
 }
+
+// ---- MomentumUpdater (weightupdaters/MomentumUpdater.cpp:291-345) ----------------------------
+// applyMomentum then prev_dW = dW then HebbianUpdater::updateWeights (W += dW), one thread per
+// weight, every operation separately rounded as the reference's loop does.
+namespace {
+__global__ void momentum_weights_kernel(int64_t n, float dwFactor, float wFactor, float *__restrict__ dw,
+                                        float *__restrict__ prevDw, float *__restrict__ w) {
+   const float keep = __fadd_rn(1.0f, -dwFactor);
+   for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+      float d = __fmul_rn(dw[k], keep);
+      d = __fadd_rn(d, __fmul_rn(dwFactor, prevDw[k]));
+      const float wk = w[k];
+      d = __fadd_rn(d, -__fmul_rn(wFactor, wk));
+      dw[k] = d;
+      prevDw[k] = d;
+      w[k] = __fadd_rn(wk, d);
+   }
+}
+}  // namespace
+
+extern "C" pvgpu_status pvgpu_momentum_factors(char method, float tau, float decay, float dWMax, float *dwFactor,
+                                               float *wFactor) {
+   if (!dwFactor || !wFactor) return PVGPU_ERR_BAD_ARG;
+   switch (method) {
+      case 'v':  // viscosity: exp(-1/tau), 0 when tau is 0 (host expf, as the reference)
+         *dwFactor = tau != 0.0f ? std::exp(-1.0f / tau) : 0.0f;
+         *wFactor = decay;
+         return PVGPU_OK;
+      case 's':
+         *dwFactor = tau;
+         *wFactor = decay;
+         return PVGPU_OK;
+      case 'a':
+         *dwFactor = tau;
+         *wFactor = decay * dWMax;
+         return PVGPU_OK;
+      default: return PVGPU_ERR_BAD_ARG;
+   }
+}
+
+extern "C" pvgpu_status pvgpu_momentum_update_weights(int64_t n, float dwFactor, float wFactor, float *dw,
+                                                      float *prevDw, float *w, void *stream) {
+   if (n < 0 || (n > 0 && (!dw || !prevDw || !w))) return PVGPU_ERR_BAD_ARG;
+   if (n == 0) return PVGPU_OK;
+   const int64_t blocks = (n + 255) / 256;
+   momentum_weights_kernel<<<(unsigned)(blocks < 4096 ? blocks : 4096), 256, 0, pvgpu::as_stream(stream)>>>(
+         n, dwFactor, wFactor, dw, prevDw, w);
+   PVGPU_CHECK_LAUNCH("momentum_update_weights");
+   return PVGPU_OK;
+}

@@ -128,6 +128,8 @@ def _declare(L):
         "pvo_taus_init": (None, [vp, C.c_size_t, C.c_uint32]),
         "pvo_taus_next": (None, [vp, C.c_size_t]),
         "pvo_lif_update": (i, [C.c_char, lp, vp, f, vp, vp, vp, vp, vp, vp, vp, vp]),
+        "pvo_momentum_factors": (i, [C.c_char, f, f, f, C.POINTER(f), C.POINTER(f)]),
+        "pvo_momentum_update_weights": (None, [C.c_int64, f, f, vp, vp, vp]),
         "pvo_ista_update": (None, [lp, f, vp, f, vp, vp, vp]),
         "pvo_lca_update_f64": (None, [lp, i, vp, d, vp, vp, vp]),
         "pvo_ann_activity": (None, [lp, vp, f, f, f, f, f, vp]),
@@ -307,6 +309,21 @@ def lif_update(method, loc, params, dt, state, gsyn_head, a_ext):
                               _p(_c(gsyn_head, np.float32)), _p(a))
     _check(rc, "lif_update")
     return st, a
+
+
+def momentum_factors(method, tau, decay=0.0, dw_max=1.0):
+    """(dwFactor, wFactor) of MomentumUpdater::applyMomentum for momentumMethod viscosity / simple / alex."""
+    a, b = C.c_float(), C.c_float()
+    _check(lib().pvo_momentum_factors(method.encode()[:1], tau, decay, dw_max, C.byref(a), C.byref(b)),
+           "momentum_factors")
+    return a.value, b.value
+
+
+def momentum_update_weights(dw, prev_dw, w, dw_factor, w_factor):
+    """MomentumUpdater::updateWeights: returns (dw, prev_dw, w) after one update."""
+    dw, prev_dw, w = (_c(x, np.float32).copy() for x in (dw, prev_dw, w))
+    lib().pvo_momentum_update_weights(dw.size, dw_factor, w_factor, _p(dw), _p(prev_dw), _p(w))
+    return dw, prev_dw, w
 
 
 def ista_update(loc, g, a_ext, v, dt_adapt, tau, vthresh):

@@ -549,3 +549,30 @@ int pvo_lif_update(char method, const pvo_loc *loc, const pvo_lif_params *p, flo
    }
    return 0;
 }
+
+/* ---- MomentumUpdater (weightupdaters/MomentumUpdater.cpp:291-345) ---------------------------- */
+
+/* The momentum factors of applyMomentum: viscosity dwFactor = exp(-1/tau) (0 when tau is 0),
+ * simple and alex dwFactor = tau; wFactor = momentumDecay, times dWMax for alex. */
+int pvo_momentum_factors(char method, float tau, float decay, float dWMax, float *dwFactor, float *wFactor) {
+   switch (method) {
+      case 'v': *dwFactor = tau != 0.0f ? expf(-1.0f / tau) : 0.0f; *wFactor = decay; return 0;
+      case 's': *dwFactor = tau; *wFactor = decay; return 0;
+      case 'a': *dwFactor = tau; *wFactor = decay * dWMax; return 0;
+      default: return -1;
+   }
+}
+
+/* applyMomentum, then prev_dW = dW and HebbianUpdater::updateWeights (W += dW), element by
+ * element in float: dW = dW * (1 - f); dW = dW + f * prev; dW = dW - g * W. */
+void pvo_momentum_update_weights(int64_t n, float dwFactor, float wFactor, float *dw, float *prevDw, float *w) {
+   const float keep = 1 - dwFactor;
+   for (int64_t k = 0; k < n; k++) {
+      float d = dw[k] * keep;
+      d = d + dwFactor * prevDw[k];
+      d = d - wFactor * w[k];
+      dw[k] = d;
+      prevDw[k] = d;
+      w[k] = w[k] + d;
+   }
+}

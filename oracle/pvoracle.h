@@ -329,6 +329,11 @@ void pvo_taus_next(pvo_taus *state, size_t count);
 int pvo_lif_update(char method, const pvo_loc *loc, const pvo_lif_params *p, float dt, pvo_taus *rnd, float *V,
                    float *Vth, float *GE, float *GI, float *GIB, const float *gsynHead, float *aExt);
 
+/* ---- MomentumUpdater (weightupdaters/MomentumUpdater.cpp:291-345) ---- */
+/* method 'v' viscosity, 's' simple, 'a' alex; -1 otherwise. */
+int pvo_momentum_factors(char method, float tau, float decay, float dWMax, float *dwFactor, float *wFactor);
+void pvo_momentum_update_weights(int64_t n, float dwFactor, float wFactor, float *dw, float *prevDw, float *w);
+
 #ifdef __cplusplus
 }
 #endif

@@ -350,3 +350,27 @@ def test_deliver_ident_matches_reference_rule(cuda, oracle):
     vd = T(torch, v)
     assert L.pvgpu_err_scale(v.size, C.c_float(0.3), capi._ptr(vd), capi._stream()) == 0
     assert np.array_equal(H(vd), v * np.float32(0.3))
+
+
+@pytest.mark.parametrize("method", ["v", "s", "a"])
+def test_momentum_weight_update_bitexact(cuda, oracle, method):
+    """MomentumUpdater::updateWeights on the device (pvgpu_momentum_update_weights) equals the
+    oracle's restatement over several updates, with the Hebbian dW of each update from
+    pvgpu_hebbian_dw (itself bit-exact vs the oracle)."""
+    torch = cuda
+    from openpv_gb300 import capi
+    rng = np.random.default_rng(ord(method))
+    n = 64 * 8 * 8 * 3 + 5
+    f_d = capi.momentum_factors(method, 0.8 if method != "v" else 20.0, 0.01, 0.5)
+    f_o = oracle.momentum_factors(method, 0.8 if method != "v" else 20.0, 0.01, 0.5)
+    assert f_d == f_o
+    w = rng.normal(size=n).astype(np.float32)
+    prev = np.zeros(n, np.float32)
+    wd, pd = T(torch, w), T(torch, prev)
+    for _ in range(4):
+        dw = rng.normal(0, 0.1, n).astype(np.float32)
+        dd = T(torch, dw)
+        dw, prev, w = oracle.momentum_update_weights(dw, prev, w, *f_o)
+        capi.momentum_update_weights(dd, pd, wd, *f_d)
+        for a, b in ((dd, dw), (pd, prev), (wd, w)):
+            assert np.array_equal(H(a).view(np.uint32), b.view(np.uint32))
