@@ -290,125 +290,172 @@ def delivery_bench(torch, capi, reps=5):
 
 
 # ---------------------------------------------------------------------------------------------
-# LIF network step (Poisson input -> excitatory LIF layer), 16 images
+# LIF spiking network (the spiking configuration): 8 images, 1000 timesteps in one CUDA graph
 # ---------------------------------------------------------------------------------------------
-def lif_bench(torch, capi, steps=40, cpu_sample=True):
-    """One timestep of the spiking path on 16 images: input spikes 256x256x1 (Poisson, rates
-    U[5, 50] Hz at dt = 1 ms, pre-generated as SparseLists, 8 frames cycled) delivered
-    presynaptically through 11x11x32 Gaussian weights into the EXC channel of a 256x256x32 LIF
-    layer (arma method), the LIF update, and the compaction of its spikes into a SparseList."""
-    nb, n, nf, p = 16, 256, 32, 11
-    pre = capi.Loc.make(nb, n, n, 1, 5)
-    post = capi.Loc.make(nb, n, n, nf, 0)
-    conn = capi.conn_desc(pre, post, p, p)
-    g = torch.Generator(device="cuda").manual_seed(1234 + 5)
-    yy, xx = torch.meshgrid(torch.arange(-5, 6, device="cuda"), torch.arange(-5, 6, device="cuda"), indexing="ij")
-    gauss = torch.exp(-(xx ** 2 + yy ** 2).float() / (2 * 2.5 ** 2))
-    w = (0.5 * gauss[None, :, :, None] * (0.5 + torch.rand((1, p, p, nf), device="cuda", generator=g))).contiguous()
-    rates = 5.0 + 45.0 * torch.rand((nb, n, n, 1), device="cuda", generator=g)
-    frames, ents, nums = 8, [], []
-    for _ in range(frames):
-        x = torch.zeros(pre.ext_shape(), device="cuda")
-        x[:, 5:5 + n, 5:5 + n, :] = (torch.rand((nb, n, n, 1), device="cuda", generator=g) < rates * 1e-3).float()
-        e = torch.zeros((nb, pre.num_ext, 2), dtype=torch.int32, device="cuda")
-        c = torch.zeros(nb, dtype=torch.int64, device="cuda")
-        capi.compact_active(x, nb, pre.num_ext, e, c)
-        ents.append(e)
-        nums.append(c)
+def gaussian_weights(torch, nfpre, p, nfpost, sigma, peak, device="cuda"):
+    r = torch.arange(p, device=device, dtype=torch.float32) - (p - 1) / 2.0
+    g = torch.exp(-(r[:, None] ** 2 + r[None, :] ** 2) / (2 * sigma ** 2))
+    return (peak * g[None, :, :, None].expand(nfpre, p, p, nfpost)).contiguous()
+
+
+class LifNet:
+    """Input (256x256x1 Poisson spikes, rates U[5, 50] Hz at dt = 1 ms, pre-generated on the device
+    as dense frames and compacted each step) -> excitatory LIF 256x256x32 (11x11 Gaussian, sigma 3,
+    peak 0.5, EXC channel) -> inhibitory LIF 128x128x8 (stride 2, 3x3 weights 0.05, EXC channel)
+    -> back to the excitatory layer (8x8 Gaussian, sigma 2, peak 1.0, INH channel; one-to-many at
+    stride 2 needs an even patch, so 8 rather than 7).  Default LIF parameters, arma method, noise
+    off.  One step: compact the input frame, the three deliveries (presynaptic, from SparseLists),
+    the two LIF updates, the compaction of each layer's spikes."""
+
+    def __init__(self, torch, capi, nb=8, steps=1000, seed=1234 + 5):
+        self.t, self.c, self.nb, self.steps = torch, capi, nb, steps
+        n, ne, ni = 256, 32, 8
+        self.inp = capi.Loc.make(nb, n, n, 1, 5)
+        self.exc = capi.Loc.make(nb, n, n, ne, 2)
+        self.inh = capi.Loc.make(nb, n // 2, n // 2, ni, 2)
+        exc_res = capi.Loc.make(nb, n, n, ne, 0)
+        inh_res = capi.Loc.make(nb, n // 2, n // 2, ni, 0)
+        self.c_in_exc = capi.conn_desc(self.inp, exc_res, 11, 11)
+        self.c_exc_inh = capi.conn_desc(self.exc, inh_res, 3, 3)
+        self.c_inh_exc = capi.conn_desc(self.inh, exc_res, 8, 8)
+        self.w_in_exc = gaussian_weights(torch, 1, 11, ne, 3.0, 0.5)
+        self.w_exc_inh = torch.full((ne * 4, 3, 3, ni), 0.05, device="cuda")  # 4 kernel phases x 32 features
+        self.w_inh_exc = gaussian_weights(torch, ni, 8, ne, 2.0, 1.0)
+        g = torch.Generator(device="cuda").manual_seed(seed)
+        rates = 5.0 + 45.0 * torch.rand((nb, n, n, 1), device="cuda", generator=g)
+        self.frames = torch.zeros((steps,) + tuple(self.inp.ext_shape()), device="cuda")
+        self.frames[:, :, 5:5 + n, 5:5 + n, :] = (torch.rand((steps, nb, n, n, 1), device="cuda", generator=g)
+                                                  < rates * 1e-3).float()
+        self.layers = {}
+        for name, loc in (("in", self.inp), ("exc", self.exc), ("inh", self.inh)):
+            d = {"loc": loc,
+                 "ent": torch.zeros((nb, loc.num_ext, 2), dtype=torch.int32, device="cuda"),
+                 "num": torch.zeros(nb, dtype=torch.int64, device="cuda"),
+                 "scratch": torch.empty(max(1, capi.lib().pvgpu_compact_scratch_bytes(nb, loc.num_ext)),
+                                        dtype=torch.uint8, device="cuda")}
+            if name != "in":
+                nres = nb * loc.nx * loc.ny * loc.nf
+                d.update(rnd=torch.zeros((nres, 4), dtype=torch.int32, device="cuda"),
+                         V=torch.full((nres,), -70.0, device="cuda"), Vth=torch.full((nres,), -55.0, device="cuda"),
+                         GE=torch.zeros(nres, device="cuda"), GI=torch.zeros(nres, device="cuda"),
+                         GIB=torch.zeros(nres, device="cuda"), gs=torch.zeros((3, nres), device="cuda"),
+                         A=torch.zeros(loc.ext_shape(), device="cuda"), spikes=torch.zeros(nres, device="cuda"))
+                capi.taus_init(d["rnd"], nres, 17 if name == "exc" else 18)
+            self.layers[name] = d
+        self.prm = capi.LifParams.make()
+
+    def compact(self, d, a):
+        self.c.compact_active(a, self.nb, d["loc"].num_ext, d["ent"], d["num"], scratch=d["scratch"])
+
+    def step(self, i, ev=None):
+        c, L = self.c, self.layers
+        rec = (lambda k: ev[k].record()) if ev else (lambda k: None)
+        rec(0)
+        self.compact(L["in"], self.frames[i])
+        e, h = L["exc"], L["inh"]
+        e["gs"].zero_()
+        h["gs"].zero_()
+        c.deliver_pre(self.c_in_exc, self.w_in_exc, e["gs"][0], entries=L["in"]["ent"], num_active=L["in"]["num"])
+        c.deliver_pre(self.c_inh_exc, self.w_inh_exc, e["gs"][1], entries=h["ent"], num_active=h["num"])
+        rec(1)
+        c.lif_update(e["loc"], "a", self.prm, 1.0, e["rnd"], e["V"], e["Vth"], e["GE"], e["GI"], e["GIB"], e["gs"], e["A"])
+        rec(2)
+        self.compact(e, e["A"])
+        c.deliver_pre(self.c_exc_inh, self.w_exc_inh, h["gs"][0], entries=e["ent"], num_active=e["num"])
+        c.lif_update(h["loc"], "a", self.prm, 1.0, h["rnd"], h["V"], h["Vth"], h["GE"], h["GI"], h["GIB"], h["gs"], h["A"])
+        self.compact(h, h["A"])
+        rec(3)
+
+
+def lif_bench(torch, capi, steps=1000, cpu_sample=True):
+    nb = 8
+    net = LifNet(torch, capi, nb=nb, steps=steps)
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        for i in range(3):  # warm-up, uncaptured
+            net.step(i)
+    torch.cuda.current_stream().wait_stream(s)
     torch.cuda.synchronize()
-    spikes_in = float(torch.stack(nums).float().mean().item())
-    nres = nb * n * n * nf
-    rnd = torch.zeros((nres, 4), dtype=torch.int32, device="cuda")
-    capi.taus_init(rnd, nres, 17)
-    V = torch.full((nres,), -70.0, device="cuda")
-    Vth = torch.full((nres,), -55.0, device="cuda")
-    GE, GI, GIB = (torch.zeros(nres, device="cuda") for _ in range(3))
-    gs = torch.zeros((3, nres), device="cuda")
-    a = torch.zeros(post.ext_shape(), device="cuda")
-    out_e = torch.zeros((nb, post.num_ext, 2), dtype=torch.int32, device="cuda")
-    out_n = torch.zeros(nb, dtype=torch.int64, device="cuda")
-    scratch = torch.empty(max(1, capi.lib().pvgpu_compact_scratch_bytes(nb, post.num_ext)), dtype=torch.uint8, device="cuda")
-    prm = capi.LifParams.make()
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
-    t_deliv = t_lif = t_comp = 0.0
-
-    def step(i, split=False):
-        nonlocal t_deliv, t_lif, t_comp
-        if split:
-            ev[0].record()
-        gs[0].zero_()
-        capi.deliver_pre(conn, w, gs[0], entries=ents[i % frames], num_active=nums[i % frames])
-        if split:
-            ev[1].record()
-        capi.lif_update(post, "a", prm, 1.0, rnd, V, Vth, GE, GI, GIB, gs, a)
-        if split:
-            ev[2].record()
-        capi.compact_active(a, nb, post.num_ext, out_e, out_n, scratch=scratch)
-        if split:
-            ev[3].record()
-            torch.cuda.synchronize()
-            t_deliv += ev[0].elapsed_time(ev[1])
-            t_lif += ev[1].elapsed_time(ev[2])
-            t_comp += ev[2].elapsed_time(ev[3])
-
-    for i in range(5):
-        step(i)
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        for i in range(steps):
+            net.step(i)
+    torch.cuda.synchronize()
+    graph.replay()  # warm-up replay
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
-    for i in range(steps):
-        step(i)
+    graph.replay()
     e1.record()
     torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / steps
-    ksplit = 10
-    for i in range(ksplit):
-        step(i, split=True)
-    spikes_out = float(out_n.float().mean().item())
-    mac = spikes_in * p * p * nf
-    lif_bytes = nres * (12 + 40 + 32 + 4)
-    out = {"workload": "16 images: Poisson input 256x256x1 (rates U[5,50] Hz, dt 1 ms) -> 11x11x32 Gaussian "
-                       "weights -> LIF 256x256x32 (arma) -> spike compaction; input SparseLists pre-generated",
-           "ms_per_step": ms, "image_steps_per_s": nb / (ms / 1e3),
-           "input_spikes_per_image": spikes_in, "output_spikes_per_image": spikes_out,
-           "delivery_ms": t_deliv / ksplit, "delivery_GFLOP_s": 2 * mac * nb / (t_deliv / ksplit) / 1e6,
-           "lif_update_ms": t_lif / ksplit, "lif_update_GB_s": lif_bytes / (t_lif / ksplit) / 1e6,
-           "compaction_ms": t_comp / ksplit}
+    ms = e0.elapsed_time(e1)
+    # per-phase split of one step (outside the graph)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    k, t_in, t_lif, t_rest = 10, 0.0, 0.0, 0.0
+    for i in range(k):
+        net.step(i, ev)
+        torch.cuda.synchronize()
+        t_in += ev[0].elapsed_time(ev[1])
+        t_lif += ev[1].elapsed_time(ev[2])
+        t_rest += ev[2].elapsed_time(ev[3])
+    ex, ih = net.layers["exc"], net.layers["inh"]
+    exc_n = nb * 256 * 256 * 32
+    out = {"workload": "8 images: Poisson input 256x256x1 (U[5,50] Hz, dt 1 ms) -> exc LIF 256x256x32 (11x11 Gaussian "
+                       "sigma 3 peak 0.5) -> inh LIF 128x128x8 (stride 2, 3x3) -> exc (INH channel, 8x8 Gaussian sigma 2 "
+                       "peak 1); arma, noise off; 1000 timesteps in one CUDA graph",
+           "timesteps": steps, "graph_ms": ms, "ms_per_step": ms / steps, "image_steps_per_s": nb * steps / (ms / 1e3),
+           "exc_spikes_per_image_step": float(ex["num"].float().mean().item()),
+           "inh_spikes_per_image_step": float(ih["num"].float().mean().item()),
+           "split_ms": {"input_compaction_and_exc_deliveries": t_in / k, "exc_lif_update": t_lif / k,
+                        "exc_compaction_inh_delivery_update_compaction": t_rest / k},
+           "exc_lif_update_GB_s": exc_n * 88 / (t_lif / k) / 1e6}
     if cpu_sample:
         out["cpu_oracle"] = lif_cpu_sample()
     return out
 
 
-def lif_cpu_sample():
-    """The same step for one image on one host core through the oracle (pinned to the reference's
-    own LIF loops and delivery): delivery from the SparseList, LIF update; 20 steps (about 2 s)."""
+def lif_cpu_sample(steps=6):
+    """The same network for one image on one host core through the oracle (its LIF update and
+    presynaptic delivery, pinned to the reference's own loops): a bounded sample of timesteps."""
     from oracle import oracle as O
     O.build()
     rng = np.random.default_rng(1234 + 5)
-    n, nf, p = 256, 32, 11
-    pre = O.Loc.make(1, n, n, 1, 5, 5)
-    post = O.Loc.make(1, n, n, nf, 0, 0)
-    yy, xx = np.mgrid[-5:6, -5:6]
-    w = (0.5 * np.exp(-(xx ** 2 + yy ** 2) / (2 * 2.5 ** 2))[None, :, :, None] *
-         rng.uniform(0.5, 1.5, (1, p, p, nf))).astype(np.float32)
-    nres = n * n * nf
-    st = {"rnd": O.taus_init(nres, 17), "V": np.full(nres, -70.0, np.float32), "Vth": np.full(nres, -55.0, np.float32),
-          "GE": np.zeros(nres, np.float32), "GI": np.zeros(nres, np.float32), "GIB": np.zeros(nres, np.float32)}
-    a = np.zeros(post.ext_shape(), np.float32)
+    n, ne, ni = 256, 32, 8
+    inp, exc, inh = O.Loc.make(1, n, n, 1, 5, 5), O.Loc.make(1, n, n, ne, 2, 2), O.Loc.make(1, n // 2, n // 2, ni, 2, 2)
+    exc_r, inh_r = O.Loc.make(1, n, n, ne, 0, 0), O.Loc.make(1, n // 2, n // 2, ni, 0, 0)
+
+    def gauss(nfpre, p, nfpost, sigma, peak):
+        r = np.arange(p) - (p - 1) / 2.0
+        g = np.exp(-(r[:, None] ** 2 + r[None, :] ** 2) / (2 * sigma ** 2))
+        return np.ascontiguousarray(np.broadcast_to(peak * g[None, :, :, None], (nfpre, p, p, nfpost))).astype(np.float32)
+
+    w_ie, w_ei, w_he = gauss(1, 11, ne, 3.0, 0.5), np.full((ne * 4, 3, 3, ni), 0.05, np.float32), gauss(ni, 8, ne, 2.0, 1.0)
     prm = O.lif_params_array()
+
+    def state(loc, seed):
+        m = loc.nx * loc.ny * loc.nf
+        return {"rnd": O.taus_init(m, seed), "V": np.full(m, -70.0, np.float32), "Vth": np.full(m, -55.0, np.float32),
+                "GE": np.zeros(m, np.float32), "GI": np.zeros(m, np.float32), "GIB": np.zeros(m, np.float32)}
+
+    se, sh = state(exc, 17), state(inh, 18)
+    ae, ah = np.zeros(exc.ext_shape(), np.float32), np.zeros(inh.ext_shape(), np.float32)
     rates = rng.uniform(5, 50, (1, n, n, 1))
-    reps = 20
     t0 = time.perf_counter()
-    for _ in range(reps):
-        x = np.zeros(pre.ext_shape(), np.float32)
+    for _ in range(steps):
+        x = np.zeros(inp.ext_shape(), np.float32)
         x[:, 5:5 + n, 5:5 + n, :] = (rng.random((1, n, n, 1)) < rates * 1e-3).astype(np.float32)
         e, c = O.compact(x.reshape(1, -1))
-        g = O.deliver_pre(pre, post, p, p, w, entries=e, num_active=c)
-        gs = np.stack([g.reshape(-1), np.zeros(nres, np.float32), np.zeros(nres, np.float32)])
-        st, a = O.lif_update("a", post, prm, 1.0, st, gs, a)
+        eh, ch = O.compact(ah.reshape(1, -1))
+        g0 = O.deliver_pre(inp, exc_r, 11, 11, w_ie, entries=e, num_active=c)
+        g1 = O.deliver_pre(inh, exc_r, 8, 8, w_he, entries=eh, num_active=ch)
+        se, ae = O.lif_update("a", exc, prm, 1.0, se, np.stack([g0.reshape(-1), g1.reshape(-1), 0 * g0.reshape(-1)]), ae)
+        ee, ce = O.compact(ae.reshape(1, -1))
+        gi = O.deliver_pre(exc, inh_r, 3, 3, w_ei, entries=ee, num_active=ce).reshape(-1)
+        sh, ah = O.lif_update("a", inh, prm, 1.0, sh, np.stack([gi, 0 * gi, 0 * gi]), ah)
     dt = time.perf_counter() - t0
-    return {"value": reps / dt, "unit": "image-steps/s", "cores": 1, "kind": "port",
-            "sample": f"oracle, 1 image x {reps} steps ({dt:.2f} s)"}
+    return {"value": steps / dt, "unit": "image-steps/s", "cores": 1, "kind": "port",
+            "sample": f"oracle, the whole network for 1 image x {steps} timesteps ({dt:.2f} s)"}
 
 
 # ---------------------------------------------------------------------------------------------
@@ -629,14 +676,15 @@ def main():
     ap.add_argument("--delivery", action="store_true",
                     help="run the presynaptic delivery microbenchmark only (profiling runs; not a bench line)")
     ap.add_argument("--lif", action="store_true",
-                    help="run the LIF network step only (profiling runs; not a bench line)")
+                    help="run the LIF network only (profiling runs; not a bench line)")
+    ap.add_argument("--lif-steps", type=int, default=1000, help="timesteps of the LIF network graph (--lif)")
     args = ap.parse_args()
     if args.lif:
         import torch
         from openpv_gb300 import build
         build.build()
         from openpv_gb300 import capi
-        print(json.dumps({"lif_network": lif_bench(torch, capi, steps=10, cpu_sample=False)}))
+        print(json.dumps({"lif_network": lif_bench(torch, capi, steps=args.lif_steps, cpu_sample=False)}))
         return
     if args.delivery:
         import torch

@@ -409,6 +409,9 @@ pvgpu_status launch(const PreGeom &g, int epl, dim3 grid, cudaStream_t s, const 
    return PVGPU_OK;
 }
 
+// post columns one presynaptic patch covers (the patch is counted in post neurons)
+int post_patch_cols(const pvgpu_conn_desc *conn) { return conn->nxp; }
+
 }  // namespace
 
 extern "C" pvgpu_status pvgpu_deliver_pre(const pvgpu_conn_desc *conn, const pvgpu_entry *entries,
@@ -438,6 +441,13 @@ extern "C" pvgpu_status pvgpu_deliver_pre(const pvgpu_conn_desc *conn, const pvg
    g.dtf = conn->dt_factor;
    g.FT = g.nfp < kMaxElemsPerRow ? g.nfp : kMaxElemsPerRow;
    g.TX = kMaxElemsPerRow / g.FT;
+   // Every entry is broadcast to the whole warp and tested against each of its tile elements,
+   // but covers only nxp post columns: a tile about twice the patch width keeps most of that
+   // work useful (the per-element summation order does not depend on the tile).
+   {
+      const int want = 2 * post_patch_cols(conn) > 8 ? 2 * post_patch_cols(conn) : 8;
+      if (g.TX > want) g.TX = want;
+   }
    if (g.TX > post.nx) g.TX = post.nx;
    int elems = g.TX * g.FT;
    int epl = (elems + 31) / 32;
