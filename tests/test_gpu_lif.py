@@ -151,3 +151,89 @@ def test_spiking_network_steps(cuda, oracle, method, mode):
                 np.testing.assert_allclose(got[k], st[k], rtol=1e-5, atol=1e-5)
             st = {k: (v.copy() if k == "rnd" else got[k].copy()) for k, v in st.items()}
     assert total_spikes > 0
+
+
+def gauss_w(nfpre, p, nfpost, sigma, peak):
+    r = np.arange(p) - (p - 1) / 2.0
+    g = np.exp(-(r[:, None] ** 2 + r[None, :] ** 2) / (2 * sigma ** 2))
+    return np.ascontiguousarray(np.broadcast_to(peak * g[None, :, :, None], (nfpre, p, p, nfpost))).astype(np.float32)
+
+
+@pytest.mark.parametrize("method, mode", [("b", "reference"), ("a", "fast")])
+def test_exc_inh_network_spike_counts(cuda, oracle, method, mode):
+    """The spiking configuration at reduced size (2 images, input 48x48, exc 48x48x8, inh 24x24x4,
+    40 steps): input -> exc (11x11 Gaussian, EXC), exc -> inh (stride 2, 3x3, EXC), inh -> exc (8x8
+    Gaussian, INH), arma or Heun.  Spike counts per neuron against the oracle composed the same way:
+    identical for Heun with reference-order delivery; for arma with FAST delivery the total within
+    1 % and at least 99 % of neurons with identical counts."""
+    torch = cuda
+    from openpv_gb300 import capi
+    nb, n, ne, ni, steps = 2, 48, 8, 4, 40
+    inp, exc, inh = capi.Loc.make(nb, n, n, 1, 5), capi.Loc.make(nb, n, n, ne, 2), capi.Loc.make(nb, n // 2, n // 2, ni, 2)
+    exc_r, inh_r = capi.Loc.make(nb, n, n, ne, 0), capi.Loc.make(nb, n // 2, n // 2, ni, 0)
+    conns = [(capi.conn_desc(inp, exc_r, 11, 11), gauss_w(1, 11, ne, 3.0, 0.5)),
+             (capi.conn_desc(exc, inh_r, 3, 3), np.full((ne * 4, 3, 3, ni), 0.05, np.float32)),
+             (capi.conn_desc(inh, exc_r, 8, 8), gauss_w(ni, 8, ne, 2.0, 1.0))]
+    dmode = capi.DELIVER_REFERENCE_ORDER if mode == "reference" else capi.DELIVER_FAST
+    rng = np.random.default_rng(77)
+    rates = rng.uniform(5, 50, (nb, n, n, 1))
+    ne_res, ni_res = nb * n * n * ne, nb * (n // 2) ** 2 * ni
+    p_o, p_d = oracle.lif_params_array(), capi.LifParams.make()
+
+    def init(m, seed):
+        return {"rnd": oracle.taus_init(m, seed), "V": np.full(m, -70.0, np.float32), "Vth": np.full(m, -55.0, np.float32),
+                "GE": np.zeros(m, np.float32), "GI": np.zeros(m, np.float32), "GIB": np.zeros(m, np.float32)}
+
+    so_e, so_h = init(ne_res, 17), init(ni_res, 18)
+    sd_e, sd_h = to_dev(torch, so_e), to_dev(torch, so_h)
+    ao_e, ao_h = np.zeros(exc.ext_shape(), np.float32), np.zeros(inh.ext_shape(), np.float32)
+    ad_e, ad_h = T(torch, ao_e), T(torch, ao_h)
+    gd_e, gd_h = torch.zeros((3, ne_res), device="cuda"), torch.zeros((3, ni_res), device="cuda")
+    wd = [T(torch, w) for _, w in conns]
+    cnt_o_e, cnt_d_e = np.zeros(ne_res), np.zeros(ne_res)
+    cnt_o_h, cnt_d_h = np.zeros(ni_res), np.zeros(ni_res)
+
+    def sparse(torch_a, loc):
+        ent = torch.zeros((nb, loc.num_ext, 2), dtype=torch.int32, device="cuda")
+        num = torch.zeros(nb, dtype=torch.int64, device="cuda")
+        capi.compact_active(torch_a, nb, loc.num_ext, ent, num)
+        return ent, num
+
+    res = lambda a, h: a[:, h:a.shape[1] - h, h:a.shape[2] - h, :].reshape(-1)
+    for t in range(steps):
+        x = np.zeros(inp.ext_shape(), np.float32)
+        x[:, 5:5 + n, 5:5 + n, :] = (rng.random((nb, n, n, 1)) < rates * 1e-3).astype(np.float32)
+        # oracle
+        e0, c0 = oracle.compact(x.reshape(nb, -1))
+        eh, ch = oracle.compact(ao_h.reshape(nb, -1))
+        g0 = oracle.deliver_pre(OL(oracle, inp), OL(oracle, exc_r), 11, 11, conns[0][1], entries=e0, num_active=c0)
+        g1 = oracle.deliver_pre(OL(oracle, inh), OL(oracle, exc_r), 8, 8, conns[2][1], entries=eh, num_active=ch)
+        so_e, ao_e = oracle.lif_update(method, OL(oracle, exc), p_o, 1.0, so_e,
+                                       np.stack([g0.reshape(-1), g1.reshape(-1), 0 * g0.reshape(-1)]), ao_e)
+        ee, ce = oracle.compact(ao_e.reshape(nb, -1))
+        gi = oracle.deliver_pre(OL(oracle, exc), OL(oracle, inh_r), 3, 3, conns[1][1], entries=ee, num_active=ce).reshape(-1)
+        so_h, ao_h = oracle.lif_update(method, OL(oracle, inh), p_o, 1.0, so_h, np.stack([gi, 0 * gi, 0 * gi]), ao_h)
+        # device
+        gd_e.zero_()
+        gd_h.zero_()
+        ent, num = sparse(T(torch, x), inp)
+        capi.deliver_pre(conns[0][0], wd[0], gd_e[0], entries=ent, num_active=num, mode=dmode)
+        ent, num = sparse(ad_h, inh)
+        capi.deliver_pre(conns[2][0], wd[2], gd_e[1], entries=ent, num_active=num, mode=dmode)
+        capi.lif_update(exc, method, p_d, 1.0, sd_e["rnd"], sd_e["V"], sd_e["Vth"], sd_e["GE"], sd_e["GI"], sd_e["GIB"],
+                        gd_e, ad_e)
+        ent, num = sparse(ad_e, exc)
+        capi.deliver_pre(conns[1][0], wd[1], gd_h[0], entries=ent, num_active=num, mode=dmode)
+        capi.lif_update(inh, method, p_d, 1.0, sd_h["rnd"], sd_h["V"], sd_h["Vth"], sd_h["GE"], sd_h["GI"], sd_h["GIB"],
+                        gd_h, ad_h)
+        cnt_o_e += res(ao_e, 2)
+        cnt_o_h += res(ao_h, 2)
+        cnt_d_e += res(H(ad_e), 2)
+        cnt_d_h += res(H(ad_h), 2)
+    assert cnt_o_e.sum() > 0 and cnt_o_h.sum() > 0
+    if method == "b":
+        assert np.array_equal(cnt_d_e, cnt_o_e) and np.array_equal(cnt_d_h, cnt_o_h)
+    else:
+        for d, o in ((cnt_d_e, cnt_o_e), (cnt_d_h, cnt_o_h)):
+            assert abs(d.sum() - o.sum()) <= 0.01 * o.sum()
+            assert np.mean(d == o) >= 0.99
