@@ -500,6 +500,7 @@ def run_ours(args, rank, world, local_rank):
     # kernel shapes picked by the autotuner (timed with events on a few steps; outside the timed region)
     solver.autotune(x, trial_steps=4)
     tuned = solver.plan_info()
+    tuned["schedule"] = solver.schedule()
     for _ in range(args.warmup):
         solve(x)
     barrier()

@@ -440,12 +440,32 @@ pvgpu_status pvgpu_lca_solver_profile_end(pvgpu_lca_solver *s, double *reconMs, 
  * shape of the two BF16 kernels that fits in shared memory -- the post-delivery kernel's feature
  * tile (64/128/256/512) and its V / weight ring depths and A staging, the reconstruction
  * kernel's ring depth -- on trialSteps timesteps of x (BF16 and BF16x3 forms), keeps the fastest
- * of each, and remembers them for every solver of the same geometry created later in the
- * process.  Leaves V and A undefined: call pvgpu_lca_solver_reset before the next run. */
+ * of each, then replays graphs of max(trialSteps, 16) steps under each schedule (one chain or two
+ * half-batch chains, with and without programmatic edges: pvgpu_lca_solver_set_schedule) and keeps
+ * the fastest; remembers shapes and schedule for every solver of the same geometry created later
+ * in the process.  Leaves V and A undefined: call pvgpu_lca_solver_reset before the next run. */
 pvgpu_status pvgpu_lca_solver_autotune(pvgpu_lca_solver *s, const float *x, int trialSteps, void *stream);
 /* The shapes in use: out[0..4] = {feature tile, V ring slots, weight ring slots, A staged (0/1),
  * reconstruction ring stages} of the BF16 form, out[5..9] the same for BF16x3 steps. */
 pvgpu_status pvgpu_lca_solver_plan_info(const pvgpu_lca_solver *s, int *out);
+
+/* No counterpart in the reference.  How a BF16 run is laid out as a CUDA graph: chains = 1 runs
+ * the whole batch through kernel R and kernel P in turn; chains = 2 runs the two halves of the
+ * batch (images [0, n0) and [n0, nbatch), n0 = nbatch / 2 rounded up to even when that leaves
+ * images for the second half) as two independent chains on parallel graph branches, so that the
+ * kernels of one half run in the ramp and tail of the other's.  reconCtas / postCtas cap the
+ * persistent grids of kernel R (rounded down to clusters of two) and kernel P (0 = as many as
+ * fit).  programmatic = 1 launches each kernel of a chain early (programmatic stream
+ * serialisation) so that its set-up overlaps the kernel before it.  The images' results do not
+ * depend on the schedule.  Default {1, 0, 0, 1}; per-kernel profiling runs always use one chain. */
+typedef struct {
+   int chains;
+   int reconCtas;
+   int postCtas;
+   int programmatic;
+} pvgpu_lca_schedule;
+pvgpu_status pvgpu_lca_solver_set_schedule(pvgpu_lca_solver *s, const pvgpu_lca_schedule *sc);
+pvgpu_status pvgpu_lca_solver_get_schedule(const pvgpu_lca_solver *s, pvgpu_lca_schedule *sc);
 
 /* ---- diagnostics ----------------------------------------------------------------------------
  * No counterpart in the reference.  C[M][N] (FP32) = A[M][K] * B[N][K]^T with BF16 row-major

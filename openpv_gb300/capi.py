@@ -82,6 +82,10 @@ class LcaSolverDesc(C.Structure):
                 ("VWidth", C.c_float), ("tau", C.c_float), ("dt", C.c_float), ("selfInteract", C.c_int)]
 
 
+class LcaSchedule(C.Structure):
+    _fields_ = [("chains", C.c_int), ("reconCtas", C.c_int), ("postCtas", C.c_int), ("programmatic", C.c_int)]
+
+
 LCA_FP32 = 0
 LCA_BF16 = 1
 
@@ -132,6 +136,8 @@ def _declare(L):
         "pvgpu_lca_solver_profile_end": (i, [vp, C.POINTER(d), C.POINTER(d), C.POINTER(i)]),
         "pvgpu_lca_solver_autotune": (i, [vp, vp, i, vp]),
         "pvgpu_lca_solver_plan_info": (i, [vp, C.POINTER(i)]),
+        "pvgpu_lca_solver_set_schedule": (i, [vp, C.POINTER(LcaSchedule)]),
+        "pvgpu_lca_solver_get_schedule": (i, [vp, C.POINTER(LcaSchedule)]),
         "pvgpu_deliver_ident": (i, [lp, lp, vp, vp, vp, vp, vp]),
         "pvgpu_momentum_lca_update": (i, [lp, i, f, vp, f, vp, vp, vp, vp, vp]),
         "pvgpu_ista_update": (i, [lp, f, vp, f, vp, vp, vp, vp]),
@@ -395,6 +401,18 @@ class LcaSolver:
         check(lib().pvgpu_lca_solver_plan_info(self.h, out), "lca_solver_plan_info")
         keys = ("feature_tile", "v_slots", "w_slots", "a_staged", "recon_stages")
         return {form: dict(zip(keys, out[5 * i:5 * i + 5])) for i, form in enumerate(("bf16", "bf16x3"))}
+
+    def set_schedule(self, chains=1, recon_ctas=0, post_ctas=0, programmatic=True):
+        """Graph layout of BF16 runs: one chain over the batch or two half-batch chains on
+        parallel branches; caps on the persistent grids; early launch within a chain."""
+        sc = LcaSchedule(chains, recon_ctas, post_ctas, int(programmatic))
+        check(lib().pvgpu_lca_solver_set_schedule(self.h, C.byref(sc)), "lca_solver_set_schedule")
+
+    def schedule(self):
+        sc = LcaSchedule()
+        check(lib().pvgpu_lca_solver_get_schedule(self.h, C.byref(sc)), "lca_solver_get_schedule")
+        return {"chains": sc.chains, "recon_ctas": sc.reconCtas, "post_ctas": sc.postCtas,
+                "programmatic": bool(sc.programmatic)}
 
     def profile_begin(self, max_steps):
         check(lib().pvgpu_lca_solver_profile_begin(self.h, max_steps), "lca_solver_profile_begin")

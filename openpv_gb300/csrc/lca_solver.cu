@@ -898,6 +898,15 @@ pvgpu_status lca_fp32_step(int S, int P, int C, const LcaGeom &g, const float *x
                            float *partials, float *V, float *A32, cudaStream_t s, cudaEvent_t mid);
 }
 
+// Images [img0, img0 + g.nb) of the batch as a batch of their own: the geometry and the tensor
+// maps of the activity rows they own (every other per-image array is addressed from a base
+// pointer, shifted by img0 images at launch).
+struct LcaHalf {
+   LcaGeom g;
+   int img0;
+   CUtensorMap tmA, tmAlo, tmAst;
+};
+
 struct pvgpu_lca_solver {
    pvgpu_lca_solver_desc d;
    LcaGeom g;
@@ -923,6 +932,13 @@ struct pvgpu_lca_solver {
    cudaGraphExec_t graph = nullptr;
    const float *graphX = nullptr;
    int graphSteps = -1, graphX3 = -1;
+   // the graph's schedule: one chain of kernels over the batch, or two independent chains over
+   // the two halves captured as parallel graph branches (one half's kernels fill the ramp and
+   // tail of the other's); caps on the persistent grids; programmatic edges within a chain
+   pvgpu_lca_schedule sched = {1, 0, 0, 1};
+   LcaHalf half[2];
+   cudaStream_t capStream2 = nullptr;
+   cudaEvent_t forkEv = nullptr, joinEv = nullptr;
 };
 
 namespace {
@@ -974,6 +990,7 @@ PostPlan post_plan_for(const LcaGeom &g, int S, int P, int C, bool x3, int numSm
 }
 
 constexpr uint32_t kSmemBudget = 227u * 1024u - 512u;  // dynamic shared memory; static shares the budget
+constexpr uint32_t kSmemHalfSm = 116u * 1024u;         // more than half of an SM's 228 KB
 
 // ring shapes, best first: V tiles first (they come from HBM), then weight tiles (from L2); A
 // staged for TMA stores where it fits with at least two V slots (not in BF16x3 steps, which
@@ -1028,6 +1045,63 @@ ReconPlan make_recon_plan(const LcaGeom &g, int S, int P, int C, bool x3, int ma
    return rp;
 }
 
+// The launch arguments of one timestep over a batch view (the whole batch or one half).
+struct StepArgs {
+   LcaGeom g;
+   ReconPlan rp;
+   PostPlan pl;
+   const CUtensorMap *tmA, *tmAlo, *tmAst, *tmWtH, *tmWtloH, *tmW, *tmWlo;
+   const float *x;
+   float *rpad, *V;
+   bf16 *A, *Alo;
+   int *err;
+};
+
+// Kernel R's and kernel P's persistent grids for nb images under the schedule's caps.
+void size_grids(const pvgpu_lca_solver *s, int nb, bool x3, ReconPlan &rp, PostPlan &pl) {
+   int pairs = std::min(s->maxPairs[x3 ? 1 : 0], (nb + 1) / 2);
+   if (s->sched.reconCtas >= 2) pairs = std::min(pairs, s->sched.reconCtas / 2);
+   rp.G = 2 * std::max(pairs, 1);
+   const int nTiles = nb * s->g.MB * (s->g.F / pl.FT);
+   int ctas = g_num_sms;
+   if (s->sched.postCtas > 0) ctas = std::min(ctas, s->sched.postCtas);
+   pl.G = std::min(ctas, nTiles);
+}
+
+// view = -1: the whole batch; 0 / 1: that half.
+StepArgs step_args(const pvgpu_lca_solver *s, int view, const float *x, bool x3) {
+   StepArgs a;
+   const LcaHalf *h = view >= 0 ? &s->half[view] : nullptr;
+   a.g = h ? h->g : s->g;
+   a.rp = x3 ? s->rplanX3 : s->rplan;
+   a.pl = x3 ? s->planX3 : s->plan;
+   size_grids(s, a.g.nb, x3, a.rp, a.pl);
+   if (h) {
+      // The two chains' kernels never share an SM: with two CTAs on one SM, a kernel R CTA
+      // (which takes all 512 TMEM columns) could block in its allocation behind a CTA of the
+      // other chain that in turn waits, through its own chain, on that kernel R's pair.  More
+      // than half of the SM's shared memory per CTA rules the pairing out.
+      a.rp.total = std::max(a.rp.total, kSmemHalfSm);
+      a.pl.total = std::max(a.pl.total, kSmemHalfSm);
+   }
+   const size_t i0 = h ? (size_t)h->img0 : 0;
+   const size_t state = (size_t)s->g.Npos * s->g.F;
+   a.tmA = h ? &h->tmA : &s->tmA;
+   a.tmAlo = h ? &h->tmAlo : &s->tmAlo;
+   a.tmAst = h ? &h->tmAst : &s->tmAst;
+   a.tmWtH = &s->tmWtH;
+   a.tmWtloH = &s->tmWtloH;
+   a.tmW = &s->tmW;
+   a.tmWlo = &s->tmWlo;
+   a.x = x + i0 * (size_t)s->g.inNx * s->g.inNy * s->C;
+   a.rpad = s->rpad + i0 * (size_t)a.rp.rowsPad * a.rp.RP;
+   a.V = s->V + i0 * state;
+   a.A = s->A + i0 * state;
+   a.Alo = s->Alo + i0 * state;
+   a.err = s->err;
+   return a;
+}
+
 template <int S, int P, int C>
 struct Launcher {
    // shared-memory limits of both kernels (once, at create: not inside a stream capture)
@@ -1042,31 +1116,30 @@ struct Launcher {
       }
       return PVGPU_OK;
    }
-   // One LCA timestep: kernel R then kernel P, each launched with programmatic stream
-   // serialisation, so that its set-up overlaps the tail of the kernel before it.
+   // One LCA timestep of a batch view: kernel R then kernel P, each launched with programmatic
+   // stream serialisation (unless the schedule turns it off), so that its set-up overlaps the
+   // tail of the kernel before it.
    template <bool X3>
-   static pvgpu_status step(pvgpu_lca_solver *s, const float *x, cudaStream_t st, cudaEvent_t mid) {
+   static pvgpu_status step(const StepArgs &a, cudaStream_t st, cudaEvent_t mid, bool programmatic) {
       cudaLaunchAttribute attr[1];
       attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
       attr[0].val.programmaticStreamSerializationAllowed = 1;
-      const ReconPlan &rp = X3 ? s->rplanX3 : s->rplan;
       cudaLaunchConfig_t cr = {};
-      cr.gridDim = dim3(rp.G);
+      cr.gridDim = dim3(a.rp.G);
       cr.blockDim = dim3(320);
-      cr.dynamicSmemBytes = rp.total;
+      cr.dynamicSmemBytes = a.rp.total;
       cr.stream = st;
       cr.attrs = attr;
-      cr.numAttrs = mid ? 0 : 1;  // per-kernel timing keeps the kernels apart
-      cudaError_t e = cudaLaunchKernelEx(&cr, recon_tc_kernel<S, P, C, X3>, s->tmA, s->tmAlo, s->tmWtH, s->tmWtloH,
-                                         s->g, rp, x, s->rpad, s->err);
+      cr.numAttrs = (mid || !programmatic) ? 0 : 1;  // per-kernel timing keeps the kernels apart
+      cudaError_t e = cudaLaunchKernelEx(&cr, recon_tc_kernel<S, P, C, X3>, *a.tmA, *a.tmAlo, *a.tmWtH, *a.tmWtloH,
+                                         a.g, a.rp, a.x, a.rpad, a.err);
       if (e != cudaSuccess) return pvgpu::record_cuda_error(e, "lca recon");
       if (mid) cudaEventRecord(mid, st);
-      const PostPlan &pl = X3 ? s->planX3 : s->plan;
       cudaLaunchConfig_t cp = cr;
-      cp.gridDim = dim3(pl.G);
-      cp.dynamicSmemBytes = pl.total;
-      e = cudaLaunchKernelEx(&cp, post_tc_kernel<S, P, C, X3>, s->tmW, s->tmWlo, s->tmAst, s->g, pl,
-                             (const float *)s->rpad, s->V, s->A, s->Alo, s->err);
+      cp.gridDim = dim3(a.pl.G);
+      cp.dynamicSmemBytes = a.pl.total;
+      e = cudaLaunchKernelEx(&cp, post_tc_kernel<S, P, C, X3>, *a.tmW, *a.tmWlo, *a.tmAst, a.g, a.pl,
+                             (const float *)a.rpad, a.V, a.A, a.Alo, a.err);
       if (e != cudaSuccess) return pvgpu::record_cuda_error(e, "lca post");
       return PVGPU_OK;
    }
@@ -1093,8 +1166,8 @@ struct Launcher {
       const uint32_t pt = x3 ? s->planX3.total : s->plan.total;
       return (x3 ? s->rplanX3.total : s->rplan.total) <= kSmemBudget && pt && pt <= kSmemBudget;
    }
-   static pvgpu_status run_step(pvgpu_lca_solver *s, const float *x, bool x3, cudaStream_t st, cudaEvent_t mid) {
-      return x3 ? step<true>(s, x, st, mid) : step<false>(s, x, st, mid);
+   static pvgpu_status run_step(const StepArgs &a, bool x3, cudaStream_t st, cudaEvent_t mid, bool programmatic) {
+      return x3 ? step<true>(a, st, mid, programmatic) : step<false>(a, st, mid, programmatic);
    }
 };
 
@@ -1110,6 +1183,9 @@ void free_solver(pvgpu_lca_solver *s) {
    for (cudaEvent_t e : s->ev) cudaEventDestroy(e);
    if (s->graph) cudaGraphExecDestroy(s->graph);
    if (s->capStream) cudaStreamDestroy(s->capStream);
+   if (s->capStream2) cudaStreamDestroy(s->capStream2);
+   if (s->forkEv) cudaEventDestroy(s->forkEv);
+   if (s->joinEv) cudaEventDestroy(s->joinEv);
    void *ptrs[] = {s->V, s->partials, s->rpad, s->A32, s->W32, s->Wt32, s->A, s->Alo, s->W, s->Wlo, s->Wt, s->Wtlo, s->err};
    for (void *p : ptrs)
       if (p) cudaFree(p);
@@ -1123,6 +1199,7 @@ void free_solver(pvgpu_lca_solver *s) {
 struct TunedShapes {
    int post[2][4];
    int recon[2];
+   pvgpu_lca_schedule sched;
 };
 
 std::mutex g_tune_mu;
@@ -1141,6 +1218,7 @@ void set_shapes(pvgpu_lca_solver *s, const TunedShapes &t) {
       ReconPlan rp = recon_plan_for(s->g, s->S, s->P, s->C, x3 != 0, s->maxPairs[x3], t.recon[x3]);
       if (rp.total <= kSmemBudget) (x3 ? s->rplanX3 : s->rplan) = rp;
    }
+   if (t.sched.chains == 1 || (s->g.nb >= 2 && s->capStream2)) s->sched = t.sched;
    if (s->graph) cudaGraphExecDestroy(s->graph);
    s->graph = nullptr;
 }
@@ -1217,22 +1295,39 @@ extern "C" pvgpu_status pvgpu_lca_solver_create(const pvgpu_lca_solver_desc *d, 
       return PVGPU_ERR_OOM;
    }
    cudaMemset(s->err, 0, sizeof(int));
-   const uint64_t rowsA = (uint64_t)g.nb * Npos;
-   ok = pvgpu::make_tmap_bf16_sw128(&s->tmA, s->A, rowsA, g.F, g.F, 128) &&
-        pvgpu::make_tmap_bf16_sw128(&s->tmAlo, s->Alo, rowsA, g.F, g.F, 128) &&
+   // the activity maps of images [i0, i0 + n): A and its low half as 128-row MMA tiles, and A as
+   // one epilogue warp's 32 x 32 part (64-byte swizzle) for the staged stores
+   auto activity_maps = [&](int i0, int n, CUtensorMap *tA, CUtensorMap *tAlo, CUtensorMap *tAst) {
+      const uint64_t rows = (uint64_t)n * Npos;
+      bf16 *a = s->A + (size_t)i0 * Npos * g.F, *alo = s->Alo + (size_t)i0 * Npos * g.F;
+      if (!pvgpu::make_tmap_bf16_sw128(tA, a, rows, g.F, g.F, 128) ||
+          !pvgpu::make_tmap_bf16_sw128(tAlo, alo, rows, g.F, g.F, 128))
+         return false;
+      pvgpu::EncodeTiledFn enc = pvgpu::encode_tiled_fn();
+      cuuint64_t dims[2] = {(cuuint64_t)g.F, rows};
+      cuuint64_t strides[1] = {(cuuint64_t)g.F * 2};
+      cuuint32_t box[2] = {32, 32};
+      cuuint32_t estr[2] = {1, 1};
+      return enc && enc(tAst, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, a, dims, strides, box, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+   };
+   ok = activity_maps(0, g.nb, &s->tmA, &s->tmAlo, &s->tmAst) &&
         pvgpu::make_tmap_bf16_sw128(&s->tmWtH, s->Wt, KP, g.F, g.F, KP / 2) &&
         pvgpu::make_tmap_bf16_sw128(&s->tmWtloH, s->Wtlo, KP, g.F, g.F, KP / 2) &&
         pvgpu::make_tmap_bf16_sw128(&s->tmW, s->W, g.F, KP, KP, g.NT) &&
         pvgpu::make_tmap_bf16_sw128(&s->tmWlo, s->Wlo, g.F, KP, KP, g.NT);
-   if (ok) {  // A: BF16 [rows][F], one epilogue warp's 32 x 32 part, 64-byte swizzle
-      pvgpu::EncodeTiledFn enc = pvgpu::encode_tiled_fn();
-      cuuint64_t dims[2] = {(cuuint64_t)g.F, rowsA};
-      cuuint64_t strides[1] = {(cuuint64_t)g.F * 2};
-      cuuint32_t box[2] = {32, 32};
-      cuuint32_t estr[2] = {1, 1};
-      ok = enc && enc(&s->tmAst, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, s->A, dims, strides, box, estr,
-                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+   if (ok && g.nb >= 2) {
+      // the two halves: an even first half where that leaves images for the second
+      int n0 = (g.nb / 2 + 1) & ~1;
+      if (n0 >= g.nb) n0 = g.nb / 2;
+      for (int c = 0; c < 2 && ok; c++) {
+         LcaHalf &h = s->half[c];
+         h.g = g;
+         h.img0 = c ? n0 : 0;
+         h.g.nb = c ? g.nb - n0 : n0;
+         ok = activity_maps(h.img0, h.g.nb, &h.tmA, &h.tmAlo, &h.tmAst);
+      }
    }
    if (!ok) {
       free_solver(s);
@@ -1261,7 +1356,6 @@ extern "C" pvgpu_status pvgpu_lca_solver_create(const pvgpu_lca_solver_desc *d, 
       }
       return PVGPU_OK;
    });
-   apply_tuned(s);  // shapes an earlier autotune picked for this geometry, if any
    bool fits = true;
    dispatch(S, P, C, [&](auto L) {
       fits = L.fits(s, false);
@@ -1276,6 +1370,14 @@ extern "C" pvgpu_status pvgpu_lca_solver_create(const pvgpu_lca_solver_desc *d, 
       cudaGetLastError();
       s->capStream = nullptr;  // runs then launch kernel by kernel
    }
+   if (s->capStream && (cudaStreamCreateWithFlags(&s->capStream2, cudaStreamNonBlocking) != cudaSuccess ||
+                        cudaEventCreateWithFlags(&s->forkEv, cudaEventDisableTiming) != cudaSuccess ||
+                        cudaEventCreateWithFlags(&s->joinEv, cudaEventDisableTiming) != cudaSuccess)) {
+      cudaGetLastError();  // one chain only
+      if (s->capStream2) cudaStreamDestroy(s->capStream2);
+      s->capStream2 = nullptr;
+   }
+   apply_tuned(s);  // shapes (only ones that fit) and schedule an earlier autotune picked, if any
    if (ra != PVGPU_OK) {
       free_solver(s);
       return ra;
@@ -1355,9 +1457,23 @@ extern "C" pvgpu_status pvgpu_lca_solver_run(pvgpu_lca_solver *s, const float *x
          s->graph = nullptr;
          PVGPU_CUDA(cudaStreamBeginCapture(s->capStream, cudaStreamCaptureModeThreadLocal), "lca graph capture");
          pvgpu_status r = PVGPU_OK;
+         const bool two = s->sched.chains == 2;
+         if (two) {  // the second half's chain on a branch of its own, joined at the end
+            cudaEventRecord(s->forkEv, s->capStream);
+            cudaStreamWaitEvent(s->capStream2, s->forkEv, 0);
+         }
          for (int t = 0; t < numSteps && r == PVGPU_OK; t++) {
             const bool x3 = t >= numSteps - numX3Steps;
-            r = dispatch(s->S, s->P, s->C, [&](auto L) { return L.run_step(s, x, x3, s->capStream, nullptr); });
+            for (int c = 0; c < (two ? 2 : 1) && r == PVGPU_OK; c++) {
+               const StepArgs a = step_args(s, two ? c : -1, x, x3);
+               r = dispatch(s->S, s->P, s->C, [&](auto L) {
+                  return L.run_step(a, x3, c ? s->capStream2 : s->capStream, nullptr, s->sched.programmatic != 0);
+               });
+            }
+         }
+         if (two) {
+            cudaEventRecord(s->joinEv, s->capStream2);
+            cudaStreamWaitEvent(s->capStream, s->joinEv, 0);
          }
          cudaGraph_t g = nullptr;
          cudaError_t ee = cudaStreamEndCapture(s->capStream, &g);
@@ -1385,8 +1501,9 @@ extern "C" pvgpu_status pvgpu_lca_solver_run(pvgpu_lca_solver *s, const float *x
       const bool x3 = t >= numSteps - numX3Steps;
       const bool rec = s->profiling && s->evNext + 3 <= s->ev.size();
       if (rec) cudaEventRecord(s->ev[s->evNext], st);
+      const StepArgs a = step_args(s, -1, x, x3);
       pvgpu_status r = dispatch(s->S, s->P, s->C, [&](auto L) {
-         return L.run_step(s, x, x3, st, rec ? s->ev[s->evNext + 1] : nullptr);
+         return L.run_step(a, x3, st, rec ? s->ev[s->evNext + 1] : nullptr, s->sched.programmatic != 0);
       });
       if (r != PVGPU_OK) return r;
       if (rec) {
@@ -1522,7 +1639,44 @@ extern "C" pvgpu_status pvgpu_lca_solver_autotune(pvgpu_lca_solver *s, const flo
          }
       }
    }
+   best.sched = s->sched;
    set_shapes(s, best);
+   // the graph schedule: each candidate replayed as a graph of max(trialSteps, 16) BF16 steps,
+   // best of two replays
+   {
+      const int n = std::max(trialSteps, 16);
+      const pvgpu_lca_schedule cands[4] = {{1, 0, 0, 1}, {1, 0, 0, 0}, {2, 0, 0, 1}, {2, 0, 0, 0}};
+      cudaStream_t st = pvgpu::as_stream(stream);
+      cudaEvent_t e0 = nullptr, e1 = nullptr;
+      if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+         if (e0) cudaEventDestroy(e0);
+         return pvgpu::record_cuda_error(cudaGetLastError(), "lca autotune events");
+      }
+      double bestMs = 1e30;
+      pvgpu_status st2 = PVGPU_OK;
+      for (const pvgpu_lca_schedule &c : cands) {
+         if (pvgpu_lca_solver_set_schedule(s, &c) != PVGPU_OK) continue;  // no second half
+         st2 = pvgpu_lca_solver_run(s, x, n, 0, PVGPU_LCA_BF16, stream);  // captures the graph
+         for (int rep = 0; rep < 2 && st2 == PVGPU_OK; rep++) {
+            cudaEventRecord(e0, st);
+            st2 = pvgpu_lca_solver_run(s, x, n, 0, PVGPU_LCA_BF16, stream);
+            cudaEventRecord(e1, st);
+            float ms = 0.0f;
+            if (st2 == PVGPU_OK && cudaEventSynchronize(e1) == cudaSuccess &&
+                cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess && ms < bestMs) {
+               bestMs = ms;
+               best.sched = c;
+            }
+         }
+         if (st2 != PVGPU_OK) break;
+      }
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      s->sched = best.sched;
+      if (s->graph) cudaGraphExecDestroy(s->graph);
+      s->graph = nullptr;
+      if (st2 != PVGPU_OK) return st2;
+   }
    std::lock_guard<std::mutex> lk(g_tune_mu);
    g_tuned[tune_key(s)] = best;
    return PVGPU_OK;
@@ -1540,6 +1694,23 @@ extern "C" pvgpu_status pvgpu_lca_solver_plan_info(const pvgpu_lca_solver *s, in
       o[3] = pl.stageA;
       o[4] = rp.nStage;
    }
+   return PVGPU_OK;
+}
+
+extern "C" pvgpu_status pvgpu_lca_solver_set_schedule(pvgpu_lca_solver *s, const pvgpu_lca_schedule *sc) {
+   if (!s || !sc || (sc->chains != 1 && sc->chains != 2) || sc->reconCtas < 0 || sc->postCtas < 0 ||
+       (sc->programmatic != 0 && sc->programmatic != 1))
+      return PVGPU_ERR_BAD_ARG;
+   if (sc->chains == 2 && (s->g.nb < 2 || !s->capStream2)) return PVGPU_ERR_UNSUPPORTED_SHAPE;
+   s->sched = *sc;
+   if (s->graph) cudaGraphExecDestroy(s->graph);
+   s->graph = nullptr;
+   return PVGPU_OK;
+}
+
+extern "C" pvgpu_status pvgpu_lca_solver_get_schedule(const pvgpu_lca_solver *s, pvgpu_lca_schedule *sc) {
+   if (!s || !sc) return PVGPU_ERR_BAD_ARG;
+   *sc = s->sched;
    return PVGPU_OK;
 }
 

@@ -197,8 +197,10 @@ def test_lca_autotune_picks_valid_shapes_and_keeps_parity(torch, oracle):
         assert q["feature_tile"] in (64, 128) and v1s[2] % q["feature_tile"] == 0, info
         assert 1 <= q["v_slots"] <= 3 and 1 <= q["w_slots"] <= 2 and 2 <= q["recon_stages"] <= 4, info
     assert info["bf16x3"]["a_staged"] == 0
+    sched = s.schedule()
+    assert sched["chains"] in (1, 2) and sched["recon_ctas"] == 0 and sched["post_ctas"] == 0, sched
     s2 = capi.LcaSolver(nb, ins, v1s, nxp, vth)
-    assert s2.plan_info() == info
+    assert s2.plan_info() == info and s2.schedule() == sched
     e = torch.zeros(nb, dtype=torch.float64, device="cuda")
     for x3 in (0, 5):
         s.reset()
@@ -208,3 +210,43 @@ def test_lca_autotune_picks_valid_shapes_and_keeps_parity(torch, oracle):
         assert s.error_flag() == 0
         rel = np.abs(e.cpu().numpy() - e64[-1]) / np.abs(e64[-1])
         assert rel.max() < 1e-3, (x3, rel, info)
+
+
+@pytest.mark.parametrize("nb", [3, 6])
+def test_lca_bf16_schedules_leave_identical_state(torch, oracle, nb):
+    """The graph's schedule -- one chain or two half-batch chains on parallel branches (halves of
+    4 + 2 and 2 + 1 images, the odd half with an empty slot in kernel R's image pairs), capped
+    persistent grids, with and without programmatic edges -- moves work between CTAs and SMs
+    only: the state is bit-identical to the kernel-by-kernel run, BF16x3 steps included."""
+    from openpv_gb300 import capi
+    _, ins, v1s, nxp, vth, steps, w, _, _ = setup(oracle, "colour")
+    x = one_over_f(np.random.default_rng(11), nb, *ins)
+    wd = torch.from_numpy(w).cuda()
+    xd = torch.from_numpy(x).cuda()
+    s = capi.LcaSolver(nb, ins, v1s, nxp, vth)
+    s.set_weights(wd)
+    assert s.schedule() == {"chains": 1, "recon_ctas": 0, "post_ctas": 0, "programmatic": True}
+
+    def state(direct):
+        s.reset()
+        if direct:
+            s.profile_begin(steps)
+        s.run(xd, steps, x3_steps=4, precision=capi.LCA_BF16)
+        if direct:
+            s.profile_end()
+        v = torch.zeros((nb,) + v1s, device="cuda")
+        s.state(v)
+        torch.cuda.synchronize()
+        assert s.error_flag() == 0
+        return v.cpu().numpy().view(np.uint32)
+
+    ref = state(direct=True)
+    for sc in ((2, 0, 0, True), (2, 0, 0, False), (2, 2, 5, True), (1, 2, 3, False), (2, 4, 16, True)):
+        s.set_schedule(*sc)
+        assert s.schedule()["chains"] == sc[0]
+        assert np.array_equal(state(direct=False), ref), sc
+    with pytest.raises(capi.PvgpuError):
+        s.set_schedule(chains=3)
+    one = capi.LcaSolver(1, ins, v1s, nxp, vth)
+    with pytest.raises(capi.PvgpuError):
+        one.set_schedule(chains=2)  # one image has no second half
