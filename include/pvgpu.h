@@ -474,6 +474,10 @@ pvgpu_status pvgpu_lca_solver_get_schedule(const pvgpu_lca_solver *s, pvgpu_lca_
  * 16 <= N <= 256 with N % 16 == 0, K % 64 == 0; A, B 16-byte aligned.  *errFlag (device int)
  * is set to 1 if a bounded device wait gave up. */
 pvgpu_status pvgpu_tc_gemm_bf16(const void *A, const void *B, float *C, int M, int N, int K, int *errFlag, void *stream);
+/* The same with B given as [K][N] (N contiguous, N % 64 == 0), read by the MMA as an MN-major
+ * operand: C = A * B. */
+pvgpu_status pvgpu_tc_gemm_bf16_kn(const void *A, const void *B, float *C, int M, int N, int K, int *errFlag,
+                                   void *stream);
 
 #ifdef __cplusplus
 }

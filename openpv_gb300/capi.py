@@ -124,6 +124,7 @@ def _declare(L):
         "pvgpu_cost_sum": (i, [lp, vp, i, d, d, vp, vp]),
         "pvgpu_hebbian_dw": (i, [cp, f, vp, vp, vp, vp]),
         "pvgpu_tc_gemm_bf16": (i, [vp, vp, vp, i, i, i, vp, vp]),
+        "pvgpu_tc_gemm_bf16_kn": (i, [vp, vp, vp, i, i, i, vp, vp]),
         "pvgpu_lca_solver_create": (i, [C.POINTER(LcaSolverDesc), C.POINTER(vp)]),
         "pvgpu_lca_solver_destroy": (i, [vp]),
         "pvgpu_lca_solver_set_weights": (i, [vp, vp, vp]),
@@ -340,6 +341,12 @@ def hebbian_dw(conn, dw_max, pre_ext, post_ext, dw, stream=None):
 
 def tc_gemm_bf16(A, B, C, M, N, K, err, stream=None):
     check(lib().pvgpu_tc_gemm_bf16(_ptr(A), _ptr(B), _ptr(C), M, N, K, _ptr(err), _stream(stream)), "tc_gemm_bf16")
+
+
+def tc_gemm_bf16_kn(A, B, C, M, N, K, err, stream=None):
+    """C = A @ B with B [K][N] read as the MN-major tcgen05 operand."""
+    check(lib().pvgpu_tc_gemm_bf16_kn(_ptr(A), _ptr(B), _ptr(C), M, N, K, _ptr(err), _stream(stream)),
+          "tc_gemm_bf16_kn")
 
 
 ENTRY_DTYPE = np.dtype([("index", np.uint32), ("value", np.float32)])

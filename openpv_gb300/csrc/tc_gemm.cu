@@ -1,8 +1,9 @@
-// tc_gemm.cu -- diagnostic: C[M][N] = A[M][K] * B[N][K]^T with BF16 operands and FP32
-// accumulation on the 5th-generation tensor cores (TMA -> SW128 shared tiles ->
-// tcgen05.mma -> TMEM -> tcgen05.ld).  It exercises the exact descriptor, pipeline and
-// TMEM conventions the fused LCA kernels use, on a plain GEMM that a test compares with
-// a host reference.  One CTA per 128-row tile, all N (<= 256) columns; 2-stage TMA ring.
+// tc_gemm.cu -- diagnostic: C[M][N] = A[M][K] * B[N][K]^T (B K-major) or A[M][K] * B[K][N]
+// (B MN-major) with BF16 operands and FP32 accumulation on the 5th-generation tensor cores
+// (TMA -> SW128 shared tiles -> tcgen05.mma -> TMEM -> tcgen05.ld).  It exercises the exact
+// descriptor, pipeline and TMEM conventions the fused LCA kernels use, on a plain GEMM that a
+// test compares with a host reference.  One CTA per 128-row tile, all N (<= 256) columns;
+// 2-stage TMA ring.
 #include "pvgpu_internal.cuh"
 #include "tc_ptx.cuh"
 #include "tmap.cuh"
@@ -13,6 +14,9 @@ using namespace pvgpu::tc;
 
 constexpr int kBM = 128, kBK = 64;
 
+// BMN: B is [K][N] in global memory; each 64-deep K chunk lands as N / 64 tiles of 64 K rows x
+// 128 B, 8 KB apart -- the layout of a K-major weight tile read as the MN-major operand.
+template <bool BMN>
 __global__ void __launch_bounds__(128) tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA,
                                                       const __grid_constant__ CUtensorMap tmB, float *__restrict__ C,
                                                       int M, int N, int K, int *__restrict__ err) {
@@ -47,12 +51,19 @@ __global__ void __launch_bounds__(128) tc_gemm_kernel(const __grid_constant__ CU
 
    const int nk = K / kBK;
    if (threadIdx.x == 0) {
-      const uint32_t idesc = idesc_bf16(kBM, N);
+      const uint32_t idesc = BMN ? idesc_bf16_bmn(kBM, N) : idesc_bf16(kBM, N);
       int issued = 0, consumed = 0;  // TMA stage loads issued / waited for
+      auto load_b = [&](int s, int kc) {
+         if (BMN) {
+            for (int j = 0; j < N / 64; j++) tma_load_2d(sB[s] + j * 8192, &tmB, &full[s], j * 64, kc * kBK);
+         } else {
+            tma_load_2d(sB[s], &tmB, &full[s], kc * kBK, 0);
+         }
+      };
       for (int kc = 0; kc < nk && kc < 2; kc++, issued++) {
          mbar_arrive_expect_tx(&full[kc], bytesA + bytesB);
          tma_load_2d(sA[kc], &tmA, &full[kc], kc * kBK, m0);
-         tma_load_2d(sB[kc], &tmB, &full[kc], kc * kBK, 0);
+         load_b(kc, kc);
       }
       bool ok = true;
       for (int kc = 0; kc < nk && ok; kc++) {
@@ -64,13 +75,14 @@ __global__ void __launch_bounds__(128) tc_gemm_kernel(const __grid_constant__ CU
          const uint32_t a0 = smem_u32(sA[s]), b0 = smem_u32(sB[s]);
 #pragma unroll
          for (int k = 0; k < kBK / 16; k++)
-            mma_bf16(tmem, sdesc_sw128(a0 + k * 32), sdesc_sw128(b0 + k * 32), idesc, (kc | k) != 0);
+            mma_bf16(tmem, sdesc_sw128(a0 + k * 32), BMN ? sdesc_sw128_mn(b0 + k * 2048, 8192) : sdesc_sw128(b0 + k * 32),
+                     idesc, (kc | k) != 0);
          mma_commit(&empty[s]);
          if (kc + 2 < nk) {
             if (!mbar_wait(&empty[s], ph)) { ok = false; break; }
             mbar_arrive_expect_tx(&full[s], bytesA + bytesB);
             tma_load_2d(sA[s], &tmA, &full[s], (kc + 2) * kBK, m0);
-            tma_load_2d(sB[s], &tmB, &full[s], (kc + 2) * kBK, 0);
+            load_b(s, kc + 2);
             issued++;
          }
       }
@@ -105,17 +117,33 @@ __global__ void __launch_bounds__(128) tc_gemm_kernel(const __grid_constant__ CU
 
 }  // namespace
 
-extern "C" pvgpu_status pvgpu_tc_gemm_bf16(const void *A, const void *B, float *C, int M, int N, int K, int *errFlag,
-                                           void *stream) {
-   if (!A || !B || !C || !errFlag || M <= 0 || N < 16 || N > 256 || (N % 16) || K < 64 || (K % 64) || (M % 128))
+namespace {
+
+pvgpu_status tc_gemm(const void *A, const void *B, float *C, int M, int N, int K, int *errFlag, void *stream, bool bmn) {
+   if (!A || !B || !C || !errFlag || M <= 0 || N < 16 || N > 256 || (N % 16) || K < 64 || (K % 64) || (M % 128) ||
+       (bmn && N % 64))
       return PVGPU_ERR_BAD_ARG;
    CUtensorMap tmA, tmB;
-   if (!pvgpu::make_tmap_bf16_sw128(&tmA, A, M, K, K, kBM) || !pvgpu::make_tmap_bf16_sw128(&tmB, B, N, K, K, N))
+   if (!pvgpu::make_tmap_bf16_sw128(&tmA, A, M, K, K, kBM) ||
+       !(bmn ? pvgpu::make_tmap_bf16_sw128(&tmB, B, K, N, N, kBK) : pvgpu::make_tmap_bf16_sw128(&tmB, B, N, K, K, N)))
       return PVGPU_ERR_BAD_ARG;
    size_t smem = 2 * (size_t)(kBM * kBK * 2 + N * kBK * 2) + 1024;
-   cudaError_t e = cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+   auto fn = bmn ? tc_gemm_kernel<true> : tc_gemm_kernel<false>;
+   cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
    if (e != cudaSuccess) return pvgpu::record_cuda_error(e, "tc_gemm attr");
-   tc_gemm_kernel<<<M / kBM, 128, smem, pvgpu::as_stream(stream)>>>(tmA, tmB, C, M, N, K, errFlag);
+   fn<<<M / kBM, 128, smem, pvgpu::as_stream(stream)>>>(tmA, tmB, C, M, N, K, errFlag);
    PVGPU_CHECK_LAUNCH("tc_gemm");
    return PVGPU_OK;
+}
+
+}  // namespace
+
+extern "C" pvgpu_status pvgpu_tc_gemm_bf16(const void *A, const void *B, float *C, int M, int N, int K, int *errFlag,
+                                           void *stream) {
+   return tc_gemm(A, B, C, M, N, K, errFlag, stream, false);
+}
+
+extern "C" pvgpu_status pvgpu_tc_gemm_bf16_kn(const void *A, const void *B, float *C, int M, int N, int K,
+                                              int *errFlag, void *stream) {
+   return tc_gemm(A, B, C, M, N, K, errFlag, stream, true);
 }

@@ -106,6 +106,20 @@ __device__ __forceinline__ uint64_t sdesc_sw128(uint32_t smem_addr) {
    return d;
 }
 
+// Descriptor of an MN-major operand in 128-byte swizzled tiles: 128-byte rows along K (64 BF16
+// values of consecutive M / N each), 8-row swizzle atoms 1024 B apart along K (SBO), and groups
+// of 64 M / N values lbo bytes apart (LBO) -- a K-major SW128 tile of the transposed matrix read
+// the other way round.
+__device__ __forceinline__ uint64_t sdesc_sw128_mn(uint32_t smem_addr, uint32_t lbo) {
+   uint64_t d = 0;
+   d |= (uint64_t)((smem_addr >> 4) & 0x3FFFu);
+   d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+   d |= (uint64_t)(1024u >> 4) << 32;
+   d |= (uint64_t)1 << 46;
+   d |= (uint64_t)2 << 61;
+   return d;
+}
+
 // Instruction descriptor, kind::f16: D = FP32, A = B = BF16, both K-major, M x N.
 __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
    return (1u << 4)                        // D format F32
@@ -114,6 +128,9 @@ __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
           | ((uint32_t)(N >> 3) << 17)     // N / 8
           | ((uint32_t)(M >> 4) << 24);    // M / 16
 }
+
+// The same with B MN-major (transpose-B bit).
+__host__ __device__ constexpr uint32_t idesc_bf16_bmn(int M, int N) { return idesc_bf16(M, N) | (1u << 16); }
 
 // D[tmem] (+)= A[smem] * B[smem]^T, one instruction (M x N x 16), issued by one thread.
 __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,

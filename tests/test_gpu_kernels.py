@@ -320,6 +320,24 @@ def test_tc_gemm_bf16(cuda, M, N, K):
     np.testing.assert_allclose(C.cpu().numpy(), ref.numpy(), rtol=1e-4, atol=1e-3)
 
 
+@pytest.mark.parametrize("M,N,K", [(128, 64, 64), (256, 192, 512), (128, 256, 128)])
+def test_tc_gemm_bf16_mn_major_b(cuda, M, N, K):
+    """The MN-major B operand (B stored [K][N], 128-byte rows along K, 64-column groups 8 KB apart:
+    a K-major weight tile read transposed) against the same host GEMM."""
+    torch = cuda
+    from openpv_gb300 import capi
+    g = torch.Generator().manual_seed(7 * M + N + K)
+    A = torch.randn(M, K, generator=g).to(torch.bfloat16)
+    B = torch.randn(K, N, generator=g).to(torch.bfloat16)
+    ref = A.float() @ B.float()
+    C = torch.zeros(M, N, device="cuda")
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    capi.tc_gemm_bf16_kn(A.cuda(), B.cuda(), C, M, N, K, err)
+    torch.cuda.synchronize()
+    assert int(err.item()) == 0, "a bounded device wait timed out"
+    np.testing.assert_allclose(C.cpu().numpy(), ref.numpy(), rtol=1e-4, atol=1e-3)
+
+
 def test_deliver_ident_matches_reference_rule(cuda, oracle):
     """IdentDelivery (delivery/IdentDelivery.cpp:99-180): GSyn += the restricted activity, from the
     dense extended buffer or from the SparseList (entries in the halo skipped); one contribution
