@@ -501,6 +501,7 @@ def run_ours(args, rank, world, local_rank):
     solver.autotune(x, trial_steps=4)
     tuned = solver.plan_info()
     tuned["schedule"] = solver.schedule()
+    tuned["fused"] = solver.fused_plan_info()
     for _ in range(args.warmup):
         solve(x)
     barrier()
@@ -517,7 +518,8 @@ def run_ours(args, rank, world, local_rank):
     solver.profile_begin(T)
     solve(x)
     torch.cuda.synchronize()
-    recon_ms, post_ms, nprof = solver.profile_end()
+    recon_ms, post_ms, fused_ms, nprof, nfused = solver.profile_end_fused()
+    fused_shape = solver.fused_plan_info()
     ms = e0.elapsed_time(e1) / args.steps
     ms_all = max_over_ranks(ms, dist, dev)
     value = job_value(world, nb, T, ms_all)
@@ -558,7 +560,9 @@ def run_ours(args, rank, world, local_rank):
             dist.destroy_process_group()
         if args.quick and rank == 0:
             print(json.dumps({"quick": True, "value": value, "ms_per_step": ms_all, "timesteps": T,
-                              "recon_ms": recon_ms / max(nprof, 1), "post_ms": post_ms / max(nprof, 1)}))
+                              "recon_ms": recon_ms / max(nprof, 1), "post_ms": post_ms / max(nprof, 1),
+                              "fused_ms_per_launch": fused_ms / max(nfused, 1), "fused_launches": nfused,
+                              "fused_shape": fused_shape, "schedule": tuned["schedule"]}))
         return
 
     # plain FP32 form, same structure, no tensor cores
@@ -581,7 +585,8 @@ def run_ours(args, rank, world, local_rank):
     rel_bf16 = float(np.max(np.abs(e_gpu[:nchk] - e64) / np.abs(e64)))
     rel_fp32 = float(np.max(np.abs(e_fp32[:nchk] - e64) / np.abs(e64)))
 
-    # dominant kernel roofline: the post-delivery + update kernel (HBM-bound)
+    # dominant kernel roofline: the fused timestep kernel F (or, with no fused steps, kernel P),
+    # HBM-bound
     pk = peaks()
     npos, F = cfg["v1_shape"][0] * cfg["v1_shape"][1], cfg["v1_shape"][2]
     npix = int(np.prod(cfg["in_shape"]))
@@ -597,23 +602,52 @@ def run_ours(args, rank, world, local_rank):
     rows_pad = cfg["in_shape"][0] + 2 * E
     FT = min(F, 256)
     window_bytes = (S * (rows_per_block - 1) + P) * RP * 4
-    post_bytes_unit = npos * F * (4 + 4 + 2 + 2 * x3_frac) + mb * (F // FT) * window_bytes
+    # kernel P runs the BF16x3 steps and the run's last BF16 step when kernel F is on
+    nP = nprof - nfused
+    x3_frac_p = X3 / max(nP, 1)
+    post_bytes_unit = npos * F * (4 + 4 + 2 + 2 * x3_frac_p) + mb * (F // FT) * window_bytes
     post_bytes_launch = post_bytes_unit * nb
-    post_avg_ms = post_ms / nprof
-    achieved = post_bytes_launch / (post_avg_ms / 1000.0) / 1e9
+    post_avg_ms = post_ms / max(nP, 1)
+    # kernel F per image-timestep: V read + write (FP32); per (block, feature tile) tile the stage
+    # (the block's bands of every feature tile + the P - S overlapping rows of each neighbour's)
+    # read, its band written, and x on the rows the block owns read (feature tile 0)
+    FTf = fused_shape["feature_tile"] or F
+    nfh = F // FTf
+    band = window_bytes
+    slice_b = (P - S) * RP * 4
+    stage = sum(nfh * band + ((mb_i > 0) + (mb_i < mb - 1)) * nfh * slice_b for mb_i in range(mb)) * nfh
+    owned = sum(((S * (rows_per_block - 1) + P) if mb_i == mb - 1 else S * rows_per_block) * RP * 4
+                for mb_i in range(mb))
+    fused_bytes_unit = npos * F * 8 + stage + mb * nfh * band + owned
+    fused_bytes_launch = fused_bytes_unit * nb
+    fused_avg_ms = fused_ms / max(nfused, 1)
+    if nfused:
+        dom_name = "step_tc_kernel (fused timestep: post delivery GEMM, LCA update, reconstruction bands)"
+        dom_bytes, dom_ms, dom_share = fused_bytes_launch, fused_avg_ms, fused_ms / (fused_ms + post_ms + recon_ms)
+    else:
+        dom_name = "post_tc_kernel (post delivery GEMM + LCA update, residual windows in)"
+        dom_bytes, dom_ms, dom_share = post_bytes_launch, post_avg_ms, post_ms / (post_ms + recon_ms)
+    achieved = dom_bytes / (dom_ms / 1000.0) / 1e9
     # kernel R: A read (BF16; + lo), x read, the padded residual written
     recon_bytes_unit = npos * F * (2 + 2 * x3_frac) + npix * 4 + rows_pad * RP * 4
-    recon_avg_ms = recon_ms / nprof
+    nR = nprof - nfused + (1 if nfused else 0)  # kernel R: every unfused step and the first fused one
+    recon_avg_ms = recon_ms / max(nR, 1)
     recon_flops_launch = 2 * npos * F * (cfg["nxp"] ** 2 * cfg["in_shape"][2]) * nb * (1 + 2 * x3_frac)
 
     # DRAM bytes per launch from the committed ncu summary of the same kernel and workload
     traffic = None
-    trafficf = os.path.join(ROOT, "profiles", "post_tc_kernel_batched_lca.md")
+    trafficf = os.path.join(ROOT, "profiles", ("step_tc_kernel_batched_lca.md" if nfused else
+                                               "post_tc_kernel_batched_lca.md"))
     if os.path.exists(trafficf):
         for line in open(trafficf):
             if line.startswith("dram bytes per launch:"):
                 traffic = float(line.split(":")[1])
 
+    # kernels per solve: reset and energy, and per chain: x padded, kernel R + F on the first fused
+    # step, F on the others, R + P on the rest (BF16x3 and the last BF16 step)
+    chains = tuned["schedule"]["chains"]
+    per_chain = (2 + nfused + 2 * (T - nfused)) if nfused else 2 * T
+    launches_per_solve = 2 + chains * per_chain
     cpu_val, cpu_dt = cpu_sample(cfg, cores, warm_steps=25, timed_steps=25)
     deliv = delivery_bench(torch, capi)
     lifb = lif_bench(torch, capi)
@@ -637,12 +671,14 @@ def run_ours(args, rank, world, local_rank):
                    "global_batch": nb * world, "timesteps_per_step": T, "parallelism": f"replicas{world}",
                    "l2": "state streamed each timestep (V 134 MB + activity 67 MB per step > 129 MB L2)",
                    "kernel_shapes": tuned},
-        "gpu_launches": args.steps * (2 * T + 2),
+        "gpu_launches": args.steps * launches_per_solve,
         "e2e": {"value": e2e_value, "unit": "images*steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-        "roofline": {"bound": "hbm", "kernel": "post_tc_kernel (post delivery GEMM + LCA update, residual windows in)",
+        "roofline": {"bound": "hbm", "kernel": dom_name,
                      "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": achieved / pk["hbm_gbs"],
-                     "peak_source": pk["source"], "traffic": traffic, "bytes_per_launch": post_bytes_launch,
-                     "avg_launch_ms": post_avg_ms, "share_of_step": post_ms / (post_ms + recon_ms)},
+                     "peak_source": pk["source"], "traffic": traffic, "bytes_per_launch": dom_bytes,
+                     "avg_launch_ms": dom_ms, "share_of_step": dom_share, "launches_per_solve": nfused or nprof},
+        "post_kernel": {"avg_launch_ms": post_avg_ms, "launches_per_solve": nP,
+                        "GB_s": post_bytes_launch / (post_avg_ms / 1e3) / 1e9 if nP else None},
         "recon_kernel": {"avg_launch_ms": recon_avg_ms, "GB_s": recon_bytes_unit * nb / (recon_avg_ms / 1e3) / 1e9,
                          "TFLOP_s": recon_flops_launch / (recon_avg_ms / 1e3) / 1e12},
         "fp32_form": {"value": value32, "unit": "images*steps/s", "speedup_bf16_over_fp32": value / world / value32,

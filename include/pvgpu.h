@@ -436,6 +436,10 @@ pvgpu_status pvgpu_lca_solver_error_flag(pvgpu_lca_solver *s, int *hostFlag);
  * reconstruction kernel and of the post-delivery/update kernel over the recorded steps. */
 pvgpu_status pvgpu_lca_solver_profile_begin(pvgpu_lca_solver *s, int maxSteps);
 pvgpu_status pvgpu_lca_solver_profile_end(pvgpu_lca_solver *s, double *reconMs, double *postMs, int *steps);
+/* The same split three ways: kernel R, kernel P, and the fused single-launch timesteps (kernel
+ * F, see pvgpu_lca_schedule.fused), with the number of timesteps that ran kernel F. */
+pvgpu_status pvgpu_lca_solver_profile_end_fused(pvgpu_lca_solver *s, double *reconMs, double *postMs,
+                                                double *fusedMs, int *steps, int *fusedSteps);
 /* No counterpart in the reference (its CUDA kernels have fixed launch shapes).  Times every
  * shape of the two BF16 kernels that fits in shared memory -- the post-delivery kernel's feature
  * tile (64/128/256/512) and its V / weight ring depths and A staging, the reconstruction
@@ -448,21 +452,35 @@ pvgpu_status pvgpu_lca_solver_autotune(pvgpu_lca_solver *s, const float *x, int 
 /* The shapes in use: out[0..4] = {feature tile, V ring slots, weight ring slots, A staged (0/1),
  * reconstruction ring stages} of the BF16 form, out[5..9] the same for BF16x3 steps. */
 pvgpu_status pvgpu_lca_solver_plan_info(const pvgpu_lca_solver *s, int *out);
+/* The fused kernel's shape: out[0..2] = {feature tile, V ring slots, weight ring slots}, zeros
+ * when the geometry has no fused form. */
+pvgpu_status pvgpu_lca_solver_fused_plan_info(const pvgpu_lca_solver *s, int *out);
+/* Sets the fused kernel's shape (what the autotuner otherwise picks): feature tile (a multiple
+ * of 64 dividing v1Nf), V ring slots (1..3), weight ring slots (2..3); PVGPU_ERR_UNSUPPORTED_SHAPE
+ * when it does not fit shared memory.  The ring depths do not change results; the feature tile
+ * sets how the reconstruction is split into bands (FP32 summation order of the residual). */
+pvgpu_status pvgpu_lca_solver_set_fused_plan(pvgpu_lca_solver *s, int featureTile, int vSlots, int wSlots);
 
-/* No counterpart in the reference.  How a BF16 run is laid out as a CUDA graph: chains = 1 runs
- * the whole batch through kernel R and kernel P in turn; chains = 2 runs the two halves of the
- * batch (images [0, n0) and [n0, nbatch), n0 = nbatch / 2 rounded up to even when that leaves
- * images for the second half) as two independent chains on parallel graph branches, so that the
- * kernels of one half run in the ramp and tail of the other's.  reconCtas / postCtas cap the
- * persistent grids of kernel R (rounded down to clusters of two) and kernel P (0 = as many as
- * fit).  programmatic = 1 launches each kernel of a chain early (programmatic stream
- * serialisation) so that its set-up overlaps the kernel before it.  The images' results do not
- * depend on the schedule.  Default {1, 0, 0, 1}; per-kernel profiling runs always use one chain. */
+/* No counterpart in the reference.  How a BF16 run is laid out: fused = 1 runs the BF16
+ * timesteps as one launch each (kernel F: post delivery, update and the reconstruction of the
+ * new activity, which stays on chip; each block's reconstruction leaves as a band of padded rows
+ * that the next step's windows sum) except the run's first (kernel R then F) and its final BF16
+ * step and BF16x3 steps (kernels R and P); fused = 0 runs kernels R and P on every step.  The
+ * two forms differ only in FP32 summation order of the residual.  chains = 1 runs the whole
+ * batch as one chain of kernels; chains = 2 runs the two halves of the batch (images [0, n0)
+ * and [n0, nbatch), n0 = nbatch / 2 rounded up to even when that leaves images for the second
+ * half) as two independent chains on parallel graph branches, so that the kernels of one half
+ * run in the ramp and tail of the other's.  reconCtas / postCtas cap the persistent grids of
+ * kernel R (rounded down to clusters of two) and of kernels P and F (0 = as many as fit).
+ * programmatic = 1 launches each kernel of a chain early (programmatic stream serialisation) so
+ * that its set-up overlaps the kernel before it.  chains, the caps and programmatic do not
+ * change the results.  Default {1, 0, 0, 1, 1}; per-kernel profiling runs use one chain. */
 typedef struct {
    int chains;
    int reconCtas;
    int postCtas;
    int programmatic;
+   int fused;
 } pvgpu_lca_schedule;
 pvgpu_status pvgpu_lca_solver_set_schedule(pvgpu_lca_solver *s, const pvgpu_lca_schedule *sc);
 pvgpu_status pvgpu_lca_solver_get_schedule(const pvgpu_lca_solver *s, pvgpu_lca_schedule *sc);

@@ -83,7 +83,8 @@ class LcaSolverDesc(C.Structure):
 
 
 class LcaSchedule(C.Structure):
-    _fields_ = [("chains", C.c_int), ("reconCtas", C.c_int), ("postCtas", C.c_int), ("programmatic", C.c_int)]
+    _fields_ = [("chains", C.c_int), ("reconCtas", C.c_int), ("postCtas", C.c_int), ("programmatic", C.c_int),
+                ("fused", C.c_int)]
 
 
 LCA_FP32 = 0
@@ -138,6 +139,10 @@ def _declare(L):
         "pvgpu_lca_solver_autotune": (i, [vp, vp, i, vp]),
         "pvgpu_lca_solver_plan_info": (i, [vp, C.POINTER(i)]),
         "pvgpu_lca_solver_set_schedule": (i, [vp, C.POINTER(LcaSchedule)]),
+        "pvgpu_lca_solver_fused_plan_info": (i, [vp, C.POINTER(i)]),
+        "pvgpu_lca_solver_set_fused_plan": (i, [vp, i, i, i]),
+        "pvgpu_lca_solver_profile_end_fused": (i, [vp, C.POINTER(d), C.POINTER(d), C.POINTER(d), C.POINTER(i),
+                                                   C.POINTER(i)]),
         "pvgpu_lca_solver_get_schedule": (i, [vp, C.POINTER(LcaSchedule)]),
         "pvgpu_deliver_ident": (i, [lp, lp, vp, vp, vp, vp, vp]),
         "pvgpu_momentum_lca_update": (i, [lp, i, f, vp, f, vp, vp, vp, vp, vp]),
@@ -409,17 +414,34 @@ class LcaSolver:
         keys = ("feature_tile", "v_slots", "w_slots", "a_staged", "recon_stages")
         return {form: dict(zip(keys, out[5 * i:5 * i + 5])) for i, form in enumerate(("bf16", "bf16x3"))}
 
-    def set_schedule(self, chains=1, recon_ctas=0, post_ctas=0, programmatic=True):
-        """Graph layout of BF16 runs: one chain over the batch or two half-batch chains on
-        parallel branches; caps on the persistent grids; early launch within a chain."""
-        sc = LcaSchedule(chains, recon_ctas, post_ctas, int(programmatic))
+    def set_schedule(self, chains=1, recon_ctas=0, post_ctas=0, programmatic=True, fused=True):
+        """Layout of BF16 runs: fused single-launch timesteps or kernels R + P on every step; one
+        chain over the batch or two half-batch chains on parallel graph branches; caps on the
+        persistent grids; early launch within a chain."""
+        sc = LcaSchedule(chains, recon_ctas, post_ctas, int(programmatic), int(fused))
         check(lib().pvgpu_lca_solver_set_schedule(self.h, C.byref(sc)), "lca_solver_set_schedule")
 
     def schedule(self):
         sc = LcaSchedule()
         check(lib().pvgpu_lca_solver_get_schedule(self.h, C.byref(sc)), "lca_solver_get_schedule")
         return {"chains": sc.chains, "recon_ctas": sc.reconCtas, "post_ctas": sc.postCtas,
-                "programmatic": bool(sc.programmatic)}
+                "programmatic": bool(sc.programmatic), "fused": bool(sc.fused)}
+
+    def fused_plan_info(self):
+        """{feature_tile, v_slots, w_slots} of the fused kernel (zeros: no fused form here)."""
+        out = (C.c_int * 3)()
+        check(lib().pvgpu_lca_solver_fused_plan_info(self.h, out), "lca_solver_fused_plan_info")
+        return {"feature_tile": out[0], "v_slots": out[1], "w_slots": out[2]}
+
+    def set_fused_plan(self, feature_tile, v_slots, w_slots=2):
+        check(lib().pvgpu_lca_solver_set_fused_plan(self.h, feature_tile, v_slots, w_slots), "lca_solver_set_fused_plan")
+
+    def profile_end_fused(self):
+        """(recon ms, post ms, fused ms, steps, fused steps) over the profiled timesteps."""
+        r, p, f, n, nf = C.c_double(), C.c_double(), C.c_double(), C.c_int(), C.c_int()
+        check(lib().pvgpu_lca_solver_profile_end_fused(self.h, C.byref(r), C.byref(p), C.byref(f), C.byref(n),
+                                                       C.byref(nf)), "lca_solver_profile_end_fused")
+        return r.value, p.value, f.value, n.value, nf.value
 
     def profile_begin(self, max_steps):
         check(lib().pvgpu_lca_solver_profile_begin(self.h, max_steps), "lca_solver_profile_begin")

@@ -120,6 +120,7 @@ struct ReconPlan {
    int nStage;         // A + W^T ring stages
    int RP, rowsPad;    // padded residual rows
    uint32_t stageBytes, offRec, offX[2];
+   uint32_t xStride;   // offX[1] - offX[0] (kernels index slots arithmetically, not through the array)
    uint32_t total;
 };
 
@@ -222,7 +223,8 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(320, 1)
                   const int xb = ui & 1;
                   if (ui >= 2 && !(ok = wait_or_abort(&xEmpty[xb], (uint32_t)(((ui >> 1) - 1) & 1)))) break;
                   mbar_arrive_expect_tx(&xFull[xb], (uint32_t)nPix * 4);
-                  bulk_load(smem + rp.offX[xb], x + (size_t)b * nPix, (uint32_t)nPix * 4, &xFull[xb]);
+                  bulk_load(smem + rp.offX[0] + xb * rp.xStride, x + (size_t)b * nPix, (uint32_t)nPix * 4,
+                            &xFull[xb]);
                   xIssued = ui + 1;
                }
             }
@@ -351,7 +353,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(320, 1)
          const int xb = ui & 1;
          if (tid == 0) wait_or_abort(&xFull[xb], (uint32_t)((ui >> 1) & 1));
          if (named_bar_or(1, FOLD, abortFlag != 0)) break;
-         const float *xs = reinterpret_cast<const float *>(smem + rp.offX[xb]);
+         const float *xs = reinterpret_cast<const float *>(smem + rp.offX[0] + xb * rp.xStride);
          float *out = rpad + (size_t)b * rp.rowsPad * rp.RP;
          const int rowElems = g.inNx * C;
          // trip counts uniform across each warp (a divergent inner loop costs far more than
@@ -423,6 +425,7 @@ struct PostPlan {
    uint32_t offIM, offIMlo;
    uint32_t offW[kMaxWSlots], offWlo[kMaxWSlots];
    uint32_t offVT[kMaxVSlots];
+   uint32_t wStride;                  // offW[s+1] - offW[s]; V slots are 32 KB apart
    uint32_t offWin;                   // residual window, RWR rows x RP floats
    uint32_t offA;                     // A staging, 2 KB per epilogue warp (when stageA)
    int stageA;                        // A leaves through shared memory and TMA stores
@@ -545,14 +548,15 @@ __global__ void __launch_bounds__(320, 1) post_tc_kernel(const __grid_constant__
             if (uw > 0 && !(ok = wait_or_abort(&wEmpty[sw], (uint32_t)((uw - 1) & 1)))) break;
             mbar_arrive_expect_tx(&wFull[sw], (X3 ? 2 : 1) * WBYTES);
             for (int kc = 0; kc < NKC; kc++) {
-               tma_load_2d(smem + pl.offW[sw] + kc * kPostNT * 128, &tmW, &wFull[sw], kc * 64, f0);
-               if (X3) tma_load_2d(smem + pl.offWlo[sw] + kc * kPostNT * 128, &tmWlo, &wFull[sw], kc * 64, f0);
+               const uint32_t wo = sw * pl.wStride + kc * kPostNT * 128;
+               tma_load_2d(smem + pl.offW[0] + wo, &tmW, &wFull[sw], kc * 64, f0);
+               if (X3) tma_load_2d(smem + pl.offWlo[0] + wo, &tmWlo, &wFull[sw], kc * 64, f0);
             }
             wIssued = q + 1;
             const int sv = q % nV, uv = q / nV;
             if (uv > 0 && !(ok = wait_or_abort(&vEmpty[sv], (uint32_t)((uv - 1) & 1)))) break;
             mbar_arrive_expect_tx(&vFull[sv], 32768);
-            bulk_load(smem + pl.offVT[sv], V + v_index(g, b, mb * 128, f0), 32768, &vFull[sv]);
+            bulk_load(smem + pl.offVT[0] + sv * 32768u, V + v_index(g, b, mb * 128, f0), 32768, &vFull[sv]);
             vIssued = q + 1;
          }
          while (ok && rowsIssued < myTiles) {
@@ -588,7 +592,7 @@ __global__ void __launch_bounds__(320, 1) post_tc_kernel(const __grid_constant__
             const int npass = X3 ? 3 : 1;
             for (int pass = 0; pass < npass; pass++) {
                const uint32_t a0 = smem_u32(smem + ((X3 && pass == 2) ? pl.offIMlo : pl.offIM));
-               const uint32_t w0 = smem_u32(smem + ((X3 && pass == 1) ? pl.offWlo[sw] : pl.offW[sw]));
+               const uint32_t w0 = smem_u32(smem + ((X3 && pass == 1) ? pl.offWlo[0] : pl.offW[0]) + sw * pl.wStride);
                for (int kc = 0; kc < NKC; kc++)
 #pragma unroll
                   for (int k = 0; k < 4; k++)
@@ -692,7 +696,7 @@ __global__ void __launch_bounds__(320, 1) post_tc_kernel(const __grid_constant__
             tmem_ld32(tmem + a * kPostNT + ((uint32_t)(32 * qd) << 16) + 32 * h, d);
             tc_fence_before();
             if (lane == 0) mbar_arrive(&accEmpty[a]);  // this warp is done with the accumulator
-            uint8_t *vsub = smem + pl.offVT[sv] + h * 16384 + 32 * qd * 128;  // this warp's 32 x 32 part
+            uint8_t *vsub = smem + pl.offVT[0] + sv * 32768u + h * 16384 + 32 * qd * 128;  // this warp's 32 x 32 part
             uint8_t *vt = vsub + lane * 128;
 #pragma unroll
             for (int qq = 0; qq < 8; qq++) {
@@ -779,6 +783,570 @@ __global__ void __launch_bounds__(320, 1) post_tc_kernel(const __grid_constant__
    tc_fence_before();
    __syncthreads();
    if (warp == 0) tmem_dealloc(tmem, kAcc * kPostNT);
+}
+
+// -------------------------------------------------------------------------------------------
+// Kernel F: a whole BF16 LCA timestep in one launch -- kernel P's post delivery and update,
+// then the reconstruction of the new activity, without the activity leaving the SM.
+//
+// Tile (image b, block mb of 128 positions, feature tile fh of FT features) as in kernel P.
+// Per 64-feature block q of the tile, after kernel P's GEMM (D1 = im2col(r) . W_q^T) and the
+// update, the block's new activity A_q (BF16, 128 positions x 64 features) goes to a shared
+// K-major tile and a second GEMM accumulates D2[pos][k] += sum_f A_q[pos][f] W_q[f][k]
+// (N = P*P*C) in TMEM, reading the block's weight tile again as an MN-major operand.  After
+// the tile's last block the 8 epilogue warps fold D2 into a band: padded rows S*mb*rpb ..
+// +RWR (every row the block's patches reach), starting from x on the rows the block owns when
+// fh == 0 and from 0 otherwise, each tap subtracted (kernel R's fold: 16 tap groups, no two
+// threads on one pixel inside a group, every pixel's taps in one fixed order).  The band goes
+// to HBM.  Block mb owns padded rows S*mb*rpb .. S*(mb+1)*rpb - 1, the last block also the
+// rows below; bands of blocks mb and mb + 1 overlap in P - S rows (P - S <= S*rpb).
+// The next timestep's tile (b, mb) sums its residual window r = x - W^T a from the bands of
+// (b, mb) and the overlapping rows of (b, mb - 1) and (b, mb + 1), all feature tiles: per
+// pixel (sum over fh of the lower block's band) + (sum over fh of the upper block's band),
+// so that both windows holding a pixel compute it in the same order.  The first timestep of
+// a run reads kernel R's padded residual window instead (mode 0).
+// Roles: as kernel P (warp 8 loads, warp 9 MMA, warps 0-7 epilogue), and
+//   loads:    the tile's bands (or residual window) as one stage, once the tile before has read
+//             the stage and the fold of the tile before that (which runs in the stage) is
+//             stored;
+//   MMA:      GEMM1 of block q, then GEMM2 of block q - 1 (one behind, so that the epilogue of
+//             block q - 1 overlaps GEMM1 of block q); a weight slot is freed by GEMM2's commit;
+//   epilogue: A_q into the shared A tile (after GEMM2 of block q - 1 has read it); x of the
+//             owned rows into registers at the start of the tile's last block; after that block
+//             (and after the next tile's im2col, which GEMM1 of the next tile -- and so GEMM2 of
+//             this tile's last block -- waits for) the fold in the stage and the band store.
+// Hand-offs added to kernel P's: aFull / aEmpty, d2Full (the tile's D2 complete), foldFree (the
+// band store has read the stage).  D2 is overwritten by the next tile's first GEMM2 only after
+// that block's aFull, which the epilogue signals after the fold's TMEM reads have completed.
+// -------------------------------------------------------------------------------------------
+struct FusePlan {
+   int G;                         // persistent CTAs
+   int FT;                        // features per tile (multiple of 64)
+   int nV, nW;                    // V and weight ring slots
+   int RP, rowsPad, RWR;          // padded rows: floats per row, rows per image, rows per band
+   uint32_t bandFloats, sliceFloats;
+   uint32_t offIM, offW[3], offVT[kMaxVSlots], offStage, offTop, offBot, offAop, offFold;
+   uint32_t wStride;              // offW[s+1] - offW[s]; V slots are 32 KB apart
+   uint32_t total;
+};
+
+template <int S, int P, int C>
+__global__ void __launch_bounds__(352, 1) step_tc_kernel(const __grid_constant__ CUtensorMap tmW, LcaGeom g,
+                                                         FusePlan fp, int mode, int writeA,
+                                                         const float *__restrict__ rin,
+                                                         float *__restrict__ bandsOut,
+                                                         const float *__restrict__ xpad, float *__restrict__ V,
+                                                         bf16 *__restrict__ A, bf16 *__restrict__ Alo,
+                                                         int *__restrict__ err) {
+   constexpr int KP = P * P * C, NKC = KP / 64;
+   constexpr uint32_t WBYTES = NKC * kPostNT * 128;
+   constexpr int EPI = 256;
+   constexpr int kMaxW = 3;
+   static_assert((S * C) % 2 == 0, "window reads are 8-byte pairs");
+   static_assert(KP % 16 == 0 && KP <= 256, "GEMM2 is one MMA of N = P*P*C");
+   extern __shared__ uint8_t smem_raw[];
+   uint8_t *smem = align1024(smem_raw);
+   __shared__ __align__(8) uint64_t stFull, stEmpty, imFull, imEmpty, wFull[kMaxW], wEmpty[kMaxW], vFull[kMaxVSlots],
+         vEmpty[kMaxVSlots], accFull[kAcc], accEmpty[kAcc], aFull, aEmpty, d2Full, foldFree, drain;
+   __shared__ uint32_t tmemBase;
+   __shared__ volatile int abortFlag;
+
+   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+   const int nFH = g.F / fp.FT, nBlk = fp.FT / kPostNT;
+   const int nTiles = g.nb * g.MB * nFH;
+   const int myTiles = blockIdx.x < nTiles ? (nTiles - 1 - blockIdx.x) / fp.G + 1 : 0;
+   const int Q = myTiles * nBlk;
+   const int nV = fp.nV, nW = fp.nW;
+   const int lagV = nV >= 2 ? nV - 1 : nV;
+   const int RWR = fp.RWR, RP = fp.RP, rpb = g.rowsPerBlock;
+   const uint32_t bandBytes = fp.bandFloats * 4u, sliceBytes = fp.sliceFloats * 4u;
+   auto owned_rows = [&](int mb) { return mb == g.MB - 1 ? RWR : S * rpb; };
+
+   if (tid == 0) {
+      mbar_init(&stFull, 1);
+      mbar_init(&stEmpty, 1);
+      mbar_init(&imFull, 1);
+      mbar_init(&imEmpty, 1);
+      for (int i = 0; i < kMaxW; i++) {
+         mbar_init(&wFull[i], 1);
+         mbar_init(&wEmpty[i], 1);
+      }
+      for (int i = 0; i < kMaxVSlots; i++) {
+         mbar_init(&vFull[i], 1);
+         mbar_init(&vEmpty[i], 8);
+      }
+      for (int i = 0; i < kAcc; i++) {
+         mbar_init(&accFull[i], 1);
+         mbar_init(&accEmpty[i], 8);
+      }
+      mbar_init(&aFull, 8);  // one arrival per epilogue warp
+      mbar_init(&aEmpty, 1);
+      mbar_init(&d2Full, 1);
+      mbar_init(&foldFree, 1);
+      mbar_init(&drain, 1);
+      abortFlag = 0;
+      fence_mbar_init();
+   }
+   if (warp == 0) tmem_alloc(&tmemBase, 512);
+   tc_fence_before();
+   __syncthreads();
+   tc_fence_after();
+   const uint32_t tmem = tmemBase;
+   const uint32_t tmemD2 = tmem + kAcc * kPostNT;
+   // Set-up above overlaps the previous kernel's tail; everything below reads the bands or the
+   // residual (written by the previous launch) or V (which the previous launch writes).
+   griddep_launch_dependents();
+   griddep_wait();
+
+   auto tile_of = [&](int ti, int &b, int &mb, int &fh) {
+      const int j = blockIdx.x + ti * fp.G;
+      fh = j % nFH;
+      const int r = j / nFH;
+      mb = r % g.MB;
+      b = r / g.MB;
+   };
+   auto wait_or_abort = [&](uint64_t *bar, uint32_t parity) {
+      if (abortFlag) return false;
+      if (mbar_wait(bar, parity)) return true;
+      abortFlag = 1;
+      return false;
+   };
+   auto last_use = [](int n, int sl, int slots) { return sl < n ? n - 1 - ((n - 1 - sl) % slots) : -1; };
+   auto band_in = [&](int b, int mb, int fh) {
+      return rin + (((size_t)b * g.MB + mb) * nFH + fh) * fp.bandFloats;
+   };
+
+   if (warp == 8) {
+      // ============================== weight loads ==============================
+      if (lane == 0 && Q > 0) {
+         prefetch_tmap(&tmW);
+         int wIssued = 0;
+         bool ok = true;
+         for (int q = 0; ok && q < Q; q++) {
+            const int ti = q / nBlk, nb = q % nBlk;
+            int b, mb, fh;
+            tile_of(ti, b, mb, fh);
+            const int f0 = fh * fp.FT + nb * kPostNT;
+            const int sw = q % nW, uw = q / nW;
+            if (uw > 0 && !(ok = wait_or_abort(&wEmpty[sw], (uint32_t)((uw - 1) & 1)))) break;
+            mbar_arrive_expect_tx(&wFull[sw], WBYTES);
+            for (int kc = 0; kc < NKC; kc++)
+               tma_load_2d(smem + fp.offW[0] + sw * fp.wStride + kc * kPostNT * 128, &tmW, &wFull[sw], kc * 64, f0);
+            wIssued = q + 1;
+         }
+         if (!ok) {  // the copies still in flight land before shared memory goes away
+            for (int sl = 0; sl < nW; sl++) {
+               const int u = last_use(wIssued, sl, nW);
+               if (u >= 0) mbar_wait(&wFull[sl], (uint32_t)((u / nW) & 1));
+            }
+         }
+      }
+   } else if (warp == 10) {
+      // ============================== V and stage loads ==============================
+      if (lane == 0 && Q > 0) {
+         int rowsIssued = 0, vIssued = 0;
+         auto issue_stage = [&](int ti) {
+            int b, mb, fh;
+            tile_of(ti, b, mb, fh);
+            uint8_t *st = smem + fp.offStage;
+            if (mode == 0) {
+               // kernel R's padded residual: rows S*mb*rpb .. +RWR of image b
+               const float *src = rin + ((size_t)b * fp.rowsPad + (size_t)S * mb * rpb) * RP;
+               mbar_arrive_expect_tx(&stFull, bandBytes);
+               bulk_load(st, src, bandBytes, &stFull);
+            } else {
+               const uint32_t bytes = nFH * bandBytes + (mb > 0 ? nFH * sliceBytes : 0u) +
+                                      (mb < g.MB - 1 ? nFH * sliceBytes : 0u);
+               mbar_arrive_expect_tx(&stFull, bytes);
+               for (int f = 0; f < nFH; f++) bulk_load(st + f * bandBytes, band_in(b, mb, f), bandBytes, &stFull);
+               if (mb > 0)  // the upper neighbour's last P - S rows
+                  for (int f = 0; f < nFH; f++)
+                     bulk_load(smem + fp.offTop + f * sliceBytes, band_in(b, mb - 1, f) + (size_t)S * rpb * RP,
+                               sliceBytes, &stFull);
+               if (mb < g.MB - 1)  // the lower neighbour's first P - S rows
+                  for (int f = 0; f < nFH; f++)
+                     bulk_load(smem + fp.offBot + f * sliceBytes, band_in(b, mb + 1, f), sliceBytes, &stFull);
+            }
+            rowsIssued = ti + 1;
+         };
+         bool ok = true;
+         issue_stage(0);
+         // stage t goes out once tile t - 1's im2col has read the stage and tile t - 2's fold
+         // (which runs in the stage after that im2col) has been stored
+         auto stage_free = [&](int t) {
+            return wait_or_abort(&stEmpty, (uint32_t)((t - 1) & 1)) &&
+                   (t < 2 || wait_or_abort(&foldFree, (uint32_t)((t - 2) & 1)));
+         };
+         for (int q = 0; ok && q < Q; q++) {
+            // the next stage before the first V load that waits for the current tile's epilogue
+            while (ok && rowsIssued < myTiles && (rowsIssued - 1) * nBlk + lagV <= q) {
+               ok = stage_free(rowsIssued);
+               if (ok) issue_stage(rowsIssued);
+            }
+            if (!ok) break;
+            const int ti = q / nBlk, nb = q % nBlk;
+            int b, mb, fh;
+            tile_of(ti, b, mb, fh);
+            const int f0 = fh * fp.FT + nb * kPostNT;
+            const int sv = q % nV, uv = q / nV;
+            if (uv > 0 && !(ok = wait_or_abort(&vEmpty[sv], (uint32_t)((uv - 1) & 1)))) break;
+            mbar_arrive_expect_tx(&vFull[sv], 32768);
+            bulk_load(smem + fp.offVT[0] + sv * 32768u, V + v_index(g, b, mb * 128, f0), 32768, &vFull[sv]);
+            vIssued = q + 1;
+         }
+         while (ok && rowsIssued < myTiles) {
+            ok = stage_free(rowsIssued);
+            if (ok) issue_stage(rowsIssued);
+         }
+         if (!ok) {
+            // the copies still in flight land before shared memory goes away
+            mbar_wait(&stFull, (uint32_t)((rowsIssued - 1) & 1));
+            for (int sl = 0; sl < nV; sl++) {
+               const int u = last_use(vIssued, sl, nV);
+               if (u >= 0) mbar_wait(&vFull[sl], (uint32_t)((u / nV) & 1));
+            }
+         }
+      }
+   } else if (warp == 9) {
+      // ============================== MMA ==============================
+      if (lane == 0 && Q > 0) {
+         const uint32_t idesc1 = idesc_bf16(128, kPostNT), idesc2 = idesc_bf16_bmn(128, KP);
+         bool ok = true;
+         int issued = 0;
+         // GEMM2 of block q: its A tile times its weight tile (MN-major: 64-tap groups 8 KB apart)
+         auto gemm2 = [&](int q) {
+            const int nb = q % nBlk, sw = q % nW;
+            if (!(ok = wait_or_abort(&aFull, (uint32_t)(q & 1)))) return;
+            tc_fence_after();
+            const uint32_t a0 = smem_u32(smem + fp.offAop), w0 = smem_u32(smem + fp.offW[0] + sw * fp.wStride);
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+               mma_bf16(tmemD2, sdesc_sw128(a0 + k * 32), sdesc_sw128_mn(w0 + k * 2048, kPostNT * 128), idesc2,
+                        (nb | k) != 0);
+            mma_commit(&aEmpty);
+            mma_commit(&wEmpty[sw]);
+            if (nb == nBlk - 1) mma_commit(&d2Full);
+            issued++;
+         };
+         for (int q = 0; ok && q < Q; q++) {
+            const int ti = q / nBlk, nb = q % nBlk, sw = q % nW, a = q % kAcc;
+            if (nb == 0 && !(ok = wait_or_abort(&imFull, (uint32_t)(ti & 1)))) break;
+            if (!(ok = wait_or_abort(&wFull[sw], (uint32_t)((q / nW) & 1)))) break;
+            if (q >= kAcc && !(ok = wait_or_abort(&accEmpty[a], (uint32_t)((q / kAcc - 1) & 1)))) break;
+            tc_fence_after();
+            const uint32_t d = tmem + a * kPostNT;
+            const uint32_t a0 = smem_u32(smem + fp.offIM), w0 = smem_u32(smem + fp.offW[0] + sw * fp.wStride);
+            for (int kc = 0; kc < NKC; kc++)
+#pragma unroll
+               for (int k = 0; k < 4; k++)
+                  mma_bf16(d, sdesc_sw128(a0 + kc * 16384 + k * 32), sdesc_sw128(w0 + kc * kPostNT * 128 + k * 32),
+                           idesc1, (kc | k) != 0);
+            mma_commit(&accFull[a]);
+            if (nb == nBlk - 1) mma_commit(&imEmpty);
+            issued++;
+            if (q >= 1) gemm2(q - 1);
+         }
+         if (ok) gemm2(Q - 1);
+         // MMAs still in flight finish before shared memory and TMEM go away
+         if (!ok && issued > 0) {
+            mma_commit(&drain);
+            mbar_wait(&drain, 0);
+         }
+      }
+   } else if (warp < 8) {
+      // ============================== epilogue (warps 0-7) ==============================
+      const float *win = reinterpret_cast<const float *>(smem + fp.offStage);
+      float *fold = reinterpret_cast<float *>(smem + fp.offFold);
+      const int qd = warp & 3, h = warp >> 2;
+      const int pw = 32 * qd + lane;
+      int pendingV = -1;
+      auto im2col = [&](int t) {
+         if (tid == 0 && wait_or_abort(&stFull, (uint32_t)(t & 1)) && t > 0)
+            wait_or_abort(&imEmpty, (uint32_t)((t - 1) & 1));
+         if (named_bar_or(1, EPI, abortFlag != 0)) return false;
+         if (mode != 0) {
+            // ---- the residual window from the bands ----
+            int b, mb, fh;
+            tile_of(t, b, mb, fh);
+            float *w = reinterpret_cast<float *>(smem + fp.offStage);
+            const float *top = reinterpret_cast<const float *>(smem + fp.offTop);
+            const float *bot = reinterpret_cast<const float *>(smem + fp.offBot);
+            const int n = RWR * RP, ovl = P - S, own = S * rpb;
+            const bool hasTop = mb > 0, hasBot = mb < g.MB - 1;
+            for (int i = tid; i < n; i += EPI) {
+               const int r = i / RP;
+               float v = w[i];
+               for (int f = 1; f < nFH; f++) v = __fadd_rn(v, w[f * fp.bandFloats + i]);
+               if (hasTop && r < ovl) {
+                  float u = top[i];
+                  for (int f = 1; f < nFH; f++) u = __fadd_rn(u, top[f * fp.sliceFloats + i]);
+                  v = __fadd_rn(u, v);
+               } else if (hasBot && r >= own) {
+                  const int j = i - own * RP;
+                  float u = bot[j];
+                  for (int f = 1; f < nFH; f++) u = __fadd_rn(u, bot[f * fp.sliceFloats + j]);
+                  v = __fadd_rn(v, u);
+               }
+               w[i] = v;
+            }
+            named_bar_sync(1, EPI);
+         }
+         {
+            // ---- BF16 im2col of the window (as kernel P) ----
+            constexpr int RUN = P * C;
+            constexpr int CPR = RUN / 8;
+            static_assert(RUN % 8 == 0, "patch rows must fill whole 16-byte chunks");
+            const int p = tid & 127, half = tid >> 7;
+            const int yl = p / g.v1Nx, x1 = p % g.v1Nx;
+            const float *src0 = win + (S * yl) * RP + S * x1 * C;
+#pragma unroll 1
+            for (int ky = half * (P / 2); ky < (half + 1) * (P / 2); ky++) {
+               const float2 *src = reinterpret_cast<const float2 *>(src0 + ky * RP);
+#pragma unroll
+               for (int cc = 0; cc < CPR; cc++) {
+                  float vals[8];
+#pragma unroll
+                  for (int jj = 0; jj < 4; jj++) {
+                     const float2 t2 = src[cc * 4 + jj];
+                     vals[2 * jj] = t2.x;
+                     vals[2 * jj + 1] = t2.y;
+                  }
+                  const int c8 = ky * CPR + cc;
+                  const uint32_t off = (c8 >> 3) * 16384 + sw128_offset(p, (c8 & 7) * 8);
+                  *reinterpret_cast<uint4 *>(smem + fp.offIM + off) =
+                        make_uint4(pack2(vals[0], vals[1]), pack2(vals[2], vals[3]), pack2(vals[4], vals[5]),
+                                   pack2(vals[6], vals[7]));
+               }
+            }
+         }
+         fence_proxy_async_smem();
+         named_bar_sync(1, EPI);
+         if (tid == 0) {
+            mbar_arrive(&imFull);
+            mbar_arrive(&stEmpty);
+         }
+         return true;
+      };
+      // x on the rows the tile's block owns (fh == 0), read from HBM / L2 into registers at
+      // the start of the tile's last block, so that the loads are in flight during its update
+      constexpr int kXPre = 4;  // float4 per thread held in registers; the rest is read at the fold
+      float4 xr[kXPre];
+      auto x_prefetch = [&](int t) {
+         int b, mb, fh;
+         tile_of(t, b, mb, fh);
+         const int n4 = fh == 0 ? owned_rows(mb) * RP / 4 : 0;
+         const float4 *src = reinterpret_cast<const float4 *>(xpad + ((size_t)b * fp.rowsPad + (size_t)S * mb * rpb) * RP);
+#pragma unroll
+         for (int k = 0; k < kXPre; k++) {
+            const int i = tid + k * EPI;
+            xr[k] = i < n4 ? __ldg(src + i) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+         }
+      };
+      // the fold of tile t's D2 into its band (in the stage, which the next tile's im2col has
+      // read), starting from x on the owned rows and 0 elsewhere, and the band store
+      auto fold_tile = [&](int t) {
+         int b, mb, fh;
+         tile_of(t, b, mb, fh);
+         {
+            const int n4 = (int)fp.bandFloats / 4, x4 = fh == 0 ? owned_rows(mb) * RP / 4 : 0;
+            float4 *f4 = reinterpret_cast<float4 *>(fold);
+            const float4 *src =
+                  reinterpret_cast<const float4 *>(xpad + ((size_t)b * fp.rowsPad + (size_t)S * mb * rpb) * RP);
+#pragma unroll
+            for (int k = 0; k < kXPre; k++) {
+               const int i = tid + k * EPI;
+               if (i < n4) f4[i] = xr[k];
+            }
+            for (int i = tid + kXPre * EPI; i < n4; i += EPI)
+               f4[i] = i < x4 ? __ldg(src + i) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+         }
+         if (tid == 0) wait_or_abort(&d2Full, (uint32_t)(t & 1));
+         if (named_bar_or(1, EPI, abortFlag != 0)) return false;
+         tc_fence_after();
+         constexpr int DH = S / 2;  // patch rows per half
+         const int p = tid & 127, hh = tid >> 7;
+         const uint32_t lanes = tmemD2 + ((uint32_t)((warp & 3) * 32) << 16);
+         const int y1 = p / g.v1Nx, x1 = p % g.v1Nx;
+         const int yImg0 = S * (mb * rpb + y1) - (P - S) / 2, xImg0 = S * x1 - (P - S) / 2;
+#pragma unroll 1
+         for (int ty = 0; ty < P / S; ty++) {
+            float rowv[DH][P * C];
+#pragma unroll
+            for (int dd = 0; dd < DH; dd++)
+               tmem_ld_cols<P * C>(lanes + (uint32_t)((S * ty + hh * DH + dd) * P * C), rowv[dd]);
+#pragma unroll
+            for (int tx = 0; tx < P / S; tx++) {
+               float old[DH][S][C];
+               bool in[DH][S];
+#pragma unroll
+               for (int dd = 0; dd < DH; dd++) {
+                  const int ky = S * ty + hh * DH + dd;
+                  const int py = yImg0 + ky;
+#pragma unroll
+                  for (int dx = 0; dx < S; dx++) {
+                     const int kx = S * tx + dx;
+                     const int px = xImg0 + kx;
+                     in[dd][dx] = py >= 0 && py < g.inNy && px >= 0 && px < g.inNx;
+                     const int o = (S * y1 + ky) * RP + (S * x1 + kx) * C;
+#pragma unroll
+                     for (int c = 0; c < C; c++) old[dd][dx][c] = in[dd][dx] ? fold[o + c] : 0.0f;
+                  }
+               }
+#pragma unroll
+               for (int dd = 0; dd < DH; dd++) {
+                  const int ky = S * ty + hh * DH + dd;
+#pragma unroll
+                  for (int dx = 0; dx < S; dx++) {
+                     const int kx = S * tx + dx;
+                     const int o = (S * y1 + ky) * RP + (S * x1 + kx) * C;
+                     if (in[dd][dx]) {
+#pragma unroll
+                        for (int c = 0; c < C; c++) fold[o + c] = __fadd_rn(old[dd][dx][c], -rowv[dd][kx * C + c]);
+                     }
+                  }
+               }
+               named_bar_sync(1, EPI);
+            }
+         }
+         tc_fence_before();  // the D2 reads are complete before the next block's aFull
+         fence_proxy_async_smem();
+         named_bar_sync(1, EPI);
+         if (tid == 0) {
+            bulk_store(bandsOut + (((size_t)b * g.MB + mb) * nFH + fh) * fp.bandFloats, fold, bandBytes);
+            bulk_commit();
+            bulk_wait_read_all();
+            mbar_arrive(&foldFree);
+         }
+         return true;
+      };
+      int kIm = nBlk - 1 - lagV;
+      if (kIm < 1) kIm = 1;
+      if (kIm > nBlk - 1) kIm = nBlk - 1;
+      bool go = myTiles > 0 && im2col(0), dead = false;
+      for (int q = 0; go && q < Q; q++) {
+         const int ti = q / nBlk, nb = q % nBlk;
+         int b, mb, fh;
+         tile_of(ti, b, mb, fh);
+         const int sv = q % nV, a = q % kAcc;
+         const int f0 = fh * fp.FT + nb * kPostNT, rowV = b * g.Npos + mb * 128;
+         if (nb == nBlk - 1) x_prefetch(ti);
+         int okw = !dead;
+         if (lane == 0 && okw)
+            okw = wait_or_abort(&accFull[a], (uint32_t)((q / kAcc) & 1)) &&
+                  wait_or_abort(&vFull[sv], (uint32_t)((q / nV) & 1));
+         okw = __shfl_sync(0xffffffffu, okw, 0);
+         dead = !okw;
+         if (okw) {
+            tc_fence_after();
+            float d[32], vo[32];
+            tmem_ld32(tmem + a * kPostNT + ((uint32_t)(32 * qd) << 16) + 32 * h, d);
+            tc_fence_before();
+            if (lane == 0) mbar_arrive(&accEmpty[a]);
+            uint8_t *vsub = smem + fp.offVT[0] + sv * 32768u + h * 16384 + 32 * qd * 128;
+            uint8_t *vt = vsub + lane * 128;
+#pragma unroll
+            for (int qq = 0; qq < 8; qq++) {
+               const float4 t4 = *reinterpret_cast<const float4 *>(vt + ((qq ^ (pw & 7)) << 4));
+               vo[4 * qq] = t4.x;
+               vo[4 * qq + 1] = t4.y;
+               vo[4 * qq + 2] = t4.z;
+               vo[4 * qq + 3] = t4.w;
+            }
+            float vn[32], an[32];
+            const float om = 1.0f - g.e;
+            if (g.simple) {
+#pragma unroll
+               for (int jj = 0; jj < 32; jj++) {
+                  const float ao = vo[jj] < g.VThresh ? g.AMin : vo[jj] - g.AShift;
+                  vn[jj] = fmaf(g.e, vo[jj], om * (d[jj] + g.si * ao));
+                  an[jj] = vn[jj] < g.VThresh ? g.AMin : vn[jj] - g.AShift;
+               }
+            } else {
+#pragma unroll
+               for (int jj = 0; jj < 32; jj++) {
+                  vn[jj] = fmaf(g.e, vo[jj], om * (d[jj] + g.si * thresh(vo[jj], g)));
+                  an[jj] = thresh(vn[jj], g);
+               }
+            }
+            if (lane == 0 && pendingV >= 0) {
+               bulk_wait_read_all();
+               mbar_arrive(&vEmpty[pendingV]);
+            }
+            __syncwarp();
+#pragma unroll
+            for (int qq = 0; qq < 8; qq++)
+               *reinterpret_cast<float4 *>(vt + ((qq ^ (pw & 7)) << 4)) =
+                     make_float4(vn[4 * qq], vn[4 * qq + 1], vn[4 * qq + 2], vn[4 * qq + 3]);
+            // A_q into the shared A tile once GEMM2 of block q - 1 has read it: row pw (128 B,
+            // 128-byte swizzle), 16-byte chunks 4h .. 4h + 3
+            int oka = 1;
+            if (lane == 0 && q >= 1) oka = wait_or_abort(&aEmpty, (uint32_t)((q - 1) & 1));
+            oka = __shfl_sync(0xffffffffu, oka, 0);
+            if (oka) {
+               uint8_t *arow = smem + fp.offAop + pw * 128;
+#pragma unroll
+               for (int c = 0; c < 4; c++)
+                  *reinterpret_cast<uint4 *>(arow + (((4 * h + c) ^ (pw & 7)) << 4)) =
+                        make_uint4(pack2(an[8 * c], an[8 * c + 1]), pack2(an[8 * c + 2], an[8 * c + 3]),
+                                   pack2(an[8 * c + 4], an[8 * c + 5]), pack2(an[8 * c + 6], an[8 * c + 7]));
+            }
+            if (writeA) {  // the activity for the kernels of a later unfused step
+               bf16 *ag = A + (size_t)(rowV + pw) * g.F + f0 + 32 * h;
+               uint4 *lg = reinterpret_cast<uint4 *>(Alo + (size_t)(rowV + pw) * g.F + f0 + 32 * h);
+#pragma unroll
+               for (int t = 0; t < 2; t++)
+                  st_global_32B(ag + 16 * t,
+                                make_uint4(pack2(an[16 * t], an[16 * t + 1]), pack2(an[16 * t + 2], an[16 * t + 3]),
+                                           pack2(an[16 * t + 4], an[16 * t + 5]), pack2(an[16 * t + 6], an[16 * t + 7])),
+                                make_uint4(pack2(an[16 * t + 8], an[16 * t + 9]), pack2(an[16 * t + 10], an[16 * t + 11]),
+                                           pack2(an[16 * t + 12], an[16 * t + 13]),
+                                           pack2(an[16 * t + 14], an[16 * t + 15])));
+#pragma unroll
+               for (int t = 0; t < 4; t++) {
+                  float l[8];
+#pragma unroll
+                  for (int u = 0; u < 8; u++) l[u] = an[8 * t + u] - __bfloat162float(__float2bfloat16_rn(an[8 * t + u]));
+                  lg[t] = make_uint4(pack2(l[0], l[1]), pack2(l[2], l[3]), pack2(l[4], l[5]), pack2(l[6], l[7]));
+               }
+            }
+            fence_proxy_async_smem();
+            __syncwarp();
+            if (lane == 0) {
+               if (oka) mbar_arrive(&aFull);
+               bulk_store(V + v_index(g, b, mb * 128 + 32 * qd, f0 + 32 * h), vsub, 4096);
+               bulk_commit();
+               if (nV == 1) {
+                  bulk_wait_read_all();
+                  mbar_arrive(&vEmpty[sv]);
+               }
+            }
+            pendingV = nV == 1 ? -1 : sv;
+            dead = !oka;
+         }
+         if (nb == kIm && ti + 1 < myTiles) go = im2col(ti + 1);
+         if (go && nb == nBlk - 1) go = fold_tile(ti);
+      }
+      if (lane == 0) bulk_wait_all();
+   }
+   __syncthreads();
+   if (tid == 0 && abortFlag) atomicExch(err, 1);
+   tc_fence_before();
+   __syncthreads();
+   if (warp == 0) tmem_dealloc(tmem, 512);
+}
+
+// x into the zero-bordered padded layout of the residual (kernel F starts its bands from it).
+__global__ void pad_x_kernel(LcaGeom g, int C, int E, int rowsPad, int RP, const float *__restrict__ x,
+                             float *__restrict__ xpad) {
+   const size_t n = (size_t)g.nb * rowsPad * RP;
+   const int rowElems = g.inNx * C;
+   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+      const int col = (int)(i % RP);
+      const size_t r = i / RP;
+      const int yp = (int)(r % rowsPad), b = (int)(r / rowsPad);
+      const int ye = yp - E, j = col - E * C;
+      xpad[i] = (ye >= 0 && ye < g.inNy && j >= 0 && j < rowElems) ? x[((size_t)b * g.inNy + ye) * rowElems + j] : 0.0f;
+   }
 }
 
 // -------------------------------------------------------------------------------------------
@@ -919,10 +1487,15 @@ struct pvgpu_lca_solver {
    CUtensorMap tmA, tmAlo, tmWtH, tmWtloH, tmW, tmWlo, tmAst;  // tmWtH*: half-height W^T tiles
    PostPlan plan, planX3;
    ReconPlan rplan, rplanX3;
+   FusePlan fplan;
+   float *bands = nullptr;  // kernel F's bands, two buffers (a step reads one and writes the other)
+   float *xpad = nullptr;   // x in the padded layout (kernel F)
+   size_t bandsPerBuf = 0;  // floats in one band buffer (sized for 128-feature tiles)
    bool padValid = false;  // rpad holds the residual of the last step (BF16 form) rather than partials
    bool weightsSet = false;
    // optional per-kernel timing: events before kernel R, between R and P, after P
    std::vector<cudaEvent_t> ev;
+   std::vector<uint8_t> evKind;  // per recorded step: 0 kernels R + P, 1 R + F, 2 F alone
    size_t evNext = 0;
    bool profiling = false;
    // the BF16 run as one CUDA graph: captured on capStream, replayed on the caller's stream;
@@ -935,7 +1508,7 @@ struct pvgpu_lca_solver {
    // the graph's schedule: one chain of kernels over the batch, or two independent chains over
    // the two halves captured as parallel graph branches (one half's kernels fill the ramp and
    // tail of the other's); caps on the persistent grids; programmatic edges within a chain
-   pvgpu_lca_schedule sched = {1, 0, 0, 1};
+   pvgpu_lca_schedule sched = {1, 0, 0, 1, 1};
    LcaHalf half[2];
    cudaStream_t capStream2 = nullptr;
    cudaEvent_t forkEv = nullptr, joinEv = nullptr;
@@ -975,6 +1548,7 @@ PostPlan post_plan_for(const LcaGeom &g, int S, int P, int C, bool x3, int numSm
       pl.offVT[sl] = o;
       if (sl < nV) o = al(o + vtB);
    }
+   pl.wStride = (x3 ? 2u : 1u) * al(wB);
    pl.offWin = o;
    o = al(o + winB);
    pl.offA = o;
@@ -1028,6 +1602,7 @@ ReconPlan recon_plan_for(const LcaGeom &g, int S, int P, int C, bool x3, int max
    rp.offX[0] = o;
    o += imgB;
    rp.offX[1] = o;
+   rp.xStride = imgB;
    o += imgB;
    rp.total = o + 1024;
    const int units = (g.nb + 1) / 2;
@@ -1045,15 +1620,83 @@ ReconPlan make_recon_plan(const LcaGeom &g, int S, int P, int C, bool x3, int ma
    return rp;
 }
 
+// Shared-memory layout of kernel F for a feature tile FT and nV V slots; total = 0 when the
+// geometry does not allow it (FT not a multiple of 64 dividing F, or bands reaching past the
+// neighbouring blocks).
+FusePlan fuse_plan_for(const LcaGeom &g, int S, int P, int C, int numSms, int FT, int nV, int nW) {
+   const int KP = P * P * C, NKC = KP / 64, E = (P - S) / 2;
+   auto al = [](uint32_t v) { return (v + 1023u) & ~1023u; };
+   FusePlan fp;
+   std::memset(&fp, 0, sizeof(fp));
+   if (FT < 64 || FT % 64 || g.F % FT || nV < 1 || nV > kMaxVSlots || nW < 2 || nW > 3 ||
+       P - S > S * g.rowsPerBlock || g.MB < 1)
+      return fp;
+   const int nFH = g.F / FT;
+   fp.FT = FT;
+   fp.nV = nV;
+   fp.nW = nW;
+   fp.RP = ((g.inNx + 2 * E) * C + 3) & ~3;
+   fp.rowsPad = g.inNy + 2 * E;
+   fp.RWR = rwin_rows(S, P, g.rowsPerBlock);
+   fp.bandFloats = (uint32_t)(fp.RWR * fp.RP);
+   fp.sliceFloats = (uint32_t)((P - S) * fp.RP);
+   const uint32_t wB = NKC * kPostNT * 128;
+   uint32_t o = 0;
+   fp.offIM = o;
+   o = al(o + NKC * 16384);
+   fp.wStride = al(wB);
+   for (int sl = 0; sl < 3; sl++) {
+      fp.offW[sl] = o;
+      if (sl < nW) o = al(o + wB);
+   }
+   for (int sl = 0; sl < kMaxVSlots; sl++) {
+      fp.offVT[sl] = o;
+      if (sl < nV) o = al(o + 32768);
+   }
+   fp.offAop = o;
+   o = al(o + 16384);
+   fp.offStage = o;
+   o += nFH * fp.bandFloats * 4;
+   fp.offTop = o;
+   o += nFH * fp.sliceFloats * 4;
+   fp.offBot = o;
+   o += nFH * fp.sliceFloats * 4;
+   fp.offFold = fp.offStage;  // the fold runs in the stage once the next tile's im2col has read it
+   o = al(o);
+   fp.total = o + 1024;
+   const int nTiles = g.nb * g.MB * nFH;
+   fp.G = numSms < nTiles ? numSms : nTiles;
+   return fp;
+}
+
+// The default: 256-feature tiles (or the largest multiple of 64 dividing F), the deepest V ring
+// that fits with two weight slots.
+FusePlan make_fuse_plan(const LcaGeom &g, int S, int P, int C, int numSms) {
+   FusePlan fp;
+   std::memset(&fp, 0, sizeof(fp));
+   for (int FT = std::min(256, g.F); FT >= 64; FT -= 64) {
+      if (g.F % FT || FT % 64) continue;
+      for (int nV = kMaxVSlots; nV >= 1; nV--) {
+         fp = fuse_plan_for(g, S, P, C, numSms, FT, nV, 2);
+         if (fp.total && fp.total <= kSmemBudget) return fp;
+      }
+   }
+   std::memset(&fp, 0, sizeof(fp));
+   return fp;
+}
+
 // The launch arguments of one timestep over a batch view (the whole batch or one half).
 struct StepArgs {
    LcaGeom g;
    ReconPlan rp;
    PostPlan pl;
+   FusePlan fp;
    const CUtensorMap *tmA, *tmAlo, *tmAst, *tmWtH, *tmWtloH, *tmW, *tmWlo;
    const float *x;
    float *rpad, *V;
    bf16 *A, *Alo;
+   float *bands[2];
+   float *xpad;
    int *err;
 };
 
@@ -1068,6 +1711,14 @@ void size_grids(const pvgpu_lca_solver *s, int nb, bool x3, ReconPlan &rp, PostP
    pl.G = std::min(ctas, nTiles);
 }
 
+void size_fuse_grid(const pvgpu_lca_solver *s, int nb, FusePlan &fp) {
+   if (!fp.FT) return;
+   const int nTiles = nb * s->g.MB * (s->g.F / fp.FT);
+   int ctas = g_num_sms;
+   if (s->sched.postCtas > 0) ctas = std::min(ctas, s->sched.postCtas);
+   fp.G = std::min(ctas, nTiles);
+}
+
 // view = -1: the whole batch; 0 / 1: that half.
 StepArgs step_args(const pvgpu_lca_solver *s, int view, const float *x, bool x3) {
    StepArgs a;
@@ -1076,14 +1727,17 @@ StepArgs step_args(const pvgpu_lca_solver *s, int view, const float *x, bool x3)
    a.rp = x3 ? s->rplanX3 : s->rplan;
    a.pl = x3 ? s->planX3 : s->plan;
    size_grids(s, a.g.nb, x3, a.rp, a.pl);
-   if (h) {
-      // The two chains' kernels never share an SM: with two CTAs on one SM, a kernel R CTA
-      // (which takes all 512 TMEM columns) could block in its allocation behind a CTA of the
-      // other chain that in turn waits, through its own chain, on that kernel R's pair.  More
-      // than half of the SM's shared memory per CTA rules the pairing out.
-      a.rp.total = std::max(a.rp.total, kSmemHalfSm);
-      a.pl.total = std::max(a.pl.total, kSmemHalfSm);
-   }
+   a.fp = s->fplan;
+   size_fuse_grid(s, a.g.nb, a.fp);
+   // Kernels R and F take all 512 TMEM columns, whose allocation waits without a bound: a CTA
+   // of either never shares an SM (more than half of the SM's shared memory per CTA), or two
+   // kernel R clusters placed across the same two SMs could each hold one SM's TMEM while
+   // waiting for the other at their cluster barrier.  With two chains kernel P (256 columns)
+   // gets an SM to itself as well: a CTA of one chain must not wait for TMEM held by a CTA that
+   // waits, through its own chain, on the first one.
+   a.rp.total = std::max(a.rp.total, kSmemHalfSm);
+   a.fp.total = std::max(a.fp.total, kSmemHalfSm);
+   if (h) a.pl.total = std::max(a.pl.total, kSmemHalfSm);
    const size_t i0 = h ? (size_t)h->img0 : 0;
    const size_t state = (size_t)s->g.Npos * s->g.F;
    a.tmA = h ? &h->tmA : &s->tmA;
@@ -1098,6 +1752,10 @@ StepArgs step_args(const pvgpu_lca_solver *s, int view, const float *x, bool x3)
    a.V = s->V + i0 * state;
    a.A = s->A + i0 * state;
    a.Alo = s->Alo + i0 * state;
+   // bands: [image][block][feature tile][RWR x RP] per buffer
+   const size_t perImage = a.fp.FT ? (size_t)s->g.MB * (s->g.F / a.fp.FT) * a.fp.bandFloats : 0;
+   for (int k = 0; k < 2; k++) a.bands[k] = s->bands ? s->bands + k * s->bandsPerBuf + i0 * perImage : nullptr;
+   a.xpad = s->xpad ? s->xpad + i0 * (size_t)a.rp.rowsPad * a.rp.RP : nullptr;
    a.err = s->err;
    return a;
 }
@@ -1106,42 +1764,61 @@ template <int S, int P, int C>
 struct Launcher {
    // shared-memory limits of both kernels (once, at create: not inside a stream capture)
    static pvgpu_status set_attrs(const pvgpu_lca_solver *) {
-      const void *fns[4] = {reinterpret_cast<const void *>(recon_tc_kernel<S, P, C, false>),
+      const void *fns[5] = {reinterpret_cast<const void *>(recon_tc_kernel<S, P, C, false>),
                             reinterpret_cast<const void *>(recon_tc_kernel<S, P, C, true>),
                             reinterpret_cast<const void *>(post_tc_kernel<S, P, C, false>),
-                            reinterpret_cast<const void *>(post_tc_kernel<S, P, C, true>)};
-      for (int i = 0; i < 4; i++) {
+                            reinterpret_cast<const void *>(post_tc_kernel<S, P, C, true>),
+                            reinterpret_cast<const void *>(step_tc_kernel<S, P, C>)};
+      for (int i = 0; i < 5; i++) {
          cudaError_t e = cudaFuncSetAttribute(fns[i], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBudget);
          if (e != cudaSuccess) return pvgpu::record_cuda_error(e, "lca kernel attributes");
       }
       return PVGPU_OK;
    }
-   // One LCA timestep of a batch view: kernel R then kernel P, each launched with programmatic
-   // stream serialisation (unless the schedule turns it off), so that its set-up overlaps the
-   // tail of the kernel before it.
-   template <bool X3>
-   static pvgpu_status step(const StepArgs &a, cudaStream_t st, cudaEvent_t mid, bool programmatic) {
-      cudaLaunchAttribute attr[1];
+   // Launches over a batch view, each with programmatic stream serialisation unless the
+   // schedule (or per-kernel timing, which keeps the kernels apart) turns it off, so that its
+   // set-up overlaps the tail of the kernel before it.
+   static cudaLaunchConfig_t config(int grid, uint32_t smem, cudaStream_t st, bool programmatic,
+                                    cudaLaunchAttribute *attr, int threads = 320) {
       attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
       attr[0].val.programmaticStreamSerializationAllowed = 1;
-      cudaLaunchConfig_t cr = {};
-      cr.gridDim = dim3(a.rp.G);
-      cr.blockDim = dim3(320);
-      cr.dynamicSmemBytes = a.rp.total;
-      cr.stream = st;
-      cr.attrs = attr;
-      cr.numAttrs = (mid || !programmatic) ? 0 : 1;  // per-kernel timing keeps the kernels apart
-      cudaError_t e = cudaLaunchKernelEx(&cr, recon_tc_kernel<S, P, C, X3>, *a.tmA, *a.tmAlo, *a.tmWtH, *a.tmWtloH,
-                                         a.g, a.rp, a.x, a.rpad, a.err);
-      if (e != cudaSuccess) return pvgpu::record_cuda_error(e, "lca recon");
-      if (mid) cudaEventRecord(mid, st);
-      cudaLaunchConfig_t cp = cr;
-      cp.gridDim = dim3(a.pl.G);
-      cp.dynamicSmemBytes = a.pl.total;
-      e = cudaLaunchKernelEx(&cp, post_tc_kernel<S, P, C, X3>, *a.tmW, *a.tmWlo, *a.tmAst, a.g, a.pl,
-                             (const float *)a.rpad, a.V, a.A, a.Alo, a.err);
-      if (e != cudaSuccess) return pvgpu::record_cuda_error(e, "lca post");
-      return PVGPU_OK;
+      cudaLaunchConfig_t c = {};
+      c.gridDim = dim3(grid);
+      c.blockDim = dim3(threads);
+      c.dynamicSmemBytes = smem;
+      c.stream = st;
+      c.attrs = attr;
+      c.numAttrs = programmatic ? 1 : 0;
+      return c;
+   }
+   // kernel R: the residual x - W^T a into the padded layout
+   static pvgpu_status launch_R(const StepArgs &a, bool x3, cudaStream_t st, bool programmatic) {
+      cudaLaunchAttribute attr[1];
+      cudaLaunchConfig_t c = config(a.rp.G, a.rp.total, st, programmatic, attr);
+      cudaError_t e = x3 ? cudaLaunchKernelEx(&c, recon_tc_kernel<S, P, C, true>, *a.tmA, *a.tmAlo, *a.tmWtH,
+                                              *a.tmWtloH, a.g, a.rp, a.x, a.rpad, a.err)
+                         : cudaLaunchKernelEx(&c, recon_tc_kernel<S, P, C, false>, *a.tmA, *a.tmAlo, *a.tmWtH,
+                                              *a.tmWtloH, a.g, a.rp, a.x, a.rpad, a.err);
+      return e == cudaSuccess ? PVGPU_OK : pvgpu::record_cuda_error(e, "lca recon");
+   }
+   // kernel P: post delivery of the residual and the LCA update
+   static pvgpu_status launch_P(const StepArgs &a, bool x3, cudaStream_t st, bool programmatic) {
+      cudaLaunchAttribute attr[1];
+      cudaLaunchConfig_t c = config(a.pl.G, a.pl.total, st, programmatic, attr);
+      cudaError_t e = x3 ? cudaLaunchKernelEx(&c, post_tc_kernel<S, P, C, true>, *a.tmW, *a.tmWlo, *a.tmAst, a.g,
+                                              a.pl, (const float *)a.rpad, a.V, a.A, a.Alo, a.err)
+                         : cudaLaunchKernelEx(&c, post_tc_kernel<S, P, C, false>, *a.tmW, *a.tmWlo, *a.tmAst, a.g,
+                                              a.pl, (const float *)a.rpad, a.V, a.A, a.Alo, a.err);
+      return e == cudaSuccess ? PVGPU_OK : pvgpu::record_cuda_error(e, "lca post");
+   }
+   // kernel F: a whole timestep; mode 0 reads kernel R's residual, mode 1 the bands in rin
+   static pvgpu_status launch_F(const StepArgs &a, int mode, int writeA, const float *rin, float *bout,
+                                cudaStream_t st, bool programmatic) {
+      cudaLaunchAttribute attr[1];
+      cudaLaunchConfig_t c = config(a.fp.G, a.fp.total, st, programmatic, attr, 352);
+      cudaError_t e = cudaLaunchKernelEx(&c, step_tc_kernel<S, P, C>, *a.tmW, a.g, a.fp, mode, writeA, rin, bout,
+                                         (const float *)a.xpad, a.V, a.A, a.Alo, a.err);
+      return e == cudaSuccess ? PVGPU_OK : pvgpu::record_cuda_error(e, "lca fused step");
    }
    // clusters of two recon CTAs that can be resident at once (one CTA per SM)
    static int max_pairs(const ReconPlan &rp, bool x3) {
@@ -1166,9 +1843,7 @@ struct Launcher {
       const uint32_t pt = x3 ? s->planX3.total : s->plan.total;
       return (x3 ? s->rplanX3.total : s->rplan.total) <= kSmemBudget && pt && pt <= kSmemBudget;
    }
-   static pvgpu_status run_step(const StepArgs &a, bool x3, cudaStream_t st, cudaEvent_t mid, bool programmatic) {
-      return x3 ? step<true>(a, st, mid, programmatic) : step<false>(a, st, mid, programmatic);
-   }
+
 };
 
 template <typename Fn>
@@ -1179,6 +1854,60 @@ pvgpu_status dispatch(int S, int P, int C, Fn &&fn) {
    return PVGPU_ERR_UNSUPPORTED_SHAPE;
 }
 
+// Whether a BF16 run of n steps (the last m BF16x3) takes kernel F: it needs the fused plan,
+// the schedule's consent and at least two fused steps (the run's final BF16 step and its
+// BF16x3 steps run as kernels R + P, which leave the residual for the energy probe).
+bool use_fusion(const pvgpu_lca_solver *s, int n, int m) {
+   const int nF = n - m - (m == 0 ? 1 : 0);
+   return s->sched.fused && s->bands && s->fplan.total && s->fplan.total <= kSmemBudget && nF >= 2;
+}
+
+// One BF16 run over a batch view, launched on st.  With kernel F: x padded once; timestep 1 =
+// kernel R + kernel F reading R's residual (mode 0); then kernel F alone reading the bands of
+// the step before (mode 1); the last fused step also writes A and its low half for the
+// kernels R that follow.  Every other step is kernel R + kernel P.  With prof, three events
+// per timestep: before it, after its kernel R (or at once), after it.
+pvgpu_status enqueue_run(pvgpu_lca_solver *s, const float *x, int n, int m, int view, cudaStream_t st, bool prof) {
+   const bool fuse = use_fusion(s, n, m);
+   const int nF = fuse ? n - m - (m == 0 ? 1 : 0) : 0;
+   return dispatch(s->S, s->P, s->C, [&](auto L) -> pvgpu_status {
+      const StepArgs a16 = step_args(s, view, x, false), a3 = step_args(s, view, x, true);
+      const bool pg = s->sched.programmatic != 0 && !prof;
+      if (fuse) {
+         const int E = (s->P - s->S) / 2;
+         pad_x_kernel<<<g_num_sms * 4, 256, 0, st>>>(a16.g, s->C, E, a16.rp.rowsPad, a16.rp.RP, a16.x, a16.xpad);
+         cudaError_t e = cudaGetLastError();
+         if (e != cudaSuccess) return pvgpu::record_cuda_error(e, "lca pad x");
+      }
+      pvgpu_status r = PVGPU_OK;
+      for (int t = 0; t < n && r == PVGPU_OK; t++) {
+         const bool x3 = t >= n - m;
+         const StepArgs &a = x3 ? a3 : a16;
+         const bool rec = prof && s->evNext + 3 <= s->ev.size();
+         if (rec) cudaEventRecord(s->ev[s->evNext], st);
+         uint8_t kind = 0;
+         if (t < nF) {
+            if (t == 0) r = L.launch_R(a, false, st, pg);
+            if (rec) cudaEventRecord(s->ev[s->evNext + 1], st);
+            if (r == PVGPU_OK)
+               r = L.launch_F(a, t == 0 ? 0 : 1, t == nF - 1 ? 1 : 0, t == 0 ? a.rpad : a.bands[(t - 1) & 1],
+                              a.bands[t & 1], st, pg);
+            kind = t == 0 ? 1 : 2;
+         } else {
+            r = L.launch_R(a, x3, st, pg);
+            if (rec) cudaEventRecord(s->ev[s->evNext + 1], st);
+            if (r == PVGPU_OK) r = L.launch_P(a, x3, st, pg);
+         }
+         if (rec) {
+            cudaEventRecord(s->ev[s->evNext + 2], st);
+            s->evKind[s->evNext / 3] = kind;
+            s->evNext += 3;
+         }
+      }
+      return r;
+   });
+}
+
 void free_solver(pvgpu_lca_solver *s) {
    for (cudaEvent_t e : s->ev) cudaEventDestroy(e);
    if (s->graph) cudaGraphExecDestroy(s->graph);
@@ -1186,7 +1915,8 @@ void free_solver(pvgpu_lca_solver *s) {
    if (s->capStream2) cudaStreamDestroy(s->capStream2);
    if (s->forkEv) cudaEventDestroy(s->forkEv);
    if (s->joinEv) cudaEventDestroy(s->joinEv);
-   void *ptrs[] = {s->V, s->partials, s->rpad, s->A32, s->W32, s->Wt32, s->A, s->Alo, s->W, s->Wlo, s->Wt, s->Wtlo, s->err};
+   void *ptrs[] = {s->V,   s->partials, s->rpad, s->A32, s->W32, s->Wt32,  s->A,
+                   s->Alo, s->W,        s->Wlo,  s->Wt,  s->Wtlo, s->bands, s->xpad, s->err};
    for (void *p : ptrs)
       if (p) cudaFree(p);
    delete s;
@@ -1199,6 +1929,7 @@ void free_solver(pvgpu_lca_solver *s) {
 struct TunedShapes {
    int post[2][4];
    int recon[2];
+   int fuse[3];  // kernel F {FT, nV, nW}; FT = 0: none
    pvgpu_lca_schedule sched;
 };
 
@@ -1211,6 +1942,10 @@ std::array<int, 10> tune_key(const pvgpu_lca_solver *s) {
 }
 
 void set_shapes(pvgpu_lca_solver *s, const TunedShapes &t) {
+   if (t.fuse[0] && s->bands) {
+      FusePlan fp = fuse_plan_for(s->g, s->S, s->P, s->C, g_num_sms, t.fuse[0], t.fuse[1], t.fuse[2]);
+      if (fp.total && fp.total <= kSmemBudget) s->fplan = fp;
+   }
    for (int x3 = 0; x3 < 2; x3++) {
       const int *q = t.post[x3];
       PostPlan pl = post_plan_for(s->g, s->S, s->P, s->C, x3 != 0, g_num_sms, q[0], q[1], q[2], q[3]);
@@ -1341,6 +2076,23 @@ extern "C" pvgpu_status pvgpu_lca_solver_create(const pvgpu_lca_solver_desc *d, 
    }
    s->plan = make_post_plan(g, S, P, C, false, g_num_sms);
    s->planX3 = make_post_plan(g, S, P, C, true, g_num_sms);
+   s->fplan = make_fuse_plan(g, S, P, C, g_num_sms);
+   if (s->fplan.total) {
+      // band buffers sized for the smallest feature tile that divides F (the most bands)
+      int ftMin = 0;
+      for (int FT = 64; FT <= g.F && !ftMin; FT += 64)
+         if (g.F % FT == 0) ftMin = FT;
+      s->bandsPerBuf = (size_t)g.nb * g.MB * (g.F / ftMin) * s->fplan.bandFloats;
+      if (cudaMalloc(&s->bands, 2 * s->bandsPerBuf * 4) != cudaSuccess ||
+          cudaMalloc(&s->xpad, nPad * 4) != cudaSuccess) {
+         cudaGetLastError();  // no fused steps
+         if (s->bands) cudaFree(s->bands);
+         if (s->xpad) cudaFree(s->xpad);
+         s->bands = nullptr;
+         s->xpad = nullptr;
+         std::memset(&s->fplan, 0, sizeof(s->fplan));
+      }
+   }
    s->rplan = make_recon_plan(g, S, P, C, false, g_num_sms / 2);
    s->rplanX3 = make_recon_plan(g, S, P, C, true, g_num_sms / 2);
    s->maxPairs[0] = s->maxPairs[1] = g_num_sms / 2;
@@ -1451,29 +2203,21 @@ extern "C" pvgpu_status pvgpu_lca_solver_run(pvgpu_lca_solver *s, const float *x
       if (!x3ok) return PVGPU_ERR_UNSUPPORTED_SHAPE;
    }
    if (numSteps > 0 && !s->profiling && s->capStream) {
-      // the whole run as one graph of 2 x numSteps kernel nodes (programmatic edges between them)
+      // the whole run as one CUDA graph (programmatic edges between the kernels of a chain)
       if (!s->graph || s->graphX != x || s->graphSteps != numSteps || s->graphX3 != numX3Steps) {
          if (s->graph) cudaGraphExecDestroy(s->graph);
          s->graph = nullptr;
          PVGPU_CUDA(cudaStreamBeginCapture(s->capStream, cudaStreamCaptureModeThreadLocal), "lca graph capture");
          pvgpu_status r = PVGPU_OK;
-         const bool two = s->sched.chains == 2;
-         if (two) {  // the second half's chain on a branch of its own, joined at the end
+         if (s->sched.chains == 2) {  // the second half's chain on a branch of its own, joined at the end
             cudaEventRecord(s->forkEv, s->capStream);
             cudaStreamWaitEvent(s->capStream2, s->forkEv, 0);
-         }
-         for (int t = 0; t < numSteps && r == PVGPU_OK; t++) {
-            const bool x3 = t >= numSteps - numX3Steps;
-            for (int c = 0; c < (two ? 2 : 1) && r == PVGPU_OK; c++) {
-               const StepArgs a = step_args(s, two ? c : -1, x, x3);
-               r = dispatch(s->S, s->P, s->C, [&](auto L) {
-                  return L.run_step(a, x3, c ? s->capStream2 : s->capStream, nullptr, s->sched.programmatic != 0);
-               });
-            }
-         }
-         if (two) {
+            r = enqueue_run(s, x, numSteps, numX3Steps, 0, s->capStream, false);
+            if (r == PVGPU_OK) r = enqueue_run(s, x, numSteps, numX3Steps, 1, s->capStream2, false);
             cudaEventRecord(s->joinEv, s->capStream2);
             cudaStreamWaitEvent(s->capStream, s->joinEv, 0);
+         } else {
+            r = enqueue_run(s, x, numSteps, numX3Steps, -1, s->capStream, false);
          }
          cudaGraph_t g = nullptr;
          cudaError_t ee = cudaStreamEndCapture(s->capStream, &g);
@@ -1493,23 +2237,9 @@ extern "C" pvgpu_status pvgpu_lca_solver_run(pvgpu_lca_solver *s, const float *x
          s->graphX3 = numX3Steps;
       }
       PVGPU_CUDA(cudaGraphLaunch(s->graph, st), "lca graph launch");
-      s->stepsRun += numSteps;
-      s->padValid = true;
-      return PVGPU_OK;
-   }
-   for (int t = 0; t < numSteps; t++) {
-      const bool x3 = t >= numSteps - numX3Steps;
-      const bool rec = s->profiling && s->evNext + 3 <= s->ev.size();
-      if (rec) cudaEventRecord(s->ev[s->evNext], st);
-      const StepArgs a = step_args(s, -1, x, x3);
-      pvgpu_status r = dispatch(s->S, s->P, s->C, [&](auto L) {
-         return L.run_step(a, x3, st, rec ? s->ev[s->evNext + 1] : nullptr, s->sched.programmatic != 0);
-      });
+   } else {
+      pvgpu_status r = enqueue_run(s, x, numSteps, numX3Steps, -1, st, s->profiling);
       if (r != PVGPU_OK) return r;
-      if (rec) {
-         cudaEventRecord(s->ev[s->evNext + 2], st);
-         s->evNext += 3;
-      }
    }
    s->stepsRun += numSteps;
    if (numSteps > 0) s->padValid = true;
@@ -1557,6 +2287,7 @@ extern "C" pvgpu_status pvgpu_lca_solver_profile_begin(pvgpu_lca_solver *s, int 
       PVGPU_CUDA(cudaEventCreate(&e), "lca profile");
       s->ev.push_back(e);
    }
+   s->evKind.assign((size_t)maxSteps, 0);
    s->evNext = 0;
    s->profiling = true;
    return PVGPU_OK;
@@ -1565,12 +2296,15 @@ extern "C" pvgpu_status pvgpu_lca_solver_profile_begin(pvgpu_lca_solver *s, int 
 namespace {
 
 // Kernel R and kernel P times summed over n timesteps of x, launched one by one with events.
-pvgpu_status time_steps(pvgpu_lca_solver *s, const float *x, int n, bool x3, void *stream, double *r, double *p) {
+pvgpu_status time_steps(pvgpu_lca_solver *s, const float *x, int n, bool x3, void *stream, double *r, double *p,
+                        double *f = nullptr) {
    pvgpu_status st = pvgpu_lca_solver_profile_begin(s, n);
    if (st != PVGPU_OK) return st;
    st = pvgpu_lca_solver_run(s, x, n, x3 ? n : 0, PVGPU_LCA_BF16, stream);
-   int k = 0;
-   pvgpu_status st2 = pvgpu_lca_solver_profile_end(s, r, p, &k);
+   int k = 0, kf = 0;
+   double fm = 0.0;
+   pvgpu_status st2 = pvgpu_lca_solver_profile_end_fused(s, r, p, &fm, &k, &kf);
+   if (f) *f = kf > 0 ? fm / kf : 1e30;
    return st != PVGPU_OK ? st : st2;
 }
 
@@ -1581,6 +2315,11 @@ extern "C" pvgpu_status pvgpu_lca_solver_autotune(pvgpu_lca_solver *s, const flo
    TunedShapes best;
    const PostPlan keepP[2] = {s->plan, s->planX3};
    const ReconPlan keepR[2] = {s->rplan, s->rplanX3};
+   const int fusedKeep = s->sched.fused;
+   s->sched.fused = 0;  // kernels R and P on every step while their shapes are timed
+   best.fuse[0] = s->fplan.FT;
+   best.fuse[1] = s->fplan.nV;
+   best.fuse[2] = s->fplan.nW;
    for (int x3 = 0; x3 < 2; x3++) {
       PostPlan &cur = x3 ? s->planX3 : s->plan;
       ReconPlan &curR = x3 ? s->rplanX3 : s->rplan;
@@ -1606,6 +2345,7 @@ extern "C" pvgpu_status pvgpu_lca_solver_autotune(pvgpu_lca_solver *s, const flo
             if (st != PVGPU_OK) {
                s->plan = keepP[0];
                s->planX3 = keepP[1];
+               s->sched.fused = fusedKeep;
                return st;
             }
             if (p < bestMs) {
@@ -1631,6 +2371,7 @@ extern "C" pvgpu_status pvgpu_lca_solver_autotune(pvgpu_lca_solver *s, const flo
          if (st != PVGPU_OK) {
             s->rplan = keepR[0];
             s->rplanX3 = keepR[1];
+            s->sched.fused = fusedKeep;
             return st;
          }
          if (r < bestMs) {
@@ -1639,13 +2380,48 @@ extern "C" pvgpu_status pvgpu_lca_solver_autotune(pvgpu_lca_solver *s, const flo
          }
       }
    }
+   s->sched.fused = fusedKeep;
+   // kernel F: every feature tile (multiple of 64 dividing F), V and weight ring depth that fits,
+   // timed on trialSteps + 2 BF16 steps (all but the first and last fused)
+   if (s->bands && s->fplan.total) {
+      const FusePlan keepF = s->fplan;
+      const int fusedWas = s->sched.fused;
+      s->sched.fused = 1;
+      double bestMs = 1e30;
+      for (int FT = 64; FT <= 512 && FT <= s->g.F; FT += 64) {
+         for (int nV = 1; nV <= kMaxVSlots; nV++) {
+            for (int nW = 2; nW <= 3; nW++) {
+               FusePlan fp = fuse_plan_for(s->g, s->S, s->P, s->C, g_num_sms, FT, nV, nW);
+               if (!fp.total || fp.total > kSmemBudget) continue;
+               if ((size_t)s->g.nb * s->g.MB * (s->g.F / FT) * fp.bandFloats > s->bandsPerBuf) continue;
+               s->fplan = fp;
+               double r = 0, p = 0, f = 0;
+               pvgpu_status st = time_steps(s, x, 3, false, stream, &r, &p, &f);  // warm-up
+               if (st == PVGPU_OK) st = time_steps(s, x, trialSteps + 2, false, stream, &r, &p, &f);
+               if (st != PVGPU_OK) {
+                  s->fplan = keepF;
+                  s->sched.fused = fusedWas;
+                  return st;
+               }
+               if (f < bestMs) {
+                  bestMs = f;
+                  best.fuse[0] = FT;
+                  best.fuse[1] = nV;
+                  best.fuse[2] = nW;
+               }
+            }
+         }
+      }
+      s->sched.fused = fusedWas;
+   }
    best.sched = s->sched;
    set_shapes(s, best);
    // the graph schedule: each candidate replayed as a graph of max(trialSteps, 16) BF16 steps,
    // best of two replays
    {
       const int n = std::max(trialSteps, 16);
-      const pvgpu_lca_schedule cands[4] = {{1, 0, 0, 1}, {1, 0, 0, 0}, {2, 0, 0, 1}, {2, 0, 0, 0}};
+      const int fz = s->sched.fused;
+      const pvgpu_lca_schedule cands[4] = {{1, 0, 0, 1, fz}, {1, 0, 0, 0, fz}, {2, 0, 0, 1, fz}, {2, 0, 0, 0, fz}};
       cudaStream_t st = pvgpu::as_stream(stream);
       cudaEvent_t e0 = nullptr, e1 = nullptr;
       if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
@@ -1697,9 +2473,31 @@ extern "C" pvgpu_status pvgpu_lca_solver_plan_info(const pvgpu_lca_solver *s, in
    return PVGPU_OK;
 }
 
+extern "C" pvgpu_status pvgpu_lca_solver_fused_plan_info(const pvgpu_lca_solver *s, int *out) {
+   if (!s || !out) return PVGPU_ERR_BAD_ARG;
+   const bool ok = s->bands && s->fplan.total && s->fplan.total <= kSmemBudget;
+   out[0] = ok ? s->fplan.FT : 0;
+   out[1] = ok ? s->fplan.nV : 0;
+   out[2] = ok ? s->fplan.nW : 0;
+   return PVGPU_OK;
+}
+
+extern "C" pvgpu_status pvgpu_lca_solver_set_fused_plan(pvgpu_lca_solver *s, int featureTile, int vSlots, int wSlots) {
+   if (!s) return PVGPU_ERR_BAD_ARG;
+   if (!s->bands) return PVGPU_ERR_UNSUPPORTED_SHAPE;
+   FusePlan fp = fuse_plan_for(s->g, s->S, s->P, s->C, g_num_sms, featureTile, vSlots, wSlots);
+   if (!fp.total || fp.total > kSmemBudget ||
+       (size_t)s->g.nb * s->g.MB * (s->g.F / featureTile) * fp.bandFloats > s->bandsPerBuf)
+      return PVGPU_ERR_UNSUPPORTED_SHAPE;
+   s->fplan = fp;
+   if (s->graph) cudaGraphExecDestroy(s->graph);
+   s->graph = nullptr;
+   return PVGPU_OK;
+}
+
 extern "C" pvgpu_status pvgpu_lca_solver_set_schedule(pvgpu_lca_solver *s, const pvgpu_lca_schedule *sc) {
    if (!s || !sc || (sc->chains != 1 && sc->chains != 2) || sc->reconCtas < 0 || sc->postCtas < 0 ||
-       (sc->programmatic != 0 && sc->programmatic != 1))
+       (sc->programmatic != 0 && sc->programmatic != 1) || (sc->fused != 0 && sc->fused != 1))
       return PVGPU_ERR_BAD_ARG;
    if (sc->chains == 2 && (s->g.nb < 2 || !s->capStream2)) return PVGPU_ERR_UNSUPPORTED_SHAPE;
    s->sched = *sc;
@@ -1714,22 +2512,39 @@ extern "C" pvgpu_status pvgpu_lca_solver_get_schedule(const pvgpu_lca_solver *s,
    return PVGPU_OK;
 }
 
-extern "C" pvgpu_status pvgpu_lca_solver_profile_end(pvgpu_lca_solver *s, double *reconMs, double *postMs, int *steps) {
-   if (!s || !reconMs || !postMs || !steps) return PVGPU_ERR_BAD_ARG;
+extern "C" pvgpu_status pvgpu_lca_solver_profile_end_fused(pvgpu_lca_solver *s, double *reconMs, double *postMs,
+                                                           double *fusedMs, int *steps, int *fusedSteps) {
+   if (!s || !reconMs || !postMs || !fusedMs || !steps || !fusedSteps) return PVGPU_ERR_BAD_ARG;
    s->profiling = false;
-   double r = 0.0, p = 0.0;
-   int n = (int)(s->evNext / 3);
+   double r = 0.0, p = 0.0, f = 0.0;
+   int n = (int)(s->evNext / 3), nf = 0;
    if (n > 0) PVGPU_CUDA(cudaEventSynchronize(s->ev[s->evNext - 1]), "lca profile");
    for (int i = 0; i < n; i++) {
       float a = 0.0f, b = 0.0f;
       PVGPU_CUDA(cudaEventElapsedTime(&a, s->ev[3 * i], s->ev[3 * i + 1]), "lca profile");
       PVGPU_CUDA(cudaEventElapsedTime(&b, s->ev[3 * i + 1], s->ev[3 * i + 2]), "lca profile");
       r += a;
-      p += b;
+      if (s->evKind[i] == 0) {
+         p += b;
+      } else {
+         f += b;
+         nf++;
+      }
    }
    *reconMs = r;
    *postMs = p;
+   *fusedMs = f;
    *steps = n;
+   *fusedSteps = nf;
    s->evNext = 0;
    return PVGPU_OK;
+}
+
+extern "C" pvgpu_status pvgpu_lca_solver_profile_end(pvgpu_lca_solver *s, double *reconMs, double *postMs, int *steps) {
+   if (!s || !reconMs || !postMs || !steps) return PVGPU_ERR_BAD_ARG;
+   double f = 0.0;
+   int nf = 0;
+   pvgpu_status st = pvgpu_lca_solver_profile_end_fused(s, reconMs, postMs, &f, steps, &nf);
+   *postMs += f;
+   return st;
 }

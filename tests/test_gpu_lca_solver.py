@@ -225,7 +225,7 @@ def test_lca_bf16_schedules_leave_identical_state(torch, oracle, nb):
     xd = torch.from_numpy(x).cuda()
     s = capi.LcaSolver(nb, ins, v1s, nxp, vth)
     s.set_weights(wd)
-    assert s.schedule() == {"chains": 1, "recon_ctas": 0, "post_ctas": 0, "programmatic": True}
+    assert s.schedule() == {"chains": 1, "recon_ctas": 0, "post_ctas": 0, "programmatic": True, "fused": True}
 
     def state(direct):
         s.reset()
@@ -250,3 +250,98 @@ def test_lca_bf16_schedules_leave_identical_state(torch, oracle, nb):
     one = capi.LcaSolver(1, ins, v1s, nxp, vth)
     with pytest.raises(capi.PvgpuError):
         one.set_schedule(chains=2)  # one image has no second half
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_lca_fused_steps_match_unfused_and_oracle(torch, oracle, name):
+    """Fused timesteps (kernel F: post delivery, update and the reconstruction of the new
+    activity in one launch, residual windows summed from the previous step's bands) against the
+    two-kernel form: the same final energy to 1e-4 relative, V within 1e-3 of max|V|, both within
+    the 1e-3 bar of the FP64 oracle; the profiled run reports the expected number of fused
+    steps; graph replay (one and two chains) equals the kernel-by-kernel run bit for bit."""
+    from openpv_gb300 import capi
+    nb, ins, v1s, nxp, vth, steps, w, x, p = setup(oracle, name)
+    v0 = np.zeros((nb,) + v1s)
+    _, _, _, e64 = oracle.lca_run(p, w.astype(np.float64), x[None].astype(np.float64), steps, v0, f64=True,
+                                  want_recon=False)
+    wd = torch.from_numpy(w).cuda()
+    xd = torch.from_numpy(x).cuda()
+    s = capi.LcaSolver(nb, ins, v1s, nxp, vth)
+    s.set_weights(wd)
+    info = s.fused_plan_info()
+    assert info["feature_tile"] > 0, info
+    e = torch.zeros(nb, dtype=torch.float64, device="cuda")
+
+    def run(fused, x3, n=steps, direct=False, chains=1):
+        s.set_schedule(chains=chains, fused=fused)
+        s.reset()
+        if direct:
+            s.profile_begin(n)
+        s.run(xd, n, x3_steps=x3, precision=capi.LCA_BF16)
+        prof = s.profile_end_fused() if direct else None
+        s.energy(xd, e)
+        v = torch.zeros((nb,) + v1s, device="cuda")
+        s.state(v)
+        torch.cuda.synchronize()
+        assert s.error_flag() == 0
+        return v.cpu().numpy(), e.cpu().numpy().copy(), prof
+
+    for x3 in ((0,) if name == "stride4" else (0, 4)):  # no BF16x3 form for 16 x 16 patches
+        vf, ef, prof = run(True, x3, direct=True)
+        assert prof[3] == steps and prof[4] == steps - x3 - (1 if x3 == 0 else 0), prof
+        vu, eu, prof_u = run(False, x3, direct=True)
+        assert prof_u[4] == 0
+        assert np.abs(ef - eu).max() / np.abs(eu).max() < 1e-4, (ef, eu)
+        assert np.abs(vf - vu).max() <= 1e-3 * np.abs(vu).max()
+        rel = np.abs(ef - e64[-1]) / np.abs(e64[-1])
+        assert rel.max() < 1e-3, rel
+        for chains in ((1, 2) if nb >= 2 else (1,)):
+            vg, _, _ = run(True, x3, chains=chains)
+            assert np.array_equal(vg.view(np.uint32), vf.view(np.uint32)), chains
+    # the shortest fused run: R + F (residual window), F (bands, writes A), R + P
+    vf3, _, _ = run(True, 0, n=3, direct=True)
+    vu3, _, _ = run(False, 0, n=3, direct=True)
+    assert np.abs(vf3 - vu3).max() <= 1e-3 * max(np.abs(vu3).max(), 1e-6)
+
+
+def test_lca_fused_plan_shapes(torch, oracle):
+    """Every fused-kernel shape that fits: the ring depths change nothing (bit-identical state for
+    one feature tile); other feature tiles split the reconstruction into other bands and stay
+    within 1e-3 of max|V| of the two-kernel form."""
+    from openpv_gb300 import capi
+    nb, ins, v1s, nxp, vth, steps, w, x, p = setup(oracle, "colour")
+    wd = torch.from_numpy(w).cuda()
+    xd = torch.from_numpy(x).cuda()
+    s = capi.LcaSolver(nb, ins, v1s, nxp, vth)
+    s.set_weights(wd)
+
+    def state():
+        s.reset()
+        s.run(xd, steps, x3_steps=0, precision=capi.LCA_BF16)
+        v = torch.zeros((nb,) + v1s, device="cuda")
+        s.state(v)
+        torch.cuda.synchronize()
+        assert s.error_flag() == 0
+        return v.cpu().numpy()
+
+    s.set_schedule(fused=False)
+    ref = state()
+    s.set_schedule(fused=True)
+    per_tile = {}
+    for ft in (64, 128):
+        for nv in (1, 2, 3):
+            for nw in (2, 3):
+                try:
+                    s.set_fused_plan(ft, nv, nw)
+                except capi.PvgpuError:
+                    continue
+                assert s.fused_plan_info() == {"feature_tile": ft, "v_slots": nv, "w_slots": nw}
+                v = state()
+                if ft in per_tile:
+                    assert np.array_equal(v.view(np.uint32), per_tile[ft].view(np.uint32)), (ft, nv, nw)
+                else:
+                    per_tile[ft] = v
+                assert np.abs(v - ref).max() <= 1e-3 * np.abs(ref).max(), (ft, nv, nw)
+    assert set(per_tile) == {64, 128}
+    with pytest.raises(capi.PvgpuError):
+        s.set_fused_plan(96, 2, 2)  # not a multiple of 64
