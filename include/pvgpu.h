@@ -496,6 +496,10 @@ pvgpu_status pvgpu_tc_gemm_bf16(const void *A, const void *B, float *C, int M, i
  * operand: C = A * B. */
 pvgpu_status pvgpu_tc_gemm_bf16_kn(const void *A, const void *B, float *C, int M, int N, int K, int *errFlag,
                                    void *stream);
+/* The same as pvgpu_tc_gemm_bf16 with A read by the MMA from tensor memory (each row stored into
+ * its TMEM lane, two K elements per column); 64 <= K <= 256. */
+pvgpu_status pvgpu_tc_gemm_bf16_atmem(const void *A, const void *B, float *C, int M, int N, int K, int *errFlag,
+                                      void *stream);
 
 #ifdef __cplusplus
 }

@@ -126,6 +126,7 @@ def _declare(L):
         "pvgpu_hebbian_dw": (i, [cp, f, vp, vp, vp, vp]),
         "pvgpu_tc_gemm_bf16": (i, [vp, vp, vp, i, i, i, vp, vp]),
         "pvgpu_tc_gemm_bf16_kn": (i, [vp, vp, vp, i, i, i, vp, vp]),
+        "pvgpu_tc_gemm_bf16_atmem": (i, [vp, vp, vp, i, i, i, vp, vp]),
         "pvgpu_lca_solver_create": (i, [C.POINTER(LcaSolverDesc), C.POINTER(vp)]),
         "pvgpu_lca_solver_destroy": (i, [vp]),
         "pvgpu_lca_solver_set_weights": (i, [vp, vp, vp]),
@@ -346,6 +347,12 @@ def hebbian_dw(conn, dw_max, pre_ext, post_ext, dw, stream=None):
 
 def tc_gemm_bf16(A, B, C, M, N, K, err, stream=None):
     check(lib().pvgpu_tc_gemm_bf16(_ptr(A), _ptr(B), _ptr(C), M, N, K, _ptr(err), _stream(stream)), "tc_gemm_bf16")
+
+
+def tc_gemm_bf16_atmem(A, B, C, M, N, K, err, stream=None):
+    """C = A @ B^T with A read by the MMA from tensor memory."""
+    check(lib().pvgpu_tc_gemm_bf16_atmem(_ptr(A), _ptr(B), _ptr(C), M, N, K, _ptr(err), _stream(stream)),
+          "tc_gemm_bf16_atmem")
 
 
 def tc_gemm_bf16_kn(A, B, C, M, N, K, err, stream=None):

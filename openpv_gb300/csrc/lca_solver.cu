@@ -822,16 +822,16 @@ __global__ void __launch_bounds__(320, 1) post_tc_kernel(const __grid_constant__
 struct FusePlan {
    int G;                         // persistent CTAs
    int FT;                        // features per tile (multiple of 64)
-   int nV, nW;                    // V and weight ring slots
+   int nV, nW;                    // V (1..4) and weight (2..3) ring slots
    int RP, rowsPad, RWR;          // padded rows: floats per row, rows per image, rows per band
    uint32_t bandFloats, sliceFloats;
-   uint32_t offIM, offW[3], offVT[kMaxVSlots], offStage, offTop, offBot, offAop, offFold;
+   uint32_t offIM, offW[3], offVT[4], offStage, offTop, offBot, offFold;
    uint32_t wStride;              // offW[s+1] - offW[s]; V slots are 32 KB apart
    uint32_t total;
 };
 
 template <int S, int P, int C>
-__global__ void __launch_bounds__(352, 1) step_tc_kernel(const __grid_constant__ CUtensorMap tmW, LcaGeom g,
+__global__ void __launch_bounds__(608, 1) step_tc_kernel(const __grid_constant__ CUtensorMap tmW, LcaGeom g,
                                                          FusePlan fp, int mode, int writeA,
                                                          const float *__restrict__ rin,
                                                          float *__restrict__ bandsOut,
@@ -840,14 +840,23 @@ __global__ void __launch_bounds__(352, 1) step_tc_kernel(const __grid_constant__
                                                          int *__restrict__ err) {
    constexpr int KP = P * P * C, NKC = KP / 64;
    constexpr uint32_t WBYTES = NKC * kPostNT * 128;
-   constexpr int EPI = 256;
+   constexpr int EPI = 256;  // im2col, fold and band threads: epilogue warps 0-7
+   constexpr int EW = 16;    // epilogue warps for the per-block update: 32 positions x 16 features each
    constexpr int kMaxW = 3;
+   // TMEM columns: two GEMM1 accumulators, D2 (KP), two A tiles of GEMM2 (64 BF16 = 32 columns
+   // each; block q writes tile q % 2 while GEMM2 of block q - 1 reads the other) and, where it
+   // fits, the im2col operand of GEMM1 (KP BF16 = KP / 2 columns) -- the MMAs read both A
+   // operands from TMEM, not shared memory
+   constexpr int kAccF = 2;
+   constexpr uint32_t colD2 = kAccF * kPostNT, colA = colD2 + KP, colIM = colA + 64;
+   constexpr bool IMT = colIM + KP / 2 <= 512;
    static_assert((S * C) % 2 == 0, "window reads are 8-byte pairs");
    static_assert(KP % 16 == 0 && KP <= 256, "GEMM2 is one MMA of N = P*P*C");
    extern __shared__ uint8_t smem_raw[];
    uint8_t *smem = align1024(smem_raw);
-   __shared__ __align__(8) uint64_t stFull, stEmpty, imFull, imEmpty, wFull[kMaxW], wEmpty[kMaxW], vFull[kMaxVSlots],
-         vEmpty[kMaxVSlots], accFull[kAcc], accEmpty[kAcc], aFull, aEmpty, d2Full, foldFree, drain;
+   constexpr int kMaxVF = 4;
+   __shared__ __align__(8) uint64_t stFull, stEmpty, imFull, imEmpty, wFull[kMaxW], wEmpty[kMaxW], vFull[kMaxVF],
+         vEmpty[kMaxVF], accFull[kAccF], accEmpty[kAccF], aFull[2], aEmpty[2], d2Full, foldFree, drain;
    __shared__ uint32_t tmemBase;
    __shared__ volatile int abortFlag;
 
@@ -871,16 +880,20 @@ __global__ void __launch_bounds__(352, 1) step_tc_kernel(const __grid_constant__
          mbar_init(&wFull[i], 1);
          mbar_init(&wEmpty[i], 1);
       }
-      for (int i = 0; i < kMaxVSlots; i++) {
+      for (int i = 0; i < kMaxVF; i++) {
          mbar_init(&vFull[i], 1);
-         mbar_init(&vEmpty[i], 8);
+         mbar_init(&vEmpty[i], EW / 2);  // one arrival per warp pair (the pair's store has read it)
       }
-      for (int i = 0; i < kAcc; i++) {
+      for (int i = 0; i < kAccF; i++) {
          mbar_init(&accFull[i], 1);
-         mbar_init(&accEmpty[i], 8);
+         mbar_init(&accEmpty[i], EW);
       }
-      mbar_init(&aFull, 8);  // one arrival per epilogue warp
-      mbar_init(&aEmpty, 1);
+      // one full / empty pair per TMEM A tile: the epilogue can be two blocks ahead of GEMM2,
+      // which one barrier's parity could not tell apart
+      for (int i = 0; i < 2; i++) {
+         mbar_init(&aFull[i], EW);  // one arrival per epilogue warp
+         mbar_init(&aEmpty[i], 1);
+      }
       mbar_init(&d2Full, 1);
       mbar_init(&foldFree, 1);
       mbar_init(&drain, 1);
@@ -892,7 +905,7 @@ __global__ void __launch_bounds__(352, 1) step_tc_kernel(const __grid_constant__
    __syncthreads();
    tc_fence_after();
    const uint32_t tmem = tmemBase;
-   const uint32_t tmemD2 = tmem + kAcc * kPostNT;
+   const uint32_t tmemD2 = tmem + colD2;
    // Set-up above overlaps the previous kernel's tail; everything below reads the bands or the
    // residual (written by the previous launch) or V (which the previous launch writes).
    griddep_launch_dependents();
@@ -916,23 +929,29 @@ __global__ void __launch_bounds__(352, 1) step_tc_kernel(const __grid_constant__
       return rin + (((size_t)b * g.MB + mb) * nFH + fh) * fp.bandFloats;
    };
 
-   if (warp == 8) {
+   if (warp == EW) {
       // ============================== weight loads ==============================
       if (lane == 0 && Q > 0) {
          prefetch_tmap(&tmW);
          int wIssued = 0;
          bool ok = true;
+         int ti = 0, nb = 0, sw = 0, uw = 0, b = 0, mb = 0, fh = 0;
+         tile_of(0, b, mb, fh);
          for (int q = 0; ok && q < Q; q++) {
-            const int ti = q / nBlk, nb = q % nBlk;
-            int b, mb, fh;
-            tile_of(ti, b, mb, fh);
             const int f0 = fh * fp.FT + nb * kPostNT;
-            const int sw = q % nW, uw = q / nW;
             if (uw > 0 && !(ok = wait_or_abort(&wEmpty[sw], (uint32_t)((uw - 1) & 1)))) break;
             mbar_arrive_expect_tx(&wFull[sw], WBYTES);
             for (int kc = 0; kc < NKC; kc++)
                tma_load_2d(smem + fp.offW[0] + sw * fp.wStride + kc * kPostNT * 128, &tmW, &wFull[sw], kc * 64, f0);
             wIssued = q + 1;
+            if (++sw == nW) {
+               sw = 0;
+               uw++;
+            }
+            if (++nb == nBlk) {
+               nb = 0;
+               if (++ti < myTiles) tile_of(ti, b, mb, fh);
+            }
          }
          if (!ok) {  // the copies still in flight land before shared memory goes away
             for (int sl = 0; sl < nW; sl++) {
@@ -941,7 +960,7 @@ __global__ void __launch_bounds__(352, 1) step_tc_kernel(const __grid_constant__
             }
          }
       }
-   } else if (warp == 10) {
+   } else if (warp == EW + 2) {
       // ============================== V and stage loads ==============================
       if (lane == 0 && Q > 0) {
          int rowsIssued = 0, vIssued = 0;
@@ -977,6 +996,8 @@ __global__ void __launch_bounds__(352, 1) step_tc_kernel(const __grid_constant__
             return wait_or_abort(&stEmpty, (uint32_t)((t - 1) & 1)) &&
                    (t < 2 || wait_or_abort(&foldFree, (uint32_t)((t - 2) & 1)));
          };
+         int ti = 0, nb = 0, sv = 0, uv = 0, b = 0, mb = 0, fh = 0;
+         tile_of(0, b, mb, fh);
          for (int q = 0; ok && q < Q; q++) {
             // the next stage before the first V load that waits for the current tile's epilogue
             while (ok && rowsIssued < myTiles && (rowsIssued - 1) * nBlk + lagV <= q) {
@@ -984,15 +1005,19 @@ __global__ void __launch_bounds__(352, 1) step_tc_kernel(const __grid_constant__
                if (ok) issue_stage(rowsIssued);
             }
             if (!ok) break;
-            const int ti = q / nBlk, nb = q % nBlk;
-            int b, mb, fh;
-            tile_of(ti, b, mb, fh);
             const int f0 = fh * fp.FT + nb * kPostNT;
-            const int sv = q % nV, uv = q / nV;
             if (uv > 0 && !(ok = wait_or_abort(&vEmpty[sv], (uint32_t)((uv - 1) & 1)))) break;
             mbar_arrive_expect_tx(&vFull[sv], 32768);
             bulk_load(smem + fp.offVT[0] + sv * 32768u, V + v_index(g, b, mb * 128, f0), 32768, &vFull[sv]);
             vIssued = q + 1;
+            if (++sv == nV) {
+               sv = 0;
+               uv++;
+            }
+            if (++nb == nBlk) {
+               nb = 0;
+               if (++ti < myTiles) tile_of(ti, b, mb, fh);
+            }
          }
          while (ok && rowsIssued < myTiles) {
             ok = stage_free(rowsIssued);
@@ -1007,58 +1032,97 @@ __global__ void __launch_bounds__(352, 1) step_tc_kernel(const __grid_constant__
             }
          }
       }
-   } else if (warp == 9) {
+   } else if (warp == EW + 1) {
       // ============================== MMA ==============================
+      // An event loop over two in-order streams: GEMM1 of block g1 as soon as its weight tile,
+      // its accumulator and (first block of a tile) the im2col operand are ready; GEMM2 of
+      // block g2 < g1 as soon as the epilogue has written its A tile.  GEMM1 of the next block
+      // therefore never waits behind GEMM2 of an earlier one.  Polls never suspend; a bounded
+      // count of idle polls (or the abort flag) ends the loop.
       if (lane == 0 && Q > 0) {
          const uint32_t idesc1 = idesc_bf16(128, kPostNT), idesc2 = idesc_bf16_bmn(128, KP);
          bool ok = true;
          int issued = 0;
-         // GEMM2 of block q: its A tile times its weight tile (MN-major: 64-tap groups 8 KB apart)
-         auto gemm2 = [&](int q) {
-            const int nb = q % nBlk, sw = q % nW;
-            if (!(ok = wait_or_abort(&aFull, (uint32_t)(q & 1)))) return;
-            tc_fence_after();
-            const uint32_t a0 = smem_u32(smem + fp.offAop), w0 = smem_u32(smem + fp.offW[0] + sw * fp.wStride);
+         int g1 = 0, ti1 = 0, nb1 = 0, sw1 = 0, uw1 = 0;
+         int g2 = 0, nb2 = 0, sw2 = 0;
+         uint32_t idle = 0;
+         while (ok && g2 < Q) {
+            bool did = false;
+            if (g1 < Q) {
+               const int a = g1 & (kAccF - 1);
+               if ((nb1 != 0 || mbar_test(&imFull, (uint32_t)(ti1 & 1))) && mbar_test(&wFull[sw1], (uint32_t)(uw1 & 1)) &&
+                   (g1 < kAccF || mbar_test(&accEmpty[a], (uint32_t)((g1 / kAccF - 1) & 1)))) {
+                  tc_fence_after();
+                  const uint32_t d = tmem + a * kPostNT;
+                  const uint32_t w0 = smem_u32(smem + fp.offW[0] + sw1 * fp.wStride);
+                  for (int kc = 0; kc < NKC; kc++)
 #pragma unroll
-            for (int k = 0; k < 4; k++)
-               mma_bf16(tmemD2, sdesc_sw128(a0 + k * 32), sdesc_sw128_mn(w0 + k * 2048, kPostNT * 128), idesc2,
-                        (nb | k) != 0);
-            mma_commit(&aEmpty);
-            mma_commit(&wEmpty[sw]);
-            if (nb == nBlk - 1) mma_commit(&d2Full);
-            issued++;
-         };
-         for (int q = 0; ok && q < Q; q++) {
-            const int ti = q / nBlk, nb = q % nBlk, sw = q % nW, a = q % kAcc;
-            if (nb == 0 && !(ok = wait_or_abort(&imFull, (uint32_t)(ti & 1)))) break;
-            if (!(ok = wait_or_abort(&wFull[sw], (uint32_t)((q / nW) & 1)))) break;
-            if (q >= kAcc && !(ok = wait_or_abort(&accEmpty[a], (uint32_t)((q / kAcc - 1) & 1)))) break;
-            tc_fence_after();
-            const uint32_t d = tmem + a * kPostNT;
-            const uint32_t a0 = smem_u32(smem + fp.offIM), w0 = smem_u32(smem + fp.offW[0] + sw * fp.wStride);
-            for (int kc = 0; kc < NKC; kc++)
+                     for (int k = 0; k < 4; k++) {
+                        const uint64_t bd = sdesc_sw128(w0 + kc * kPostNT * 128 + k * 32);
+                        if constexpr (IMT)
+                           mma_bf16_ta(d, tmem + colIM + 32 * kc + 8 * k, bd, idesc1, (kc | k) != 0);
+                        else
+                           mma_bf16(d, sdesc_sw128(smem_u32(smem + fp.offIM) + kc * 16384 + k * 32), bd, idesc1,
+                                    (kc | k) != 0);
+                     }
+                  mma_commit(&accFull[a]);
+                  if (nb1 == nBlk - 1) mma_commit(&imEmpty);
+                  issued++;
+                  g1++;
+                  if (++sw1 == nW) {
+                     sw1 = 0;
+                     uw1++;
+                  }
+                  if (++nb1 == nBlk) {
+                     nb1 = 0;
+                     ti1++;
+                  }
+                  did = true;
+               }
+            }
+            if (g2 < g1 && mbar_test(&aFull[g2 & 1], (uint32_t)((g2 >> 1) & 1))) {
+               // GEMM2 of block g2: its A tile (TMEM) times its weight tile read MN-major
+               tc_fence_after();
+               const uint32_t w0 = smem_u32(smem + fp.offW[0] + sw2 * fp.wStride);
+               const uint32_t at = tmem + colA + 32 * (g2 & 1);
 #pragma unroll
                for (int k = 0; k < 4; k++)
-                  mma_bf16(d, sdesc_sw128(a0 + kc * 16384 + k * 32), sdesc_sw128(w0 + kc * kPostNT * 128 + k * 32),
-                           idesc1, (kc | k) != 0);
-            mma_commit(&accFull[a]);
-            if (nb == nBlk - 1) mma_commit(&imEmpty);
-            issued++;
-            if (q >= 1) gemm2(q - 1);
+                  mma_bf16_ta(tmemD2, at + 8 * k, sdesc_sw128_mn(w0 + k * 2048, kPostNT * 128), idesc2,
+                              (nb2 | k) != 0);
+               mma_commit(&aEmpty[g2 & 1]);
+               mma_commit(&wEmpty[sw2]);
+               if (nb2 == nBlk - 1) mma_commit(&d2Full);
+               g2++;
+               if (++sw2 == nW) sw2 = 0;
+               if (++nb2 == nBlk) nb2 = 0;
+               did = true;
+            }
+            if (did) {
+               idle = 0;
+            } else if (abortFlag || ++idle > kWaitLimit) {
+               abortFlag = 1;
+               ok = false;
+            } else if (idle > 16) {
+               __nanosleep(32);  // leave the issue slots to the epilogue warps on this sub-partition
+            }
          }
-         if (ok) gemm2(Q - 1);
          // MMAs still in flight finish before shared memory and TMEM go away
          if (!ok && issued > 0) {
             mma_commit(&drain);
             mbar_wait(&drain, 0);
          }
       }
-   } else if (warp < 8) {
-      // ============================== epilogue (warps 0-7) ==============================
+   } else if (warp < EW) {
+      // ============================== epilogue (warps 0-15) ==============================
       const float *win = reinterpret_cast<const float *>(smem + fp.offStage);
       float *fold = reinterpret_cast<float *>(smem + fp.offFold);
-      const int qd = warp & 3, h = warp >> 2;
+      // block update: warp = (lane quarter qd, 16-feature group h4 of the 64); the two warps of a
+      // 32-feature half (hh2) share its 32 x 32 part of the V chunk, which the second (sub = 1)
+      // stores once both have written it (named barrier 2 + pair)
+      const int qd = warp & 3, h4 = warp >> 2, hh2 = h4 >> 1, sub = h4 & 1;
       const int pw = 32 * qd + lane;
+      const int pairBar = 2 + 2 * qd + hh2;
+      const bool lead = warp < 8;  // im2col, fold, band sums: warps 0-7
       int pendingV = -1;
       auto im2col = [&](int t) {
          if (tid == 0 && wait_or_abort(&stFull, (uint32_t)(t & 1)) && t > 0)
@@ -1091,7 +1155,27 @@ __global__ void __launch_bounds__(352, 1) step_tc_kernel(const __grid_constant__
             }
             named_bar_sync(1, EPI);
          }
-         {
+         if constexpr (IMT) {
+            // ---- BF16 im2col of the window into TMEM: lane p, K element k in column k / 2 ----
+            constexpr int RUN = P * C;
+            constexpr int COLS = (P / 2) * RUN / 2;  // columns per thread (its half of the patch rows)
+            static_assert(RUN % 2 == 0 && COLS % 8 == 0, "im2col columns in groups of 8");
+            tc_fence_after();  // the previous tile's GEMM1s (imEmpty) are done reading
+            const int p = tid & 127, half = tid >> 7;
+            const int yl = p / g.v1Nx, x1 = p % g.v1Nx;
+            const float *src0 = win + (S * yl) * RP + S * x1 * C + half * (P / 2) * RP;
+            const uint32_t t0 = tmem + ((uint32_t)((warp & 3) * 32) << 16) + colIM + half * COLS;
+            uint32_t buf[8];
+#pragma unroll
+            for (int i = 0; i < COLS; i++) {
+               const int ky = i / (RUN / 2), e = 2 * (i % (RUN / 2));
+               const float2 t2 = *reinterpret_cast<const float2 *>(src0 + ky * RP + e);
+               buf[i & 7] = pack2(t2.x, t2.y);
+               if ((i & 7) == 7) tmem_st8(t0 + (i & ~7), buf);
+            }
+            tmem_wait_st();
+            tc_fence_before();
+         } else {
             // ---- BF16 im2col of the window (as kernel P) ----
             constexpr int RUN = P * C;
             constexpr int CPR = RUN / 8;
@@ -1131,9 +1215,7 @@ __global__ void __launch_bounds__(352, 1) step_tc_kernel(const __grid_constant__
       // the start of the tile's last block, so that the loads are in flight during its update
       constexpr int kXPre = 4;  // float4 per thread held in registers; the rest is read at the fold
       float4 xr[kXPre];
-      auto x_prefetch = [&](int t) {
-         int b, mb, fh;
-         tile_of(t, b, mb, fh);
+      auto x_prefetch = [&](int b, int mb, int fh) {
          const int n4 = fh == 0 ? owned_rows(mb) * RP / 4 : 0;
          const float4 *src = reinterpret_cast<const float4 *>(xpad + ((size_t)b * fp.rowsPad + (size_t)S * mb * rpb) * RP);
 #pragma unroll
@@ -1144,9 +1226,7 @@ __global__ void __launch_bounds__(352, 1) step_tc_kernel(const __grid_constant__
       };
       // the fold of tile t's D2 into its band (in the stage, which the next tile's im2col has
       // read), starting from x on the owned rows and 0 elsewhere, and the band store
-      auto fold_tile = [&](int t) {
-         int b, mb, fh;
-         tile_of(t, b, mb, fh);
+      auto fold_tile = [&](int t, int b, int mb, int fh) {
          {
             const int n4 = (int)fp.bandFloats / 4, x4 = fh == 0 ? owned_rows(mb) * RP / 4 : 0;
             float4 *f4 = reinterpret_cast<float4 *>(fold);
@@ -1219,90 +1299,93 @@ __global__ void __launch_bounds__(352, 1) step_tc_kernel(const __grid_constant__
          }
          return true;
       };
+      // The next tile's im2col goes in after block kIm, once the loads of the tile's later blocks
+      // are out, and no earlier than block nBlk - 3: it waits for the tile's last GEMM1, and the
+      // MMA thread runs at most two blocks ahead of the epilogue (GEMM1 of block q + 2 issues,
+      // GEMM2 of block q + 1 then waits for this epilogue), so an earlier im2col would wait
+      // for a GEMM1 that waits for it.
       int kIm = nBlk - 1 - lagV;
-      if (kIm < 1) kIm = 1;
+      if (kIm < nBlk - 3) kIm = nBlk - 3;
+      if (kIm < 0) kIm = 0;
       if (kIm > nBlk - 1) kIm = nBlk - 1;
-      bool go = myTiles > 0 && im2col(0), dead = false;
+      bool go = myTiles > 0 && (!lead || im2col(0)), dead = false;
+      // block q = (tile ti, block nb); V slot sv in its use uv, accumulator a: stepped, not divided
+      int ti = 0, nb = 0, sv = 0, uv = 0, b = 0, mb = 0, fh = 0;
+      if (myTiles > 0) tile_of(0, b, mb, fh);
       for (int q = 0; go && q < Q; q++) {
-         const int ti = q / nBlk, nb = q % nBlk;
-         int b, mb, fh;
-         tile_of(ti, b, mb, fh);
-         const int sv = q % nV, a = q % kAcc;
+         const int a = q & (kAccF - 1);
          const int f0 = fh * fp.FT + nb * kPostNT, rowV = b * g.Npos + mb * 128;
-         if (nb == nBlk - 1) x_prefetch(ti);
+         if (lead && nb == nBlk - 1) x_prefetch(b, mb, fh);
          int okw = !dead;
          if (lane == 0 && okw)
-            okw = wait_or_abort(&accFull[a], (uint32_t)((q / kAcc) & 1)) &&
-                  wait_or_abort(&vFull[sv], (uint32_t)((q / nV) & 1));
+            okw = wait_or_abort(&accFull[a], (uint32_t)((q / kAccF) & 1)) &&
+                  wait_or_abort(&vFull[sv], (uint32_t)(uv & 1));
          okw = __shfl_sync(0xffffffffu, okw, 0);
          dead = !okw;
          if (okw) {
             tc_fence_after();
-            float d[32], vo[32];
-            tmem_ld32(tmem + a * kPostNT + ((uint32_t)(32 * qd) << 16) + 32 * h, d);
+            float d[16], vo[16];
+            tmem_ld16(tmem + a * kPostNT + ((uint32_t)(32 * qd) << 16) + 16 * h4, d);
             tc_fence_before();
             if (lane == 0) mbar_arrive(&accEmpty[a]);
-            uint8_t *vsub = smem + fp.offVT[0] + sv * 32768u + h * 16384 + 32 * qd * 128;
+            uint8_t *vsub = smem + fp.offVT[0] + sv * 32768u + hh2 * 16384 + 32 * qd * 128;
             uint8_t *vt = vsub + lane * 128;
 #pragma unroll
-            for (int qq = 0; qq < 8; qq++) {
-               const float4 t4 = *reinterpret_cast<const float4 *>(vt + ((qq ^ (pw & 7)) << 4));
+            for (int qq = 0; qq < 4; qq++) {
+               const float4 t4 = *reinterpret_cast<const float4 *>(vt + (((4 * sub + qq) ^ (pw & 7)) << 4));
                vo[4 * qq] = t4.x;
                vo[4 * qq + 1] = t4.y;
                vo[4 * qq + 2] = t4.z;
                vo[4 * qq + 3] = t4.w;
             }
-            float vn[32], an[32];
+            float vn[16], an[16];
             const float om = 1.0f - g.e;
             if (g.simple) {
 #pragma unroll
-               for (int jj = 0; jj < 32; jj++) {
+               for (int jj = 0; jj < 16; jj++) {
                   const float ao = vo[jj] < g.VThresh ? g.AMin : vo[jj] - g.AShift;
                   vn[jj] = fmaf(g.e, vo[jj], om * (d[jj] + g.si * ao));
                   an[jj] = vn[jj] < g.VThresh ? g.AMin : vn[jj] - g.AShift;
                }
             } else {
 #pragma unroll
-               for (int jj = 0; jj < 32; jj++) {
+               for (int jj = 0; jj < 16; jj++) {
                   vn[jj] = fmaf(g.e, vo[jj], om * (d[jj] + g.si * thresh(vo[jj], g)));
                   an[jj] = thresh(vn[jj], g);
                }
             }
-            if (lane == 0 && pendingV >= 0) {
+            if (sub && lane == 0 && pendingV >= 0) {  // the pair's previous store has read its slot
                bulk_wait_read_all();
                mbar_arrive(&vEmpty[pendingV]);
             }
-            __syncwarp();
 #pragma unroll
-            for (int qq = 0; qq < 8; qq++)
-               *reinterpret_cast<float4 *>(vt + ((qq ^ (pw & 7)) << 4)) =
+            for (int qq = 0; qq < 4; qq++)
+               *reinterpret_cast<float4 *>(vt + (((4 * sub + qq) ^ (pw & 7)) << 4)) =
                      make_float4(vn[4 * qq], vn[4 * qq + 1], vn[4 * qq + 2], vn[4 * qq + 3]);
-            // A_q into the shared A tile once GEMM2 of block q - 1 has read it: row pw (128 B,
-            // 128-byte swizzle), 16-byte chunks 4h .. 4h + 3
+            // A_q into TMEM A tile q % 2 once GEMM2 of block q - 2 has read it: lane pw, features
+            // 16 h4 .. 16 h4 + 15 as 8 columns of BF16 pairs
             int oka = 1;
-            if (lane == 0 && q >= 1) oka = wait_or_abort(&aEmpty, (uint32_t)((q - 1) & 1));
+            if (lane == 0 && q >= 2) oka = wait_or_abort(&aEmpty[q & 1], (uint32_t)(((q >> 1) - 1) & 1));
             oka = __shfl_sync(0xffffffffu, oka, 0);
             if (oka) {
-               uint8_t *arow = smem + fp.offAop + pw * 128;
+               tc_fence_after();
+               uint32_t ap[8];
 #pragma unroll
-               for (int c = 0; c < 4; c++)
-                  *reinterpret_cast<uint4 *>(arow + (((4 * h + c) ^ (pw & 7)) << 4)) =
-                        make_uint4(pack2(an[8 * c], an[8 * c + 1]), pack2(an[8 * c + 2], an[8 * c + 3]),
-                                   pack2(an[8 * c + 4], an[8 * c + 5]), pack2(an[8 * c + 6], an[8 * c + 7]));
+               for (int j = 0; j < 8; j++) ap[j] = pack2(an[2 * j], an[2 * j + 1]);
+               tmem_st8(tmem + ((uint32_t)(32 * qd) << 16) + colA + 32 * (q & 1) + 8 * h4, ap);
+               tmem_wait_st();
+               tc_fence_before();
             }
             if (writeA) {  // the activity for the kernels of a later unfused step
-               bf16 *ag = A + (size_t)(rowV + pw) * g.F + f0 + 32 * h;
-               uint4 *lg = reinterpret_cast<uint4 *>(Alo + (size_t)(rowV + pw) * g.F + f0 + 32 * h);
+               bf16 *ag = A + (size_t)(rowV + pw) * g.F + f0 + 16 * h4;
+               uint4 *lg = reinterpret_cast<uint4 *>(Alo + (size_t)(rowV + pw) * g.F + f0 + 16 * h4);
+               st_global_32B(ag,
+                             make_uint4(pack2(an[0], an[1]), pack2(an[2], an[3]), pack2(an[4], an[5]),
+                                        pack2(an[6], an[7])),
+                             make_uint4(pack2(an[8], an[9]), pack2(an[10], an[11]), pack2(an[12], an[13]),
+                                        pack2(an[14], an[15])));
 #pragma unroll
-               for (int t = 0; t < 2; t++)
-                  st_global_32B(ag + 16 * t,
-                                make_uint4(pack2(an[16 * t], an[16 * t + 1]), pack2(an[16 * t + 2], an[16 * t + 3]),
-                                           pack2(an[16 * t + 4], an[16 * t + 5]), pack2(an[16 * t + 6], an[16 * t + 7])),
-                                make_uint4(pack2(an[16 * t + 8], an[16 * t + 9]), pack2(an[16 * t + 10], an[16 * t + 11]),
-                                           pack2(an[16 * t + 12], an[16 * t + 13]),
-                                           pack2(an[16 * t + 14], an[16 * t + 15])));
-#pragma unroll
-               for (int t = 0; t < 4; t++) {
+               for (int t = 0; t < 2; t++) {
                   float l[8];
 #pragma unroll
                   for (int u = 0; u < 8; u++) l[u] = an[8 * t + u] - __bfloat162float(__float2bfloat16_rn(an[8 * t + u]));
@@ -1311,9 +1394,17 @@ __global__ void __launch_bounds__(352, 1) step_tc_kernel(const __grid_constant__
             }
             fence_proxy_async_smem();
             __syncwarp();
-            if (lane == 0) {
-               if (oka) mbar_arrive(&aFull);
-               bulk_store(V + v_index(g, b, mb * 128 + 32 * qd, f0 + 32 * h), vsub, 4096);
+            if (lane == 0 && oka) mbar_arrive(&aFull[q & 1]);
+            dead = !oka;
+         }
+         // both halves of the pair's 32 x 32 part are written; every warp passes this barrier
+         // on every block (a warp that gave up on a wait skips only the work), so that no warp
+         // waits here for a partner that has left
+         named_bar_sync(pairBar, 64);
+         if (!dead) {
+            if (sub && lane == 0) {
+               uint8_t *vsub = smem + fp.offVT[0] + sv * 32768u + hh2 * 16384 + 32 * qd * 128;
+               bulk_store(V + v_index(g, b, mb * 128 + 32 * qd, f0 + 32 * hh2), vsub, 4096);
                bulk_commit();
                if (nV == 1) {
                   bulk_wait_read_all();
@@ -1321,10 +1412,17 @@ __global__ void __launch_bounds__(352, 1) step_tc_kernel(const __grid_constant__
                }
             }
             pendingV = nV == 1 ? -1 : sv;
-            dead = !oka;
          }
-         if (nb == kIm && ti + 1 < myTiles) go = im2col(ti + 1);
-         if (go && nb == nBlk - 1) go = fold_tile(ti);
+         if (lead && nb == kIm && ti + 1 < myTiles) go = im2col(ti + 1);
+         if (lead && go && nb == nBlk - 1) go = fold_tile(ti, b, mb, fh);
+         if (++sv == nV) {
+            sv = 0;
+            uv++;
+         }
+         if (++nb == nBlk) {
+            nb = 0;
+            if (++ti < myTiles) tile_of(ti, b, mb, fh);
+         }
       }
       if (lane == 0) bulk_wait_all();
    }
@@ -1628,7 +1726,7 @@ FusePlan fuse_plan_for(const LcaGeom &g, int S, int P, int C, int numSms, int FT
    auto al = [](uint32_t v) { return (v + 1023u) & ~1023u; };
    FusePlan fp;
    std::memset(&fp, 0, sizeof(fp));
-   if (FT < 64 || FT % 64 || g.F % FT || nV < 1 || nV > kMaxVSlots || nW < 2 || nW > 3 ||
+   if (FT < 64 || FT % 64 || g.F % FT || nV < 1 || nV > 4 || nW < 2 || nW > 3 ||
        P - S > S * g.rowsPerBlock || g.MB < 1)
       return fp;
    const int nFH = g.F / FT;
@@ -1641,20 +1739,21 @@ FusePlan fuse_plan_for(const LcaGeom &g, int S, int P, int C, int numSms, int FT
    fp.bandFloats = (uint32_t)(fp.RWR * fp.RP);
    fp.sliceFloats = (uint32_t)((P - S) * fp.RP);
    const uint32_t wB = NKC * kPostNT * 128;
+   // the im2col operand lives in TMEM when it fits beside the accumulators and the A tiles
+   // (kernel F's column budget: 2 x 64 + KP + 2 x 32 + KP / 2 <= 512), else in shared memory
+   const bool imTmem = 2 * kPostNT + KP + 64 + KP / 2 <= 512;
    uint32_t o = 0;
    fp.offIM = o;
-   o = al(o + NKC * 16384);
+   if (!imTmem) o = al(o + NKC * 16384);
    fp.wStride = al(wB);
    for (int sl = 0; sl < 3; sl++) {
       fp.offW[sl] = o;
       if (sl < nW) o = al(o + wB);
    }
-   for (int sl = 0; sl < kMaxVSlots; sl++) {
+   for (int sl = 0; sl < 4; sl++) {
       fp.offVT[sl] = o;
       if (sl < nV) o = al(o + 32768);
    }
-   fp.offAop = o;
-   o = al(o + 16384);
    fp.offStage = o;
    o += nFH * fp.bandFloats * 4;
    fp.offTop = o;
@@ -1676,7 +1775,7 @@ FusePlan make_fuse_plan(const LcaGeom &g, int S, int P, int C, int numSms) {
    std::memset(&fp, 0, sizeof(fp));
    for (int FT = std::min(256, g.F); FT >= 64; FT -= 64) {
       if (g.F % FT || FT % 64) continue;
-      for (int nV = kMaxVSlots; nV >= 1; nV--) {
+      for (int nV = 4; nV >= 1; nV--) {
          fp = fuse_plan_for(g, S, P, C, numSms, FT, nV, 2);
          if (fp.total && fp.total <= kSmemBudget) return fp;
       }
@@ -1815,7 +1914,7 @@ struct Launcher {
    static pvgpu_status launch_F(const StepArgs &a, int mode, int writeA, const float *rin, float *bout,
                                 cudaStream_t st, bool programmatic) {
       cudaLaunchAttribute attr[1];
-      cudaLaunchConfig_t c = config(a.fp.G, a.fp.total, st, programmatic, attr, 352);
+      cudaLaunchConfig_t c = config(a.fp.G, a.fp.total, st, programmatic, attr, 608);
       cudaError_t e = cudaLaunchKernelEx(&c, step_tc_kernel<S, P, C>, *a.tmW, a.g, a.fp, mode, writeA, rin, bout,
                                          (const float *)a.xpad, a.V, a.A, a.Alo, a.err);
       return e == cudaSuccess ? PVGPU_OK : pvgpu::record_cuda_error(e, "lca fused step");
@@ -2389,7 +2488,7 @@ extern "C" pvgpu_status pvgpu_lca_solver_autotune(pvgpu_lca_solver *s, const flo
       s->sched.fused = 1;
       double bestMs = 1e30;
       for (int FT = 64; FT <= 512 && FT <= s->g.F; FT += 64) {
-         for (int nV = 1; nV <= kMaxVSlots; nV++) {
+         for (int nV = 1; nV <= 4; nV++) {
             for (int nW = 2; nW <= 3; nW++) {
                FusePlan fp = fuse_plan_for(s->g, s->S, s->P, s->C, g_num_sms, FT, nV, nW);
                if (!fp.total || fp.total > kSmemBudget) continue;

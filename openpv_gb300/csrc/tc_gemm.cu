@@ -136,7 +136,99 @@ pvgpu_status tc_gemm(const void *A, const void *B, float *C, int M, int N, int K
    return PVGPU_OK;
 }
 
+// A from tensor memory: each thread (row m of the 128-row tile) loads its row of A (BF16, K
+// <= 256) from global memory and stores it into TMEM lane m, two K elements per column; B (K-
+// major, [N][K]) by TMA into SW128 shared tiles, all of K at once; MMAs read A from TMEM.
+__global__ void __launch_bounds__(128) tc_gemm_atmem_kernel(const __grid_constant__ CUtensorMap tmB,
+                                                            const uint16_t *__restrict__ A, float *__restrict__ C,
+                                                            int M, int N, int K, int *__restrict__ err) {
+   extern __shared__ uint8_t smem_raw[];
+   uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+   __shared__ __align__(8) uint64_t full, done;
+   __shared__ uint32_t tmemBase;
+   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+   const int m0 = blockIdx.x * kBM, nk = K / kBK;
+   if (threadIdx.x == 0) {
+      mbar_init(&full, 1);
+      mbar_init(&done, 1);
+      fence_mbar_init();
+      prefetch_tmap(&tmB);
+   }
+   if (warp == 0) tmem_alloc(&tmemBase, 512);
+   tc_fence_before();
+   __syncthreads();
+   tc_fence_after();
+   const uint32_t tmem = tmemBase, aCol = 256;  // D in columns 0..N-1, A from column 256
+   if (threadIdx.x == 0) {
+      mbar_arrive_expect_tx(&full, (uint32_t)(nk * N * kBK * 2));
+      for (int kc = 0; kc < nk; kc++) tma_load_2d(smem + kc * N * kBK * 2, &tmB, &full, kc * kBK, 0);
+   }
+   // row m of A into lane m: columns aCol + k/2 hold (A[m][k], A[m][k+1])
+   const int row = m0 + warp * 32 + lane;
+   const uint32_t *arow = reinterpret_cast<const uint32_t *>(A + (size_t)row * K);
+   for (int c = 0; c < K / 2; c += 8) {
+      uint32_t r[8];
+#pragma unroll
+      for (int j = 0; j < 8; j++) r[j] = arow[c + j];
+      tmem_st8(tmem + ((uint32_t)(warp * 32) << 16) + aCol + c, r);
+   }
+   tmem_wait_st();
+   tc_fence_before();
+   __syncthreads();
+   tc_fence_after();
+   int ok = 1;
+   if (threadIdx.x == 0) {
+      ok = mbar_wait(&full, 0);
+      if (ok) {
+         tc_fence_after();
+         const uint32_t idesc = idesc_bf16(kBM, N);
+         for (int kc = 0; kc < nk; kc++) {
+            const uint32_t b0 = smem_u32(smem + kc * N * kBK * 2);
+#pragma unroll
+            for (int k = 0; k < kBK / 16; k++)
+               mma_bf16_ta(tmem, tmem + aCol + (uint32_t)((kc * kBK + k * 16) / 2), sdesc_sw128(b0 + k * 32), idesc,
+                           (kc | k) != 0);
+         }
+      }
+      mma_commit(&done);
+   }
+   ok = __syncthreads_and(ok && mbar_wait(&done, 0));
+   tc_fence_after();
+   if (ok) {
+      for (int c = 0; c < N; c += 32) {
+         float v[32];
+         tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + c, v);
+         if (row < M) {
+#pragma unroll
+            for (int j = 0; j < 32; j++)
+               if (c + j < N) C[(size_t)row * N + c + j] = v[j];
+         }
+      }
+   } else if (threadIdx.x == 0) {
+      atomicExch(err, 1);
+   }
+   tc_fence_before();
+   __syncthreads();
+   if (warp == 0) tmem_dealloc(tmem, 512);
+}
+
 }  // namespace
+
+extern "C" pvgpu_status pvgpu_tc_gemm_bf16_atmem(const void *A, const void *B, float *C, int M, int N, int K,
+                                                 int *errFlag, void *stream) {
+   if (!A || !B || !C || !errFlag || M <= 0 || N < 16 || N > 256 || (N % 16) || K < 64 || K > 256 || (K % 64) ||
+       (M % 128) || (reinterpret_cast<uintptr_t>(A) & 3))
+      return PVGPU_ERR_BAD_ARG;
+   CUtensorMap tmB;
+   if (!pvgpu::make_tmap_bf16_sw128(&tmB, B, N, K, K, N)) return PVGPU_ERR_BAD_ARG;
+   const size_t smem = (size_t)(K / kBK) * N * kBK * 2 + 1024;
+   cudaError_t e = cudaFuncSetAttribute(tc_gemm_atmem_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+   if (e != cudaSuccess) return pvgpu::record_cuda_error(e, "tc_gemm attr");
+   tc_gemm_atmem_kernel<<<M / kBM, 128, smem, pvgpu::as_stream(stream)>>>(tmB, static_cast<const uint16_t *>(A), C, M,
+                                                                          N, K, errFlag);
+   PVGPU_CHECK_LAUNCH("tc_gemm atmem");
+   return PVGPU_OK;
+}
 
 extern "C" pvgpu_status pvgpu_tc_gemm_bf16(const void *A, const void *B, float *C, int M, int N, int K, int *errFlag,
                                            void *stream) {

@@ -47,6 +47,17 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
    return ok != 0;
 }
 
+// Non-blocking test of the phase with the given parity (never suspends the thread).
+__device__ __forceinline__ bool mbar_test(uint64_t *bar, uint32_t parity) {
+   uint32_t ok;
+   asm volatile(
+         "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+         : "=r"(ok)
+         : "r"(smem_u32(bar)), "r"(parity)
+         : "memory");
+   return ok != 0;
+}
+
 // Bounded wait for the phase with the given parity; false on timeout.
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
    for (uint32_t i = 0; i < kWaitLimit; i++) {
@@ -143,6 +154,27 @@ __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64
 }
 
 // Arrive on *bar once every tcgen05.mma this thread issued so far has completed.
+// D[tmem] (+)= A[tmem] * B[smem]^T (M x N x 16, kind::f16): A is read from tensor memory, row m
+// in lane m, two consecutive K elements per 32-bit column (8 columns per instruction).
+__device__ __forceinline__ void mma_bf16_ta(uint32_t d_tmem, uint32_t a_tmem, uint64_t bdesc, uint32_t idesc,
+                                            uint32_t accumulate) {
+   asm volatile(
+         "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+         " tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n}\n" ::"r"(d_tmem),
+         "r"(a_tmem), "l"(bdesc), "r"(idesc), "r"(accumulate)
+         : "memory");
+}
+
+// Warp-collective: 8 consecutive 32-bit columns of this warp's 32 TMEM lanes from registers.
+__device__ __forceinline__ void tmem_st8(uint32_t taddr, const uint32_t *r) {
+   asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"r"(taddr), "r"(r[0]),
+                "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7])
+                : "memory");
+}
+
+// Stores issued by this thread have completed (before a fence and the hand-off to the MMA).
+__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+
 __device__ __forceinline__ void mma_commit(uint64_t *bar) {
    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
                 : "memory");

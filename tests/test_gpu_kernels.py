@@ -338,6 +338,24 @@ def test_tc_gemm_bf16_mn_major_b(cuda, M, N, K):
     np.testing.assert_allclose(C.cpu().numpy(), ref.numpy(), rtol=1e-4, atol=1e-3)
 
 
+@pytest.mark.parametrize("M,N,K", [(128, 64, 64), (256, 192, 192), (128, 256, 256)])
+def test_tc_gemm_bf16_a_from_tmem(cuda, M, N, K):
+    """A read by tcgen05.mma from tensor memory (row m in lane m, two K elements per 32-bit
+    column, stored with tcgen05.st) against the same host GEMM."""
+    torch = cuda
+    from openpv_gb300 import capi
+    g = torch.Generator().manual_seed(3 * M + N + K)
+    A = torch.randn(M, K, generator=g).to(torch.bfloat16)
+    B = torch.randn(N, K, generator=g).to(torch.bfloat16)
+    ref = A.float() @ B.float().T
+    C = torch.zeros(M, N, device="cuda")
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    capi.tc_gemm_bf16_atmem(A.cuda(), B.cuda(), C, M, N, K, err)
+    torch.cuda.synchronize()
+    assert int(err.item()) == 0, "a bounded device wait timed out"
+    np.testing.assert_allclose(C.cpu().numpy(), ref.numpy(), rtol=1e-4, atol=1e-3)
+
+
 def test_deliver_ident_matches_reference_rule(cuda, oracle):
     """IdentDelivery (delivery/IdentDelivery.cpp:99-180): GSyn += the restricted activity, from the
     dense extended buffer or from the SparseList (entries in the halo skipped); one contribution
