@@ -48,7 +48,13 @@ CASES = {
     "plain_lca": (2, (32, 32, 1), (16, 16, 64), 8, 0.1, 30),
     "colour": (2, (32, 32, 3), (16, 16, 128), 8, 0.15, 30),
     "stride4": (1, (64, 64, 1), (16, 16, 64), 16, 0.1, 20),
+    # four 128-position blocks per image: interior blocks sum bands from both neighbours
+    "tall": (2, (64, 32, 3), (32, 16, 128), 8, 0.15, 20),
 }
+# BF16x3 is offered where its operands fit in shared memory: 8x8 patches and input images of at
+# most ~4 K floats (kernel R holds x twice and the reconstruction of one image beside two
+# double-width stages)
+X3_CASES = ("plain_lca", "colour")
 
 
 def setup(oracle, name, seed=3):
@@ -97,8 +103,7 @@ def test_lca_bf16_form_energy_within_1e3_of_fp64(torch, oracle, name):
     s.set_weights(torch.from_numpy(w).cuda())
     xd = torch.from_numpy(x).cuda()
     e = torch.zeros(nb, dtype=torch.float64, device="cuda")
-    # BF16x3 is offered where its operands fit in shared memory (the 3-channel and 8x8 cases)
-    for x3 in ((0, 5) if nxp == 8 else (0,)):
+    for x3 in ((0, 5) if name in X3_CASES else (0,)):
         s.reset()
         s.run(xd, steps, x3_steps=x3, precision=capi.LCA_BF16)
         s.energy(xd, e)
@@ -286,7 +291,7 @@ def test_lca_fused_steps_match_unfused_and_oracle(torch, oracle, name):
         assert s.error_flag() == 0
         return v.cpu().numpy(), e.cpu().numpy().copy(), prof
 
-    for x3 in ((0,) if name == "stride4" else (0, 4)):  # no BF16x3 form for 16 x 16 patches
+    for x3 in ((0, 4) if name in X3_CASES else (0,)):
         vf, ef, prof = run(True, x3, direct=True)
         assert prof[3] == steps and prof[4] == steps - x3 - (1 if x3 == 0 else 0), prof
         vu, eu, prof_u = run(False, x3, direct=True)
