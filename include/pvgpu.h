@@ -445,8 +445,8 @@ pvgpu_status pvgpu_lca_solver_profile_end_fused(pvgpu_lca_solver *s, double *rec
  * tile (64/128/256/512) and its V / weight ring depths and A staging, the reconstruction
  * kernel's ring depth -- on trialSteps timesteps of x (BF16 and BF16x3 forms), keeps the fastest
  * of each, then replays graphs of max(trialSteps, 16) steps under each schedule (one chain or two
- * half-batch chains, with and without programmatic edges: pvgpu_lca_solver_set_schedule) and keeps
- * the fastest; remembers shapes and schedule for every solver of the same geometry created later
+ * half-batch chains, with and without programmatic edges, two chains with capped grids for
+ * kernels P and F: pvgpu_lca_solver_set_schedule) and keeps the fastest; remembers shapes and schedule for every solver of the same geometry created later
  * in the process.  Leaves V and A undefined: call pvgpu_lca_solver_reset before the next run. */
 pvgpu_status pvgpu_lca_solver_autotune(pvgpu_lca_solver *s, const float *x, int trialSteps, void *stream);
 /* The shapes in use: out[0..4] = {feature tile, V ring slots, weight ring slots, A staged (0/1),

@@ -2519,8 +2519,12 @@ extern "C" pvgpu_status pvgpu_lca_solver_autotune(pvgpu_lca_solver *s, const flo
    // best of two replays
    {
       const int n = std::max(trialSteps, 16);
+      // one or two chains, with and without programmatic edges, and two chains with the persistent
+      // grids of kernels P and F capped (each chain's last wave then leaves whole SMs to the other)
       const int fz = s->sched.fused;
-      const pvgpu_lca_schedule cands[4] = {{1, 0, 0, 1, fz}, {1, 0, 0, 0, fz}, {2, 0, 0, 1, fz}, {2, 0, 0, 0, fz}};
+      const int cap1 = (g_num_sms * 5 / 6) & ~1, cap2 = (g_num_sms * 2 / 3) & ~1;
+      const pvgpu_lca_schedule cands[6] = {{1, 0, 0, 1, fz}, {1, 0, 0, 0, fz},    {2, 0, 0, 1, fz},
+                                           {2, 0, 0, 0, fz}, {2, 0, cap1, 1, fz}, {2, 0, cap2, 1, fz}};
       cudaStream_t st = pvgpu::as_stream(stream);
       cudaEvent_t e0 = nullptr, e1 = nullptr;
       if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {

@@ -203,7 +203,8 @@ def test_lca_autotune_picks_valid_shapes_and_keeps_parity(torch, oracle):
         assert 1 <= q["v_slots"] <= 3 and 1 <= q["w_slots"] <= 2 and 2 <= q["recon_stages"] <= 4, info
     assert info["bf16x3"]["a_staged"] == 0
     sched = s.schedule()
-    assert sched["chains"] in (1, 2) and sched["recon_ctas"] == 0 and sched["post_ctas"] == 0, sched
+    assert sched["chains"] in (1, 2) and sched["recon_ctas"] == 0, sched
+    assert sched["post_ctas"] == 0 or sched["chains"] == 2, sched  # capped grids only with two chains
     s2 = capi.LcaSolver(nb, ins, v1s, nxp, vth)
     assert s2.plan_info() == info and s2.schedule() == sched
     e = torch.zeros(nb, dtype=torch.float64, device="cuda")
