@@ -1,6 +1,8 @@
-// lca_solver.cu -- the batched LCA module (input -> error <-> V1) as two fused kernels per
-// timestep, on the tcgen05 tensor cores (BF16 operands, FP32 accumulation) or, for the
-// plain FP32 form, on the FP32 pipes with the same structure.
+// lca_solver.cu -- the batched LCA module (input -> error <-> V1) on the tcgen05 tensor cores
+// (BF16 operands, FP32 accumulation): one fused kernel per BF16 timestep (kernel F, below), or
+// two kernels per timestep (kernels R and P: the first and last BF16 steps of a run, BF16x3
+// steps, and every step when fusion is off); the plain FP32 form runs the two-kernel structure
+// on the FP32 pipes.
 //
 // Reference path (per timestep, HyPerCol::advanceTime, columns/HyPerCol.cpp:659-790):
 //   error layer (phase 1): G = input - W^T a(t-1)   IdentConn ch0 + HyPerConn V1->Error ch1
@@ -790,34 +792,41 @@ __global__ void __launch_bounds__(320, 1) post_tc_kernel(const __grid_constant__
 // then the reconstruction of the new activity, without the activity leaving the SM.
 //
 // Tile (image b, block mb of 128 positions, feature tile fh of FT features) as in kernel P.
-// Per 64-feature block q of the tile, after kernel P's GEMM (D1 = im2col(r) . W_q^T) and the
-// update, the block's new activity A_q (BF16, 128 positions x 64 features) goes to a shared
-// K-major tile and a second GEMM accumulates D2[pos][k] += sum_f A_q[pos][f] W_q[f][k]
-// (N = P*P*C) in TMEM, reading the block's weight tile again as an MN-major operand.  After
-// the tile's last block the 8 epilogue warps fold D2 into a band: padded rows S*mb*rpb ..
-// +RWR (every row the block's patches reach), starting from x on the rows the block owns when
-// fh == 0 and from 0 otherwise, each tap subtracted (kernel R's fold: 16 tap groups, no two
-// threads on one pixel inside a group, every pixel's taps in one fixed order).  The band goes
-// to HBM.  Block mb owns padded rows S*mb*rpb .. S*(mb+1)*rpb - 1, the last block also the
-// rows below; bands of blocks mb and mb + 1 overlap in P - S rows (P - S <= S*rpb).
+// Per 64-feature block q of the tile: GEMM1 D1 = im2col(r) . W_q^T (the im2col operand in TMEM
+// where it fits, else in shared memory), the update, then the block's new activity A_q (BF16,
+// 128 positions x 64 features) goes into one of two TMEM A tiles and GEMM2 accumulates
+// D2[pos][k] += sum_f A_q[pos][f] W_q[f][k] (N = P*P*C) in TMEM, reading the block's weight
+// tile again as an MN-major operand.  After the tile's last block epilogue warps 0-7 fold D2
+// into a band: padded rows S*mb*rpb .. +RWR (every row the block's patches reach), starting from
+// x on the rows the block owns when fh == 0 and from 0 otherwise, each tap subtracted (kernel
+// R's fold: 16 tap groups, no two threads on one pixel inside a group, every pixel's taps in
+// one fixed order).  The band goes to HBM.  Block mb owns padded rows S*mb*rpb ..
+// S*(mb+1)*rpb - 1, the last block also the rows below; bands of blocks mb and mb + 1 overlap
+// in P - S rows (P - S <= S*rpb).
 // The next timestep's tile (b, mb) sums its residual window r = x - W^T a from the bands of
 // (b, mb) and the overlapping rows of (b, mb - 1) and (b, mb + 1), all feature tiles: per
 // pixel (sum over fh of the lower block's band) + (sum over fh of the upper block's band),
 // so that both windows holding a pixel compute it in the same order.  The first timestep of
 // a run reads kernel R's padded residual window instead (mode 0).
-// Roles: as kernel P (warp 8 loads, warp 9 MMA, warps 0-7 epilogue), and
-//   loads:    the tile's bands (or residual window) as one stage, once the tile before has read
-//             the stage and the fold of the tile before that (which runs in the stage) is
-//             stored;
-//   MMA:      GEMM1 of block q, then GEMM2 of block q - 1 (one behind, so that the epilogue of
-//             block q - 1 overlaps GEMM1 of block q); a weight slot is freed by GEMM2's commit;
-//   epilogue: A_q into the shared A tile (after GEMM2 of block q - 1 has read it); x of the
-//             owned rows into registers at the start of the tile's last block; after that block
-//             (and after the next tile's im2col, which GEMM1 of the next tile -- and so GEMM2 of
-//             this tile's last block -- waits for) the fold in the stage and the band store.
-// Hand-offs added to kernel P's: aFull / aEmpty, d2Full (the tile's D2 complete), foldFree (the
-// band store has read the stage).  D2 is overwritten by the next tile's first GEMM2 only after
-// that block's aFull, which the epilogue signals after the fold's TMEM reads have completed.
+// Roles (608 threads):
+//   warps 0-15 (epilogue): per block, warp = (lane quarter, 16-feature group): the LCA update of
+//             its 32 positions x 16 features from D1 and the shared V chunk, V back in place,
+//             A into the TMEM A tile of the block's parity (after GEMM2 of block q - 2 has read
+//             it); the two warps of a 32-feature half meet at a named barrier and the second
+//             bulk-stores their 4 KB.  Warps 0-7 also sum the next tile's window from the
+//             bands and build its im2col (after block kIm), prefetch x of the owned rows at the
+//             start of the tile's last block, and after it fold D2 into the band (in the
+//             stage, which the next tile's im2col has read) and store the band;
+//   warp 16 (weights): each block's weight tile by TMA into a 2- or 3-slot ring;
+//   warp 17 (MMA):     an event loop issuing GEMM1 of the next block as soon as its weight
+//             tile, accumulator and im2col operand are ready, and GEMM2 of the oldest block
+//             whose A tile is written; a weight slot is freed by GEMM2's commit;
+//   warp 18 (V, stage): V chunks by bulk copy into a 1- to 4-slot ring, and the tile's bands (or
+//             residual window) as one stage once the tile before has read the stage and the
+//             fold of the tile before that (which runs in the stage) is stored.
+// Hand-offs added to kernel P's: aFull / aEmpty per A tile, d2Full (the tile's D2 complete),
+// foldFree (the band store has read the stage).  D2 is overwritten by the next tile's first
+// GEMM2 only after that block's aFull, which warps 0-7 signal after the fold's TMEM reads.
 // -------------------------------------------------------------------------------------------
 struct FusePlan {
    int G;                         // persistent CTAs
