@@ -1138,29 +1138,35 @@ __global__ void __launch_bounds__(608, 1) step_tc_kernel(const __grid_constant__
             wait_or_abort(&imEmpty, (uint32_t)((t - 1) & 1));
          if (named_bar_or(1, EPI, abortFlag != 0)) return false;
          if (mode != 0) {
-            // ---- the residual window from the bands ----
+            // ---- the residual window from the bands (float4 runs: rows are RP floats, RP a
+            // multiple of 4, so row r's run is [r * RP / 4, (r + 1) * RP / 4)) ----
             int b, mb, fh;
             tile_of(t, b, mb, fh);
-            float *w = reinterpret_cast<float *>(smem + fp.offStage);
-            const float *top = reinterpret_cast<const float *>(smem + fp.offTop);
-            const float *bot = reinterpret_cast<const float *>(smem + fp.offBot);
-            const int n = RWR * RP, ovl = P - S, own = S * rpb;
+            float4 *w4 = reinterpret_cast<float4 *>(smem + fp.offStage);
+            const float4 *top4 = reinterpret_cast<const float4 *>(smem + fp.offTop);
+            const float4 *bot4 = reinterpret_cast<const float4 *>(smem + fp.offBot);
+            const int RP4 = RP / 4, bandF4 = (int)fp.bandFloats / 4, sliceF4 = (int)fp.sliceFloats / 4;
+            const int nAll = RWR * RP4, topEnd = (P - S) * RP4, botStart = S * rpb * RP4;
             const bool hasTop = mb > 0, hasBot = mb < g.MB - 1;
-            for (int i = tid; i < n; i += EPI) {
-               const int r = i / RP;
-               float v = w[i];
-               for (int f = 1; f < nFH; f++) v = __fadd_rn(v, w[f * fp.bandFloats + i]);
-               if (hasTop && r < ovl) {
-                  float u = top[i];
-                  for (int f = 1; f < nFH; f++) u = __fadd_rn(u, top[f * fp.sliceFloats + i]);
-                  v = __fadd_rn(u, v);
-               } else if (hasBot && r >= own) {
-                  const int j = i - own * RP;
-                  float u = bot[j];
-                  for (int f = 1; f < nFH; f++) u = __fadd_rn(u, bot[f * fp.sliceFloats + j]);
-                  v = __fadd_rn(v, u);
+            auto add4 = [](float4 a, float4 c) {
+               return make_float4(__fadd_rn(a.x, c.x), __fadd_rn(a.y, c.y), __fadd_rn(a.z, c.z), __fadd_rn(a.w, c.w));
+            };
+            for (int i = tid; i < nAll; i += EPI) {
+               float4 v = w4[i];
+               for (int f = 1; f < nFH; f++) v = add4(v, w4[f * bandF4 + i]);
+               if (i < topEnd) {
+                  if (hasTop) {  // the upper neighbour's rows first
+                     float4 u = top4[i];
+                     for (int f = 1; f < nFH; f++) u = add4(u, top4[f * sliceF4 + i]);
+                     v = add4(u, v);
+                  }
+               } else if (i >= botStart && hasBot) {
+                  const int j = i - botStart;
+                  float4 u = bot4[j];
+                  for (int f = 1; f < nFH; f++) u = add4(u, bot4[f * sliceF4 + j]);
+                  v = add4(v, u);
                }
-               w[i] = v;
+               w4[i] = v;
             }
             named_bar_sync(1, EPI);
          }
