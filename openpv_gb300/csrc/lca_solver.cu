@@ -533,6 +533,10 @@ __global__ void __launch_bounds__(320, 1) post_tc_kernel(const __grid_constant__
          if (pl.stageA) prefetch_tmap(&tmAst);
          bool ok = true;
          issue_rows(0);
+         // block q = (tile ti, block nb), weight slot sw in its use uw, V slot sv in its use uv:
+         // stepped, not divided
+         int ti = 0, nb = 0, sw = 0, uw = 0, sv = 0, uv = 0, b = 0, mb = 0, fh = 0;
+         tile_of(0, b, mb, fh);
          for (int q = 0; ok && q < Q; q++) {
             // tile t+1's window goes out once tile t's has been read, before the first load that
             // waits for tile t's epilogue (V slot) or MMAs (weight slot): that load could not
@@ -542,11 +546,7 @@ __global__ void __launch_bounds__(320, 1) post_tc_kernel(const __grid_constant__
                if (ok) issue_rows(rowsIssued);
             }
             if (!ok) break;
-            const int ti = q / nBlk, nb = q % nBlk;
-            int b, mb, fh;
-            tile_of(ti, b, mb, fh);
-            const int f0 = fh * pl.FT + nb * kPostNT, rowV = b * g.Npos + mb * 128;
-            const int sw = q % nW, uw = q / nW;
+            const int f0 = fh * pl.FT + nb * kPostNT;
             if (uw > 0 && !(ok = wait_or_abort(&wEmpty[sw], (uint32_t)((uw - 1) & 1)))) break;
             mbar_arrive_expect_tx(&wFull[sw], (X3 ? 2 : 1) * WBYTES);
             for (int kc = 0; kc < NKC; kc++) {
@@ -555,11 +555,22 @@ __global__ void __launch_bounds__(320, 1) post_tc_kernel(const __grid_constant__
                if (X3) tma_load_2d(smem + pl.offWlo[0] + wo, &tmWlo, &wFull[sw], kc * 64, f0);
             }
             wIssued = q + 1;
-            const int sv = q % nV, uv = q / nV;
             if (uv > 0 && !(ok = wait_or_abort(&vEmpty[sv], (uint32_t)((uv - 1) & 1)))) break;
             mbar_arrive_expect_tx(&vFull[sv], 32768);
             bulk_load(smem + pl.offVT[0] + sv * 32768u, V + v_index(g, b, mb * 128, f0), 32768, &vFull[sv]);
             vIssued = q + 1;
+            if (++sw == nW) {
+               sw = 0;
+               uw++;
+            }
+            if (++sv == nV) {
+               sv = 0;
+               uv++;
+            }
+            if (++nb == nBlk) {
+               nb = 0;
+               if (++ti < myTiles) tile_of(ti, b, mb, fh);
+            }
          }
          while (ok && rowsIssued < myTiles) {
             ok = wait_or_abort(&stEmpty, (uint32_t)((rowsIssued - 1) & 1));
@@ -583,10 +594,11 @@ __global__ void __launch_bounds__(320, 1) post_tc_kernel(const __grid_constant__
       if (lane == 0 && Q > 0) {
          int mmaDone = 0;
          bool ok = true;
+         int ti = 0, nb = 0, sw = 0, uw = 0;
          for (int q = 0; ok && q < Q; q++) {
-            const int ti = q / nBlk, nb = q % nBlk, sw = q % nW, a = q % kAcc;
+            const int a = q & (kAcc - 1);
             if (nb == 0 && !(ok = wait_or_abort(&imFull, (uint32_t)(ti & 1)))) break;
-            if (!(ok = wait_or_abort(&wFull[sw], (uint32_t)((q / nW) & 1)))) break;
+            if (!(ok = wait_or_abort(&wFull[sw], (uint32_t)(uw & 1)))) break;
             if (q >= kAcc && !(ok = wait_or_abort(&accEmpty[a], (uint32_t)((q / kAcc - 1) & 1)))) break;
             tc_fence_after();
             const uint32_t idesc = idesc_bf16(128, kPostNT);
@@ -605,6 +617,14 @@ __global__ void __launch_bounds__(320, 1) post_tc_kernel(const __grid_constant__
             mma_commit(&wEmpty[sw]);
             if (nb == nBlk - 1) mma_commit(&imEmpty);
             mmaDone = q + 1;
+            if (++sw == nW) {
+               sw = 0;
+               uw++;
+            }
+            if (++nb == nBlk) {
+               nb = 0;
+               ti++;
+            }
          }
          // MMAs still in flight finish before shared memory and TMEM go away
          if (!ok && mmaDone > 0) mbar_wait(&accFull[(mmaDone - 1) % kAcc], (uint32_t)(((mmaDone - 1) / kAcc) & 1));
@@ -679,17 +699,16 @@ __global__ void __launch_bounds__(320, 1) post_tc_kernel(const __grid_constant__
       if (kIm < 1) kIm = 1;
       if (kIm > nBlk - 1) kIm = nBlk - 1;
       bool go = myTiles > 0 && im2col(0), dead = false;
+      int ti = 0, nb = 0, sv = 0, uv = 0, b = 0, mb = 0, fh = 0;  // stepped, not divided
+      if (myTiles > 0) tile_of(0, b, mb, fh);
       for (int q = 0; go && q < Q; q++) {
-         const int ti = q / nBlk, nb = q % nBlk;
-         int b, mb, fh;
-         tile_of(ti, b, mb, fh);
          // ---- block q, each warp on its own ----
-         const int sv = q % nV, a = q % kAcc;
+         const int a = q & (kAcc - 1);
          const int f0 = fh * pl.FT + nb * kPostNT, rowV = b * g.Npos + mb * 128;
          int okw = !dead;
          if (lane == 0 && okw)
             okw = wait_or_abort(&accFull[a], (uint32_t)((q / kAcc) & 1)) &&
-                  wait_or_abort(&vFull[sv], (uint32_t)((q / nV) & 1));
+                  wait_or_abort(&vFull[sv], (uint32_t)(uv & 1));
          okw = __shfl_sync(0xffffffffu, okw, 0);
          dead = !okw;
          if (okw) {
@@ -777,6 +796,14 @@ __global__ void __launch_bounds__(320, 1) post_tc_kernel(const __grid_constant__
             pendingV = nV == 1 ? -1 : sv;
          }
          if (nb == kIm && ti + 1 < myTiles) go = im2col(ti + 1);
+         if (++sv == nV) {
+            sv = 0;
+            uv++;
+         }
+         if (++nb == nBlk) {
+            nb = 0;
+            if (++ti < myTiles) tile_of(ti, b, mb, fh);
+         }
       }
       if (lane == 0) bulk_wait_all();
    }
