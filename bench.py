@@ -367,6 +367,49 @@ class LifNet:
         rec(3)
 
 
+def dictlearn_bench(torch, reps=2):
+    """Differentiable dictionary learning at full size: 32 images 64x64x1 (1/f, unit std), V1
+    16x16x256 stride 4, 256 features of 16x16x1, 100 unrolled LCA timesteps from V = 0 with a
+    checkpoint every 10, loss 0.5 ||x - W^T a||^2 + 0.1 ||a||_1; one gradient = the forward pass,
+    the recomputation of each checkpointed segment and the adjoint pass, all through the C-ABI
+    delivery kernels and their adjoints (pvgpu_deliver_pre / _post, pvgpu_hebbian_dw) driven by
+    the autograd harness of the tests."""
+    from tests import lca_autograd as LA
+    rng = np.random.default_rng(1234 + 4)
+    nb, n, v1, P, T, lam = 32, 64, (16, 16, 256), 16, 100, 0.1
+    geo = LA.Geometry(nb, (n, n, 1), v1, P)
+    w = rng.normal(size=(v1[2], P, P, 1))
+    w = (w / np.sqrt((w ** 2).sum(axis=(1, 2, 3), keepdims=True))).astype(np.float32)
+    f = np.sqrt(np.fft.fftfreq(n)[:, None] ** 2 + np.fft.fftfreq(n)[None, :] ** 2)
+    f[0, 0] = 1.0
+    amp = 1.0 / f
+    amp[0, 0] = 0.0
+    xi = np.real(np.fft.ifft2(amp[None] * np.exp(1j * rng.uniform(0, 2 * np.pi, (nb, n, n)))))
+    xi = (xi - xi.mean(axis=(1, 2), keepdims=True)) / xi.std(axis=(1, 2), keepdims=True)
+    x = torch.from_numpy(np.ascontiguousarray(xi[..., None].astype(np.float32))).cuda()
+    wd = torch.from_numpy(w).cuda().requires_grad_(True)
+
+    def gradient():
+        wd.grad = None
+        loss = LA.unrolled_lca_loss(wd, x, geo, T, lam, lam, checkpoint_every=10)
+        loss.backward()
+        return loss
+
+    gradient()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        loss = gradient()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    return {"workload": "32 x 64x64x1 -> V1 16x16x256 stride 4, 256 x 16x16x1 dictionary, 100 unrolled "
+                        "timesteps (checkpoint every 10), gradient of 0.5||x - W^T a||^2 + 0.1||a||_1 w.r.t. W",
+            "ms_per_gradient": ms, "image_steps_per_s": nb * T / (ms / 1000.0), "loss": float(loss.item()),
+            "grad_norm": float(wd.grad.norm().item()), "dtype": "f32"}
+
+
 def lif_bench(torch, capi, steps=1000, cpu_sample=True):
     nb = 8
     net = LifNet(torch, capi, nb=nb, steps=steps)
@@ -654,6 +697,7 @@ def run_ours(args, rank, world, local_rank):
     cpu_val, cpu_dt = cpu_sample(cfg, cores, warm_steps=25, timed_steps=25)
     deliv = delivery_bench(torch, capi)
     lifb = lif_bench(torch, capi)
+    dlb = dictlearn_bench(torch)
     clocks = clk.summary()
 
     line = {
@@ -697,6 +741,7 @@ def run_ours(args, rank, world, local_rank):
                      "by_density": {k: v for k, v in deliv.items() if k != "post"}, "post": deliv["post"],
                      "hbm_peak_gbs": pk["hbm_gbs"], "tf32_tensor_peak_tflops": pk["bf16_tflops"] / 2},
         "lif_network": lifb,
+        "dictionary_learning": dlb,
         "clocks": clocks,
     }
     print(json.dumps(line), flush=True)
