@@ -31,7 +31,7 @@ typedef enum {
    PVGPU_ERR_OOM = 2,               /* device allocation failed */
    PVGPU_ERR_LAUNCH = 3,            /* kernel launch or CUDA runtime error */
    PVGPU_ERR_TIMEOUT = 4,           /* a bounded device-side wait gave up */
-   PVGPU_ERR_UNSUPPORTED_SHAPE = 5, /* legal OpenPV geometry this build does not handle */
+   PVGPU_ERR_UNSUPPORTED_SHAPE = 5, /* legal OpenPV geometry the library does not handle */
    PVGPU_ERR_ILLEGAL_GEOMETRY = 6   /* geometry OpenPV itself rejects (PatchGeometry::verifyPatchSize) */
 } pvgpu_status;
 

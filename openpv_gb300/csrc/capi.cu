@@ -30,7 +30,7 @@ extern "C" const char *pvgpu_status_string(pvgpu_status s) {
       case PVGPU_ERR_OOM: return "out of device memory";
       case PVGPU_ERR_LAUNCH: return "kernel launch or CUDA runtime error";
       case PVGPU_ERR_TIMEOUT: return "bounded device wait timed out";
-      case PVGPU_ERR_UNSUPPORTED_SHAPE: return "shape not supported by this build";
+      case PVGPU_ERR_UNSUPPORTED_SHAPE: return "shape not supported by this library";
       case PVGPU_ERR_ILLEGAL_GEOMETRY: return "geometry rejected by OpenPV's patch rules";
    }
    return "unknown status";
