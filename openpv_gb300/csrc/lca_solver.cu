@@ -840,10 +840,11 @@ __global__ void __launch_bounds__(320, 1) post_tc_kernel(const __grid_constant__
 //             its 32 positions x 16 features from D1 and the shared V chunk, V back in place,
 //             A into the TMEM A tile of the block's parity (after GEMM2 of block q - 2 has read
 //             it); the two warps of a 32-feature half meet at a named barrier and the second
-//             bulk-stores their 4 KB.  Warps 0-7 also sum the next tile's window from the
-//             bands and build its im2col (after block kIm), prefetch x of the owned rows at the
-//             start of the tile's last block, and after it fold D2 into the band (in the
-//             stage, which the next tile's im2col has read) and store the band;
+//             bulk-stores their 4 KB.  After block kIm all 16 sum the next tile's window from
+//             the bands and build its im2col (a quarter of the patch rows per thread); warps
+//             0-7 prefetch x of the owned rows at the start of the tile's last block, and after
+//             it fold D2 into the band (in the stage, which the next tile's im2col has read)
+//             and store the band;
 //   warp 16 (weights): each block's weight tile by TMA into a 2- or 3-slot ring;
 //   warp 17 (MMA):     an event loop issuing GEMM1 of the next block as soon as its weight
 //             tile, accumulator and im2col operand are ready, and GEMM2 of the oldest block
@@ -876,8 +877,11 @@ __global__ void __launch_bounds__(608, 1) step_tc_kernel(const __grid_constant__
                                                          int *__restrict__ err) {
    constexpr int KP = P * P * C, NKC = KP / 64;
    constexpr uint32_t WBYTES = NKC * kPostNT * 128;
-   constexpr int EPI = 256;  // im2col, fold and band threads: epilogue warps 0-7
-   constexpr int EW = 16;    // epilogue warps for the per-block update: 32 positions x 16 features each
+   constexpr int EPI = 256;  // fold threads: epilogue warps 0-7 (named barrier 1)
+   constexpr int EW = 16;    // epilogue warps: per-block update (32 positions x 16 features each),
+                             // band sums and im2col (named barrier 10, all 16)
+   constexpr int IMC = EW * 32;
+   static_assert(P % 4 == 0, "im2col splits the patch rows in four");
    constexpr int kMaxW = 3;
    // TMEM columns: two GEMM1 accumulators, D2 (KP), two A tiles of GEMM2 (64 BF16 = 32 columns
    // each; block q writes tile q % 2 while GEMM2 of block q - 1 reads the other) and, where it
@@ -1158,12 +1162,12 @@ __global__ void __launch_bounds__(608, 1) step_tc_kernel(const __grid_constant__
       const int qd = warp & 3, h4 = warp >> 2, hh2 = h4 >> 1, sub = h4 & 1;
       const int pw = 32 * qd + lane;
       const int pairBar = 2 + 2 * qd + hh2;
-      const bool lead = warp < 8;  // im2col, fold, band sums: warps 0-7
+      const bool lead = warp < 8;  // x prefetch and fold: warps 0-7
       int pendingV = -1;
       auto im2col = [&](int t) {
          if (tid == 0 && wait_or_abort(&stFull, (uint32_t)(t & 1)) && t > 0)
             wait_or_abort(&imEmpty, (uint32_t)((t - 1) & 1));
-         if (named_bar_or(1, EPI, abortFlag != 0)) return false;
+         if (named_bar_or(10, IMC, abortFlag != 0)) return false;
          if (mode != 0) {
             // ---- the residual window from the bands (float4 runs: rows are RP floats, RP a
             // multiple of 4, so row r's run is [r * RP / 4, (r + 1) * RP / 4)) ----
@@ -1178,7 +1182,7 @@ __global__ void __launch_bounds__(608, 1) step_tc_kernel(const __grid_constant__
             auto add4 = [](float4 a, float4 c) {
                return make_float4(__fadd_rn(a.x, c.x), __fadd_rn(a.y, c.y), __fadd_rn(a.z, c.z), __fadd_rn(a.w, c.w));
             };
-            for (int i = tid; i < nAll; i += EPI) {
+            for (int i = tid; i < nAll; i += IMC) {
                float4 v = w4[i];
                for (int f = 1; f < nFH; f++) v = add4(v, w4[f * bandF4 + i]);
                if (i < topEnd) {
@@ -1195,18 +1199,19 @@ __global__ void __launch_bounds__(608, 1) step_tc_kernel(const __grid_constant__
                }
                w4[i] = v;
             }
-            named_bar_sync(1, EPI);
+            named_bar_sync(10, IMC);
          }
          if constexpr (IMT) {
-            // ---- BF16 im2col of the window into TMEM: lane p, K element k in column k / 2 ----
+            // ---- BF16 im2col of the window into TMEM: lane p, K element k in column k / 2;
+            // thread = (position p, quarter kq of the patch rows) ----
             constexpr int RUN = P * C;
-            constexpr int COLS = (P / 2) * RUN / 2;  // columns per thread (its half of the patch rows)
+            constexpr int COLS = (P / 4) * RUN / 2;  // columns per thread
             static_assert(RUN % 2 == 0 && COLS % 8 == 0, "im2col columns in groups of 8");
             tc_fence_after();  // the previous tile's GEMM1s (imEmpty) are done reading
-            const int p = tid & 127, half = tid >> 7;
+            const int p = tid & 127, kq = tid >> 7;
             const int yl = p / g.v1Nx, x1 = p % g.v1Nx;
-            const float *src0 = win + (S * yl) * RP + S * x1 * C + half * (P / 2) * RP;
-            const uint32_t t0 = tmem + ((uint32_t)((warp & 3) * 32) << 16) + colIM + half * COLS;
+            const float *src0 = win + (S * yl) * RP + S * x1 * C + kq * (P / 4) * RP;
+            const uint32_t t0 = tmem + ((uint32_t)((warp & 3) * 32) << 16) + colIM + kq * COLS;
             uint32_t buf[8];
 #pragma unroll
             for (int i = 0; i < COLS; i++) {
@@ -1222,11 +1227,11 @@ __global__ void __launch_bounds__(608, 1) step_tc_kernel(const __grid_constant__
             constexpr int RUN = P * C;
             constexpr int CPR = RUN / 8;
             static_assert(RUN % 8 == 0, "patch rows must fill whole 16-byte chunks");
-            const int p = tid & 127, half = tid >> 7;
+            const int p = tid & 127, kq = tid >> 7;
             const int yl = p / g.v1Nx, x1 = p % g.v1Nx;
             const float *src0 = win + (S * yl) * RP + S * x1 * C;
 #pragma unroll 1
-            for (int ky = half * (P / 2); ky < (half + 1) * (P / 2); ky++) {
+            for (int ky = kq * (P / 4); ky < (kq + 1) * (P / 4); ky++) {
                const float2 *src = reinterpret_cast<const float2 *>(src0 + ky * RP);
 #pragma unroll
                for (int cc = 0; cc < CPR; cc++) {
@@ -1246,7 +1251,7 @@ __global__ void __launch_bounds__(608, 1) step_tc_kernel(const __grid_constant__
             }
          }
          fence_proxy_async_smem();
-         named_bar_sync(1, EPI);
+         named_bar_sync(10, IMC);
          if (tid == 0) {
             mbar_arrive(&imFull);
             mbar_arrive(&stEmpty);
@@ -1350,11 +1355,14 @@ __global__ void __launch_bounds__(608, 1) step_tc_kernel(const __grid_constant__
       if (kIm < nBlk - 3) kIm = nBlk - 3;
       if (kIm < 0) kIm = 0;
       if (kIm > nBlk - 1) kIm = nBlk - 1;
-      bool go = myTiles > 0 && (!lead || im2col(0)), dead = false;
+      // Every warp runs all Q blocks and passes every named barrier in the same order; a warp
+      // that gave up on a wait (abort flag) skips the work, not the barriers.
+      bool dead = false;
+      if (myTiles > 0) im2col(0);
       // block q = (tile ti, block nb); V slot sv in its use uv, accumulator a: stepped, not divided
       int ti = 0, nb = 0, sv = 0, uv = 0, b = 0, mb = 0, fh = 0;
       if (myTiles > 0) tile_of(0, b, mb, fh);
-      for (int q = 0; go && q < Q; q++) {
+      for (int q = 0; q < Q; q++) {
          const int a = q & (kAccF - 1);
          const int f0 = fh * fp.FT + nb * kPostNT, rowV = b * g.Npos + mb * 128;
          if (lead && nb == nBlk - 1) x_prefetch(b, mb, fh);
@@ -1455,8 +1463,8 @@ __global__ void __launch_bounds__(608, 1) step_tc_kernel(const __grid_constant__
             }
             pendingV = nV == 1 ? -1 : sv;
          }
-         if (lead && nb == kIm && ti + 1 < myTiles) go = im2col(ti + 1);
-         if (lead && go && nb == nBlk - 1) go = fold_tile(ti, b, mb, fh);
+         if (nb == kIm && ti + 1 < myTiles) im2col(ti + 1);
+         if (lead && nb == nBlk - 1) fold_tile(ti, b, mb, fh);
          if (++sv == nV) {
             sv = 0;
             uv++;
