@@ -82,23 +82,17 @@ __device__ __forceinline__ void tmem_ld_cols(uint32_t taddr, float *v) {
 }
 
 // -------------------------------------------------------------------------------------------
-// Kernel R: reconstruction W^T a and the residual x - W^T a (persistent, warp-specialised,
-// clusters of two CTAs sharing the weight stream)
+// Kernel R: reconstruction W^T a and the residual x - W^T a (persistent, warp-specialised)
 //
-// Each cluster (a pair of SMs) walks units of two images; CTA r of the pair takes image 2u + r
-// (the second CTA of an odd batch's last unit has no image and only takes part in the weight
-// stream).  Per image and 128-position block mb:
+// CTA i of the persistent grid walks images i, i + G, ...  Per image and 128-position block mb:
 //   D[pos][k] = sum_f A[pos][f] * W[f][k],  k = (ky*P + kx)*C + c  (M = 128, N = P*P*C, K = F)
 // Roles:
 //   warp 8, lane 0 (loads): per block and chunk of 64 features, into one stage of an nStage
-//                           ring: its own A tile [128 x 64] by TMA, and half of the W^T tile
-//                           [P*P*C x 64] by TMA multicast to both CTAs (each CTA fetches half and
-//                           receives the whole tile, so a weight byte crosses each SM's L2 port
-//                           once per pair); plus each image's x (bulk copy, two buffers);
+//                           ring: the A tile [128 x 64] and the W^T tile [P*P*C x 64] (two TMA
+//                           boxes of P*P*C/2 rows), plus each image's x (bulk copy, two buffers);
 //   warp 9, lane 0 (MMA):   per block the tcgen05.mma chain over F into one of two TMEM
 //                           accumulators (256 columns apart); each stage is released by a
-//                           commit multicast to both CTAs, so a stage is refilled only when both
-//                           CTAs' MMAs are done with it;
+//                           tcgen05.commit once its MMAs are done;
 //   warps 0-7 (fold):       thread = position (TMEM lane) and half of the patch rows.  The fold
 //                           of D into the image (patch (ky,kx) of position (y,x) lands on pixel
 //                           (S*y - E + ky, S*x - E + kx)) runs in (P/S)^2 tap groups; one group
@@ -109,16 +103,15 @@ __device__ __forceinline__ void tmem_ld_cols(uint32_t taddr, float *v) {
 //                           r = x - recon with a zero border of E pixels and rows padded to RP
 //                           floats (the layout kernel P bulk-copies its windows from); the image
 //                           buffer is then cleared.
-// Hand-offs (mbarriers): full (local, armed with the bytes the CTA receives) / empty (two
-// arrivals: both CTAs' commits) per stage, accFull / accEmpty per accumulator, xFull / xEmpty
-// per x buffer.  Waits are bounded; a timeout raises the abort flag, the roles drain their
-// copies and MMAs in flight, and the kernel reports through *err.  The pair meets at a cluster
-// barrier after the barriers are initialised and before either CTA exits.
+// Hand-offs (mbarriers): full (armed with the stage's bytes) / empty (the MMA commit) per stage,
+// accFull / accEmpty per accumulator, xFull / xEmpty per x buffer.  Waits are bounded; a timeout
+// raises the abort flag, the roles drain their copies and MMAs in flight, and the kernel reports
+// through *err.
 // -------------------------------------------------------------------------------------------
 constexpr int kMaxRStages = 4;
 
 struct ReconPlan {
-   int G;              // persistent CTAs (clusters of two)
+   int G;              // persistent CTAs
    int nStage;         // A + W^T ring stages
    int RP, rowsPad;    // padded residual rows
    uint32_t stageBytes, offRec, offX[2];
@@ -127,7 +120,7 @@ struct ReconPlan {
 };
 
 template <int S, int P, int C, bool X3>
-__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(320, 1)
+__global__ void __launch_bounds__(320, 1)
       recon_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmAlo,
                       const __grid_constant__ CUtensorMap tmWtH, const __grid_constant__ CUtensorMap tmWtloH,
                       LcaGeom g, ReconPlan rp, const float *__restrict__ x, float *__restrict__ rpad,
@@ -147,20 +140,17 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(320, 1)
    __shared__ volatile int abortFlag;
 
    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-   const uint32_t crank = cluster_ctarank();
-   constexpr uint16_t kPair = 3;
-   const int pairIdx = blockIdx.x >> 1, nPairs = gridDim.x >> 1;
-   const int nUnits = (g.nb + 1) >> 1;
-   const int myUnits = pairIdx < nUnits ? (nUnits - 1 - pairIdx) / nPairs + 1 : 0;
+   const int G = gridDim.x;
+   const int myUnits = (int)blockIdx.x < g.nb ? (g.nb - 1 - (int)blockIdx.x) / G + 1 : 0;
    const int nkc = g.F / 64;
    const int nStage = rp.nStage;
    const int nPix = g.inNx * g.inNy * C;
-   auto image_of = [&](int ui) { return 2 * (pairIdx + ui * nPairs) + (int)crank; };
+   auto image_of = [&](int ui) { return (int)blockIdx.x + ui * G; };
 
    if (tid == 0) {
       for (int i = 0; i < kMaxRStages; i++) {
          mbar_init(&full[i], 1);
-         mbar_init(&empty[i], 2);  // both CTAs' MMA commits
+         mbar_init(&empty[i], 1);  // the MMA commit
       }
       for (int i = 0; i < 2; i++) {
          mbar_init(&accFull[i], 1);
@@ -173,7 +163,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(320, 1)
    }
    if (warp == 0) tmem_alloc(&tmemBase, 512);
    tc_fence_before();
-   cluster_sync();  // the peer multicasts into this CTA's stages and barriers from here on
+   __syncthreads();
    tc_fence_after();
    const uint32_t tmem = tmemBase;
    // Set-up above overlaps the previous kernel's tail; everything below reads A (written by the
@@ -202,25 +192,24 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(320, 1)
          bool ok = true;
          for (int ui = 0; ok && ui < myUnits; ui++) {
             const int b = image_of(ui);
-            const bool ghost = b >= g.nb;
             for (int mb = 0; ok && mb < g.MB; mb++) {
                const int rowA = b * g.Npos + mb * 128;
                for (int kc = 0; kc < nkc; kc++) {
                   const int j = issued, st = j % nStage, u = j / nStage;
                   if (u > 0 && !(ok = wait_or_abort(&empty[st], (uint32_t)((u - 1) & 1)))) break;
                   uint8_t *base = smem + st * rp.stageBytes;
-                  mbar_arrive_expect_tx(&full[st], (ghost ? 0u : AB) + (X3 ? 2u : 1u) * BW);
-                  if (!ghost) {
-                     tma_load_2d(base, &tmA, &full[st], kc * 64, rowA);
-                     if (X3) tma_load_2d(base + BA, &tmAlo, &full[st], kc * 64, rowA);
+                  mbar_arrive_expect_tx(&full[st], AB + (X3 ? 2u : 1u) * BW);
+                  tma_load_2d(base, &tmA, &full[st], kc * 64, rowA);
+                  if (X3) tma_load_2d(base + BA, &tmAlo, &full[st], kc * 64, rowA);
+                  // the W^T tile as two boxes of KP/2 rows
+#pragma unroll
+                  for (int h = 0; h < 2; h++) {
+                     tma_load_2d(base + AB + h * (BW / 2), &tmWtH, &full[st], kc * 64, h * (KP / 2));
+                     if (X3) tma_load_2d(base + AB + BW + h * (BW / 2), &tmWtloH, &full[st], kc * 64, h * (KP / 2));
                   }
-                  // this CTA's half of the W^T tile, to both CTAs
-                  const uint32_t hoff = crank * (BW / 2);
-                  tma_load_2d_mc(base + AB + hoff, &tmWtH, &full[st], kc * 64, (int)crank * (KP / 2), kPair);
-                  if (X3) tma_load_2d_mc(base + AB + BW + hoff, &tmWtloH, &full[st], kc * 64, (int)crank * (KP / 2), kPair);
                   issued++;
                }
-               if (ok && mb == 0 && !ghost) {
+               if (ok && mb == 0) {
                   // the image's x, into buffer ui % 2 once the residual of unit ui-2 has read it
                   const int xb = ui & 1;
                   if (ui >= 2 && !(ok = wait_or_abort(&xEmpty[xb], (uint32_t)(((ui >> 1) - 1) & 1)))) break;
@@ -249,35 +238,30 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(320, 1)
          int j = 0, blk = 0, mmaBlocks = 0;
          bool ok = true;
          for (int ui = 0; ok && ui < myUnits; ui++) {
-            const bool ghost = image_of(ui) >= g.nb;
             for (int mb = 0; ok && mb < g.MB; mb++) {
                const int a = blk & 1;
-               if (!ghost && blk >= 2 && !(ok = wait_or_abort(&accEmpty[a], (uint32_t)(((blk >> 1) - 1) & 1)))) break;
+               if (blk >= 2 && !(ok = wait_or_abort(&accEmpty[a], (uint32_t)(((blk >> 1) - 1) & 1)))) break;
                const uint32_t d = tmem + a * 256;
                for (int kc = 0; kc < nkc; kc++, j++) {
                   const int st = j % nStage;
                   if (!(ok = wait_or_abort(&full[st], (uint32_t)((j / nStage) & 1)))) break;
-                  if (!ghost) {
-                     tc_fence_after();
-                     const uint32_t base = smem_u32(smem + st * rp.stageBytes);
-                     const int npass = X3 ? 3 : 1;
-                     for (int pass = 0; pass < npass; pass++) {
-                        // hi x hi, then hi x lo(W), then lo(A) x hi
-                        const uint32_t a0 = base + ((X3 && pass == 2) ? BA : 0);
-                        const uint32_t w0 = base + AB + ((X3 && pass == 1) ? BW : 0);
+                  tc_fence_after();
+                  const uint32_t base = smem_u32(smem + st * rp.stageBytes);
+                  const int npass = X3 ? 3 : 1;
+                  for (int pass = 0; pass < npass; pass++) {
+                     // hi x hi, then hi x lo(W), then lo(A) x hi
+                     const uint32_t a0 = base + ((X3 && pass == 2) ? BA : 0);
+                     const uint32_t w0 = base + AB + ((X3 && pass == 1) ? BW : 0);
 #pragma unroll
-                        for (int k = 0; k < 4; k++)
-                           mma_bf16(d, sdesc_sw128(a0 + k * 32), sdesc_sw128(w0 + k * 32), idesc, (kc | pass | k) != 0);
-                     }
+                     for (int k = 0; k < 4; k++)
+                        mma_bf16(d, sdesc_sw128(a0 + k * 32), sdesc_sw128(w0 + k * 32), idesc, (kc | pass | k) != 0);
                   }
-                  mma_commit_mc(&empty[st], kPair);  // the stage is free here once both CTAs are done
+                  mma_commit(&empty[st]);  // the stage is free once these MMAs are done
                }
                if (!ok) break;
-               if (!ghost) {
-                  mma_commit(&accFull[a]);
-                  blk++;
-                  mmaBlocks = blk;
-               }
+               mma_commit(&accFull[a]);
+               blk++;
+               mmaBlocks = blk;
             }
          }
          if (!ok && mmaBlocks > 0) mbar_wait(&accFull[(mmaBlocks - 1) & 1], (uint32_t)(((mmaBlocks - 1) >> 1) & 1));
@@ -295,7 +279,6 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(320, 1)
       int blk = 0;
       for (int ui = 0; ui < myUnits; ui++) {
          const int b = image_of(ui);
-         if (b >= g.nb) break;  // only the last unit can lack an image
          bool stop = false;
          for (int mb = 0; mb < g.MB; mb++, blk++) {
             const int a = blk & 1;
@@ -381,7 +364,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(320, 1)
    __syncthreads();
    if (tid == 0 && abortFlag) atomicExch(err, 1);
    tc_fence_before();
-   cluster_sync();  // neither CTA leaves while the other may still write into it
+   __syncthreads();
    if (warp == 0) tmem_dealloc(tmem, 512);
 }
 
@@ -1077,8 +1060,8 @@ __global__ void __launch_bounds__(608, 1) step_tc_kernel(const __grid_constant__
       // An event loop over two in-order streams: GEMM1 of block g1 as soon as its weight tile,
       // its accumulator and (first block of a tile) the im2col operand are ready; GEMM2 of
       // block g2 < g1 as soon as the epilogue has written its A tile.  GEMM1 of the next block
-      // therefore never waits behind GEMM2 of an earlier one.  Polls never suspend; a bounded
-      // count of idle polls (or the abort flag) ends the loop.
+      // therefore never waits behind GEMM2 of an earlier one.  Polls never suspend; the loop
+      // ends when nothing has been ready for the wait limit's time (or on the abort flag).
       if (lane == 0 && Q > 0) {
          const uint32_t idesc1 = idesc_bf16(128, kPostNT), idesc2 = idesc_bf16_bmn(128, KP);
          bool ok = true;
@@ -1086,6 +1069,7 @@ __global__ void __launch_bounds__(608, 1) step_tc_kernel(const __grid_constant__
          int g1 = 0, ti1 = 0, nb1 = 0, sw1 = 0, uw1 = 0;
          int g2 = 0, nb2 = 0, sw2 = 0;
          uint32_t idle = 0;
+         uint64_t idleSince = 0;
          while (ok && g2 < Q) {
             bool did = false;
             if (g1 < Q) {
@@ -1139,11 +1123,16 @@ __global__ void __launch_bounds__(608, 1) step_tc_kernel(const __grid_constant__
             }
             if (did) {
                idle = 0;
-            } else if (abortFlag || ++idle > kWaitLimit) {
-               abortFlag = 1;
+            } else if (abortFlag) {
                ok = false;
-            } else if (idle > 16) {
-               __nanosleep(32);  // leave the issue slots to the epilogue warps on this sub-partition
+            } else {
+               if (idle == 0) idleSince = global_ns();
+               if ((++idle & 255) == 0 && global_ns() - idleSince > kWaitNs) {
+                  abortFlag = 1;
+                  ok = false;
+               } else if (idle > 16) {
+                  __nanosleep(32);  // leave the issue slots to the epilogue warps on this sub-partition
+               }
             }
          }
          // MMAs still in flight finish before shared memory and TMEM go away
@@ -1648,7 +1637,7 @@ struct pvgpu_lca_solver {
    bool profiling = false;
    // the BF16 run as one CUDA graph: captured on capStream, replayed on the caller's stream;
    // rebuilt when the input pointer or the step counts change
-   int maxPairs[2] = {0, 0};  // co-resident kernel-R clusters (BF16, BF16x3)
+   int maxRecon[2] = {0, 0};  // co-resident kernel-R CTAs (BF16, BF16x3)
    cudaStream_t capStream = nullptr;
    cudaGraphExec_t graph = nullptr;
    const float *graphX = nullptr;
@@ -1734,7 +1723,7 @@ PostPlan make_post_plan(const LcaGeom &g, int S, int P, int C, bool x3, int numS
    return pl;
 }
 
-ReconPlan recon_plan_for(const LcaGeom &g, int S, int P, int C, bool x3, int maxPairs, int nStage) {
+ReconPlan recon_plan_for(const LcaGeom &g, int S, int P, int C, bool x3, int maxCtas, int nStage) {
    const int KP = P * P * C, E = (P - S) / 2;
    auto al = [](uint32_t v) { return (v + 1023u) & ~1023u; };
    ReconPlan rp;
@@ -1753,16 +1742,15 @@ ReconPlan recon_plan_for(const LcaGeom &g, int S, int P, int C, bool x3, int max
    rp.xStride = imgB;
    o += imgB;
    rp.total = o + 1024;
-   const int units = (g.nb + 1) / 2;
-   rp.G = 2 * (maxPairs < units ? maxPairs : units);
+   rp.G = maxCtas < g.nb ? maxCtas : g.nb;
    return rp;
 }
 
 // The default shape: the deepest ring that fits.
-ReconPlan make_recon_plan(const LcaGeom &g, int S, int P, int C, bool x3, int maxPairs) {
-   ReconPlan rp = recon_plan_for(g, S, P, C, x3, maxPairs, 2);
+ReconPlan make_recon_plan(const LcaGeom &g, int S, int P, int C, bool x3, int maxCtas) {
+   ReconPlan rp = recon_plan_for(g, S, P, C, x3, maxCtas, 2);
    for (int n = kMaxRStages; n >= 2; n--) {
-      rp = recon_plan_for(g, S, P, C, x3, maxPairs, n);
+      rp = recon_plan_for(g, S, P, C, x3, maxCtas, n);
       if (rp.total <= kSmemBudget) break;
    }
    return rp;
@@ -1851,9 +1839,9 @@ struct StepArgs {
 
 // Kernel R's and kernel P's persistent grids for nb images under the schedule's caps.
 void size_grids(const pvgpu_lca_solver *s, int nb, bool x3, ReconPlan &rp, PostPlan &pl) {
-   int pairs = std::min(s->maxPairs[x3 ? 1 : 0], (nb + 1) / 2);
-   if (s->sched.reconCtas >= 2) pairs = std::min(pairs, s->sched.reconCtas / 2);
-   rp.G = 2 * std::max(pairs, 1);
+   int rctas = std::min(s->maxRecon[x3 ? 1 : 0], nb);
+   if (s->sched.reconCtas > 0) rctas = std::min(rctas, s->sched.reconCtas);
+   rp.G = std::max(rctas, 1);
    const int nTiles = nb * s->g.MB * (s->g.F / pl.FT);
    int ctas = g_num_sms;
    if (s->sched.postCtas > 0) ctas = std::min(ctas, s->sched.postCtas);
@@ -1879,9 +1867,8 @@ StepArgs step_args(const pvgpu_lca_solver *s, int view, const float *x, bool x3)
    a.fp = s->fplan;
    size_fuse_grid(s, a.g.nb, a.fp);
    // Kernels R and F take all 512 TMEM columns, whose allocation waits without a bound: a CTA
-   // of either never shares an SM (more than half of the SM's shared memory per CTA), or two
-   // kernel R clusters placed across the same two SMs could each hold one SM's TMEM while
-   // waiting for the other at their cluster barrier.  With two chains kernel P (256 columns)
+   // of either never shares an SM (more than half of the SM's shared memory per CTA), so no CTA
+   // waits for TMEM that another CTA holds while it waits on the first.  With two chains kernel P (256 columns)
    // gets an SM to itself as well: a CTA of one chain must not wait for TMEM held by a CTA that
    // waits, through its own chain, on the first one.
    a.rp.total = std::max(a.rp.total, kSmemHalfSm);
@@ -1969,24 +1956,20 @@ struct Launcher {
                                          (const float *)a.xpad, a.V, a.A, a.Alo, a.err);
       return e == cudaSuccess ? PVGPU_OK : pvgpu::record_cuda_error(e, "lca fused step");
    }
-   // clusters of two recon CTAs that can be resident at once (one CTA per SM)
-   static int max_pairs(const ReconPlan &rp, bool x3) {
+   // recon CTAs that can be resident at once (one CTA per SM)
+   static int max_recon_ctas(const ReconPlan &rp, bool x3) {
       const void *fn = x3 ? reinterpret_cast<const void *>(recon_tc_kernel<S, P, C, true>)
                           : reinterpret_cast<const void *>(recon_tc_kernel<S, P, C, false>);
       if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rp.total) != cudaSuccess) {
          cudaGetLastError();
          return 0;
       }
-      cudaLaunchConfig_t cfg = {};
-      cfg.gridDim = dim3(2 * 76, 1, 1);
-      cfg.blockDim = dim3(320, 1, 1);
-      cfg.dynamicSmemBytes = rp.total;
       int n = 0;
-      if (cudaOccupancyMaxActiveClusters(&n, fn, &cfg) != cudaSuccess) {
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, 320, rp.total) != cudaSuccess) {
          cudaGetLastError();
          return 0;
       }
-      return n;
+      return std::min(n, 1) * g_num_sms;
    }
    static bool fits(const pvgpu_lca_solver *s, bool x3) {
       const uint32_t pt = x3 ? s->planX3.total : s->plan.total;
@@ -2099,7 +2082,7 @@ void set_shapes(pvgpu_lca_solver *s, const TunedShapes &t) {
       const int *q = t.post[x3];
       PostPlan pl = post_plan_for(s->g, s->S, s->P, s->C, x3 != 0, g_num_sms, q[0], q[1], q[2], q[3]);
       if (pl.total && pl.total <= kSmemBudget) (x3 ? s->planX3 : s->plan) = pl;
-      ReconPlan rp = recon_plan_for(s->g, s->S, s->P, s->C, x3 != 0, s->maxPairs[x3], t.recon[x3]);
+      ReconPlan rp = recon_plan_for(s->g, s->S, s->P, s->C, x3 != 0, s->maxRecon[x3], t.recon[x3]);
       if (rp.total <= kSmemBudget) (x3 ? s->rplanX3 : s->rplan) = rp;
    }
    if (t.sched.chains == 1 || (s->g.nb >= 2 && s->capStream2)) s->sched = t.sched;
@@ -2242,17 +2225,17 @@ extern "C" pvgpu_status pvgpu_lca_solver_create(const pvgpu_lca_solver_desc *d, 
          std::memset(&s->fplan, 0, sizeof(s->fplan));
       }
    }
-   s->rplan = make_recon_plan(g, S, P, C, false, g_num_sms / 2);
-   s->rplanX3 = make_recon_plan(g, S, P, C, true, g_num_sms / 2);
-   s->maxPairs[0] = s->maxPairs[1] = g_num_sms / 2;
+   s->rplan = make_recon_plan(g, S, P, C, false, g_num_sms);
+   s->rplanX3 = make_recon_plan(g, S, P, C, true, g_num_sms);
+   s->maxRecon[0] = s->maxRecon[1] = g_num_sms;
    dispatch(S, P, C, [&](auto L) {
-      // as many pairs as can be resident together (the kernel is persistent)
+      // as many CTAs as can be resident together (the kernel is persistent)
       for (int x3 = 0; x3 < 2; x3++) {
          ReconPlan &rp = x3 ? s->rplanX3 : s->rplan;
-         const int n = L.max_pairs(rp, x3 != 0);
+         const int n = L.max_recon_ctas(rp, x3 != 0);
          if (n > 0) {
-            s->maxPairs[x3] = std::min(n, g_num_sms / 2);
-            rp = make_recon_plan(g, S, P, C, x3 != 0, s->maxPairs[x3]);
+            s->maxRecon[x3] = std::min(n, g_num_sms);
+            rp = make_recon_plan(g, S, P, C, x3 != 0, s->maxRecon[x3]);
          }
       }
       return PVGPU_OK;
@@ -2511,7 +2494,7 @@ extern "C" pvgpu_status pvgpu_lca_solver_autotune(pvgpu_lca_solver *s, const flo
       // kernel R: every ring depth that fits
       bestMs = 1e30;
       for (int n = 2; n <= kMaxRStages; n++) {
-         ReconPlan rp = recon_plan_for(s->g, s->S, s->P, s->C, x3 != 0, s->maxPairs[x3], n);
+         ReconPlan rp = recon_plan_for(s->g, s->S, s->P, s->C, x3 != 0, s->maxRecon[x3], n);
          if (rp.total > kSmemBudget) continue;
          curR = rp;
          double r = 0, p = 0;

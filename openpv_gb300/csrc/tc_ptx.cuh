@@ -15,9 +15,17 @@
 namespace pvgpu {
 namespace tc {
 
-// Iteration limit of every device-side wait: well beyond any legitimate latency
-// (a few ms at ~1 ns per probe); after it the kernel records a timeout and returns.
-constexpr uint32_t kWaitLimit = 1u << 22;
+// Time limit of every device-side wait, in ns of the global timer: far beyond any legitimate
+// latency inside one launch (the longest waits here are a few microseconds); after it the
+// kernel records a timeout and returns.  Waits are bounded by elapsed time, not by a count of
+// probes, because one mbarrier.try_wait may suspend the thread for a system-dependent interval.
+constexpr uint64_t kWaitNs = 200ull * 1000ull * 1000ull;
+
+__device__ __forceinline__ uint64_t global_ns() {
+   uint64_t t;
+   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+   return t;
+}
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -58,12 +66,16 @@ __device__ __forceinline__ bool mbar_test(uint64_t *bar, uint32_t parity) {
    return ok != 0;
 }
 
-// Bounded wait for the phase with the given parity; false on timeout.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
-   for (uint32_t i = 0; i < kWaitLimit; i++) {
-      if (mbar_try_wait(bar, parity)) return true;
+// Wait for the phase with the given parity, for at most limitNs of elapsed time (the clock is
+// read once per 64 probes); false on timeout.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, uint64_t limitNs = kWaitNs) {
+   if (mbar_try_wait(bar, parity)) return true;
+   const uint64_t t0 = global_ns();
+   for (;;) {
+      for (int i = 0; i < 64; i++)
+         if (mbar_try_wait(bar, parity)) return true;
+      if (global_ns() - t0 > limitNs) return false;
    }
-   return false;
 }
 
 // ---- TMA -------------------------------------------------------------------------------
@@ -268,37 +280,6 @@ __device__ __forceinline__ void griddep_launch_dependents() { asm volatile("grid
 // Wait until the grids this one depends on have completed and their memory is visible.
 __device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 
-// ---- clusters ----------------------------------------------------------------------------
-__device__ __forceinline__ uint32_t cluster_ctarank() {
-   uint32_t r;
-   asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
-   return r;
-}
-
-// Every thread of every CTA of the cluster (release / acquire).
-__device__ __forceinline__ void cluster_sync() {
-   asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
-}
-
-// TMA tile load delivered to the same shared-memory offset in every CTA of `mask`, each CTA's
-// mbarrier at the offset of `bar` receiving the bytes it got.
-__device__ __forceinline__ void tma_load_2d_mc(void *dst, const CUtensorMap *map, uint64_t *bar, int c0, int c1,
-                                               uint16_t mask) {
-   asm volatile(
-         "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes.multicast::cluster"
-         " [%0], [%1, {%2, %3}], [%4], %5;" ::"r"(smem_u32(dst)),
-         "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(smem_u32(bar)), "h"(mask)
-         : "memory");
-}
-
-// Arrive on the mbarrier at the offset of `bar` in every CTA of `mask` once every tcgen05.mma
-// this thread issued so far has completed.
-__device__ __forceinline__ void mma_commit_mc(uint64_t *bar, uint16_t mask) {
-   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(
-                      smem_u32(bar)),
-                "h"(mask)
-                : "memory");
-}
 
 // Barrier among `count` threads (a multiple of 32) on hardware barrier `id` (1..15).
 __device__ __forceinline__ void named_bar_sync(int id, int count) {
