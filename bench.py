@@ -219,6 +219,114 @@ def run_reference(args, rank, world):
 
 
 # ---------------------------------------------------------------------------------------------
+# plain LCA, batch 1 (32x32x1 -> 16x16x64, 8x8x1 features, 200 timesteps): absolute latency
+# ---------------------------------------------------------------------------------------------
+def config1_bench(torch, capi, steps=200, reps=5):
+    """Latency of one timestep of the plain LCA configuration at batch 1, four ways: the C ABI
+    entry points composed in the reference's phase order (what the reference's GPU layer and
+    delivery classes call per timestep: error accumulate + identity threshold, postsynaptic
+    delivery, LCA update + threshold, compaction, presynaptic sparse delivery, energy probes),
+    launched one by one and as one captured CUDA graph of the 200 timesteps; the LCA solver's
+    FP32 and BF16 forms; and the CPU oracle on one core."""
+    import time
+    from oracle import oracle as O
+    rng = np.random.default_rng(1234 + 1)
+    x_np = rng.uniform(0.0, 1.0, (1, 32, 32, 1))
+    x_np = (x_np - x_np.mean()).astype(np.float32)
+    w_np = rng.normal(size=(64, 8, 8, 1))
+    w_np = (w_np / np.sqrt((w_np ** 2).sum(axis=(1, 2, 3), keepdims=True))).astype(np.float32)
+    vt, inf = 0.1, float("inf")
+    v1 = capi.Loc.make(1, 16, 16, 64, 2)
+    er = capi.Loc.make(1, 32, 32, 1, 3)
+    wd = torch.from_numpy(w_np).cuda()
+    xd = torch.from_numpy(x_np).cuda()
+    pre_conn, post_conn = capi.conn_desc(v1, er, 8, 8), capi.conn_desc(er, v1, 4, 4)
+    v = torch.zeros(v1.res_shape(), device="cuda")
+    a1 = torch.zeros(v1.ext_shape(), device="cuda")
+    gsyn_e = torch.zeros((2,) + er.res_shape(), device="cuda")
+    ge = torch.zeros(er.res_shape(), device="cuda")
+    ae = torch.zeros(er.ext_shape(), device="cuda")
+    g1 = torch.zeros(v1.res_shape(), device="cuda")
+    ent = torch.zeros((1, v1.num_ext, 2), dtype=torch.int32, device="cuda")
+    num = torch.zeros(1, dtype=torch.int64, device="cuda")
+    scr = torch.empty(capi.lib().pvgpu_compact_scratch_bytes(1, v1.num_ext), dtype=torch.uint8, device="cuda")
+    dt = torch.ones(1, dtype=torch.float64, device="cuda")
+    l2 = torch.zeros(1, dtype=torch.float64, device="cuda")
+    l1 = torch.zeros(1, dtype=torch.float64, device="cuda")
+
+    def reset():
+        v.zero_()
+        capi.ann_activity(v1, v, vt, 0.0, inf, vt, 0.0, a1)
+        gsyn_e.zero_()
+        gsyn_e[0].copy_(xd)
+
+    def timestep(mode):
+        capi.gsyn_accumulate(er.num_res, [1.0, -1.0], gsyn_e, ge)
+        capi.ann_activity(er, ge, -inf, -inf, inf, 0.0, 0.0, ae)
+        g1.zero_()
+        capi.deliver_post(post_conn, ae, wd, g1, mode=mode)
+        capi.lca_update(v1, True, dt, 100.0, g1, a1, v)
+        capi.ann_activity(v1, v, vt, 0.0, inf, vt, 0.0, a1)
+        capi.compact_active(a1, 1, v1.num_ext, ent, num, scratch=scr)
+        gsyn_e[1].zero_()
+        capi.deliver_pre(pre_conn, wd, gsyn_e[1], entries=ent, num_active=num, mode=mode)
+        capi.cost_sum(er, ae, capi.COST_L2, 0.0, 0.0, l2)
+        capi.cost_sum(v1, a1, capi.COST_L1, 0.0, 0.0, l1)
+
+    def events_ms(fn, n=reps):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(n):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / n
+
+    out = {"workload": "plain LCA, batch 1: 32x32x1 uniform[0,1] minus its mean -> V1 16x16x64 stride 2, 64 x 8x8x1 "
+                       "N(0,1) L2-normalised, VThresh=AShift=0.1, AMin=0, tau=100, dt=1, 200 timesteps",
+           "timesteps": steps}
+    per_mode = {}
+    for name, mode in (("reference_order", capi.DELIVER_REFERENCE_ORDER), ("fast", capi.DELIVER_FAST)):
+        def run_all(mode=mode):
+            reset()
+            for _ in range(steps):
+                timestep(mode)
+        launched_ms = events_ms(run_all, 2)
+        reset()
+        gr = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(gr):
+            for _ in range(steps):
+                timestep(mode)
+        graph_ms = events_ms(lambda: (reset(), gr.replay()))
+        per_mode[name] = {"launched_ms_per_step": launched_ms / steps, "graph_ms_per_step": graph_ms / steps,
+                          "kernels_per_step": 11}
+        del gr
+    out["c_abi_composed"] = per_mode
+    for name, prec, x3 in (("fp32_solver", capi.LCA_FP32, 0), ("bf16_solver", capi.LCA_BF16, 25)):
+        s = capi.LcaSolver(1, (32, 32, 1), (16, 16, 64), 8, vt)
+        s.set_weights(wd)
+
+        def solve(s=s, prec=prec, x3=x3):
+            s.reset()
+            s.run(xd, steps, x3_steps=x3, precision=prec)
+        ms = events_ms(solve)
+        assert s.error_flag() == 0
+        out[name] = {"ms_per_step": ms / steps, "image_steps_per_s": steps / (ms / 1e3)}
+        if x3:
+            out[name]["bf16x3_last_steps"] = x3
+        s.close()
+    p = O.lca_params()
+    t0 = time.perf_counter()
+    O.lca_run(p, w_np, x_np[None], steps, np.zeros((1, 16, 16, 64), np.float32), want_recon=False)
+    cpu_s = time.perf_counter() - t0
+    out["cpu_oracle"] = {"ms_per_step": cpu_s * 1e3 / steps, "cores": 1, "kind": "port",
+                         "sample": "oracle, the whole 200-timestep run at batch 1 on one core"}
+    return out
+
+
+# ---------------------------------------------------------------------------------------------
 # delivery microbenchmark (presynaptic sparse delivery, 128x128x256 -> 128x128x64, 7x7, batch 16)
 # ---------------------------------------------------------------------------------------------
 def delivery_bench(torch, capi, reps=5):
@@ -248,6 +356,27 @@ def delivery_bench(torch, capi, reps=5):
         torch.cuda.synchronize()
         return e0.elapsed_time(e1) / n
 
+    def graph_timed(fn, n, reps=3):
+        # n calls captured in one CUDA graph, so that host launch overhead does not show in
+        # the time of a kernel that runs for tens of microseconds
+        fn()
+        torch.cuda.synchronize()
+        gr = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(gr):
+            for _ in range(n):
+                fn()
+        gr.replay()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            gr.replay()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / (reps * n)
+
+    hbm_peak = peaks()["hbm_gbs"]
+    cscratch = torch.empty(capi.lib().pvgpu_compact_scratch_bytes(nb, pre.num_ext), dtype=torch.uint8,
+                           device="cuda")
     dense_flops = 2 * nb * 128 * 128 * 64 * 49 * 256
     out = {}
     for p in (0.01, 0.05, 0.2):
@@ -262,8 +391,8 @@ def delivery_bench(torch, capi, reps=5):
         # algorithmic bytes: entries read, GSyn read+write, weights once
         byts = 8 * nnz + 8 * post.num_res * nb + 4 * w.numel()
         flops = 2 * nnz * 7 * 7 * 64
-        cms = timed(lambda: capi.compact_active(a, nb, pre.num_ext, entries, num), reps)
-        cbytes = 2 * 4 * pre.num_ext * nb + 8 * nnz  # two passes over the activity + entries written
+        cms = graph_timed(lambda: capi.compact_active(a, nb, pre.num_ext, entries, num, scratch=cscratch), 10)
+        cbytes = 4 * pre.num_ext * nb + 8 * nnz  # one read of the activity + entries written
         tms = timed(lambda: capi.deliver_pre_tc(conn, a, w, gtc, ws), reps)
         # size-independent check at full size: both kernels from zero give the same GSyn
         gsyn.zero_()
@@ -274,6 +403,7 @@ def delivery_bench(torch, capi, reps=5):
         rel = float((gsyn - gtc).abs().max().item() / max(gsyn.abs().max().item(), 1e-30))
         out[str(p)] = {"nnz_per_image": nnz / nb, "ms": ms, "GB_s": byts / ms / 1e6, "GFLOP_s": flops / ms / 1e6,
                        "compaction_ms": cms, "compaction_GB_s": cbytes / cms / 1e6,
+                       "compaction_frac_of_measured_hbm": cbytes / cms / 1e6 / hbm_peak,
                        "tc_ms": tms, "tc_dense_TFLOP_s": dense_flops / tms / 1e9,
                        "best_ms": min(ms, tms), "best": "sparse" if ms <= tms else "tensor-core",
                        "sparse_vs_tc_max_rel_diff": rel}
@@ -696,14 +826,27 @@ def run_ours(args, rank, world, local_rank):
     launches_per_solve = 2 + chains * per_chain
     cpu_val, cpu_dt = cpu_sample(cfg, cores, warm_steps=25, timed_steps=25)
     deliv = delivery_bench(torch, capi)
+    c1b = config1_bench(torch, capi)
     lifb = lif_bench(torch, capi)
     dlb = dictlearn_bench(torch)
     clocks = clk.summary()
 
+    # the FP32 form against its own ceiling: FP32 FMA lanes x 2 FLOP x SM clock (nominal lanes,
+    # sampled clock), on 4 x 25,165,824 FLOP per image-timestep (post delivery + reconstruction)
+    props = torch.cuda.get_device_properties(0)
+    sm_mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz") or 2070.0
+    fp32_peak_tflops = props.multi_processor_count * 128 * 2 * sm_mhz * 1e6 / 1e12
+    flop_unit = 4 * npos * F * cfg["nxp"] ** 2 * cfg["in_shape"][2]
+    fp32_tflops = value32 * flop_unit / 1e12
     line = {
         "metric": METRIC,
         "value": value,
         "unit": "images*steps/s",
+        "final_energy_rel_err_vs_fp64": rel_bf16,
+        "speedup_bf16_over_fp32_form": value / world / value32,
+        "fp32_form": {"value": value32, "unit": "images*steps/s", "final_energy_rel_err_vs_fp64": rel_fp32,
+                      "TFLOP_s": fp32_tflops, "fp32_fma_ceiling_tflops": fp32_peak_tflops,
+                      "frac_of_fp32_fma_ceiling": fp32_tflops / fp32_peak_tflops},
         "n_gpus": world,
         "steps": args.steps,
         "warmup": args.warmup,
@@ -728,9 +871,6 @@ def run_ours(args, rank, world, local_rank):
                         "GB_s": post_bytes_launch / (post_avg_ms / 1e3) / 1e9 if nP else None},
         "recon_kernel": {"avg_launch_ms": recon_avg_ms, "GB_s": recon_bytes_unit * nb / (recon_avg_ms / 1e3) / 1e9,
                          "TFLOP_s": recon_flops_launch / (recon_avg_ms / 1e3) / 1e12},
-        "fp32_form": {"value": value32, "unit": "images*steps/s", "speedup_bf16_over_fp32": value / world / value32,
-                      "final_energy_rel_err_vs_fp64": rel_fp32},
-        "final_energy_rel_err_vs_fp64": rel_bf16,
         "energy_check_images": nchk,
         "cpu_baseline": {"value": cpu_val, "unit": "images*steps/s", "cores": cores, "kind": "port",
                          "sample": f"oracle FP32 LCA, {cores} images (one per thread) x 25 timesteps after 25 "
@@ -740,6 +880,7 @@ def run_ours(args, rank, world, local_rank):
                                  "densities; postsynaptic FP32 SIMT and tensor-core",
                      "by_density": {k: v for k, v in deliv.items() if k != "post"}, "post": deliv["post"],
                      "hbm_peak_gbs": pk["hbm_gbs"], "tf32_tensor_peak_tflops": pk["bf16_tflops"] / 2},
+        "plain_lca_batch1": c1b,
         "lif_network": lifb,
         "dictionary_learning": dlb,
         "clocks": clocks,
@@ -763,7 +904,16 @@ def main():
     ap.add_argument("--lif", action="store_true",
                     help="run the LIF network only (profiling runs; not a bench line)")
     ap.add_argument("--lif-steps", type=int, default=1000, help="timesteps of the LIF network graph (--lif)")
+    ap.add_argument("--plain-lca", action="store_true",
+                    help="run the batch-1 plain LCA latency section only (profiling runs; not a bench line)")
     args = ap.parse_args()
+    if args.plain_lca:
+        import torch
+        from openpv_gb300 import build
+        build.build()
+        from openpv_gb300 import capi
+        print(json.dumps({"plain_lca_batch1": config1_bench(torch, capi, reps=1)}))
+        return
     if args.lif:
         import torch
         from openpv_gb300 import build

@@ -76,12 +76,24 @@ const char *pvgpu_status_string(pvgpu_status s);
 /* Last CUDA error string recorded by a failing call on this thread. */
 const char *pvgpu_last_error(void);
 
+/* Diagnostic, no counterpart in the reference (whose CUDA errors are fatal): runs one CTA whose
+ * warp waits on an mbarrier that nothing arrives at, bounded by limitNs (0 < limitNs <= 1 s) of
+ * the device's global timer, and takes the path every kernel here takes when a bounded wait
+ * expires (abort flag seen by the other roles, tensor memory freed, status reported).
+ * Synchronous; hostOut2 receives {1 if the wait expired, nanoseconds waited}; returns
+ * PVGPU_ERR_TIMEOUT when the wait expired (the expected result) and leaves the context usable. */
+pvgpu_status pvgpu_selftest_wait_expiry(uint64_t limitNs, long long *hostOut2, void *stream);
+
 /* ---- a1: active-index compaction ------------------------------------------------------
  * Replaces DataStore::updateActiveIndices (columns/DataStore.cpp:46-66), which the reference
  * runs on the host after a device->host copy.  Stable: entries of each batch element are in
  * ascending extended index, value = the exact activity float; numActive[b] (long in the
  * reference) receives the count.  entries has capacity numExt per batch element.
- * Scratch: uses `scratch` (device, >= pvgpu_compact_scratch_bytes) for per-chunk counts. */
+ * One pass over the activity (chunks of 8192 values; a decoupled look-back carries the chunk
+ * prefixes).  Scratch: `scratch` (device, 8-byte aligned, >= pvgpu_compact_scratch_bytes) holds
+ * a ticket word and one status word per chunk; the call clears it on the stream first.
+ * entries must be 8-byte aligned.  numActive[b] = -1 reports a look-back that gave up waiting
+ * (bounded device wait; never expected). */
 size_t pvgpu_compact_scratch_bytes(int nbatch, int64_t numExt);
 pvgpu_status pvgpu_compact_active(
       const float *aExt,
@@ -94,16 +106,19 @@ pvgpu_status pvgpu_compact_active(
       void *stream);
 
 /* The same compaction with no device allocation and no caller scratch.  No counterpart in the
- * reference: it exists for callers that cannot allocate device memory at the call site -- code
- * in a host function enqueued on a stream, loops that must not incur cudaMalloc's implicit
- * synchronisation, hosts whose device memory belongs to their own pool allocator.  The chunk
- * counts live in a fixed 1 MiB array inside the library's device image (loaded once per device,
- * kept until the process exits), which limits a call to nbatch * ceil(numExt / 4096) <= 262144;
- * larger calls return PVGPU_ERR_BAD_ARG with a message in pvgpu_last_error().  The first call on
- * a device looks up the array's device address (cudaGetSymbolAddress, with that device current)
- * and caches it; make that first call before any stream capture.  All calls share the one array:
- * calls that overlap on the GPU (concurrent streams, or several host threads) race on it and
- * must be serialised by the caller.  Output equals pvgpu_compact_active's. */
+ * reference: it exists for callers that cannot allocate device memory at the call site -- loops
+ * that must not incur the implicit device synchronisation cudaMalloc / cudaFree may cause, and
+ * hosts whose device memory all belongs to their own pool allocator.  The ticket and chunk
+ * statuses live in a fixed 1 MiB array inside the library's device image (loaded once per
+ * device, kept until the process exits), which limits a call to
+ * nbatch * ceil(numExt / 8192) <= 131071; larger calls return PVGPU_ERR_BAD_ARG with a message
+ * in pvgpu_last_error().  Each call clears the part of the array it uses (cudaMemsetAsync on the
+ * stream) before its kernel reads it.  The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress, with that device current) and caches it per device ordinal for
+ * the life of the process (not across cudaDeviceReset); make that first call before any stream
+ * capture.  All calls share the one array: calls that overlap on the GPU (concurrent streams,
+ * or several host threads) race on it and must be serialised by the caller.  Output equals
+ * pvgpu_compact_active's. */
 pvgpu_status pvgpu_compact_active_noalloc(
       const float *aExt,
       int nbatch,

@@ -18,6 +18,7 @@ LIB_PATH = os.path.join(HERE, "libpvgpu.so")
 
 PVGPU_OK = 0
 PVGPU_ERR_BAD_ARG = 1
+PVGPU_ERR_TIMEOUT = 4
 PVGPU_ERR_UNSUPPORTED_SHAPE = 5
 DELIVER_FAST = 0
 DELIVER_REFERENCE_ORDER = 1
@@ -160,6 +161,7 @@ def _declare(L):
         "pvgpu_pvp_dense_frames": (i, [lp, vp, vp, vp]),
         "pvgpu_pvp_scatter_sparse": (i, [lp, vp, vp, vp, vp, vp]),
         "pvgpu_taus_init": (i, [vp, i64, C.c_uint32, vp]),
+        "pvgpu_selftest_wait_expiry": (i, [C.c_uint64, C.POINTER(C.c_longlong), vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -343,6 +345,13 @@ def cost_sum(loc, buf_ext, kind, p0, p1, out, stream=None):
 def hebbian_dw(conn, dw_max, pre_ext, post_ext, dw, stream=None):
     check(lib().pvgpu_hebbian_dw(C.byref(conn), dw_max, _ptr(pre_ext), _ptr(post_ext), _ptr(dw), _stream(stream)),
           "hebbian_dw")
+
+
+def selftest_wait_expiry(limit_ns, stream=None):
+    """(status, expired, ns waited) of a bounded device wait that nothing satisfies."""
+    out = (C.c_longlong * 2)()
+    st = lib().pvgpu_selftest_wait_expiry(int(limit_ns), out, _stream(stream))
+    return st, int(out[0]), int(out[1])
 
 
 def tc_gemm_bf16(A, B, C, M, N, K, err, stream=None):

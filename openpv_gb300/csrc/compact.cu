@@ -1,168 +1,309 @@
 // compact.cu -- a1: stable active-index compaction (DataStore::updateActiveIndices,
-// columns/DataStore.cpp:46-66) on the device.
+// columns/DataStore.cpp:46-66) on the device, in one pass over the activity.
 //
-// Layout: each batch element's extended activity is cut into chunks of kChunk floats.
-// Pass 1 counts nonzeros per chunk, pass 2 scans the chunk counts of each batch element
-// (and writes numActive), pass 3 re-reads each chunk and writes {index, value} entries at
-// the chunk's offset.  Inside a chunk, 256 threads take 256 consecutive elements per
-// iteration (coalesced loads); a warp ballot plus a block scan of the 8 warp counts gives
-// every nonzero its rank, so entries come out in ascending index exactly as the host loop
-// produces them.  Integer/byte work: HBM-bound, 2 reads of the activity + 8 B per entry.
+// Each batch element's extended activity is cut into chunks of kChunk = 8192 floats; one CTA of
+// 512 threads takes one chunk.  Thread t of the CTA loads the chunk's units k*512 + t
+// (k = 0 .. KU-1; a unit is a float4 when every image starts on a 16-byte boundary, else one
+// float), so every load instruction of a warp reads one contiguous run.  Entries must come out
+// in ascending extended index, i.e. in (k, warp, lane, element-of-unit) order:
+//   * inside a warp, the rank of a thread's unit k comes from a warp scan of the per-thread
+//     counts (float4 units: four 8-bit fields, one per k, scanned together in one 32-bit scan;
+//     scalar units: a ballot per k);
+//   * across the warps, warp 0 scans the KU x 16 warp totals in (k, warp) order;
+//   * across chunks, a decoupled look-back (Merrill & Garland, "Single-pass Parallel Prefix Scan
+//     with Decoupled Look-back", 2016): the CTA publishes its chunk total as soon as it is
+//     known, then warp 0 reads the status words of up to 128 predecessors per round trip,
+//     summing totals back to the nearest chunk that has published its inclusive prefix.
+// CTAs draw their (chunk, image) from an atomic ticket in the scratch, chunk-major so that the
+// chunks in flight spread over all images' chains; every predecessor a CTA waits for holds a
+// smaller ticket and is already running, so the look-back always ends.  Its spin is still bounded in time;
+// a CTA that gives up publishes an error status that propagates down the image's chain and
+// makes the image's count -1.
+//
+// Integer/byte work, HBM-bound: one read of the activity + 8 B per entry written.
+// Scratch: one 8-byte ticket word, then one 8-byte status word per chunk, zeroed before each call.
 #include "pvgpu_internal.cuh"
+#include "tc_ptx.cuh"
 
 #include <mutex>
 
 namespace {
 
-constexpr int kThreads = 256;
-constexpr int kIters = 16;
-constexpr int kChunk = kThreads * kIters;
+constexpr int kThreads = 512;
+constexpr int kWarps = kThreads / 32;
+constexpr int kChunk = 8192;
+constexpr uint64_t kFlagAgg = 1ull << 62, kFlagPre = 2ull << 62, kFlagErr = 3ull << 62;
 
-__global__ void __launch_bounds__(kThreads) count_kernel(const float *__restrict__ a, int64_t numExt, int nchunks,
-                                                         uint32_t *__restrict__ counts) {
-   const int c = blockIdx.x, b = blockIdx.y;
-   const float *ab = a + (size_t)b * numExt;
-   int64_t base = (int64_t)c * kChunk;
-   int cnt = 0;
-#pragma unroll 4
-   for (int i = 0; i < kIters; i++) {
-      int64_t e = base + i * kThreads + threadIdx.x;
-      bool nz = e < numExt && ab[e] != 0.0f;
-      cnt += __popc(__ballot_sync(0xffffffffu, nz));
-   }
-   __shared__ int wsum[kThreads / 32];
-   if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = cnt;
-   __syncthreads();
-   if (threadIdx.x == 0) {
-      int t = 0;
-      for (int w = 0; w < kThreads / 32; w++) t += wsum[w];
-      counts[(size_t)b * nchunks + c] = (uint32_t)t;
-   }
+__device__ __forceinline__ void st_release(uint64_t *p, uint64_t v) {
+   asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ uint64_t ld_acquire(const uint64_t *p) {
+   uint64_t v;
+   asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+   return v;
 }
 
-// One block per batch element: exclusive scan of the chunk counts, in place.
-__global__ void __launch_bounds__(1024) scan_kernel(uint32_t *__restrict__ counts, int nchunks,
-                                                    int64_t *__restrict__ numActive) {
-   const int b = blockIdx.x;
-   uint32_t *cb = counts + (size_t)b * nchunks;
-   __shared__ uint32_t warpTot[32];
-   __shared__ uint32_t carry;
-   if (threadIdx.x == 0) carry = 0;
+__device__ __forceinline__ uint32_t lanemask_lt() {
+   uint32_t m;
+   asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+   return m;
+}
+
+// VEC = 4: float4 units (every image 16-byte aligned); VEC = 1: scalar units.
+template <int VEC>
+__global__ void __launch_bounds__(kThreads, 3)
+      compact_kernel(const float *__restrict__ a, int64_t numExt, int nbatch, int nchunks, uint64_t *__restrict__ scratch,
+                     pvgpu_entry *__restrict__ entries, int64_t *__restrict__ numActive) {
+   constexpr int KU = kChunk / (kThreads * VEC);  // units per thread
+   __shared__ uint32_t ticketSh, prefixSh;
+   __shared__ uint32_t wtot[KU * kWarps];          // warp totals, then their exclusive scan
+   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+   uint64_t *status = scratch + 1;
+   if (tid == 0) ticketSh = atomicAdd(reinterpret_cast<unsigned long long *>(scratch), 1ull);
    __syncthreads();
-   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-   for (int base = 0; base < nchunks; base += 1024) {
-      int i = base + threadIdx.x;
-      uint32_t v = i < nchunks ? cb[i] : 0u;
-      uint32_t x = v;
+   // tickets interleave the images (chunk-major), so the chunks in flight spread over every
+   // image's chain and each look-back finds a published prefix close by
+   const uint32_t t = ticketSh;
+   const int c = (int)(t / (uint32_t)nbatch), b = (int)(t % (uint32_t)nbatch);
+   const int64_t base = (int64_t)c * kChunk;
+   const float *ab = a + (size_t)b * numExt;
+
+   // ---- load the chunk (all loads issued before any use) ----
+   float v[KU * VEC];
+   if constexpr (VEC == 4) {
+      const float4 *a4 = reinterpret_cast<const float4 *>(ab);
+#pragma unroll
+      for (int k = 0; k < KU; k++) {
+         const int64_t e = base + (int64_t)(k * kThreads + tid) * 4;
+         float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+         if (e < numExt) q = __ldcs(a4 + e / 4);  // numExt is a multiple of 4 here
+         v[4 * k] = q.x;
+         v[4 * k + 1] = q.y;
+         v[4 * k + 2] = q.z;
+         v[4 * k + 3] = q.w;
+      }
+   } else {
+#pragma unroll
+      for (int k = 0; k < KU; k++) {
+         const int64_t e = base + k * kThreads + tid;
+         v[k] = e < numExt ? __ldcs(ab + e) : 0.0f;
+      }
+   }
+
+   // ---- ranks inside the warp ----
+   uint32_t wex[KU];  // exclusive rank of this thread's unit k among the warp's units k
+   if constexpr (VEC == 4) {
+      uint32_t packed = 0;
+#pragma unroll
+      for (int k = 0; k < KU; k++) {
+         const uint32_t n = (v[4 * k] != 0.f) + (v[4 * k + 1] != 0.f) + (v[4 * k + 2] != 0.f) + (v[4 * k + 3] != 0.f);
+         packed |= n << (8 * k);  // a warp's field sum is <= 128: 8 bits never carry
+      }
+      uint32_t incl = packed;
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
-         uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-         if (lane >= o) x += y;
+         const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+         if (lane >= o) incl += y;
       }
-      if (lane == 31) warpTot[warp] = x;
-      __syncthreads();
-      if (warp == 0) {
-         uint32_t w = warpTot[lane];
-         uint32_t s = w;
+      const uint32_t ex = incl - packed;
 #pragma unroll
-         for (int o = 1; o < 32; o <<= 1) {
-            uint32_t y = __shfl_up_sync(0xffffffffu, s, o);
-            if (lane >= o) s += y;
-         }
-         warpTot[lane] = s - w;  // exclusive prefix of warp totals
+      for (int k = 0; k < KU; k++) wex[k] = (ex >> (8 * k)) & 0xffu;
+      if (lane == 31) {
+#pragma unroll
+         for (int k = 0; k < KU; k++) wtot[k * kWarps + warp] = (incl >> (8 * k)) & 0xffu;
       }
-      __syncthreads();
-      uint32_t excl = carry + warpTot[warp] + (x - v);
-      if (i < nchunks) cb[i] = excl;
-      __syncthreads();
-      if (threadIdx.x == 1023) carry = excl + v;
-      __syncthreads();
+   } else {
+      const uint32_t lt = lanemask_lt();
+#pragma unroll
+      for (int k = 0; k < KU; k++) {
+         const uint32_t m = __ballot_sync(0xffffffffu, v[k] != 0.f);
+         wex[k] = __popc(m & lt);
+         if (lane == 0) wtot[k * kWarps + warp] = __popc(m);
+      }
    }
-   if (threadIdx.x == 0) numActive[b] = (int64_t)carry;
+   __syncthreads();
+
+   // ---- warp 0: scan of the warp totals in (k, warp) order, then the chunk prefix ----
+   if (warp == 0) {
+      constexpr int PER = KU * kWarps / 32;  // consecutive totals per lane
+      uint32_t loc[PER], sum = 0;
+#pragma unroll
+      for (int i = 0; i < PER; i++) {
+         loc[i] = wtot[lane * PER + i];
+         sum += loc[i];
+      }
+      uint32_t incl = sum;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+         const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+         if (lane >= o) incl += y;
+      }
+      const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+      uint32_t run = incl - sum;
+#pragma unroll
+      for (int i = 0; i < PER; i++) {
+         wtot[lane * PER + i] = run;
+         run += loc[i];
+      }
+      // decoupled look-back over this image's chunks
+      uint64_t *st = status + (size_t)b * nchunks;
+      uint32_t excl = 0;
+      bool err = false;
+      if (c == 0) {
+         if (lane == 0) st_release(&st[0], kFlagPre | total);
+      } else {
+         if (lane == 0) st_release(&st[c], kFlagAgg | total);
+         // lane l reads the statuses of chunks j - 4l .. j - 4l - 3 (128 predecessors per round
+         // trip); chunks before 0 read as a published prefix of 0
+         int j = c - 1;
+         uint64_t t0 = 0;
+         bool timing = false;
+         for (;;) {
+            uint64_t sv[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+               const int idx = j - 4 * lane - q;
+               sv[q] = idx >= 0 ? ld_acquire(&st[idx]) : kFlagPre;
+            }
+            // this lane's nearest stop (inclusive prefix or error) and whether a status before it
+            // is not ready yet
+            int stopQ = 4;
+            bool laneNotReady = false;
+#pragma unroll
+            for (int q = 3; q >= 0; q--)
+               if ((sv[q] >> 62) >= 2) stopQ = q;
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+               if (q <= stopQ && q < 4 && (sv[q] >> 62) == 0) laneNotReady = true;
+            const uint32_t stopMask = __ballot_sync(0xffffffffu, stopQ < 4);
+            const int firstStop = stopMask ? __ffs(stopMask) - 1 : 31;
+            const uint32_t notReady = __ballot_sync(0xffffffffu, laneNotReady);
+            const uint32_t need = firstStop == 31 ? 0xffffffffu : ((2u << firstStop) - 1u);
+            if (notReady & need) {
+               if (!timing) {
+                  t0 = pvgpu::tc::global_ns();
+                  timing = true;
+               } else if (pvgpu::tc::global_ns() - t0 > pvgpu::tc::kWaitNs) {
+                  err = true;
+                  break;
+               }
+               continue;
+            }
+            uint32_t part = 0;
+            if (lane <= firstStop) {
+#pragma unroll
+               for (int q = 0; q < 4; q++)
+                  if (lane < firstStop || q <= stopQ) part += (uint32_t)sv[q];
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+            excl += part;
+            if (stopMask) {
+               const int fq = __shfl_sync(0xffffffffu, stopQ, firstStop);
+               uint64_t fs = sv[0];
+#pragma unroll
+               for (int q = 1; q < 4; q++)
+                  if (q == fq) fs = sv[q];
+               err = (uint32_t)(__shfl_sync(0xffffffffu, fs, firstStop) >> 62) == 3u;
+               break;
+            }
+            j -= 128;
+         }
+         if (lane == 0) st_release(&st[c], (err ? kFlagErr : kFlagPre) | (uint32_t)(excl + total));
+      }
+      if (lane == 0) {
+         prefixSh = excl;
+         if (c == nchunks - 1) numActive[b] = err ? (int64_t)-1 : (int64_t)(excl + total);
+      }
+   }
+   __syncthreads();
+
+   // ---- entries ----
+   const uint32_t prefix = prefixSh;
+   const uint32_t cap = (uint32_t)numExt;  // ranks stay below it; the test only guards the store
+   uint2 *eb = reinterpret_cast<uint2 *>(entries + (size_t)b * numExt);
+#pragma unroll
+   for (int k = 0; k < KU; k++) {
+      uint32_t r = prefix + wtot[k * kWarps + warp] + wex[k];
+      if constexpr (VEC == 4) {
+         const int64_t e = base + (int64_t)(k * kThreads + tid) * 4;
+#pragma unroll
+         for (int q = 0; q < 4; q++) {
+            if (v[4 * k + q] != 0.f) {
+               if (r < cap) eb[r] = make_uint2((uint32_t)(e + q), __float_as_uint(v[4 * k + q]));
+               r++;
+            }
+         }
+      } else {
+         const int64_t e = base + k * kThreads + tid;
+         if (v[k] != 0.f && r < cap) eb[r] = make_uint2((uint32_t)e, __float_as_uint(v[k]));
+      }
+   }
 }
 
-__global__ void __launch_bounds__(kThreads) write_kernel(const float *__restrict__ a, int64_t numExt, int nchunks,
-                                                         const uint32_t *__restrict__ offsets,
-                                                         pvgpu_entry *__restrict__ entries) {
-   const int c = blockIdx.x, b = blockIdx.y;
-   const float *ab = a + (size_t)b * numExt;
-   pvgpu_entry *eb = entries + (size_t)b * numExt;
-   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-   __shared__ uint32_t wpre[kThreads / 32];
-   __shared__ uint32_t wtot[kThreads / 32];
-   uint32_t running = offsets[(size_t)b * nchunks + c];
-   int64_t base = (int64_t)c * kChunk;
-   for (int i = 0; i < kIters; i++) {
-      int64_t e = base + i * kThreads + threadIdx.x;
-      float v = e < numExt ? ab[e] : 0.0f;
-      bool nz = v != 0.0f;
-      uint32_t m = __ballot_sync(0xffffffffu, nz);
-      if (lane == 0) wtot[warp] = __popc(m);
-      __syncthreads();
-      if (threadIdx.x == 0) {
-         uint32_t s = 0;
-         for (int w = 0; w < kThreads / 32; w++) {
-            wpre[w] = s;
-            s += wtot[w];
-         }
-      }
-      __syncthreads();
-      if (nz) {
-         uint32_t r = running + wpre[warp] + __popc(m & ((1u << lane) - 1u));
-         pvgpu_entry en;
-         en.index = (uint32_t)e;
-         en.value = v;
-         eb[r] = en;
-      }
-      running += wpre[kThreads / 32 - 1] + wtot[kThreads / 32 - 1];
-      __syncthreads();
-   }
+int64_t chunks_of(int64_t numExt) { return (numExt + kChunk - 1) / kChunk; }
+
+pvgpu_status check_args(const float *aExt, int nbatch, int64_t numExt, const pvgpu_entry *entries,
+                        const int64_t *numActive) {
+   if (!aExt || !entries || !numActive || nbatch <= 0 || numExt <= 0 || numExt > 0xffffffffLL) return PVGPU_ERR_BAD_ARG;
+   if (reinterpret_cast<uintptr_t>(entries) % 8 != 0 || reinterpret_cast<uintptr_t>(aExt) % 4 != 0)
+      return pvgpu::record_message(PVGPU_ERR_BAD_ARG, "compact_active: entries must be 8-byte aligned, activity 4-byte");
+   if ((int64_t)nbatch * chunks_of(numExt) > 0x7fffffffLL) return PVGPU_ERR_UNSUPPORTED_SHAPE;
+   return PVGPU_OK;
+}
+
+// Zeroes the ticket and the chunk statuses, then runs the one-pass kernel.
+pvgpu_status launch(const float *aExt, int nbatch, int64_t numExt, pvgpu_entry *entries, int64_t *numActive,
+                    uint64_t *scratch, cudaStream_t s, const char *where) {
+   const int64_t nchunks = chunks_of(numExt);
+   const size_t words = 1 + (size_t)nbatch * (size_t)nchunks;
+   cudaError_t e = cudaMemsetAsync(scratch, 0, words * sizeof(uint64_t), s);
+   if (e != cudaSuccess) return pvgpu::record_cuda_error(e, where);
+   const unsigned grid = (unsigned)(nbatch * nchunks);
+   const bool vec = reinterpret_cast<uintptr_t>(aExt) % 16 == 0 && numExt % 4 == 0;
+   if (vec)
+      compact_kernel<4><<<grid, kThreads, 0, s>>>(aExt, numExt, nbatch, (int)nchunks, scratch, entries, numActive);
+   else
+      compact_kernel<1><<<grid, kThreads, 0, s>>>(aExt, numExt, nbatch, (int)nchunks, scratch, entries, numActive);
+   PVGPU_CHECK_LAUNCH(where);
+   return PVGPU_OK;
 }
 
 }  // namespace
 
 extern "C" size_t pvgpu_compact_scratch_bytes(int nbatch, int64_t numExt) {
    if (nbatch <= 0 || numExt <= 0) return 0;
-   int64_t nchunks = (numExt + kChunk - 1) / kChunk;
-   return (size_t)nbatch * (size_t)nchunks * sizeof(uint32_t);
+   return (1 + (size_t)nbatch * (size_t)chunks_of(numExt)) * sizeof(uint64_t);
 }
 
 extern "C" pvgpu_status pvgpu_compact_active(const float *aExt, int nbatch, int64_t numExt, pvgpu_entry *entries,
                                              int64_t *numActive, void *scratch, size_t scratchBytes, void *stream) {
-   if (!aExt || !entries || !numActive || nbatch <= 0 || numExt <= 0 || numExt > 0xffffffffLL) return PVGPU_ERR_BAD_ARG;
-   size_t need = pvgpu_compact_scratch_bytes(nbatch, numExt);
-   if (!scratch || scratchBytes < need) return PVGPU_ERR_BAD_ARG;
-   int nchunks = (int)((numExt + kChunk - 1) / kChunk);
-   if (nbatch > 65535) return PVGPU_ERR_UNSUPPORTED_SHAPE;
-   cudaStream_t s = pvgpu::as_stream(stream);
-   uint32_t *counts = static_cast<uint32_t *>(scratch);
-   dim3 grid(nchunks, nbatch);
-   count_kernel<<<grid, kThreads, 0, s>>>(aExt, numExt, nchunks, counts);
-   PVGPU_CHECK_LAUNCH("compact count");
-   scan_kernel<<<nbatch, 1024, 0, s>>>(counts, nchunks, numActive);
-   PVGPU_CHECK_LAUNCH("compact scan");
-   write_kernel<<<grid, kThreads, 0, s>>>(aExt, numExt, nchunks, counts, entries);
-   PVGPU_CHECK_LAUNCH("compact write");
-   return PVGPU_OK;
+   pvgpu_status st = check_args(aExt, nbatch, numExt, entries, numActive);
+   if (st != PVGPU_OK) return st;
+   if (!scratch || scratchBytes < pvgpu_compact_scratch_bytes(nbatch, numExt) ||
+       reinterpret_cast<uintptr_t>(scratch) % 8 != 0)
+      return PVGPU_ERR_BAD_ARG;
+   return launch(aExt, nbatch, numExt, entries, numActive, static_cast<uint64_t *>(scratch), pvgpu::as_stream(stream),
+                 "compact_active");
 }
 
 // ---------------------------------------------------------------------------------------------
 // Compaction without any device allocation.
 //
 // Some callers cannot hand this library a scratch buffer and must not make it allocate one:
-// code that runs inside a host function enqueued on a stream (CUDA API calls that allocate are
-// not allowed there), latency-critical loops that cannot afford the implicit device
-// synchronisation cudaMalloc/cudaFree may cause, and hosts whose device memory is entirely
-// owned by their own pool allocator.  For them the per-chunk counts live in a fixed array in
-// this library's device image, sized for kNoAllocMaxChunks chunks in total
-// (nbatch * ceil(numExt / 4096) <= 262144, i.e. up to 2^30 activity values per call).
-// The array is loaded with the library, once per device, and held until the process exits.
+// latency-critical loops that cannot afford the implicit device synchronisation that
+// cudaMalloc / cudaFree may cause, and hosts whose device memory is entirely owned by their own
+// pool allocator.  For them the ticket and the chunk statuses live in a fixed array in this
+// library's device image: kNoAllocWords 8-byte words, i.e. nbatch * ceil(numExt / 8192) <=
+// 131071 chunks (up to about 2^30 activity values per call).  The array is loaded with the
+// library, once per device, and held until the process exits.
 // ---------------------------------------------------------------------------------------------
 namespace {
 
-constexpr int64_t kNoAllocMaxChunks = 1 << 18;  // 262144 x 4 bytes = 1 MiB per device
+constexpr int64_t kNoAllocWords = 1 << 17;  // 131072 x 8 bytes = 1 MiB per device
+constexpr int64_t kNoAllocMaxChunks = kNoAllocWords - 1;
 
-static __device__ __align__(256) uint32_t g_compact_noalloc_scratch[kNoAllocMaxChunks];
+static __device__ __align__(256) uint64_t g_compact_noalloc_scratch[kNoAllocWords];
 
 constexpr int kMaxDevices = 64;
 std::mutex g_noalloc_mutex;
@@ -170,8 +311,10 @@ void *g_noalloc_addr[kMaxDevices] = {};
 
 // Device address of g_compact_noalloc_scratch on the current device.  The host-side symbol is
 // only a stand-in: a kernel handed its host address would read the wrong memory, so the
-// address is looked up with the device current, checked, and cached per device.
-pvgpu_status noalloc_scratch(uint32_t **out) {
+// address is looked up with the device current, checked, and cached per device ordinal.  The
+// cache assumes the device's context lives as long as the process: after cudaDeviceReset the
+// cached address is stale.
+pvgpu_status noalloc_scratch(uint64_t **out) {
    int dev = 0;
    cudaError_t e = cudaGetDevice(&dev);
    if (e != cudaSuccess) return pvgpu::record_cuda_error(e, "compact_active_noalloc: cudaGetDevice");
@@ -184,7 +327,7 @@ pvgpu_status noalloc_scratch(uint32_t **out) {
       if (e != cudaSuccess || !p) return pvgpu::record_cuda_error(e, "compact_active_noalloc: cudaGetSymbolAddress");
       g_noalloc_addr[dev] = p;
    }
-   *out = static_cast<uint32_t *>(g_noalloc_addr[dev]);
+   *out = static_cast<uint64_t *>(g_noalloc_addr[dev]);
    return PVGPU_OK;
 }
 
@@ -192,25 +335,17 @@ pvgpu_status noalloc_scratch(uint32_t **out) {
 
 extern "C" pvgpu_status pvgpu_compact_active_noalloc(const float *aExt, int nbatch, int64_t numExt,
                                                      pvgpu_entry *entries, int64_t *numActive, void *stream) {
-   if (!aExt || !entries || !numActive || nbatch <= 0 || numExt <= 0 || numExt > 0xffffffffLL) return PVGPU_ERR_BAD_ARG;
-   if (nbatch > 65535) return PVGPU_ERR_UNSUPPORTED_SHAPE;
-   const int64_t nchunks = (numExt + kChunk - 1) / kChunk;
-   if ((int64_t)nbatch * nchunks > kNoAllocMaxChunks)
-      return pvgpu::record_message(PVGPU_ERR_BAD_ARG,
-                                   "compact_active_noalloc: nbatch * ceil(numExt / 4096) exceeds the fixed scratch "
-                                   "of 262144 chunk counts; use pvgpu_compact_active with caller scratch");
-   uint32_t *counts = nullptr;
-   pvgpu_status st = noalloc_scratch(&counts);
+   pvgpu_status st = check_args(aExt, nbatch, numExt, entries, numActive);
    if (st != PVGPU_OK) return st;
-   // Every chunk count the kernels read is written earlier in the same call, so nothing has to
-   // be cleared between calls.
-   cudaStream_t s = pvgpu::as_stream(stream);
-   dim3 grid((unsigned)nchunks, nbatch);
-   count_kernel<<<grid, kThreads, 0, s>>>(aExt, numExt, (int)nchunks, counts);
-   PVGPU_CHECK_LAUNCH("compact_active_noalloc count");
-   scan_kernel<<<nbatch, 1024, 0, s>>>(counts, (int)nchunks, numActive);
-   PVGPU_CHECK_LAUNCH("compact_active_noalloc scan");
-   write_kernel<<<grid, kThreads, 0, s>>>(aExt, numExt, (int)nchunks, counts, entries);
-   PVGPU_CHECK_LAUNCH("compact_active_noalloc write");
-   return PVGPU_OK;
+   if ((int64_t)nbatch * chunks_of(numExt) > kNoAllocMaxChunks)
+      return pvgpu::record_message(PVGPU_ERR_BAD_ARG,
+                                   "compact_active_noalloc: nbatch * ceil(numExt / 8192) exceeds the fixed scratch "
+                                   "of 131071 chunk statuses; use pvgpu_compact_active with caller scratch");
+   uint64_t *scratch = nullptr;
+   st = noalloc_scratch(&scratch);
+   if (st != PVGPU_OK) return st;
+   // The ticket and the statuses left by the previous call are cleared (cudaMemsetAsync on the
+   // stream, no allocation) before the kernel reads them.
+   return launch(aExt, nbatch, numExt, entries, numActive, scratch, pvgpu::as_stream(stream),
+                 "compact_active_noalloc");
 }

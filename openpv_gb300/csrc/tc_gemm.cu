@@ -239,3 +239,64 @@ extern "C" pvgpu_status pvgpu_tc_gemm_bf16_kn(const void *A, const void *B, floa
                                               int *errFlag, void *stream) {
    return tc_gemm(A, B, C, M, N, K, errFlag, stream, true);
 }
+
+// ---------------------------------------------------------------------------------------------
+// Diagnostic: the expiry path of a bounded device wait.  One CTA holds TMEM like the
+// warp-specialised kernels do; warp 1 waits on an mbarrier that nothing arrives at, with the
+// caller's time limit; when the wait gives up it raises the CTA's abort flag, which warp 2 (a
+// role polling the flag between work items, like the load warps) sees and leaves its loop by.
+// The CTA then frees its TMEM and reports {timed out, ns waited} -- the discipline every
+// kernel of the library follows on a timeout, without a fault or a hang.
+namespace {
+
+__global__ void __launch_bounds__(96) wait_expiry_kernel(uint64_t limitNs, long long *out) {
+   __shared__ __align__(8) uint64_t never;
+   __shared__ uint32_t tmemBase;
+   __shared__ volatile int abortFlag;
+   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+   if (threadIdx.x == 0) {
+      mbar_init(&never, 1);
+      abortFlag = 0;
+      fence_mbar_init();
+   }
+   if (warp == 0) tmem_alloc(&tmemBase, 32);
+   tc_fence_before();
+   __syncthreads();
+   tc_fence_after();
+   long long waited = 0;
+   if (warp == 1 && lane == 0) {
+      const uint64_t t0 = global_ns();
+      if (!mbar_wait(&never, 0, limitNs)) abortFlag = 1;
+      waited = (long long)(global_ns() - t0);
+   } else if (warp == 2) {
+      // polls the abort flag; its own loop is bounded too (twice the wait's limit)
+      const uint64_t t0 = global_ns();
+      while (!abortFlag && global_ns() - t0 < 2 * limitNs) __nanosleep(1000);
+   }
+   __syncthreads();
+   if (threadIdx.x == 32) {
+      out[0] = abortFlag ? 1 : 0;
+      out[1] = waited;
+   }
+   tc_fence_before();
+   __syncthreads();
+   if (warp == 0) tmem_dealloc(tmemBase, 32);
+}
+
+}  // namespace
+
+extern "C" pvgpu_status pvgpu_selftest_wait_expiry(uint64_t limitNs, long long *hostOut2, void *stream) {
+   if (!hostOut2 || limitNs == 0 || limitNs > 1000000000ull) return PVGPU_ERR_BAD_ARG;
+   cudaStream_t s = pvgpu::as_stream(stream);
+   long long *d = nullptr;
+   cudaError_t e = cudaMallocAsync(&d, 2 * sizeof(long long), s);
+   if (e != cudaSuccess) return pvgpu::record_cuda_error(e, "selftest_wait_expiry");
+   wait_expiry_kernel<<<1, 96, 0, s>>>(limitNs, d);
+   e = cudaGetLastError();
+   if (e == cudaSuccess) e = cudaMemcpyAsync(hostOut2, d, 2 * sizeof(long long), cudaMemcpyDeviceToHost, s);
+   cudaError_t f = cudaFreeAsync(d, s);
+   if (e == cudaSuccess) e = f;
+   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+   if (e != cudaSuccess) return pvgpu::record_cuda_error(e, "selftest_wait_expiry");
+   return hostOut2[0] ? PVGPU_ERR_TIMEOUT : PVGPU_OK;
+}

@@ -48,9 +48,15 @@ def sparse_activity(rng, loc, p, zero_halo=True):
 
 # ---- a1: compaction --------------------------------------------------------------------
 
-@pytest.mark.parametrize("nb,n,p", [(3, 25600, 0.05), (2, 4097, 0.5), (1, 4096, 1.0), (4, 777, 0.0),
-                                    (2, 204800, 0.02), (1, 1, 1.0)])
-def test_compaction_bitexact(cuda, oracle, nb, n, p):
+# Sizes: float4 units (n % 4 == 0) and scalar units, one chunk of 8192 and long look-back
+# chains (the delivery microbenchmark's 16 x 134x134x256 extended activity: 562 chunks per
+# image), empty and full activity.  `offset` starts the activity one float past an aligned
+# address, which forces scalar units on an aligned size.
+@pytest.mark.parametrize("nb,n,p,offset", [(3, 25600, 0.05, 0), (2, 4097, 0.5, 0), (1, 4096, 1.0, 0),
+                                           (4, 777, 0.0, 0), (2, 204800, 0.02, 0), (1, 1, 1.0, 0),
+                                           (16, 134 * 134 * 256, 0.01, 0), (5, 1000003, 0.3, 0),
+                                           (3, 25600, 0.05, 1), (2, 8192 * 3, 1.0, 1)])
+def test_compaction_bitexact(cuda, oracle, nb, n, p, offset):
     torch = cuda
     from openpv_gb300 import capi
     rng = np.random.default_rng(n)
@@ -58,7 +64,9 @@ def test_compaction_bitexact(cuda, oracle, nb, n, p):
     ent_ref, num_ref = oracle.compact(a)
     ent = torch.zeros((nb, n, 2), dtype=torch.int32, device="cuda")
     num = torch.full((nb,), -7, dtype=torch.int64, device="cuda")
-    capi.compact_active(T(torch, a), nb, n, ent, num)
+    buf = torch.zeros(nb * n + offset, device="cuda")
+    buf[offset:] = T(torch, a.reshape(-1))
+    capi.compact_active(buf[offset:], nb, n, ent, num)
     num_h = H(num)
     ent_h = H(ent).view(np.uint8).reshape(nb, n, 8).view(capi.ENTRY_DTYPE).reshape(nb, n)
     assert np.array_equal(num_h, num_ref)
@@ -119,6 +127,46 @@ def test_deliver_pre_matches_oracle(cuda, oracle, case, sparse):
             assert np.array_equal(out.view(np.uint32), ref.view(np.uint32))
         else:
             np.testing.assert_allclose(out, ref, rtol=RTOL_FP32, atol=1e-5 * np.abs(ref).max())
+
+
+@pytest.mark.parametrize("p,nb", [(0.01, 2), (0.05, 2), (0.2, 1)])
+def test_deliver_pre_full_size_microbenchmark_connection(cuda, oracle, p, nb):
+    """The delivery microbenchmark's connection at full size -- pre 128x128x256 (halo 3, zero),
+    Bernoulli(p) x uniform(0,1] activity, post 128x128x64 one-to-one, 7x7 shared weights
+    N(0, 0.05^2) -- on nb images: the SparseList delivery in REFERENCE_ORDER mode bit for bit
+    against the oracle (the reference CPU loop's order), FAST mode and the tensor-core entry
+    (dense activity, split-TF32) within 1e-5 of max|GSyn|."""
+    torch = cuda
+    from openpv_gb300 import capi
+    pre = capi.Loc.make(nb, 128, 128, 256, 3)
+    post = capi.Loc.make(nb, 128, 128, 64, 0)
+    rng = np.random.default_rng(1234 + 2)
+    a = np.zeros(pre.ext_shape(), np.float32)
+    core = (rng.random(pre.res_shape()) < p) * (1.0 - rng.random(pre.res_shape()))
+    a[:, 3:131, 3:131, :] = core
+    w = rng.normal(0, 0.05, (256, 7, 7, 64)).astype(np.float32)
+    ent, num = oracle.compact(a.reshape(nb, -1))
+    ref = oracle.deliver_pre(OL(oracle, pre), OL(oracle, post), 7, 7, w, entries=ent, num_active=num)
+    scale = np.abs(ref).max()
+    conn = capi.conn_desc(pre, post, 7, 7)
+    ad, wd = T(torch, a), T(torch, w)
+    ent_d = torch.zeros((nb, pre.num_ext, 2), dtype=torch.int32, device="cuda")
+    num_d = torch.zeros(nb, dtype=torch.int64, device="cuda")
+    capi.compact_active(ad, nb, pre.num_ext, ent_d, num_d)
+    assert np.array_equal(H(num_d), num)
+    for mode in (capi.DELIVER_REFERENCE_ORDER, capi.DELIVER_FAST):
+        g = torch.zeros(post.res_shape(), device="cuda")
+        capi.deliver_pre(conn, wd, g, entries=ent_d, num_active=num_d, mode=mode)
+        out = H(g)
+        if mode == capi.DELIVER_REFERENCE_ORDER:
+            assert np.array_equal(out.view(np.uint32), ref.view(np.uint32))
+        else:
+            assert np.abs(out - ref).max() <= 1e-5 * scale
+    ws = torch.empty(capi.deliver_tc_workspace_bytes(conn), dtype=torch.uint8, device="cuda")
+    g = torch.zeros(post.res_shape(), device="cuda")
+    capi.deliver_pre_tc(conn, ad, wd, g, ws)
+    assert capi.deliver_tc_check_error() == 0
+    assert np.abs(H(g) - ref).max() <= 1e-5 * scale
 
 
 def test_deliver_pre_empty_activity(cuda, oracle):

@@ -1,9 +1,11 @@
 """The fused LCA solver (both precisions) against the CPU oracle's LCA module
 (pvo_lca_run: input -> error <-> V1 in the reference's phase order), through the C ABI.
 
-FP32 form: same math as the reference path, only GEMM summation order differs -> V, A and
-the probe energy agree with the FP32 oracle to ~1e-5 relative.  BF16 form: the final energy
-must be within 1e-3 relative of the FP64 oracle (the stated BF16 bar)."""
+FP32 form: same math as the reference path, only GEMM summation order differs -> V and A
+agree with the FP32 oracle within 1e-5 relative to max|V| (normwise: single elements near the
+threshold or near zero have no meaningful elementwise relative error) and the probe energy
+within 1e-5 relative.  BF16 form: the final energy must be within 1e-3 relative of the FP64
+oracle (the stated BF16 bar)."""
 import numpy as np
 import pytest
 
@@ -87,8 +89,9 @@ def test_lca_fp32_form_matches_oracle(torch, oracle, name):
     torch.cuda.synchronize()
     assert s.error_flag() == 0
     vs = np.abs(v_ref).max()
-    np.testing.assert_allclose(v.cpu().numpy(), v_ref, rtol=1e-4, atol=1e-5 * vs)
-    np.testing.assert_allclose(a.cpu().numpy(), a_ref, rtol=1e-4, atol=1e-5 * vs)
+    dv = np.abs(v.cpu().numpy() - v_ref).max() / vs
+    da = np.abs(a.cpu().numpy() - a_ref).max() / vs
+    assert dv <= 1e-5 and da <= 1e-5, (dv, da)
     np.testing.assert_allclose(e.cpu().numpy(), e_ref[-1], rtol=1e-5)
 
 
@@ -221,7 +224,7 @@ def test_lca_autotune_picks_valid_shapes_and_keeps_parity(torch, oracle):
 @pytest.mark.parametrize("nb", [3, 6])
 def test_lca_bf16_schedules_leave_identical_state(torch, oracle, nb):
     """The graph's schedule -- one chain or two half-batch chains on parallel branches (halves of
-    4 + 2 and 2 + 1 images, the odd half with an empty slot in kernel R's image pairs), capped
+    4 + 2 and 2 + 1 images), capped
     persistent grids, with and without programmatic edges -- moves work between CTAs and SMs
     only: the state is bit-identical to the kernel-by-kernel run, BF16x3 steps included."""
     from openpv_gb300 import capi
@@ -351,3 +354,58 @@ def test_lca_fused_plan_shapes(torch, oracle):
     assert set(per_tile) == {64, 128}
     with pytest.raises(capi.PvgpuError):
         s.set_fused_plan(96, 2, 2)  # not a multiple of 64
+
+
+def test_lca_config3_geometry_every_fused_shape(torch, oracle):
+    """The batched configuration's geometry -- 32x32x3 inputs (1/f spectrum, unit std) -> V1
+    16x16x512 at stride 2, 512 features of 8x8x3, VThresh = AShift = 0.15 -- on 4 images for 100
+    timesteps with the last 12 in BF16x3.  Every fused-kernel shape the solver accepts (feature
+    tiles 64..512, among them the 512-feature tile with 3 V and 3 weight slots the autotuner
+    picks for the full batch) against the two-kernel form: V within 1e-3 of max|V|; the final
+    energy within 1e-3 relative of the FP64 oracle for each, and for the autotuner's own pick;
+    no bounded device wait gives up."""
+    from openpv_gb300 import capi
+    nb, ins, v1s, nxp, vth, steps, x3 = 4, (32, 32, 3), (16, 16, 512), 8, 0.15, 100, 12
+    rng = np.random.default_rng(1234 + 3)
+    w = dictionary(rng, v1s[2], nxp, ins[2])
+    x = one_over_f(rng, nb, *ins)
+    p = oracle.lca_params(nbatch=nb, inNx=32, inNy=32, inNf=3, v1Nx=16, v1Ny=16, v1Nf=512, nxp=8, nyp=8,
+                          VThresh=vth, AShift=vth, AMin=0.0, VWidth=0.0, tau=100.0, dtFixed=1.0)
+    _, _, _, e64 = oracle.lca_run(p, w.astype(np.float64), x[None].astype(np.float64), steps,
+                                  np.zeros((nb,) + v1s), f64=True, threads=nb, want_recon=False)
+    s = capi.LcaSolver(nb, ins, v1s, nxp, vth)
+    s.set_weights(torch.from_numpy(w).cuda())
+    xd = torch.from_numpy(x).cuda()
+    e = torch.zeros(nb, dtype=torch.float64, device="cuda")
+
+    def solve():
+        s.reset()
+        s.run(xd, steps, x3_steps=x3, precision=capi.LCA_BF16)
+        s.energy(xd, e)
+        v = torch.zeros((nb,) + v1s, device="cuda")
+        s.state(v)
+        torch.cuda.synchronize()
+        assert s.error_flag() == 0
+        rel = np.abs(e.cpu().numpy() - e64[-1]) / np.abs(e64[-1])
+        return v.cpu().numpy(), rel.max()
+
+    s.set_schedule(fused=False)
+    ref, rel_u = solve()
+    assert rel_u < 1e-3, rel_u
+    s.set_schedule(fused=True)
+    accepted = []
+    for ft in (64, 128, 256, 512):
+        for nv in (1, 2, 3):
+            for nw in (2, 3):
+                try:
+                    s.set_fused_plan(ft, nv, nw)
+                except capi.PvgpuError:
+                    continue
+                v, rel = solve()
+                accepted.append((ft, nv, nw))
+                assert np.abs(v - ref).max() <= 1e-3 * np.abs(ref).max(), (ft, nv, nw)
+                assert rel < 1e-3, (ft, nv, nw, rel)
+    assert (512, 3, 3) in accepted, accepted
+    s.autotune(xd, trial_steps=2)
+    _, rel = solve()
+    assert rel < 1e-3, (rel, s.fused_plan_info(), s.schedule())

@@ -1,11 +1,10 @@
 """The compaction entry point that allocates nothing (pvgpu_compact_active_noalloc), through the
 C ABI, against the ordinary one (pvgpu_compact_active, caller scratch).
 
-It serves callers that cannot allocate device memory where they call (host functions enqueued
-on a stream, loops that must not pay cudaMalloc's implicit synchronisation, hosts that own all
-device memory through their own pool); its scratch is a fixed array in the library's device
-image.  Two calls in a row check that the shared array carries nothing over between calls.
-This file is collected last on purpose."""
+It serves callers that cannot allocate device memory where they call (loops that must not pay
+cudaMalloc's implicit synchronisation, hosts that own all device memory through their own pool);
+its scratch is a fixed array in the library's device image.  Two calls in a row check that the
+shared array carries nothing over between calls.  This file is collected last on purpose."""
 import numpy as np
 import pytest
 
@@ -46,11 +45,11 @@ def test_noalloc_compaction_equals_scratch_version(torch, nb, n, p_seq):
 
 def test_noalloc_rejects_sizes_beyond_its_fixed_scratch(torch):
     from openpv_gb300 import capi
-    nb, n = 65, 4096 * 4096  # 65 * 4096 chunks > 262144
+    nb, n = 65, 4096 * 4096  # 65 * 2048 chunks of 8192 values > 131071
     a = torch.zeros(1, device="cuda")
     e = torch.zeros(1, device="cuda")
     num = torch.zeros(nb, dtype=torch.int64, device="cuda")
     with pytest.raises(capi.PvgpuError) as exc:
         capi.compact_active_noalloc(a, nb, n, e, num)
     assert exc.value.status == 1
-    assert "262144" in capi.last_error()
+    assert "131071" in capi.last_error()
