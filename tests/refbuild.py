@@ -8,7 +8,21 @@ import subprocess
 import numpy as np
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF_ROOT = os.environ.get("OPENPV_REFERENCE", "/root/reference")
+def reference_root():
+    """The reference source tree: OPENPV_REFERENCE, else the root the oracle's build recipe
+    (oracle/Makefile.ref) is configured to read."""
+    env = os.environ.get("OPENPV_REFERENCE")
+    if env:
+        return env
+    try:
+        r = subprocess.run(["make", "-s", "-f", os.path.join(ROOT, "oracle", "Makefile.ref"), "print-ref"],
+                           capture_output=True, text=True, timeout=30)
+        return r.stdout.strip()
+    except (OSError, subprocess.SubprocessError):
+        return ""
+
+
+REF_ROOT = reference_root()
 LIB = os.path.join(ROOT, "oracle", "_ref", "libpvref.so")
 
 

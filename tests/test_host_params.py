@@ -76,7 +76,8 @@ def test_syntax_errors_name_the_line(capi, bad, where):
 def test_reference_lca_test_params_parse(capi):
     """The reference's own GPU LCA test params file parses, with its delivery switches (read as
     text from the reference tree when it is present)."""
-    path = "/root/reference/tests/GPULCATest/input/GPULCATest.params"
+    from tests.refbuild import REF_ROOT
+    path = os.path.join(REF_ROOT, "tests", "GPULCATest", "input", "GPULCATest.params")
     if not os.path.exists(path):
         pytest.skip("reference tree not present")
     g = groups(capi.params_dump(open(path).read()))

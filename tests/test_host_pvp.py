@@ -11,7 +11,7 @@ import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 GOLD = os.path.join(ROOT, "tests", "golden")
-REF = os.environ.get("OPENPV_REFERENCE", "/root/reference")
+from tests.refbuild import REF_ROOT as REF
 KAT = os.path.join(REF, "tests", "BufferUtilsPvpTest", "input")
 
 
