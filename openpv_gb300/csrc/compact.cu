@@ -1,36 +1,46 @@
 // compact.cu -- a1: stable active-index compaction (DataStore::updateActiveIndices,
 // columns/DataStore.cpp:46-66) on the device, in one pass over the activity.
 //
-// Each batch element's extended activity is cut into chunks of kChunk = 8192 floats; one CTA of
-// 512 threads takes one chunk.  Thread t of the CTA loads the chunk's units k*512 + t
-// (k = 0 .. KU-1; a unit is a float4 when every image starts on a 16-byte boundary, else one
-// float), so every load instruction of a warp reads one contiguous run.  Entries must come out
-// in ascending extended index, i.e. in (k, warp, lane, element-of-unit) order:
-//   * inside a warp, the rank of a thread's unit k comes from a warp scan of the per-thread
-//     counts (float4 units: four 8-bit fields, one per k, scanned together in one 32-bit scan;
-//     scalar units: a ballot per k);
-//   * across the warps, warp 0 scans the KU x 16 warp totals in (k, warp) order;
+// Each batch element's extended activity is cut into chunks of kChunk = 8192 floats (32 KB).
+// Entries must come out in ascending extended index.  Per chunk:
+//   * every thread holds a fixed set of units of the chunk (float4s, or single floats when the
+//     images are not 16-byte aligned) at unit index k * threads + t, so a warp's units of one k
+//     are one contiguous run and entries are ordered by (k, warp, lane, element-of-unit);
+//   * inside a warp, the rank of a thread's unit k comes from a warp scan of per-thread counts
+//     (float4 units: four 8-bit fields, one per k, scanned together in one 32-bit scan; scalar
+//     units: a ballot per k);
+//   * across the warps, warp 0 scans the warp totals in (k, warp) order;
 //   * across chunks, a decoupled look-back (Merrill & Garland, "Single-pass Parallel Prefix Scan
-//     with Decoupled Look-back", 2016): the CTA publishes its chunk total as soon as it is
-//     known, then warp 0 reads the status words of up to 128 predecessors per round trip,
-//     summing totals back to the nearest chunk that has published its inclusive prefix.
-// CTAs draw their (chunk, image) from an atomic ticket in the scratch, chunk-major so that the
-// chunks in flight spread over all images' chains; every predecessor a CTA waits for holds a
-// smaller ticket and is already running, so the look-back always ends.  Its spin is still bounded in time;
-// a CTA that gives up publishes an error status that propagates down the image's chain and
-// makes the image's count -1.
+//     with Decoupled Look-back", 2016): the chunk's total is published as soon as it is known,
+//     then warp 0 reads the status words of up to 128 predecessors per round trip, summing
+//     totals back to the nearest chunk that has published its inclusive prefix.
+// Chunks are handed out by an atomic ticket in the scratch, chunk-major (ticket t = chunk
+// t / nbatch of image t % nbatch), so the chunks in flight spread over every image's chain and
+// each look-back finds a published prefix close by.  A chunk only waits for chunks with smaller
+// tickets, whose owners are running and take their tickets in increasing order: the look-back
+// always ends.  Its spin is bounded in time all the same; a chunk that gives up publishes an
+// error status that propagates down the image's chain and makes the image's count -1.
+//
+// One CTA per chunk: 128 threads with float4 units (images 16-byte aligned), else 512 threads
+// with scalar units; every load of the chunk is issued before any is used.  (Tried and not
+// kept: a persistent kernel streaming chunks through a shared-memory ring -- its consumers
+// take their chunks in order, so a chunk's total is published late and look-backs convoy
+// across CTAs, 0.21 ms against 0.10 ms on 16 x 134x134x256 values; a dedicated look-back warp
+// started with the loads -- its early polling cost more than it hid, 0.14 ms.)
 //
 // Integer/byte work, HBM-bound: one read of the activity + 8 B per entry written.
 // Scratch: one 8-byte ticket word, then one 8-byte status word per chunk, zeroed before each call.
 #include "pvgpu_internal.cuh"
 #include "tc_ptx.cuh"
 
+#include <algorithm>
 #include <mutex>
 
 namespace {
 
-constexpr int kThreads = 512;
-constexpr int kWarps = kThreads / 32;
+using pvgpu::tc::global_ns;
+using pvgpu::tc::kWaitNs;
+
 constexpr int kChunk = 8192;
 constexpr uint64_t kFlagAgg = 1ull << 62, kFlagPre = 2ull << 62, kFlagErr = 3ull << 62;
 
@@ -49,26 +59,130 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
    return m;
 }
 
-// VEC = 4: float4 units (every image 16-byte aligned); VEC = 1: scalar units.
+// Warp 0 of a chunk's consumers: exclusive scan (in place) of the NT warp totals in tot, in
+// index order (NT a multiple of 32); returns the chunk's total.
+template <int NT>
+__device__ __forceinline__ uint32_t scan_totals(uint32_t *tot, int lane) {
+   constexpr int PER = NT / 32;
+   uint32_t loc[PER], sum = 0;
+#pragma unroll
+   for (int i = 0; i < PER; i++) {
+      loc[i] = tot[lane * PER + i];
+      sum += loc[i];
+   }
+   uint32_t incl = sum;
+#pragma unroll
+   for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+   }
+   uint32_t run = incl - sum;
+#pragma unroll
+   for (int i = 0; i < PER; i++) {
+      tot[lane * PER + i] = run;
+      run += loc[i];
+   }
+   return __shfl_sync(0xffffffffu, incl, 31);
+}
+
+// Warp 0: publishes chunk c's total, looks back over the image's statuses st[0 .. c-1] for the
+// exclusive prefix, publishes the inclusive prefix; *err on a timeout or an upstream error.
+__device__ __forceinline__ uint32_t look_back(uint64_t *st, int c, uint32_t total, int lane, bool *err) {
+   *err = false;
+   if (c == 0) {
+      if (lane == 0) st_release(&st[0], kFlagPre | total);
+      return 0;
+   }
+   if (lane == 0) st_release(&st[c], kFlagAgg | total);
+   // lane l reads the statuses of chunks j - 4l .. j - 4l - 3 (128 predecessors per round trip);
+   // chunks before 0 read as a published prefix of 0
+   uint32_t excl = 0;
+   int j = c - 1;
+   uint64_t t0 = 0;
+   bool timing = false;
+   for (;;) {
+      uint64_t sv[4];
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+         const int idx = j - 4 * lane - q;
+         sv[q] = idx >= 0 ? ld_acquire(&st[idx]) : kFlagPre;
+      }
+      // this lane's nearest stop (inclusive prefix or error), and whether a status up to it is
+      // not ready yet
+      int stopQ = 4;
+#pragma unroll
+      for (int q = 3; q >= 0; q--)
+         if ((sv[q] >> 62) >= 2) stopQ = q;
+      bool laneNotReady = false;
+#pragma unroll
+      for (int q = 0; q < 4; q++)
+         if (q <= stopQ && (sv[q] >> 62) == 0) laneNotReady = true;
+      const uint32_t stopMask = __ballot_sync(0xffffffffu, stopQ < 4);
+      const int firstStop = stopMask ? __ffs(stopMask) - 1 : 31;
+      const uint32_t notReady = __ballot_sync(0xffffffffu, laneNotReady);
+      const uint32_t need = firstStop == 31 ? 0xffffffffu : ((2u << firstStop) - 1u);
+      if (notReady & need) {
+         if (!timing) {
+            t0 = global_ns();
+            timing = true;
+         } else if (global_ns() - t0 > kWaitNs) {
+            *err = true;
+            break;
+         }
+         continue;
+      }
+      uint32_t part = 0;
+      if (lane <= firstStop) {
+#pragma unroll
+         for (int q = 0; q < 4; q++)
+            if (lane < firstStop || q <= stopQ) part += (uint32_t)sv[q];
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+      excl += part;
+      if (stopMask) {
+         const int fq = __shfl_sync(0xffffffffu, stopQ, firstStop);
+         uint64_t fs = sv[0];
+#pragma unroll
+         for (int q = 1; q < 4; q++)
+            if (q == fq) fs = sv[q];
+         *err = (uint32_t)(__shfl_sync(0xffffffffu, fs, firstStop) >> 62) == 3u;
+         break;
+      }
+      j -= 128;
+   }
+   if (lane == 0) st_release(&st[c], (*err ? kFlagErr : kFlagPre) | (uint32_t)(excl + total));
+   return excl;
+}
+
+// ---- one CTA per chunk -------------------------------------------------------------------------
+// VEC = 4: float4 units (images 16-byte aligned), 128 threads x 16 units: small CTAs, five per
+// SM, so that while one CTA is in its serial phases (look-back, writes) the others keep their
+// loads in flight (with 512-thread CTAs, ncu showed the warps mostly parked at the barrier
+// behind the look-back and DRAM at 29 % of peak).  VEC = 1: scalar units, 512 threads x 16
+// units.  Every load of the chunk is issued before any is used.
 template <int VEC>
-__global__ void __launch_bounds__(kThreads, 3)
-      compact_kernel(const float *__restrict__ a, int64_t numExt, int nbatch, int nchunks, uint64_t *__restrict__ scratch,
-                     pvgpu_entry *__restrict__ entries, int64_t *__restrict__ numActive) {
-   constexpr int KU = kChunk / (kThreads * VEC);  // units per thread
+struct Shape {
+   static constexpr int kThreads = VEC == 4 ? 128 : 512;
+   static constexpr int kWarps = kThreads / 32;
+   static constexpr int KU = kChunk / (kThreads * VEC);  // units per thread (16)
+};
+
+template <int VEC>
+__global__ void __launch_bounds__(Shape<VEC>::kThreads, VEC == 4 ? 5 : 3)
+      compact_kernel(const float *__restrict__ a, int64_t numExt, int nbatch, int nchunks,
+                     uint64_t *__restrict__ scratch, pvgpu_entry *__restrict__ entries,
+                     int64_t *__restrict__ numActive) {
+   constexpr int kThreads = Shape<VEC>::kThreads, kWarps = Shape<VEC>::kWarps, KU = Shape<VEC>::KU;
    __shared__ uint32_t ticketSh, prefixSh;
-   __shared__ uint32_t wtot[KU * kWarps];          // warp totals, then their exclusive scan
+   __shared__ uint32_t wtot[KU * kWarps];  // warp totals, then their exclusive scan
    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-   uint64_t *status = scratch + 1;
-   if (tid == 0) ticketSh = atomicAdd(reinterpret_cast<unsigned long long *>(scratch), 1ull);
+   if (tid == 0) ticketSh = (uint32_t)atomicAdd(reinterpret_cast<unsigned long long *>(scratch), 1ull);
    __syncthreads();
-   // tickets interleave the images (chunk-major), so the chunks in flight spread over every
-   // image's chain and each look-back finds a published prefix close by
    const uint32_t t = ticketSh;
    const int c = (int)(t / (uint32_t)nbatch), b = (int)(t % (uint32_t)nbatch);
    const int64_t base = (int64_t)c * kChunk;
    const float *ab = a + (size_t)b * numExt;
-
-   // ---- load the chunk (all loads issued before any use) ----
    float v[KU * VEC];
    if constexpr (VEC == 4) {
       const float4 *a4 = reinterpret_cast<const float4 *>(ab);
@@ -89,152 +203,71 @@ __global__ void __launch_bounds__(kThreads, 3)
          v[k] = e < numExt ? __ldcs(ab + e) : 0.0f;
       }
    }
-
-   // ---- ranks inside the warp ----
-   uint32_t wex[KU];  // exclusive rank of this thread's unit k among the warp's units k
+   // rank of this thread's unit k among the warp's units k.  float4 units: four 8-bit fields
+   // per word (a warp's field sum is <= 128, so fields never carry), one warp scan per word;
+   // scalar units: a ballot per k.
+   constexpr int NW = VEC == 4 ? KU / 4 : 1;
+   uint32_t packed[NW], incl[NW];
+   uint32_t wexs[VEC == 4 ? 1 : KU];
    if constexpr (VEC == 4) {
-      uint32_t packed = 0;
+#pragma unroll
+      for (int w = 0; w < NW; w++) packed[w] = 0u;
 #pragma unroll
       for (int k = 0; k < KU; k++) {
          const uint32_t n = (v[4 * k] != 0.f) + (v[4 * k + 1] != 0.f) + (v[4 * k + 2] != 0.f) + (v[4 * k + 3] != 0.f);
-         packed |= n << (8 * k);  // a warp's field sum is <= 128: 8 bits never carry
+         packed[k >> 2] |= n << (8 * (k & 3));
       }
-      uint32_t incl = packed;
+#pragma unroll
+      for (int w = 0; w < NW; w++) incl[w] = packed[w];
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
-         const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-         if (lane >= o) incl += y;
-      }
-      const uint32_t ex = incl - packed;
 #pragma unroll
-      for (int k = 0; k < KU; k++) wex[k] = (ex >> (8 * k)) & 0xffu;
+         for (int w = 0; w < NW; w++) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, incl[w], o);
+            if (lane >= o) incl[w] += y;
+         }
+      }
       if (lane == 31) {
 #pragma unroll
-         for (int k = 0; k < KU; k++) wtot[k * kWarps + warp] = (incl >> (8 * k)) & 0xffu;
+         for (int k = 0; k < KU; k++) wtot[k * kWarps + warp] = (incl[k >> 2] >> (8 * (k & 3))) & 0xffu;
       }
    } else {
       const uint32_t lt = lanemask_lt();
 #pragma unroll
       for (int k = 0; k < KU; k++) {
          const uint32_t m = __ballot_sync(0xffffffffu, v[k] != 0.f);
-         wex[k] = __popc(m & lt);
+         wexs[k] = __popc(m & lt);
          if (lane == 0) wtot[k * kWarps + warp] = __popc(m);
       }
    }
    __syncthreads();
-
-   // ---- warp 0: scan of the warp totals in (k, warp) order, then the chunk prefix ----
    if (warp == 0) {
-      constexpr int PER = KU * kWarps / 32;  // consecutive totals per lane
-      uint32_t loc[PER], sum = 0;
-#pragma unroll
-      for (int i = 0; i < PER; i++) {
-         loc[i] = wtot[lane * PER + i];
-         sum += loc[i];
-      }
-      uint32_t incl = sum;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-         const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-         if (lane >= o) incl += y;
-      }
-      const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
-      uint32_t run = incl - sum;
-#pragma unroll
-      for (int i = 0; i < PER; i++) {
-         wtot[lane * PER + i] = run;
-         run += loc[i];
-      }
-      // decoupled look-back over this image's chunks
-      uint64_t *st = status + (size_t)b * nchunks;
-      uint32_t excl = 0;
-      bool err = false;
-      if (c == 0) {
-         if (lane == 0) st_release(&st[0], kFlagPre | total);
-      } else {
-         if (lane == 0) st_release(&st[c], kFlagAgg | total);
-         // lane l reads the statuses of chunks j - 4l .. j - 4l - 3 (128 predecessors per round
-         // trip); chunks before 0 read as a published prefix of 0
-         int j = c - 1;
-         uint64_t t0 = 0;
-         bool timing = false;
-         for (;;) {
-            uint64_t sv[4];
-#pragma unroll
-            for (int q = 0; q < 4; q++) {
-               const int idx = j - 4 * lane - q;
-               sv[q] = idx >= 0 ? ld_acquire(&st[idx]) : kFlagPre;
-            }
-            // this lane's nearest stop (inclusive prefix or error) and whether a status before it
-            // is not ready yet
-            int stopQ = 4;
-            bool laneNotReady = false;
-#pragma unroll
-            for (int q = 3; q >= 0; q--)
-               if ((sv[q] >> 62) >= 2) stopQ = q;
-#pragma unroll
-            for (int q = 0; q < 4; q++)
-               if (q <= stopQ && q < 4 && (sv[q] >> 62) == 0) laneNotReady = true;
-            const uint32_t stopMask = __ballot_sync(0xffffffffu, stopQ < 4);
-            const int firstStop = stopMask ? __ffs(stopMask) - 1 : 31;
-            const uint32_t notReady = __ballot_sync(0xffffffffu, laneNotReady);
-            const uint32_t need = firstStop == 31 ? 0xffffffffu : ((2u << firstStop) - 1u);
-            if (notReady & need) {
-               if (!timing) {
-                  t0 = pvgpu::tc::global_ns();
-                  timing = true;
-               } else if (pvgpu::tc::global_ns() - t0 > pvgpu::tc::kWaitNs) {
-                  err = true;
-                  break;
-               }
-               continue;
-            }
-            uint32_t part = 0;
-            if (lane <= firstStop) {
-#pragma unroll
-               for (int q = 0; q < 4; q++)
-                  if (lane < firstStop || q <= stopQ) part += (uint32_t)sv[q];
-            }
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
-            excl += part;
-            if (stopMask) {
-               const int fq = __shfl_sync(0xffffffffu, stopQ, firstStop);
-               uint64_t fs = sv[0];
-#pragma unroll
-               for (int q = 1; q < 4; q++)
-                  if (q == fq) fs = sv[q];
-               err = (uint32_t)(__shfl_sync(0xffffffffu, fs, firstStop) >> 62) == 3u;
-               break;
-            }
-            j -= 128;
-         }
-         if (lane == 0) st_release(&st[c], (err ? kFlagErr : kFlagPre) | (uint32_t)(excl + total));
-      }
+      const uint32_t total = scan_totals<KU * kWarps>(wtot, lane);
+      bool err;
+      const uint32_t excl = look_back(scratch + 1 + (size_t)b * nchunks, c, total, lane, &err);
       if (lane == 0) {
          prefixSh = excl;
          if (c == nchunks - 1) numActive[b] = err ? (int64_t)-1 : (int64_t)(excl + total);
       }
    }
    __syncthreads();
-
-   // ---- entries ----
    const uint32_t prefix = prefixSh;
    const uint32_t cap = (uint32_t)numExt;  // ranks stay below it; the test only guards the store
    uint2 *eb = reinterpret_cast<uint2 *>(entries + (size_t)b * numExt);
 #pragma unroll
    for (int k = 0; k < KU; k++) {
-      uint32_t r = prefix + wtot[k * kWarps + warp] + wex[k];
       if constexpr (VEC == 4) {
-         const int64_t e = base + (int64_t)(k * kThreads + tid) * 4;
+         uint32_t r = prefix + wtot[k * kWarps + warp] + (((incl[k >> 2] - packed[k >> 2]) >> (8 * (k & 3))) & 0xffu);
+         const uint32_t e = (uint32_t)base + 4u * (uint32_t)(k * kThreads + tid);
 #pragma unroll
          for (int q = 0; q < 4; q++) {
             if (v[4 * k + q] != 0.f) {
-               if (r < cap) eb[r] = make_uint2((uint32_t)(e + q), __float_as_uint(v[4 * k + q]));
+               if (r < cap) eb[r] = make_uint2(e + q, __float_as_uint(v[4 * k + q]));
                r++;
             }
          }
       } else {
+         const uint32_t r = prefix + wtot[k * kWarps + warp] + wexs[k];
          const int64_t e = base + k * kThreads + tid;
          if (v[k] != 0.f && r < cap) eb[r] = make_uint2((uint32_t)e, __float_as_uint(v[k]));
       }
@@ -256,15 +289,17 @@ pvgpu_status check_args(const float *aExt, int nbatch, int64_t numExt, const pvg
 pvgpu_status launch(const float *aExt, int nbatch, int64_t numExt, pvgpu_entry *entries, int64_t *numActive,
                     uint64_t *scratch, cudaStream_t s, const char *where) {
    const int64_t nchunks = chunks_of(numExt);
-   const size_t words = 1 + (size_t)nbatch * (size_t)nchunks;
+   const int64_t total = (int64_t)nbatch * nchunks;
+   const size_t words = 1 + (size_t)total;
    cudaError_t e = cudaMemsetAsync(scratch, 0, words * sizeof(uint64_t), s);
    if (e != cudaSuccess) return pvgpu::record_cuda_error(e, where);
-   const unsigned grid = (unsigned)(nbatch * nchunks);
    const bool vec = reinterpret_cast<uintptr_t>(aExt) % 16 == 0 && numExt % 4 == 0;
    if (vec)
-      compact_kernel<4><<<grid, kThreads, 0, s>>>(aExt, numExt, nbatch, (int)nchunks, scratch, entries, numActive);
+      compact_kernel<4><<<(unsigned)total, Shape<4>::kThreads, 0, s>>>(aExt, numExt, nbatch, (int)nchunks, scratch,
+                                                                       entries, numActive);
    else
-      compact_kernel<1><<<grid, kThreads, 0, s>>>(aExt, numExt, nbatch, (int)nchunks, scratch, entries, numActive);
+      compact_kernel<1><<<(unsigned)total, Shape<1>::kThreads, 0, s>>>(aExt, numExt, nbatch, (int)nchunks, scratch,
+                                                                       entries, numActive);
    PVGPU_CHECK_LAUNCH(where);
    return PVGPU_OK;
 }
