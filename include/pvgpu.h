@@ -334,6 +334,22 @@ pvgpu_status pvgpu_ann_activity(
       float *aExt,
       void *stream);
 
+/* applyVerticesANNActivityBufferOnGPU (components/ANNActivityBuffer.kpp:16-77), the form the
+ * reference's GPU path uses for every ANN layer and the only one for a vertex list given in
+ * params (verticesV / verticesA / slopeNegInf / slopePosInf): numVertices vertices and
+ * numVertices + 1 slopes (slopes[0] below the first vertex, slopes[numVertices] from the last
+ * on), all device arrays.  V restricted -> A extended (halo untouched).  Products and sums
+ * rounded separately, as the CPU form of the same function. */
+pvgpu_status pvgpu_ann_vertices(
+      const pvgpu_loc *loc,
+      int numVertices,
+      const float *verticesV,
+      const float *verticesA,
+      const float *slopes,
+      const float *v,
+      float *aExt,
+      void *stream);
+
 /* The three update kernels fused (HyPerActivityComponent::updateActivity,
  * components/HyPerActivityComponent.tpp:81-90, running GSynAccumulator -> HyPerLCAInternalStateBuffer
  * -> ANNActivityBuffer): one pass over the layer.  gsyn holds numChannels channels. */

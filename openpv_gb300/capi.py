@@ -122,6 +122,7 @@ def _declare(L):
         "pvgpu_gsyn_accumulate": (i, [i64, i, vp, vp, vp, vp]),
         "pvgpu_lca_update": (i, [lp, i, vp, f, vp, vp, vp, vp]),
         "pvgpu_ann_activity": (i, [lp, vp, f, f, f, f, f, vp, vp]),
+        "pvgpu_ann_vertices": (i, [lp, i, vp, vp, vp, vp, vp, vp]),
         "pvgpu_lca_layer_update": (i, [C.POINTER(LcaLayerDesc), vp, vp, vp, vp, vp]),
         "pvgpu_cost_sum": (i, [lp, vp, i, d, d, vp, vp]),
         "pvgpu_hebbian_dw": (i, [cp, f, vp, vp, vp, vp]),
@@ -331,6 +332,11 @@ def ista_update(loc, vthresh, dt_adapt, tau, g, a_ext, v, stream=None):
 def ann_activity(loc, v, VThresh, AMin, AMax, AShift, VWidth, a_ext, stream=None):
     check(lib().pvgpu_ann_activity(C.byref(loc), _ptr(v), VThresh, AMin, AMax, AShift, VWidth, _ptr(a_ext),
                                    _stream(stream)), "ann_activity")
+
+
+def ann_vertices(loc, vertices_v, vertices_a, slopes, v, a_ext, stream=None):
+    check(lib().pvgpu_ann_vertices(C.byref(loc), vertices_v.numel(), _ptr(vertices_v), _ptr(vertices_a), _ptr(slopes),
+                                   _ptr(v), _ptr(a_ext), _stream(stream)), "ann_vertices")
 
 
 def lca_layer_update(desc, gsyn, dt_adapt, v, a_ext, stream=None):

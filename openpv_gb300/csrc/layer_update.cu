@@ -140,6 +140,37 @@ __global__ void __launch_bounds__(kThreads) ann_kernel(Loc loc, Thresh t, const 
    }
 }
 
+// The piecewise-linear transfer function given by vertices (ANNActivityBuffer::setVertices /
+// applyVerticesANNActivityBufferOnGPU, components/ANNActivityBuffer.kpp:16-77): below the first
+// vertex and from the last one on, the outer slopes; between vertices v and v + 1 the slope
+// slopes[v + 1]; a potential equal to a vertex takes the vertex's activity, the last of equal
+// vertices winning (jumps are continuous from the right).  Products and sums are rounded
+// separately, as the CPU form of the same function.
+__global__ void __launch_bounds__(kThreads) ann_vertices_kernel(Loc loc, int nv, const float *__restrict__ vV,
+                                                                const float *__restrict__ vA,
+                                                                const float *__restrict__ slopes,
+                                                                const float *__restrict__ v, float *__restrict__ aExt) {
+   const int64_t numNeurons = loc.numRes(), total = numNeurons * loc.nb;
+   const int last = nv - 1;
+   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+      const int b = (int)(i / numNeurons);
+      const int64_t k = i - (int64_t)b * numNeurons;
+      const float x = v[i];
+      float a = 0.0f;
+      if (x < vV[0]) {
+         a = __fadd_rn(vA[0], __fmul_rn(slopes[0], __fsub_rn(x, vV[0])));
+      } else if (x >= vV[last]) {
+         a = __fadd_rn(vA[last], __fmul_rn(slopes[nv], __fsub_rn(x, vV[last])));
+      } else {
+         for (int j = 0; j < last && x >= vV[j]; j++) {
+            if (x == vV[j]) a = vA[j];
+            else if (x < vV[j + 1]) a = __fadd_rn(vA[j], __fmul_rn(slopes[j + 1], __fsub_rn(x, vV[j])));
+         }
+      }
+      aExt[(size_t)b * loc.numExt() + loc.kex(k)] = a;
+   }
+}
+
 // GSynAccumulator -> HyPerLCAInternalStateBuffer -> ANNActivityBuffer in one pass.
 __global__ void __launch_bounds__(kThreads) lca_layer_kernel(Loc loc, int nch, float c0, float c1, float c2, float c3,
                                                              float si, float tau, Thresh t,
@@ -243,6 +274,21 @@ extern "C" pvgpu_status pvgpu_ann_activity(const pvgpu_loc *loc, const float *v,
    ann_kernel<<<(unsigned)blocks, kThreads, 0, pvgpu::as_stream(stream)>>>(l, Thresh{VThresh, AMin, AMax, AShift, VWidth},
                                                                            v, aExt);
    PVGPU_CHECK_LAUNCH("ann_activity");
+   return PVGPU_OK;
+}
+
+extern "C" pvgpu_status pvgpu_ann_vertices(const pvgpu_loc *loc, int numVertices, const float *verticesV,
+                                           const float *verticesA, const float *slopes, const float *v, float *aExt,
+                                           void *stream) {
+   if (!loc || !pvgpu::loc_valid(*loc) || numVertices < 1 || !verticesV || !verticesA || !slopes || !v || !aExt)
+      return PVGPU_ERR_BAD_ARG;
+   Loc l = pvgpu::to_loc(*loc);
+   int64_t total = l.numRes() * l.nb;
+   int64_t blocks = (total + kThreads - 1) / kThreads;
+   if (blocks > 152 * 64) blocks = 152 * 64;
+   ann_vertices_kernel<<<(unsigned)blocks, kThreads, 0, pvgpu::as_stream(stream)>>>(l, numVertices, verticesV,
+                                                                                    verticesA, slopes, v, aExt);
+   PVGPU_CHECK_LAUNCH("ann_vertices");
    return PVGPU_OK;
 }
 

@@ -361,6 +361,33 @@ def ann_vertices(VThresh, AMin, AMax, AShift, VWidth):
     return vV[:n].copy(), vA[:n].copy(), sl[:n + 1].copy()
 
 
+def apply_vertices(loc, v, vV, vA, slopes):
+    """applyVerticesANNActivityBufferOnCPU (components/ANNActivityBuffer.kpp:16-77), vectorised:
+    the piecewise-linear transfer function of numVertices vertices and numVertices + 1 slopes,
+    restricted V -> extended A (halo zero).  float32 throughout, every product and sum rounded
+    on its own (numpy does not fuse them), as the reference's CPU build computes it."""
+    f = np.float32
+    vV, vA, sl = (np.asarray(t, f) for t in (vV, vA, slopes))
+    x = np.asarray(v, f).reshape(loc.nbatch, -1)
+    n = len(vV)
+    last = n - 1
+    a = np.zeros_like(x)
+    lo, hi = x < vV[0], x >= vV[last]
+    a[lo] = vA[0] + sl[0] * (x[lo] - vV[0])
+    a[hi] = vA[last] + sl[n] * (x[hi] - vV[last])
+    alive = ~lo & ~hi
+    for j in range(last):
+        alive &= x >= vV[j]  # the loop stops at the first vertex above the potential
+        eq = alive & (x == vV[j])
+        a[eq] = vA[j]
+        lin = alive & (x != vV[j]) & (x < vV[j + 1])
+        a[lin] = vA[j] + sl[j + 1] * (x[lin] - vV[j])
+    out = np.zeros(loc.ext_shape(), f)
+    h = loc.halo
+    out[:, h.up:h.up + loc.ny, h.lt:h.lt + loc.nx, :] = a.reshape(loc.res_shape())
+    return out
+
+
 COST_L2, COST_L1, COST_FIRM = 0, 1, 2
 
 

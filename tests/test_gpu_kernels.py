@@ -458,3 +458,32 @@ def test_momentum_weight_update_bitexact(cuda, oracle, method):
         capi.momentum_update_weights(dd, pd, wd, *f_d)
         for a, b in ((dd, dw), (pd, prev), (wd, w)):
             assert np.array_equal(H(a).view(np.uint32), b.view(np.uint32))
+
+
+@pytest.mark.parametrize("vertices", ["soft", "firm", "list"])
+def test_ann_vertices_bitexact(cuda, oracle, vertices):
+    """pvgpu_ann_vertices (the reference GPU path's vertex form, device vertex arrays) against the
+    oracle's vertex form, itself pinned to the reference's kernel: bit for bit, potentials on the
+    vertices included."""
+    torch = cuda
+    from openpv_gb300 import capi
+    rng = np.random.default_rng(21)
+    loc = capi.Loc.make(3, 20, 12, 7, 2)
+    v = (rng.normal(size=loc.res_shape()) * 0.5).astype(np.float32)
+    if vertices == "list":
+        vV = np.array([-0.5, 0.0, 0.0, 0.25, 1.0], np.float32)
+        vA = np.array([-0.5, 0.0, 0.1, 0.3, 0.7], np.float32)
+        sl = np.array([1.0, 1.0, 0.0, 0.8, 0.533, 2.0], np.float32)
+        v.reshape(-1)[:5] = vV
+    else:
+        th = (0.1, 0.0, np.inf, 0.1, 0.0) if vertices == "soft" else (0.1, 0.0, np.inf, 0.0, 0.05)
+        vV, vA, sl = oracle.ann_vertices(*[np.float32(x) for x in th])
+    ref = oracle.apply_vertices(OL(oracle, loc), v, vV, vA, sl)
+    a = torch.full(loc.ext_shape(), 7.0, device="cuda")
+    a_ref = ref.copy()
+    h = loc.halo
+    mask = np.ones(loc.ext_shape(), bool)
+    mask[:, h.up:h.up + loc.ny, h.lt:h.lt + loc.nx, :] = False
+    a_ref[mask] = 7.0  # the halo is left as it was
+    capi.ann_vertices(loc, T(torch, vV), T(torch, vA), T(torch, sl), T(torch, v), a)
+    assert np.array_equal(H(a).view(np.uint32), a_ref.view(np.uint32))

@@ -133,6 +133,26 @@ def test_threshold_cpu_form_matches_reference_vertex_form(oracle, th):
     np.testing.assert_allclose(a_cpu, a_vert, rtol=2e-6, atol=1e-7)
 
 
+@pytest.mark.parametrize("vertices", ["soft", "firm", "list"])
+def test_vertex_form_oracle_matches_reference_kernel(oracle, vertices):
+    """The oracle's vectorised vertex form equals the reference's applyVertices kernel (its CPU
+    build, compiled from ANNActivityBuffer.kpp) bit for bit, for the thresholds ANNActivityBuffer
+    derives from its parameters and for a vertex list as params give it (with a jump)."""
+    rng = np.random.default_rng(12)
+    loc = L(oracle, 2, 6, 5, 4, 2)
+    v = (rng.normal(size=loc.res_shape()) * 0.5).astype(np.float32)
+    if vertices == "list":
+        vV = np.array([-0.5, 0.0, 0.0, 0.25, 1.0], np.float32)
+        vA = np.array([-0.5, 0.0, 0.1, 0.3, 0.7], np.float32)
+        sl = np.array([1.0, 1.0, 0.0, 0.8, 0.533, 2.0], np.float32)
+        v.reshape(-1)[:5] = vV  # potentials exactly on the vertices
+    else:
+        th = (0.1, 0.0, np.inf, 0.1, 0.0) if vertices == "soft" else (0.1, 0.0, np.inf, 0.0, 0.05)
+        vV, vA, sl = oracle.ann_vertices(*[np.float32(x) for x in th])
+    ref = refbuild.apply_vertices(loc, v, vV, vA, sl)
+    assert np.array_equal(oracle.apply_vertices(loc, v, vV, vA, sl).view(np.uint32), ref.view(np.uint32))
+
+
 @pytest.mark.parametrize("kind,p0,p1", [(0, 0, 0), (1, 0, 0), (2, 0.025, 0.025), (2, 0.1, 0.0)])
 def test_cost_functions_match_reference(oracle, kind, p0, p1):
     rng = np.random.default_rng(11)
