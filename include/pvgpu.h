@@ -241,6 +241,7 @@ pvgpu_status pvgpu_pvp_scatter_sparse(
  * extended presynaptic activity (the layer's activity buffer, which the reference's GPU
  * deliveries also receive: recv_pre_params.preData, cudakernels/CudaRecvPre.hpp:19-45), so the
  * cost does not depend on the activity's density.  GSyn of the channel is accumulated into.
+ * pvgpu_deliver_tc_workspace_bytes is 0 for a connection these entries do not take.
  * `workspace` (device, 16-byte aligned, >= pvgpu_deliver_tc_workspace_bytes) holds the split
  * (and, for the presynaptic entry, transposed) weights; calls that overlap on the GPU need
  * separate workspaces.  Other shapes return PVGPU_ERR_UNSUPPORTED_SHAPE: use

@@ -566,6 +566,14 @@ pvgpu_status run(const pvgpu_conn_desc *conn, const float *aExt, const float *po
 
 extern "C" size_t pvgpu_deliver_tc_workspace_bytes(const pvgpu_conn_desc *conn) {
    if (!conn) return 0;
+   int dev = 0, numSms = 0;
+   if (cudaGetDevice(&dev) != cudaSuccess ||
+       cudaDeviceGetAttribute(&numSms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+      cudaGetLastError();
+      numSms = 152;
+   }
+   TcGeom g;
+   if (plan(conn, g, numSms) != PVGPU_OK) return 0;  // a shape these entries do not take
    // transposed weights (presynaptic entry) + their hi / lo split
    return 3 * weights_floats(conn) * sizeof(float);
 }

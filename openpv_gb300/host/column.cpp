@@ -66,6 +66,11 @@ class PostDelivery : public Delivery {
       if (mode_ == PVGPU_DELIVER_FAST && tc_) {
          if (!ws_) {
             wsBytes_ = pvgpu_deliver_tc_workspace_bytes(&c_->desc);
+            if (wsBytes_ == 0) {  // not a shape of the tensor-core entry
+               tc_ = false;
+               engine_ = "simt";
+               return pvgpu_deliver_post(&c_->desc, c_->pre->A, c_->Wpost, channel, mode_, s);
+            }
             if (cudaMalloc(&ws_, wsBytes_) != cudaSuccess) {
                ws_ = nullptr;
                return PVGPU_ERR_OOM;

@@ -119,6 +119,7 @@ def test_deliver_tc_refuses_other_shapes(cuda):
         capi.conn_desc(capi.Loc.make(1, 16, 16, 32, 5), capi.Loc.make(1, 16, 16, 32, 0), 11, 11),  # patch > 9
     ]
     for conn in bad:
+        assert capi.deliver_tc_workspace_bytes(conn) == 0  # the size query tells the shape apart too
         with pytest.raises(capi.PvgpuError) as e:
             capi.deliver_post_tc(conn, a, w, g, ws)
         assert e.value.status == capi.PVGPU_ERR_UNSUPPORTED_SHAPE
