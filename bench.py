@@ -497,17 +497,18 @@ class LifNet:
         rec(3)
 
 
-def dictlearn_bench(torch, reps=2):
+def dictlearn_bench(torch, capi, reps=5):
     """Differentiable dictionary learning at full size: 32 images 64x64x1 (1/f, unit std), V1
     16x16x256 stride 4, 256 features of 16x16x1, 100 unrolled LCA timesteps from V = 0 with a
     checkpoint every 10, loss 0.5 ||x - W^T a||^2 + 0.1 ||a||_1; one gradient = the forward pass,
-    the recomputation of each checkpointed segment and the adjoint pass, all through the C-ABI
-    delivery kernels and their adjoints (pvgpu_deliver_pre / _post, pvgpu_hebbian_dw) driven by
-    the autograd harness of the tests."""
-    from tests import lca_autograd as LA
+    the recomputation of each checkpointed segment and the adjoint pass, through the C ABI
+    (pvgpu_lca_grad_run: one CUDA graph).  CPU baseline: the reference's own learning step on the
+    host cores -- the LCA solve of the oracle (one image per thread) for a sample of the batch --
+    since the reference learns dictionaries with the Hebbian rule after an LCA solve."""
+    import time
+    from oracle import oracle as O
     rng = np.random.default_rng(1234 + 4)
     nb, n, v1, P, T, lam = 32, 64, (16, 16, 256), 16, 100, 0.1
-    geo = LA.Geometry(nb, (n, n, 1), v1, P)
     w = rng.normal(size=(v1[2], P, P, 1))
     w = (w / np.sqrt((w ** 2).sum(axis=(1, 2, 3), keepdims=True))).astype(np.float32)
     f = np.sqrt(np.fft.fftfreq(n)[:, None] ** 2 + np.fft.fftfreq(n)[None, :] ** 2)
@@ -516,28 +517,42 @@ def dictlearn_bench(torch, reps=2):
     amp[0, 0] = 0.0
     xi = np.real(np.fft.ifft2(amp[None] * np.exp(1j * rng.uniform(0, 2 * np.pi, (nb, n, n)))))
     xi = (xi - xi.mean(axis=(1, 2), keepdims=True)) / xi.std(axis=(1, 2), keepdims=True)
-    x = torch.from_numpy(np.ascontiguousarray(xi[..., None].astype(np.float32))).cuda()
-    wd = torch.from_numpy(w).cuda().requires_grad_(True)
-
-    def gradient():
-        wd.grad = None
-        loss = LA.unrolled_lca_loss(wd, x, geo, T, lam, lam, checkpoint_every=10)
-        loss.backward()
-        return loss
-
-    gradient()
+    x_np = np.ascontiguousarray(xi[..., None].astype(np.float32))
+    x = torch.from_numpy(x_np).cuda()
+    wd = torch.from_numpy(w).cuda()
+    dw = torch.empty_like(wd)
+    loss = torch.zeros(1, dtype=torch.float64, device="cuda")
+    grad = capi.LcaGrad(nb, (n, n, 1), v1, P, lam, lam, T, checkpoint_every=10)
+    grad.run(wd, x, dw, loss)  # captures the graph
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
     for _ in range(reps):
-        loss = gradient()
+        grad.run(wd, x, dw, loss)
     e1.record()
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / reps
+    M, F, KP = nb * v1[0] * v1[1], v1[2], P * P
+    flops = (8 * T + 3) * 2 * M * F * KP  # every GEMM of the forward, the recomputation and the adjoint
+    # CPU: the oracle's LCA solve of the same geometry, one image per thread, on a sample
+    cores = min(os.cpu_count() or 1, nb)
+    p = O.lca_params(nbatch=cores, inNx=n, inNy=n, inNf=1, v1Nx=v1[1], v1Ny=v1[0], v1Nf=v1[2], nxp=P, nyp=P,
+                     VThresh=lam, AShift=lam, AMin=0.0, tau=100.0)
+    cpu_steps = 5
+    t0 = time.perf_counter()
+    O.lca_run(p, w, x_np[None, :cores], cpu_steps, np.zeros((cores,) + v1, np.float32), threads=cores,
+              want_recon=False)
+    cpu_s = time.perf_counter() - t0
     return {"workload": "32 x 64x64x1 -> V1 16x16x256 stride 4, 256 x 16x16x1 dictionary, 100 unrolled "
                         "timesteps (checkpoint every 10), gradient of 0.5||x - W^T a||^2 + 0.1||a||_1 w.r.t. W",
             "ms_per_gradient": ms, "image_steps_per_s": nb * T / (ms / 1000.0), "loss": float(loss.item()),
-            "grad_norm": float(wd.grad.norm().item()), "dtype": "f32"}
+            "grad_norm": float(dw.norm().item()), "dtype": "f32",
+            "gemm_math": "fp32 emulated on bf16 tensor cores" if grad.emulated_fp32() else "fp32",
+            "gemm_tflops_fp32_equivalent": flops / (ms / 1000.0) / 1e12,
+            "cpu_baseline": {"value": cores * cpu_steps / cpu_s, "unit": "image-steps/s", "cores": cores,
+                             "kind": "port", "sample": f"oracle LCA solve (forward only) of {cores} images x "
+                                                       f"{cpu_steps} timesteps, one image per thread "
+                                                       f"({cpu_s:.1f} s)"}}
 
 
 def lif_bench(torch, capi, steps=1000, cpu_sample=True):
@@ -828,7 +843,7 @@ def run_ours(args, rank, world, local_rank):
     deliv = delivery_bench(torch, capi)
     c1b = config1_bench(torch, capi)
     lifb = lif_bench(torch, capi)
-    dlb = dictlearn_bench(torch)
+    dlb = dictlearn_bench(torch, capi)
     clocks = clk.summary()
 
     # the FP32 form against its own ceiling: FP32 FMA lanes x 2 FLOP x SM clock (nominal lanes,
@@ -904,9 +919,18 @@ def main():
     ap.add_argument("--lif", action="store_true",
                     help="run the LIF network only (profiling runs; not a bench line)")
     ap.add_argument("--lif-steps", type=int, default=1000, help="timesteps of the LIF network graph (--lif)")
+    ap.add_argument("--dictlearn", action="store_true",
+                    help="run the dictionary-learning gradient section only (profiling runs; not a bench line)")
     ap.add_argument("--plain-lca", action="store_true",
                     help="run the batch-1 plain LCA latency section only (profiling runs; not a bench line)")
     args = ap.parse_args()
+    if args.dictlearn:
+        import torch
+        from openpv_gb300 import build
+        build.build()
+        from openpv_gb300 import capi
+        print(json.dumps({"dictionary_learning": dictlearn_bench(torch, capi)}))
+        return
     if args.plain_lca:
         import torch
         from openpv_gb300 import build

@@ -385,6 +385,37 @@ pvgpu_status pvgpu_cost_sum(
       double *out,
       void *stream);
 
+/* ---- config 4: the gradient of unrolled LCA (differentiable dictionary learning) ----------
+ * No single reference counterpart: the reference learns dictionaries with the Hebbian rule
+ * (weightupdaters/HebbianUpdater.cpp:476-629), which is minus the gradient below for a fixed
+ * activity.  L(W) = 0.5 ||x - W^T a_T||^2 + lambda ||a_T||_1 summed over the batch, a_T after
+ * `steps` LCA timesteps from V = 0 (soft threshold a = max(V - VThresh, 0); V' = e V + (1 - e)
+ * (W (x - W^T a) + a), e = exp(-dt / tau), the update of HyPerLCAInternalStateBuffer.kpp:18-63),
+ * and dL/dW through the unrolled solve, checkpointed every `checkpointEvery` timesteps.  The V1
+ * layer tiles the input with one stride S = inNx / v1Nx; patches nxp x nxp x inNf with
+ * (nxp - S) even (the LCA one-to-many geometry).  W: device FP32 [v1Nf][nxp][nxp][inNf] (the
+ * V1 -> error weights), x: device FP32 [nbatch][inNy][inNx][inNf]; dW (same layout as W) and
+ * *loss (device double) are overwritten.  The deliveries and their adjoints are GEMMs over
+ * im2col'd operands (FP32, emulated on the BF16 tensor cores where the cuBLAS in the process
+ * offers it; pvgpu_lca_grad_info tells), the rest the library's own kernels; a run is one CUDA
+ * graph, captured at the first run with a given set of pointers (make that run outside any
+ * stream capture) and replayed on `stream`.  create returns PVGPU_ERR_UNSUPPORTED_SHAPE when
+ * cuBLAS cannot be loaded. */
+typedef struct {
+   int nbatch, inNx, inNy, inNf;
+   int v1Nx, v1Ny, v1Nf;
+   int nxp;
+   float VThresh, lambda1, tau, dt; /* lambda1: the L1 coefficient of the loss */
+   int steps, checkpointEvery;
+} pvgpu_lca_grad_desc;
+typedef struct pvgpu_lca_grad pvgpu_lca_grad;
+pvgpu_status pvgpu_lca_grad_create(const pvgpu_lca_grad_desc *desc, pvgpu_lca_grad **out);
+pvgpu_status pvgpu_lca_grad_destroy(pvgpu_lca_grad *g);
+pvgpu_status pvgpu_lca_grad_run(pvgpu_lca_grad *g, const float *w, const float *x, float *dW, double *loss,
+                                void *stream);
+/* *emulatedFp32 = 1 when the GEMMs run as FP32 emulated on the BF16 tensor cores, 0 for plain FP32. */
+pvgpu_status pvgpu_lca_grad_info(const pvgpu_lca_grad *g, int *emulatedFp32);
+
 /* ---- a12: Hebbian weight update and the adjoint of delivery ------------------------------
  * HebbianUpdater::update_dW / updateInd_dW (weightupdaters/HebbianUpdater.cpp:476-629), shared
  * weights, summed over the batch, normalize_dW off: dW[kernel][item] = dWMax * sum pre*post.

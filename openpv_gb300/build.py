@@ -67,7 +67,7 @@ def build(verbose=False, extra=()):
         raise RuntimeError("libpvgpu build failed:\n" + "\n".join(errs))
     objs = [o for o, _ in results]
     if not os.path.exists(LIB) or any(os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs):
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-ldl"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"libpvgpu link failed:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")

@@ -83,6 +83,12 @@ class LcaSolverDesc(C.Structure):
                 ("VWidth", C.c_float), ("tau", C.c_float), ("dt", C.c_float), ("selfInteract", C.c_int)]
 
 
+class LcaGradDesc(C.Structure):
+    _fields_ = [("nbatch", C.c_int), ("inNx", C.c_int), ("inNy", C.c_int), ("inNf", C.c_int), ("v1Nx", C.c_int),
+                ("v1Ny", C.c_int), ("v1Nf", C.c_int), ("nxp", C.c_int), ("VThresh", C.c_float), ("lambda1", C.c_float),
+                ("tau", C.c_float), ("dt", C.c_float), ("steps", C.c_int), ("checkpointEvery", C.c_int)]
+
+
 class LcaSchedule(C.Structure):
     _fields_ = [("chains", C.c_int), ("reconCtas", C.c_int), ("postCtas", C.c_int), ("programmatic", C.c_int),
                 ("fused", C.c_int)]
@@ -163,6 +169,10 @@ def _declare(L):
         "pvgpu_pvp_scatter_sparse": (i, [lp, vp, vp, vp, vp, vp]),
         "pvgpu_taus_init": (i, [vp, i64, C.c_uint32, vp]),
         "pvgpu_selftest_wait_expiry": (i, [C.c_uint64, C.POINTER(C.c_longlong), vp]),
+        "pvgpu_lca_grad_create": (i, [C.POINTER(LcaGradDesc), C.POINTER(vp)]),
+        "pvgpu_lca_grad_destroy": (i, [vp]),
+        "pvgpu_lca_grad_run": (i, [vp, vp, vp, vp, vp, vp]),
+        "pvgpu_lca_grad_info": (i, [vp, C.POINTER(i)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -478,6 +488,42 @@ class LcaSolver:
         f = C.c_int(0)
         check(lib().pvgpu_lca_solver_error_flag(self.h, C.byref(f)), "lca_solver_error_flag")
         return f.value
+
+
+class LcaGrad:
+    """dL/dW of unrolled LCA (pvgpu_lca_grad_*): L = 0.5 ||x - W^T a_T||^2 + lam ||a_T||_1 after
+    `steps` timesteps from V = 0, checkpointed every `checkpoint_every`; device tensors in the
+    OpenPV layouts (W [F][P][P][C], x [nb][ny][nx][C])."""
+
+    def __init__(self, nbatch, in_shape, v1_shape, nxp, VThresh, lam, steps, checkpoint_every=10, tau=100.0,
+                 dt=1.0):
+        iny, inx, inf_ = in_shape
+        vy, vx, vf = v1_shape
+        self.desc = LcaGradDesc(nbatch, inx, iny, inf_, vx, vy, vf, nxp, VThresh, lam, tau, dt, steps,
+                                checkpoint_every)
+        h = C.c_void_p()
+        check(lib().pvgpu_lca_grad_create(C.byref(self.desc), C.byref(h)), "lca_grad_create")
+        self.h = h
+
+    def close(self):
+        if self.h:
+            lib().pvgpu_lca_grad_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def run(self, w, x, dw, loss, stream=None):
+        check(lib().pvgpu_lca_grad_run(self.h, _ptr(w), _ptr(x), _ptr(dw), _ptr(loss), _stream(stream)),
+              "lca_grad_run")
+
+    def emulated_fp32(self):
+        f = C.c_int(0)
+        check(lib().pvgpu_lca_grad_info(self.h, C.byref(f)), "lca_grad_info")
+        return bool(f.value)
 
 
 # ---- libpvhost.so: the C++ host side (params file -> column of layers and connections) ----------

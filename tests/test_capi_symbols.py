@@ -76,6 +76,7 @@ def test_struct_layouts_match_the_header(tmp_path):
         "pvgpu_lca_layer_desc": capi.LcaLayerDesc,
         "pvgpu_lca_solver_desc": capi.LcaSolverDesc,
         "pvgpu_lca_schedule": capi.LcaSchedule,
+        "pvgpu_lca_grad_desc": capi.LcaGradDesc,
         "pvgpu_lif_params": capi.LifParams,
     }
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "pvgpu.h"', "int main(void) {"]
