@@ -172,6 +172,7 @@ struct Blas {
    cublasStatus_t (*gemmEx)(cublasHandle_t, cublasOperation_t, cublasOperation_t, int, int, int, const void *,
                             const void *, cudaDataType, int, const void *, cudaDataType, int, const void *, void *,
                             cudaDataType, int, cublasComputeType_t, cublasGemmAlgo_t) = nullptr;
+   cublasStatus_t (*setSpecialValues)(cublasHandle_t, cudaEmulationSpecialValuesSupport) = nullptr;  // optional
    bool ok = false;
 };
 
@@ -193,6 +194,8 @@ void load_blas() {
    g_blas.setStream = reinterpret_cast<decltype(g_blas.setStream)>(dlsym(g_blas.so, "cublasSetStream_v2"));
    g_blas.setWorkspace = reinterpret_cast<decltype(g_blas.setWorkspace)>(dlsym(g_blas.so, "cublasSetWorkspace_v2"));
    g_blas.gemmEx = reinterpret_cast<decltype(g_blas.gemmEx)>(dlsym(g_blas.so, "cublasGemmEx"));
+   g_blas.setSpecialValues = reinterpret_cast<decltype(g_blas.setSpecialValues)>(
+         dlsym(g_blas.so, "cublasSetEmulationSpecialValuesSupport"));
    g_blas.ok = g_blas.create && g_blas.destroy && g_blas.setStream && g_blas.setWorkspace && g_blas.gemmEx;
 }
 
@@ -428,6 +431,9 @@ extern "C" pvgpu_status pvgpu_lca_grad_create(const pvgpu_lca_grad_desc *d, pvgp
       free_all(s);
       return pvgpu::record_message(PVGPU_ERR_LAUNCH, "lca_grad: cuBLAS handle");
    }
+   // the operands are finite (a run with an inf or NaN in W or x has no meaningful gradient), so the
+   // emulated GEMMs skip their scans for special values
+   if (g_blas.setSpecialValues) g_blas.setSpecialValues(s->blas, CUDA_EMULATION_SPECIAL_VALUES_SUPPORT_NONE);
    if (cudaStreamCreateWithFlags(&s->capStream, cudaStreamNonBlocking) != cudaSuccess) {
       cudaGetLastError();
       s->capStream = nullptr;
