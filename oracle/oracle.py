@@ -140,6 +140,7 @@ def _declare(L):
         "pvo_adaptive_timescale": (None, [i, d, d, d, d, vp, vp]),
         "pvo_hebbian_dw": (i, [lp, lp, i, i, f, vp, vp, vp]),
         "pvo_hebbian_dw_f64": (i, [lp, lp, i, i, d, vp, vp, vp]),
+        "pvo_hebbian_dw_rule": (i, [lp, lp, i, i, i, f, vp, vp, vp, vp]),
         "pvo_lca_run": (i, [C.POINTER(LcaParams), vp, vp, i, i, vp, vp, vp, vp, i]),
         "pvo_lca_run_f64": (i, [C.POINTER(LcaParams), vp, vp, i, i, vp, vp, vp, vp, i]),
     }
@@ -420,6 +421,22 @@ def hebbian_dw(pre, post, nxp, nyp, pre_ext, post_ext, dw_max=1.0, f64=False):
                                   _p(_c(post_ext, np.float32)), _p(dw))
     _check(rc, "hebbian_dw")
     return dw
+
+
+def hebbian_dw_normalized(pre, post, nxp, nyp, pre_ext, post_ext, rule=0, dw_max=1.0):
+    """HebbianUpdater's dW with normalizeDw: the accumulated dW of each kernel item divided by the
+    number of its contributions, 0 where there were none (HebbianUpdater.cpp:787-812).  rule 0:
+    dWMax * pre * post; rule 1: pre - post (the reference's PlasticConnTest updater)."""
+    nk = kernel_index_table(pre, post)[1]
+    dw = np.zeros((nk, nyp, nxp, post.nf), np.float32)
+    counts = np.zeros(dw.shape, np.int64)
+    rc = lib().pvo_hebbian_dw_rule(C.byref(pre), C.byref(post), nxp, nyp, rule, dw_max,
+                                   _p(_c(pre_ext, np.float32)), _p(_c(post_ext, np.float32)), _p(dw), _p(counts))
+    _check(rc, "hebbian_dw_rule")
+    out = np.zeros_like(dw)
+    nz = counts != 0
+    out[nz] = dw[nz] / counts[nz].astype(np.float32)
+    return out, counts
 
 
 def lca_params(**kw):

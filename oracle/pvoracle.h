@@ -245,6 +245,31 @@ int pvo_hebbian_dw_f64(
       const double *preExt,
       const double *postExt,
       double *dw);
+/* The same loop with the update rule chosen (0: dWMax * pre * post; 1: pre - post, the rule of
+ * the reference's PlasticConnTest updater) and, when counts is not NULL, the number of
+ * contributions per kernel item (the divisor of HebbianUpdater::normalize_dW). */
+int pvo_hebbian_dw_rule(
+      const pvo_loc *pre,
+      const pvo_loc *post,
+      int nxp,
+      int nyp,
+      int rule,
+      float dWMax,
+      const float *preExt,
+      const float *postExt,
+      float *dw,
+      int64_t *counts);
+int pvo_hebbian_dw_rule_f64(
+      const pvo_loc *pre,
+      const pvo_loc *post,
+      int nxp,
+      int nyp,
+      int rule,
+      double dWMax,
+      const double *preExt,
+      const double *postExt,
+      double *dw,
+      int64_t *counts);
 
 /* ---- the canonical LCA module -------------------------------------------- */
 /* Input -> Error (IdentConn ch0), V1 -> Error (pre perspective, sparse, ch1),

@@ -1,6 +1,8 @@
 """Pins the CPU oracle against the reference's own code compiled from its source tree
 (oracle/_ref/libpvref.so): PatchGeometry tables, the .kpp update kernels and the
 energy cost functions, compared bit for bit.  Skips where the reference tree is absent."""
+import os
+
 import numpy as np
 import pytest
 
@@ -275,3 +277,43 @@ def test_lif_update_matches_reference(oracle, method, noise):
         assert np.array_equal(a_o.view(np.uint32), a_r.view(np.uint32)), step
         spikes += int(a_o.sum())
     assert spikes > 0  # the inputs drive some neurons over threshold
+
+
+def test_hebbian_loop_reproduces_plastic_conn_test_fixture(oracle):
+    """The reference's own known-answer file for the plasticity loop,
+    tests/PlasticConnTest/input/CorrectValues.pvp (PlasticConnTest.params): Pre and Post
+    (32x32x1) hold their global x position (0.5 + x, PlasticConnTestActivityBuffer.cpp:38-55),
+    PreToPost (5x5, shared, from W = 0) updates every step with the rule pre - post
+    (PlasticTestUpdater.cpp:17) and normalizeDw, and TestOutput receives TestInput.pvp through a
+    clone of PreToPost; the file holds TestOutput at t = 1 .. 100.  The oracle's dW loop (the one
+    pvgpu_hebbian_dw is checked against, here with that rule and the activation counts) and its
+    presynaptic delivery reproduce every frame bit for bit."""
+    from openpv_gb300 import build
+    build.build()
+    from openpv_gb300 import capi
+    d = os.path.join(refbuild.REF_ROOT, "tests", "PlasticConnTest", "input")
+    if not os.path.isdir(d):
+        pytest.skip("reference tree not present")
+
+    def xpos(loc):
+        a = np.zeros(loc.ext_shape(), np.float32)
+        nxe = loc.nx + loc.halo.lt + loc.halo.rt
+        a[:] = (np.float32(0.5) + (np.arange(nxe) - loc.halo.lt).astype(np.float32))[None, None, :, None]
+        return a
+
+    pre, post = oracle.Loc.make(1, 32, 32, 1, 2), oracle.Loc.make(1, 32, 32, 1, 0)
+    dw, counts = oracle.hebbian_dw_normalized(pre, post, 5, 5, xpos(pre), xpos(post), rule=1)
+    assert np.all(counts == 32 * 32)
+    with capi.PvpReader(os.path.join(d, "TestInput.pvp")) as r:
+        x, _ = r.read_dense(0)
+    xe = np.zeros(pre.ext_shape(), np.float32)
+    xe[0, 2:34, 2:34, :] = x.reshape(32, 32, 1)
+    w = np.zeros_like(dw)
+    with capi.PvpReader(os.path.join(d, "CorrectValues.pvp")) as r:
+        assert r.num_frames == 100
+        for i in range(r.num_frames):
+            want, t = r.read_dense(i)
+            assert t == i + 1
+            got = oracle.deliver_pre(pre, post, 5, 5, w, a_ext=xe)
+            assert np.array_equal(got.reshape(-1), want.reshape(-1)), i
+            w = w + dw  # immediateWeightUpdate: W += dW after each step's output
