@@ -519,7 +519,7 @@ pvgpu_status pvgpu_lca_solver_plan_info(const pvgpu_lca_solver *s, int *out);
  * when the geometry has no fused form. */
 pvgpu_status pvgpu_lca_solver_fused_plan_info(const pvgpu_lca_solver *s, int *out);
 /* Sets the fused kernel's shape (what the autotuner otherwise picks): feature tile (a multiple
- * of 64 dividing v1Nf), V ring slots (1..3), weight ring slots (2..3); PVGPU_ERR_UNSUPPORTED_SHAPE
+ * of 64 dividing v1Nf), V ring slots (2 or 4), weight ring slots (2..4); PVGPU_ERR_UNSUPPORTED_SHAPE
  * when it does not fit shared memory.  The ring depths do not change results; the feature tile
  * sets how the reconstruction is split into bands (FP32 summation order of the residual). */
 pvgpu_status pvgpu_lca_solver_set_fused_plan(pvgpu_lca_solver *s, int featureTile, int vSlots, int wSlots);

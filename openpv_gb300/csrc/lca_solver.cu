@@ -806,80 +806,87 @@ __global__ void __launch_bounds__(320, 1) post_tc_kernel(const __grid_constant__
 // where it fits, else in shared memory), the update, then the block's new activity A_q (BF16,
 // 128 positions x 64 features) goes into one of two TMEM A tiles and GEMM2 accumulates
 // D2[pos][k] += sum_f A_q[pos][f] W_q[f][k] (N = P*P*C) in TMEM, reading the block's weight
-// tile again as an MN-major operand.  After the tile's last block epilogue warps 0-7 fold D2
-// into a band: padded rows S*mb*rpb .. +RWR (every row the block's patches reach), starting from
-// x on the rows the block owns when fh == 0 and from 0 otherwise, each tap subtracted (kernel
-// R's fold: 16 tap groups, no two threads on one pixel inside a group, every pixel's taps in
-// one fixed order).  The band goes to HBM.  Block mb owns padded rows S*mb*rpb ..
-// S*(mb+1)*rpb - 1, the last block also the rows below; bands of blocks mb and mb + 1 overlap
-// in P - S rows (P - S <= S*rpb).
+// tile again as an MN-major operand.  After the tile's last GEMM2 the tile warps fold D2 into a
+// band: padded rows S*mb*rpb .. +RWR (every row the block's patches reach), starting from x on
+// the rows the block owns when fh == 0 and from 0 otherwise, each tap subtracted (kernel R's
+// fold: tap groups in which no two threads touch one pixel, every pixel's taps in one fixed
+// order).  The band goes to HBM.  Block mb owns padded rows S*mb*rpb .. S*(mb+1)*rpb - 1, the
+// last block also the rows below; bands of blocks mb and mb + 1 overlap in P - S rows
+// (P - S <= S*rpb).
 // The next timestep's tile (b, mb) sums its residual window r = x - W^T a from the bands of
 // (b, mb) and the overlapping rows of (b, mb - 1) and (b, mb + 1), all feature tiles: per
 // pixel (sum over fh of the lower block's band) + (sum over fh of the upper block's band),
 // so that both windows holding a pixel compute it in the same order.  The first timestep of
 // a run reads kernel R's padded residual window instead (mode 0).
-// Roles (608 threads):
-//   warps 0-15 (epilogue): per block, warp = (lane quarter, 16-feature group): the LCA update of
-//             its 32 positions x 16 features from D1 and the shared V chunk, V back in place,
-//             A into the TMEM A tile of the block's parity (after GEMM2 of block q - 2 has read
-//             it); the two warps of a 32-feature half meet at a named barrier and the second
-//             bulk-stores their 4 KB.  After block kIm all 16 sum the next tile's window from
-//             the bands and build its im2col (a quarter of the patch rows per thread); warps
-//             0-7 prefetch x of the owned rows at the start of the tile's last block, and after
-//             it fold D2 into the band (in the stage, which the next tile's im2col has read)
-//             and store the band;
-//   warp 16 (weights): each block's weight tile by TMA into a 2- or 3-slot ring;
-//   warp 17 (MMA):     an event loop issuing GEMM1 of the next block as soon as its weight
+// Roles (736 threads):
+//   warps 0-15 (epilogue): two groups of eight on alternating 64-feature blocks (group 0 the
+//             even blocks of the CTA's sequence, group 1 the odd ones), so that the hand-off
+//             chains of two blocks (accumulator, TMEM load, update, A into TMEM, V store) are
+//             in flight at once.  Group g owns GEMM1 accumulator g, TMEM A tile g and V slots
+//             g, g + 2 (the V ring has 2 or 4 slots, so each slot's phases are waited on by one
+//             group only and an mbarrier's parity never stands for two phases).  Warp = (lane
+//             quarter qd, 32-feature half hh): the update of its 32 positions x 32 features from
+//             D1 and its 4 KB of the V chunk, V back in place and to HBM by its own bulk store,
+//             A into the group's A tile once GEMM2 of the group's previous block has read it.
+//             No named barrier: every hand-off is an mbarrier;
+//   warps 16-19 (tile): named barrier 1.  Per tile t: the window of tile t + 1 summed from the
+//             bands and its im2col (one position per thread, all P*P*C taps) once tile t's
+//             last GEMM1 has read the operand; then tile t's fold: x of the owned rows (or 0)
+//             into the stage, which tile t + 1's im2col has read, D2 folded in once tile t's
+//             last GEMM2 is done, d2Empty as soon as D2 is read, the band stored;
+//   warp 20 (weights): each block's weight tile by TMA into a 2- to 4-slot ring;
+//   warp 21 (MMA):     an event loop issuing GEMM1 of the next block as soon as its weight
 //             tile, accumulator and im2col operand are ready, and GEMM2 of the oldest block
-//             whose A tile is written; a weight slot is freed by GEMM2's commit;
-//   warp 18 (V, stage): V chunks by bulk copy into a 1- to 4-slot ring, and the tile's bands (or
-//             residual window) as one stage once the tile before has read the stage and the
-//             fold of the tile before that (which runs in the stage) is stored.
-// Hand-offs added to kernel P's: aFull / aEmpty per A tile, d2Full (the tile's D2 complete),
-// foldFree (the band store has read the stage).  D2 is overwritten by the next tile's first
-// GEMM2 only after that block's aFull, which warps 0-7 signal after the fold's TMEM reads.
+//             whose A tile is written (the first GEMM2 of a tile also once the fold of the tile
+//             before has read D2); a weight slot is freed by GEMM2's commit;
+//   warp 22 (V, stage): an event loop: V chunks by bulk copy into the ring as slots free, and
+//             tile t's bands (or residual window) as one stage once tile t - 1's im2col has
+//             read the stage and tile t - 2's fold (which runs in the stage) is stored.
+// Every wait is bounded (a wait that gives up sets the abort flag; the tile warps decide at
+// barriers that OR the flag, so all four leave together; the other roles skip their work).
 // -------------------------------------------------------------------------------------------
 struct FusePlan {
    int G;                         // persistent CTAs
    int FT;                        // features per tile (multiple of 64)
-   int nV, nW;                    // V (1..4) and weight (2..3) ring slots
+   int nV, nW;                    // V (2 or 4) and weight (2..4) ring slots
    int RP, rowsPad, RWR;          // padded rows: floats per row, rows per image, rows per band
    uint32_t bandFloats, sliceFloats;
-   uint32_t offIM, offW[3], offVT[4], offStage, offTop, offBot, offFold;
+   uint32_t offIM, offW[4], offVT[4], offStage, offTop, offBot, offFold;
    uint32_t wStride;              // offW[s+1] - offW[s]; V slots are 32 KB apart
    uint32_t total;
 };
 
+constexpr int kFuseThreads = 736;
+
 template <int S, int P, int C>
-__global__ void __launch_bounds__(608, 1) step_tc_kernel(const __grid_constant__ CUtensorMap tmW, LcaGeom g,
-                                                         FusePlan fp, int mode, int writeA,
-                                                         const float *__restrict__ rin,
-                                                         float *__restrict__ bandsOut,
-                                                         const float *__restrict__ xpad, float *__restrict__ V,
-                                                         bf16 *__restrict__ A, bf16 *__restrict__ Alo,
-                                                         int *__restrict__ err) {
+__global__ void __launch_bounds__(kFuseThreads, 1)
+      step_tc_kernel(const __grid_constant__ CUtensorMap tmW, LcaGeom g, FusePlan fp, int mode, int writeA,
+                     const float *__restrict__ rin, float *__restrict__ bandsOut, const float *__restrict__ xpad,
+                     float *__restrict__ V, bf16 *__restrict__ A, bf16 *__restrict__ Alo, int *__restrict__ err) {
    constexpr int KP = P * P * C, NKC = KP / 64;
    constexpr uint32_t WBYTES = NKC * kPostNT * 128;
-   constexpr int EPI = 256;  // fold threads: epilogue warps 0-7 (named barrier 1)
-   constexpr int EW = 16;    // epilogue warps: per-block update (32 positions x 16 features each),
-                             // band sums and im2col (named barrier 10, all 16)
-   constexpr int IMC = EW * 32;
-   static_assert(P % 4 == 0, "im2col splits the patch rows in four");
-   constexpr int kMaxW = 3;
+   constexpr int EW = 16;                    // epilogue warps: two groups of eight
+   constexpr int GW = EW / 2;                // warps per group
+   constexpr int TW = 16, TT = 128;          // tile warps 16-19 (named barrier 1, 128 threads)
+   constexpr int WW = 20, MW = 21, LW = 22;  // weights, MMA, V / stage loads
+   static_assert(kFuseThreads == 32 * (LW + 1), "one thread per role slot");
+   constexpr int kMaxW = 4, kMaxVF = 4;
    // TMEM columns: two GEMM1 accumulators, D2 (KP), two A tiles of GEMM2 (64 BF16 = 32 columns
-   // each; block q writes tile q % 2 while GEMM2 of block q - 1 reads the other) and, where it
-   // fits, the im2col operand of GEMM1 (KP BF16 = KP / 2 columns) -- the MMAs read both A
-   // operands from TMEM, not shared memory
+   // each) and, where it fits, the im2col operand of GEMM1 (KP BF16 = KP / 2 columns) -- the
+   // MMAs then read both A operands from TMEM, not shared memory
    constexpr int kAccF = 2;
    constexpr uint32_t colD2 = kAccF * kPostNT, colA = colD2 + KP, colIM = colA + 64;
    constexpr bool IMT = colIM + KP / 2 <= 512;
+   static_assert(P % S == 0, "the fold's tap groups tile the patch");
    static_assert((S * C) % 2 == 0, "window reads are 8-byte pairs");
    static_assert(KP % 16 == 0 && KP <= 256, "GEMM2 is one MMA of N = P*P*C");
+   // the fold holds FD patch rows of D2 in registers per round (all S of a tap group, or half)
+   constexpr int FH = S * P * C <= 48 ? 1 : 2, FD = S / FH;
+   static_assert(S % FH == 0, "fold halves");
    extern __shared__ uint8_t smem_raw[];
    uint8_t *smem = align1024(smem_raw);
-   constexpr int kMaxVF = 4;
    __shared__ __align__(8) uint64_t stFull, stEmpty, imFull, imEmpty, wFull[kMaxW], wEmpty[kMaxW], vFull[kMaxVF],
-         vEmpty[kMaxVF], accFull[kAccF], accEmpty[kAccF], aFull[2], aEmpty[2], d2Full, foldFree, drain;
+         vEmpty[kMaxVF], accFull[kAccF], accEmpty[kAccF], aFull[2], aEmpty[2], d2Full, d2Empty, foldFree, drain;
    __shared__ uint32_t tmemBase;
    __shared__ volatile int abortFlag;
 
@@ -889,7 +896,6 @@ __global__ void __launch_bounds__(608, 1) step_tc_kernel(const __grid_constant__
    const int myTiles = blockIdx.x < nTiles ? (nTiles - 1 - blockIdx.x) / fp.G + 1 : 0;
    const int Q = myTiles * nBlk;
    const int nV = fp.nV, nW = fp.nW;
-   const int lagV = nV >= 2 ? nV - 1 : nV;
    const int RWR = fp.RWR, RP = fp.RP, rpb = g.rowsPerBlock;
    const uint32_t bandBytes = fp.bandFloats * 4u, sliceBytes = fp.sliceFloats * 4u;
    auto owned_rows = [&](int mb) { return mb == g.MB - 1 ? RWR : S * rpb; };
@@ -905,19 +911,19 @@ __global__ void __launch_bounds__(608, 1) step_tc_kernel(const __grid_constant__
       }
       for (int i = 0; i < kMaxVF; i++) {
          mbar_init(&vFull[i], 1);
-         mbar_init(&vEmpty[i], EW / 2);  // one arrival per warp pair (the pair's store has read it)
+         mbar_init(&vEmpty[i], GW);  // one arrival per warp of the slot's group (its store has read it)
       }
       for (int i = 0; i < kAccF; i++) {
          mbar_init(&accFull[i], 1);
-         mbar_init(&accEmpty[i], EW);
+         mbar_init(&accEmpty[i], GW);
       }
-      // one full / empty pair per TMEM A tile: the epilogue can be two blocks ahead of GEMM2,
-      // which one barrier's parity could not tell apart
+      // one full / empty pair per TMEM A tile (= per group)
       for (int i = 0; i < 2; i++) {
-         mbar_init(&aFull[i], EW);  // one arrival per epilogue warp
+         mbar_init(&aFull[i], GW);
          mbar_init(&aEmpty[i], 1);
       }
       mbar_init(&d2Full, 1);
+      mbar_init(&d2Empty, TT / 32);  // one arrival per tile warp (its D2 reads are done)
       mbar_init(&foldFree, 1);
       mbar_init(&drain, 1);
       abortFlag = 0;
@@ -947,12 +953,23 @@ __global__ void __launch_bounds__(608, 1) step_tc_kernel(const __grid_constant__
       abortFlag = 1;
       return false;
    };
+   // an event loop's idle policy: after the wait limit with nothing ready, give up (abort flag)
+   auto idle_step = [&](uint32_t &idle, uint64_t &idleSince) {
+      if (abortFlag) return false;
+      if (idle == 0) idleSince = global_ns();
+      if ((++idle & 255) == 0 && global_ns() - idleSince > kWaitNs) {
+         abortFlag = 1;
+         return false;
+      }
+      if (idle > 16) __nanosleep(32);  // leave the issue slots to the epilogue warps on this sub-partition
+      return true;
+   };
    auto last_use = [](int n, int sl, int slots) { return sl < n ? n - 1 - ((n - 1 - sl) % slots) : -1; };
    auto band_in = [&](int b, int mb, int fh) {
       return rin + (((size_t)b * g.MB + mb) * nFH + fh) * fp.bandFloats;
    };
 
-   if (warp == EW) {
+   if (warp == WW) {
       // ============================== weight loads ==============================
       if (lane == 0 && Q > 0) {
          prefetch_tmap(&tmW);
@@ -983,10 +1000,9 @@ __global__ void __launch_bounds__(608, 1) step_tc_kernel(const __grid_constant__
             }
          }
       }
-   } else if (warp == EW + 2) {
+   } else if (warp == LW) {
       // ============================== V and stage loads ==============================
       if (lane == 0 && Q > 0) {
-         int rowsIssued = 0, vIssued = 0;
          auto issue_stage = [&](int ti) {
             int b, mb, fh;
             tile_of(ti, b, mb, fh);
@@ -1009,65 +1025,67 @@ __global__ void __launch_bounds__(608, 1) step_tc_kernel(const __grid_constant__
                   for (int f = 0; f < nFH; f++)
                      bulk_load(smem + fp.offBot + f * sliceBytes, band_in(b, mb + 1, f), sliceBytes, &stFull);
             }
-            rowsIssued = ti + 1;
          };
          bool ok = true;
-         issue_stage(0);
-         // stage t goes out once tile t - 1's im2col has read the stage and tile t - 2's fold
-         // (which runs in the stage after that im2col) has been stored
-         auto stage_free = [&](int t) {
-            return wait_or_abort(&stEmpty, (uint32_t)((t - 1) & 1)) &&
-                   (t < 2 || wait_or_abort(&foldFree, (uint32_t)((t - 2) & 1)));
-         };
+         int stNext = 0, vq = 0;
          int ti = 0, nb = 0, sv = 0, uv = 0, b = 0, mb = 0, fh = 0;
          tile_of(0, b, mb, fh);
-         for (int q = 0; ok && q < Q; q++) {
-            // the next stage before the first V load that waits for the current tile's epilogue
-            while (ok && rowsIssued < myTiles && (rowsIssued - 1) * nBlk + lagV <= q) {
-               ok = stage_free(rowsIssued);
-               if (ok) issue_stage(rowsIssued);
+         uint32_t idle = 0;
+         uint64_t idleSince = 0;
+         while (ok && (stNext < myTiles || vq < Q)) {
+            bool did = false;
+            // stage t once tile t - 1's im2col has read the stage and tile t - 2's fold (which
+            // runs in the stage after that im2col) has been stored
+            if (stNext < myTiles && (stNext == 0 || mbar_test(&stEmpty, (uint32_t)((stNext - 1) & 1))) &&
+                (stNext < 2 || mbar_test(&foldFree, (uint32_t)((stNext - 2) & 1)))) {
+               issue_stage(stNext++);
+               did = true;
             }
-            if (!ok) break;
-            const int f0 = fh * fp.FT + nb * kPostNT;
-            if (uv > 0 && !(ok = wait_or_abort(&vEmpty[sv], (uint32_t)((uv - 1) & 1)))) break;
-            mbar_arrive_expect_tx(&vFull[sv], 32768);
-            bulk_load(smem + fp.offVT[0] + sv * 32768u, V + v_index(g, b, mb * 128, f0), 32768, &vFull[sv]);
-            vIssued = q + 1;
-            if (++sv == nV) {
-               sv = 0;
-               uv++;
+            // V chunk vq once its slot's previous chunk has been stored by its group
+            if (vq < Q && (uv == 0 || mbar_test(&vEmpty[sv], (uint32_t)((uv - 1) & 1)))) {
+               const int f0 = fh * fp.FT + nb * kPostNT;
+               mbar_arrive_expect_tx(&vFull[sv], 32768);
+               bulk_load(smem + fp.offVT[0] + sv * 32768u, V + v_index(g, b, mb * 128, f0), 32768, &vFull[sv]);
+               vq++;
+               if (++sv == nV) {
+                  sv = 0;
+                  uv++;
+               }
+               if (++nb == nBlk) {
+                  nb = 0;
+                  if (++ti < myTiles) tile_of(ti, b, mb, fh);
+               }
+               did = true;
             }
-            if (++nb == nBlk) {
-               nb = 0;
-               if (++ti < myTiles) tile_of(ti, b, mb, fh);
-            }
-         }
-         while (ok && rowsIssued < myTiles) {
-            ok = stage_free(rowsIssued);
-            if (ok) issue_stage(rowsIssued);
+            if (did)
+               idle = 0;
+            else
+               ok = idle_step(idle, idleSince);
          }
          if (!ok) {
-            // the copies still in flight land before shared memory goes away
-            mbar_wait(&stFull, (uint32_t)((rowsIssued - 1) & 1));
+            // the copies still in flight land before shared memory goes away (a stage is issued
+            // only after the one before it has landed and been read)
+            if (stNext > 0) mbar_wait(&stFull, (uint32_t)((stNext - 1) & 1));
             for (int sl = 0; sl < nV; sl++) {
-               const int u = last_use(vIssued, sl, nV);
+               const int u = last_use(vq, sl, nV);
                if (u >= 0) mbar_wait(&vFull[sl], (uint32_t)((u / nV) & 1));
             }
          }
       }
-   } else if (warp == EW + 1) {
+   } else if (warp == MW) {
       // ============================== MMA ==============================
       // An event loop over two in-order streams: GEMM1 of block g1 as soon as its weight tile,
       // its accumulator and (first block of a tile) the im2col operand are ready; GEMM2 of
-      // block g2 < g1 as soon as the epilogue has written its A tile.  GEMM1 of the next block
-      // therefore never waits behind GEMM2 of an earlier one.  Polls never suspend; the loop
-      // ends when nothing has been ready for the wait limit's time (or on the abort flag).
+      // block g2 < g1 as soon as the epilogue has written its A tile (and, first block of a
+      // tile, the fold of the tile before has read D2).  GEMM1 of the next block therefore
+      // never waits behind GEMM2 of an earlier one.  Polls never suspend; the loop ends when
+      // nothing has been ready for the wait limit's time (or on the abort flag).
       if (lane == 0 && Q > 0) {
          const uint32_t idesc1 = idesc_bf16(128, kPostNT), idesc2 = idesc_bf16_bmn(128, KP);
          bool ok = true;
          int issued = 0;
          int g1 = 0, ti1 = 0, nb1 = 0, sw1 = 0, uw1 = 0;
-         int g2 = 0, nb2 = 0, sw2 = 0;
+         int g2 = 0, ti2 = 0, nb2 = 0, sw2 = 0;
          uint32_t idle = 0;
          uint64_t idleSince = 0;
          while (ok && g2 < Q) {
@@ -1104,7 +1122,8 @@ __global__ void __launch_bounds__(608, 1) step_tc_kernel(const __grid_constant__
                   did = true;
                }
             }
-            if (g2 < g1 && mbar_test(&aFull[g2 & 1], (uint32_t)((g2 >> 1) & 1))) {
+            if (g2 < g1 && mbar_test(&aFull[g2 & 1], (uint32_t)((g2 >> 1) & 1)) &&
+                (nb2 != 0 || ti2 == 0 || mbar_test(&d2Empty, (uint32_t)((ti2 - 1) & 1)))) {
                // GEMM2 of block g2: its A tile (TMEM) times its weight tile read MN-major
                tc_fence_after();
                const uint32_t w0 = smem_u32(smem + fp.offW[0] + sw2 * fp.wStride);
@@ -1118,22 +1137,16 @@ __global__ void __launch_bounds__(608, 1) step_tc_kernel(const __grid_constant__
                if (nb2 == nBlk - 1) mma_commit(&d2Full);
                g2++;
                if (++sw2 == nW) sw2 = 0;
-               if (++nb2 == nBlk) nb2 = 0;
+               if (++nb2 == nBlk) {
+                  nb2 = 0;
+                  ti2++;
+               }
                did = true;
             }
-            if (did) {
+            if (did)
                idle = 0;
-            } else if (abortFlag) {
-               ok = false;
-            } else {
-               if (idle == 0) idleSince = global_ns();
-               if ((++idle & 255) == 0 && global_ns() - idleSince > kWaitNs) {
-                  abortFlag = 1;
-                  ok = false;
-               } else if (idle > 16) {
-                  __nanosleep(32);  // leave the issue slots to the epilogue warps on this sub-partition
-               }
-            }
+            else
+               ok = idle_step(idle, idleSince);
          }
          // MMAs still in flight finish before shared memory and TMEM go away
          if (!ok && issued > 0) {
@@ -1141,25 +1154,20 @@ __global__ void __launch_bounds__(608, 1) step_tc_kernel(const __grid_constant__
             mbar_wait(&drain, 0);
          }
       }
-   } else if (warp < EW) {
-      // ============================== epilogue (warps 0-15) ==============================
+   } else if (warp >= TW && warp < TW + TT / 32) {
+      // ============================== tile warps (16-19) ==============================
+      const int tt = tid - TW * 32;  // the position in the tile's 128-position block
+      const int tq = warp & 3;       // TMEM lane quarter (= tt / 32)
       const float *win = reinterpret_cast<const float *>(smem + fp.offStage);
       float *fold = reinterpret_cast<float *>(smem + fp.offFold);
-      // block update: warp = (lane quarter qd, 16-feature group h4 of the 64); the two warps of a
-      // 32-feature half (hh2) share its 32 x 32 part of the V chunk, which the second (sub = 1)
-      // stores once both have written it (named barrier 2 + pair)
-      const int qd = warp & 3, h4 = warp >> 2, hh2 = h4 >> 1, sub = h4 & 1;
-      const int pw = 32 * qd + lane;
-      const int pairBar = 2 + 2 * qd + hh2;
-      const bool lead = warp < 8;  // x prefetch and fold: warps 0-7
-      int pendingV = -1;
+      const int yl = tt / g.v1Nx, xl = tt % g.v1Nx;
+      // the residual window of tile t (summed from the bands in mode 1) and its BF16 im2col
       auto im2col = [&](int t) {
-         if (tid == 0 && wait_or_abort(&stFull, (uint32_t)(t & 1)) && t > 0)
-            wait_or_abort(&imEmpty, (uint32_t)((t - 1) & 1));
-         if (named_bar_or(10, IMC, abortFlag != 0)) return false;
+         if (tt == 0) wait_or_abort(&stFull, (uint32_t)(t & 1));
+         if (named_bar_or(1, TT, abortFlag != 0)) return false;
          if (mode != 0) {
-            // ---- the residual window from the bands (float4 runs: rows are RP floats, RP a
-            // multiple of 4, so row r's run is [r * RP / 4, (r + 1) * RP / 4)) ----
+            // ---- the window from the bands (float4 runs: rows are RP floats, RP a multiple of
+            // 4, so row r's run is [r * RP / 4, (r + 1) * RP / 4)) ----
             int b, mb, fh;
             tile_of(t, b, mb, fh);
             float4 *w4 = reinterpret_cast<float4 *>(smem + fp.offStage);
@@ -1171,7 +1179,7 @@ __global__ void __launch_bounds__(608, 1) step_tc_kernel(const __grid_constant__
             auto add4 = [](float4 a, float4 c) {
                return make_float4(__fadd_rn(a.x, c.x), __fadd_rn(a.y, c.y), __fadd_rn(a.z, c.z), __fadd_rn(a.w, c.w));
             };
-            for (int i = tid; i < nAll; i += IMC) {
+            for (int i = tt; i < nAll; i += TT) {
                float4 v = w4[i];
                for (int f = 1; f < nFH; f++) v = add4(v, w4[f * bandF4 + i]);
                if (i < topEnd) {
@@ -1188,23 +1196,21 @@ __global__ void __launch_bounds__(608, 1) step_tc_kernel(const __grid_constant__
                }
                w4[i] = v;
             }
-            named_bar_sync(10, IMC);
          }
+         // the operand is rewritten once tile t - 1's last GEMM1 has read it
+         if (tt == 0 && t > 0) wait_or_abort(&imEmpty, (uint32_t)((t - 1) & 1));
+         if (named_bar_or(1, TT, abortFlag != 0)) return false;
+         const float *src0 = win + (S * yl) * RP + S * xl * C;
          if constexpr (IMT) {
-            // ---- BF16 im2col of the window into TMEM: lane p, K element k in column k / 2;
-            // thread = (position p, quarter kq of the patch rows) ----
-            constexpr int RUN = P * C;
-            constexpr int COLS = (P / 4) * RUN / 2;  // columns per thread
-            static_assert(RUN % 2 == 0 && COLS % 8 == 0, "im2col columns in groups of 8");
-            tc_fence_after();  // the previous tile's GEMM1s (imEmpty) are done reading
-            const int p = tid & 127, kq = tid >> 7;
-            const int yl = p / g.v1Nx, x1 = p % g.v1Nx;
-            const float *src0 = win + (S * yl) * RP + S * x1 * C + kq * (P / 4) * RP;
-            const uint32_t t0 = tmem + ((uint32_t)((warp & 3) * 32) << 16) + colIM + kq * COLS;
+            // ---- into TMEM: lane tt, K element k in column k / 2 ----
+            constexpr int HALF = P * C / 2, COLS = KP / 2;
+            static_assert((P * C) % 2 == 0 && COLS % 8 == 0, "im2col columns in groups of 8");
+            tc_fence_after();
+            const uint32_t t0 = tmem + ((uint32_t)(tq * 32) << 16) + colIM;
             uint32_t buf[8];
 #pragma unroll
             for (int i = 0; i < COLS; i++) {
-               const int ky = i / (RUN / 2), e = 2 * (i % (RUN / 2));
+               const int ky = i / HALF, e = 2 * (i % HALF);
                const float2 t2 = *reinterpret_cast<const float2 *>(src0 + ky * RP + e);
                buf[i & 7] = pack2(t2.x, t2.y);
                if ((i & 7) == 7) tmem_st8(t0 + (i & ~7), buf);
@@ -1212,15 +1218,12 @@ __global__ void __launch_bounds__(608, 1) step_tc_kernel(const __grid_constant__
             tmem_wait_st();
             tc_fence_before();
          } else {
-            // ---- BF16 im2col of the window (as kernel P) ----
+            // ---- into shared memory, K-major SW128 (as kernel P) ----
             constexpr int RUN = P * C;
             constexpr int CPR = RUN / 8;
             static_assert(RUN % 8 == 0, "patch rows must fill whole 16-byte chunks");
-            const int p = tid & 127, kq = tid >> 7;
-            const int yl = p / g.v1Nx, x1 = p % g.v1Nx;
-            const float *src0 = win + (S * yl) * RP + S * x1 * C;
 #pragma unroll 1
-            for (int ky = kq * (P / 4); ky < (kq + 1) * (P / 4); ky++) {
+            for (int ky = 0; ky < P; ky++) {
                const float2 *src = reinterpret_cast<const float2 *>(src0 + ky * RP);
 #pragma unroll
                for (int cc = 0; cc < CPR; cc++) {
@@ -1232,102 +1235,97 @@ __global__ void __launch_bounds__(608, 1) step_tc_kernel(const __grid_constant__
                      vals[2 * jj + 1] = t2.y;
                   }
                   const int c8 = ky * CPR + cc;
-                  const uint32_t off = (c8 >> 3) * 16384 + sw128_offset(p, (c8 & 7) * 8);
+                  const uint32_t off = (c8 >> 3) * 16384 + sw128_offset(tt, (c8 & 7) * 8);
                   *reinterpret_cast<uint4 *>(smem + fp.offIM + off) =
                         make_uint4(pack2(vals[0], vals[1]), pack2(vals[2], vals[3]), pack2(vals[4], vals[5]),
                                    pack2(vals[6], vals[7]));
                }
             }
          }
+         // on every path: the window sums above are generic-proxy writes into the stage, which
+         // the next stage's bulk copy (async proxy) overwrites once stEmpty is signalled (and
+         // the shared-memory im2col operand is read by the MMAs)
          fence_proxy_async_smem();
-         named_bar_sync(10, IMC);
-         if (tid == 0) {
+         named_bar_sync(1, TT);
+         if (tt == 0) {
             mbar_arrive(&imFull);
             mbar_arrive(&stEmpty);
          }
          return true;
       };
-      // x on the rows the tile's block owns (fh == 0), read from HBM / L2 into registers at
-      // the start of the tile's last block, so that the loads are in flight during its update
-      constexpr int kXPre = 4;  // float4 per thread held in registers; the rest is read at the fold
-      float4 xr[kXPre];
-      auto x_prefetch = [&](int b, int mb, int fh) {
-         const int n4 = fh == 0 ? owned_rows(mb) * RP / 4 : 0;
-         const float4 *src = reinterpret_cast<const float4 *>(xpad + ((size_t)b * fp.rowsPad + (size_t)S * mb * rpb) * RP);
-#pragma unroll
-         for (int k = 0; k < kXPre; k++) {
-            const int i = tid + k * EPI;
-            xr[k] = i < n4 ? __ldg(src + i) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-         }
-      };
-      // the fold of tile t's D2 into its band (in the stage, which the next tile's im2col has
+      // the fold of tile t's D2 into its band (in the stage, which tile t + 1's im2col has
       // read), starting from x on the owned rows and 0 elsewhere, and the band store
-      auto fold_tile = [&](int t, int b, int mb, int fh) {
+      auto fold_tile = [&](int t) {
+         int b, mb, fh;
+         tile_of(t, b, mb, fh);
+         // thread 0 passes this barrier only after the previous fold's band store has read the
+         // stage (bulk_wait_read_all below); a CTA's last two folds follow each other directly
+         named_bar_sync(1, TT);
          {
             const int n4 = (int)fp.bandFloats / 4, x4 = fh == 0 ? owned_rows(mb) * RP / 4 : 0;
             float4 *f4 = reinterpret_cast<float4 *>(fold);
             const float4 *src =
                   reinterpret_cast<const float4 *>(xpad + ((size_t)b * fp.rowsPad + (size_t)S * mb * rpb) * RP);
-#pragma unroll
-            for (int k = 0; k < kXPre; k++) {
-               const int i = tid + k * EPI;
-               if (i < n4) f4[i] = xr[k];
-            }
-            for (int i = tid + kXPre * EPI; i < n4; i += EPI)
-               f4[i] = i < x4 ? __ldg(src + i) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            for (int i = tt; i < n4; i += TT) f4[i] = i < x4 ? __ldg(src + i) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
          }
-         if (tid == 0) wait_or_abort(&d2Full, (uint32_t)(t & 1));
-         if (named_bar_or(1, EPI, abortFlag != 0)) return false;
+         if (tt == 0) wait_or_abort(&d2Full, (uint32_t)(t & 1));
+         if (named_bar_or(1, TT, abortFlag != 0)) return false;
          tc_fence_after();
-         constexpr int DH = S / 2;  // patch rows per half
-         const int p = tid & 127, hh = tid >> 7;
-         const uint32_t lanes = tmemD2 + ((uint32_t)((warp & 3) * 32) << 16);
-         const int y1 = p / g.v1Nx, x1 = p % g.v1Nx;
-         const int yImg0 = S * (mb * rpb + y1) - (P - S) / 2, xImg0 = S * x1 - (P - S) / 2;
+         const uint32_t lanes = tmemD2 + ((uint32_t)(tq * 32) << 16);
+         const int yImg0 = S * (mb * rpb + yl) - (P - S) / 2, xImg0 = S * xl - (P - S) / 2;
 #pragma unroll 1
          for (int ty = 0; ty < P / S; ty++) {
-            float rowv[DH][P * C];
+#pragma unroll 1
+            for (int hf = 0; hf < FH; hf++) {
+               float rowv[FD][P * C];
 #pragma unroll
-            for (int dd = 0; dd < DH; dd++)
-               tmem_ld_cols<P * C>(lanes + (uint32_t)((S * ty + hh * DH + dd) * P * C), rowv[dd]);
-#pragma unroll
-            for (int tx = 0; tx < P / S; tx++) {
-               float old[DH][S][C];
-               bool in[DH][S];
-#pragma unroll
-               for (int dd = 0; dd < DH; dd++) {
-                  const int ky = S * ty + hh * DH + dd;
-                  const int py = yImg0 + ky;
-#pragma unroll
-                  for (int dx = 0; dx < S; dx++) {
-                     const int kx = S * tx + dx;
-                     const int px = xImg0 + kx;
-                     in[dd][dx] = py >= 0 && py < g.inNy && px >= 0 && px < g.inNx;
-                     const int o = (S * y1 + ky) * RP + (S * x1 + kx) * C;
-#pragma unroll
-                     for (int c = 0; c < C; c++) old[dd][dx][c] = in[dd][dx] ? fold[o + c] : 0.0f;
-                  }
+               for (int dd = 0; dd < FD; dd++)
+                  tmem_ld_cols<P * C>(lanes + (uint32_t)((S * ty + hf * FD + dd) * P * C), rowv[dd]);
+               if (ty == P / S - 1 && hf == FH - 1) {  // D2 read: the next tile's first GEMM2 may overwrite it
+                  tc_fence_before();
+                  __syncwarp();
+                  if (lane == 0) mbar_arrive(&d2Empty);
                }
 #pragma unroll
-               for (int dd = 0; dd < DH; dd++) {
-                  const int ky = S * ty + hh * DH + dd;
+               for (int tx = 0; tx < P / S; tx++) {
+                  // the group's pixels of this thread: all loads, then all stores (they are
+                  // distinct, so the adds need not wait on one another)
+                  float old[FD][S][C];
+                  bool in[FD][S];
 #pragma unroll
-                  for (int dx = 0; dx < S; dx++) {
-                     const int kx = S * tx + dx;
-                     const int o = (S * y1 + ky) * RP + (S * x1 + kx) * C;
-                     if (in[dd][dx]) {
+                  for (int dd = 0; dd < FD; dd++) {
+                     const int ky = S * ty + hf * FD + dd;
+                     const int py = yImg0 + ky;
 #pragma unroll
-                        for (int c = 0; c < C; c++) fold[o + c] = __fadd_rn(old[dd][dx][c], -rowv[dd][kx * C + c]);
+                     for (int dx = 0; dx < S; dx++) {
+                        const int kx = S * tx + dx;
+                        const int px = xImg0 + kx;
+                        in[dd][dx] = py >= 0 && py < g.inNy && px >= 0 && px < g.inNx;
+                        const int o = (S * yl + ky) * RP + (S * xl + kx) * C;
+#pragma unroll
+                        for (int c = 0; c < C; c++) old[dd][dx][c] = in[dd][dx] ? fold[o + c] : 0.0f;
                      }
                   }
+#pragma unroll
+                  for (int dd = 0; dd < FD; dd++) {
+                     const int ky = S * ty + hf * FD + dd;
+#pragma unroll
+                     for (int dx = 0; dx < S; dx++) {
+                        const int kx = S * tx + dx;
+                        const int o = (S * yl + ky) * RP + (S * xl + kx) * C;
+                        if (in[dd][dx]) {
+#pragma unroll
+                           for (int c = 0; c < C; c++) fold[o + c] = __fadd_rn(old[dd][dx][c], -rowv[dd][kx * C + c]);
+                        }
+                     }
+                  }
+                  named_bar_sync(1, TT);
                }
-               named_bar_sync(1, EPI);
             }
          }
-         tc_fence_before();  // the D2 reads are complete before the next block's aFull
          fence_proxy_async_smem();
-         named_bar_sync(1, EPI);
-         if (tid == 0) {
+         named_bar_sync(1, TT);
+         if (tt == 0) {
             bulk_store(bandsOut + (((size_t)b * g.MB + mb) * nFH + fh) * fp.bandFloats, fold, bandBytes);
             bulk_commit();
             bulk_wait_read_all();
@@ -1335,131 +1333,126 @@ __global__ void __launch_bounds__(608, 1) step_tc_kernel(const __grid_constant__
          }
          return true;
       };
-      // The next tile's im2col goes in after block kIm, once the loads of the tile's later blocks
-      // are out, and no earlier than block nBlk - 3: it waits for the tile's last GEMM1, and the
-      // MMA thread runs at most two blocks ahead of the epilogue (GEMM1 of block q + 2 issues,
-      // GEMM2 of block q + 1 then waits for this epilogue), so an earlier im2col would wait
-      // for a GEMM1 that waits for it.
-      int kIm = nBlk - 1 - lagV;
-      if (kIm < nBlk - 3) kIm = nBlk - 3;
-      if (kIm < 0) kIm = 0;
-      if (kIm > nBlk - 1) kIm = nBlk - 1;
-      // Every warp runs all Q blocks and passes every named barrier in the same order; a warp
-      // that gave up on a wait (abort flag) skips the work, not the barriers.
+      // im2col(0), then per tile: im2col(t + 1), fold(t).  The four warps take the same
+      // decisions (named_bar_or), so they pass the same barriers and leave together.
+      if (myTiles > 0) {
+         bool ok = im2col(0);
+         for (int t = 0; ok && t < myTiles; t++) {
+            if (t + 1 < myTiles) ok = im2col(t + 1);
+            if (ok) ok = fold_tile(t);
+         }
+      }
+      if (tt == 0) bulk_wait_all();
+   } else if (warp < EW) {
+      // ============================== epilogue (warps 0-15) ==============================
+      const int gi = warp >> 3, qd = warp & 3, hh = (warp >> 2) & 1;
+      const int pw = 32 * qd + lane;
+      // this group's blocks q = gi, gi + 2, ...: the k-th is tile ti, block nb, V slot sv
+      // (q % nV) in its use uv (q / nV); stepped, not divided
+      int ti = 0, nb = gi, sv = gi, uv = 0, b = 0, mb = 0, fh = 0;
+      while (nb >= nBlk) {
+         nb -= nBlk;
+         ti++;
+      }
+      if (ti < myTiles) tile_of(ti, b, mb, fh);
       bool dead = false;
-      if (myTiles > 0) im2col(0);
-      // block q = (tile ti, block nb); V slot sv in its use uv, accumulator a: stepped, not divided
-      int ti = 0, nb = 0, sv = 0, uv = 0, b = 0, mb = 0, fh = 0;
-      if (myTiles > 0) tile_of(0, b, mb, fh);
-      for (int q = 0; q < Q; q++) {
-         const int a = q & (kAccF - 1);
+      for (int q = gi, k = 0; q < Q; q += 2, k++) {
          const int f0 = fh * fp.FT + nb * kPostNT, rowV = b * g.Npos + mb * 128;
-         if (lead && nb == nBlk - 1) x_prefetch(b, mb, fh);
          int okw = !dead;
          if (lane == 0 && okw)
-            okw = wait_or_abort(&accFull[a], (uint32_t)((q / kAccF) & 1)) &&
-                  wait_or_abort(&vFull[sv], (uint32_t)(uv & 1));
+            okw = wait_or_abort(&accFull[gi], (uint32_t)(k & 1)) && wait_or_abort(&vFull[sv], (uint32_t)(uv & 1));
          okw = __shfl_sync(0xffffffffu, okw, 0);
          dead = !okw;
          if (okw) {
             tc_fence_after();
-            float d[16], vo[16];
-            tmem_ld16(tmem + a * kPostNT + ((uint32_t)(32 * qd) << 16) + 16 * h4, d);
+            float d[32];
+            tmem_ld32(tmem + gi * kPostNT + ((uint32_t)(32 * qd) << 16) + 32 * hh, d);
             tc_fence_before();
-            if (lane == 0) mbar_arrive(&accEmpty[a]);
-            uint8_t *vsub = smem + fp.offVT[0] + sv * 32768u + hh2 * 16384 + 32 * qd * 128;
+            if (lane == 0) mbar_arrive(&accEmpty[gi]);
+            uint8_t *vsub = smem + fp.offVT[0] + sv * 32768u + hh * 16384 + 32 * qd * 128;
             uint8_t *vt = vsub + lane * 128;
-#pragma unroll
-            for (int qq = 0; qq < 4; qq++) {
-               const float4 t4 = *reinterpret_cast<const float4 *>(vt + (((4 * sub + qq) ^ (pw & 7)) << 4));
-               vo[4 * qq] = t4.x;
-               vo[4 * qq + 1] = t4.y;
-               vo[4 * qq + 2] = t4.z;
-               vo[4 * qq + 3] = t4.w;
-            }
-            float vn[16], an[16];
             const float om = 1.0f - g.e;
-            if (g.simple) {
+            uint32_t ap[16];
 #pragma unroll
-               for (int jj = 0; jj < 16; jj++) {
-                  const float ao = vo[jj] < g.VThresh ? g.AMin : vo[jj] - g.AShift;
-                  vn[jj] = fmaf(g.e, vo[jj], om * (d[jj] + g.si * ao));
-                  an[jj] = vn[jj] < g.VThresh ? g.AMin : vn[jj] - g.AShift;
+            for (int sub = 0; sub < 2; sub++) {
+               float v[16];
+#pragma unroll
+               for (int qq = 0; qq < 4; qq++) {
+                  const float4 t4 = *reinterpret_cast<const float4 *>(vt + (((4 * sub + qq) ^ (pw & 7)) << 4));
+                  v[4 * qq] = t4.x;
+                  v[4 * qq + 1] = t4.y;
+                  v[4 * qq + 2] = t4.z;
+                  v[4 * qq + 3] = t4.w;
                }
-            } else {
+               float an[16];
+               if (g.simple) {
 #pragma unroll
-               for (int jj = 0; jj < 16; jj++) {
-                  vn[jj] = fmaf(g.e, vo[jj], om * (d[jj] + g.si * thresh(vo[jj], g)));
-                  an[jj] = thresh(vn[jj], g);
+                  for (int jj = 0; jj < 16; jj++) {
+                     const float ao = v[jj] < g.VThresh ? g.AMin : v[jj] - g.AShift;
+                     v[jj] = fmaf(g.e, v[jj], om * (d[16 * sub + jj] + g.si * ao));
+                     an[jj] = v[jj] < g.VThresh ? g.AMin : v[jj] - g.AShift;
+                  }
+               } else {
+#pragma unroll
+                  for (int jj = 0; jj < 16; jj++) {
+                     v[jj] = fmaf(g.e, v[jj], om * (d[16 * sub + jj] + g.si * thresh(v[jj], g)));
+                     an[jj] = thresh(v[jj], g);
+                  }
+               }
+#pragma unroll
+               for (int qq = 0; qq < 4; qq++)
+                  *reinterpret_cast<float4 *>(vt + (((4 * sub + qq) ^ (pw & 7)) << 4)) =
+                        make_float4(v[4 * qq], v[4 * qq + 1], v[4 * qq + 2], v[4 * qq + 3]);
+#pragma unroll
+               for (int j = 0; j < 8; j++) ap[8 * sub + j] = pack2(an[2 * j], an[2 * j + 1]);
+               if (writeA) {  // the activity for the kernels of a later unfused step
+                  const size_t o = (size_t)(rowV + pw) * g.F + f0 + 32 * hh + 16 * sub;
+                  st_global_32B(A + o, make_uint4(ap[8 * sub], ap[8 * sub + 1], ap[8 * sub + 2], ap[8 * sub + 3]),
+                                make_uint4(ap[8 * sub + 4], ap[8 * sub + 5], ap[8 * sub + 6], ap[8 * sub + 7]));
+                  uint4 *lg = reinterpret_cast<uint4 *>(Alo + o);
+#pragma unroll
+                  for (int t = 0; t < 2; t++) {
+                     float l[8];
+#pragma unroll
+                     for (int u = 0; u < 8; u++) l[u] = an[8 * t + u] - __bfloat162float(__float2bfloat16_rn(an[8 * t + u]));
+                     lg[t] = make_uint4(pack2(l[0], l[1]), pack2(l[2], l[3]), pack2(l[4], l[5]), pack2(l[6], l[7]));
+                  }
                }
             }
-            if (sub && lane == 0 && pendingV >= 0) {  // the pair's previous store has read its slot
-               bulk_wait_read_all();
-               mbar_arrive(&vEmpty[pendingV]);
-            }
-#pragma unroll
-            for (int qq = 0; qq < 4; qq++)
-               *reinterpret_cast<float4 *>(vt + (((4 * sub + qq) ^ (pw & 7)) << 4)) =
-                     make_float4(vn[4 * qq], vn[4 * qq + 1], vn[4 * qq + 2], vn[4 * qq + 3]);
-            // A_q into TMEM A tile q % 2 once GEMM2 of block q - 2 has read it: lane pw, features
-            // 16 h4 .. 16 h4 + 15 as 8 columns of BF16 pairs
+            // A into the group's TMEM A tile once GEMM2 of the group's previous block has read
+            // it: lane pw, features 32 hh .. 32 hh + 31 as 16 columns of BF16 pairs
             int oka = 1;
-            if (lane == 0 && q >= 2) oka = wait_or_abort(&aEmpty[q & 1], (uint32_t)(((q >> 1) - 1) & 1));
+            if (lane == 0 && k >= 1) oka = wait_or_abort(&aEmpty[gi], (uint32_t)((k - 1) & 1));
             oka = __shfl_sync(0xffffffffu, oka, 0);
             if (oka) {
                tc_fence_after();
-               uint32_t ap[8];
-#pragma unroll
-               for (int j = 0; j < 8; j++) ap[j] = pack2(an[2 * j], an[2 * j + 1]);
-               tmem_st8(tmem + ((uint32_t)(32 * qd) << 16) + colA + 32 * (q & 1) + 8 * h4, ap);
+               const uint32_t ta = tmem + ((uint32_t)(32 * qd) << 16) + colA + 32 * gi + 16 * hh;
+               tmem_st8(ta, ap);
+               tmem_st8(ta + 8, ap + 8);
                tmem_wait_st();
                tc_fence_before();
             }
-            if (writeA) {  // the activity for the kernels of a later unfused step
-               bf16 *ag = A + (size_t)(rowV + pw) * g.F + f0 + 16 * h4;
-               uint4 *lg = reinterpret_cast<uint4 *>(Alo + (size_t)(rowV + pw) * g.F + f0 + 16 * h4);
-               st_global_32B(ag,
-                             make_uint4(pack2(an[0], an[1]), pack2(an[2], an[3]), pack2(an[4], an[5]),
-                                        pack2(an[6], an[7])),
-                             make_uint4(pack2(an[8], an[9]), pack2(an[10], an[11]), pack2(an[12], an[13]),
-                                        pack2(an[14], an[15])));
-#pragma unroll
-               for (int t = 0; t < 2; t++) {
-                  float l[8];
-#pragma unroll
-                  for (int u = 0; u < 8; u++) l[u] = an[8 * t + u] - __bfloat162float(__float2bfloat16_rn(an[8 * t + u]));
-                  lg[t] = make_uint4(pack2(l[0], l[1]), pack2(l[2], l[3]), pack2(l[4], l[5]), pack2(l[6], l[7]));
-               }
-            }
             fence_proxy_async_smem();
             __syncwarp();
-            if (lane == 0 && oka) mbar_arrive(&aFull[q & 1]);
+            if (lane == 0 && oka) {
+               mbar_arrive(&aFull[gi]);
+               // this warp's 32 x 32 part of the V chunk back to HBM; the slot is free once the
+               // store has read it
+               bulk_store(V + v_index(g, b, mb * 128 + 32 * qd, f0 + 32 * hh), vsub, 4096);
+               bulk_commit();
+               bulk_wait_read_all();
+               mbar_arrive(&vEmpty[sv]);
+            }
             dead = !oka;
          }
-         // both halves of the pair's 32 x 32 part are written; every warp passes this barrier
-         // on every block (a warp that gave up on a wait skips only the work), so that no warp
-         // waits here for a partner that has left
-         named_bar_sync(pairBar, 64);
-         if (!dead) {
-            if (sub && lane == 0) {
-               uint8_t *vsub = smem + fp.offVT[0] + sv * 32768u + hh2 * 16384 + 32 * qd * 128;
-               bulk_store(V + v_index(g, b, mb * 128 + 32 * qd, f0 + 32 * hh2), vsub, 4096);
-               bulk_commit();
-               if (nV == 1) {
-                  bulk_wait_read_all();
-                  mbar_arrive(&vEmpty[sv]);
-               }
-            }
-            pendingV = nV == 1 ? -1 : sv;
-         }
-         if (nb == kIm && ti + 1 < myTiles) im2col(ti + 1);
-         if (lead && nb == nBlk - 1) fold_tile(ti, b, mb, fh);
-         if (++sv == nV) {
-            sv = 0;
+         sv += 2;
+         if (sv >= nV) {
+            sv = gi;
             uv++;
          }
-         if (++nb == nBlk) {
-            nb = 0;
+         nb += 2;
+         while (nb >= nBlk) {
+            nb -= nBlk;
             if (++ti < myTiles) tile_of(ti, b, mb, fh);
          }
       }
@@ -1756,15 +1749,16 @@ ReconPlan make_recon_plan(const LcaGeom &g, int S, int P, int C, bool x3, int ma
    return rp;
 }
 
-// Shared-memory layout of kernel F for a feature tile FT and nV V slots; total = 0 when the
-// geometry does not allow it (FT not a multiple of 64 dividing F, or bands reaching past the
+// Shared-memory layout of kernel F for a feature tile FT, nV V slots and nW weight slots;
+// total = 0 when the geometry does not allow it (FT not a multiple of 64 dividing F, an odd V
+// ring -- each epilogue group owns every other slot --, or bands reaching past the
 // neighbouring blocks).
 FusePlan fuse_plan_for(const LcaGeom &g, int S, int P, int C, int numSms, int FT, int nV, int nW) {
    const int KP = P * P * C, NKC = KP / 64, E = (P - S) / 2;
    auto al = [](uint32_t v) { return (v + 1023u) & ~1023u; };
    FusePlan fp;
    std::memset(&fp, 0, sizeof(fp));
-   if (FT < 64 || FT % 64 || g.F % FT || nV < 1 || nV > 4 || nW < 2 || nW > 3 ||
+   if (FT < 64 || FT % 64 || g.F % FT || (nV != 2 && nV != 4) || nW < 2 || nW > 4 ||
        P - S > S * g.rowsPerBlock || g.MB < 1)
       return fp;
    const int nFH = g.F / FT;
@@ -1784,7 +1778,7 @@ FusePlan fuse_plan_for(const LcaGeom &g, int S, int P, int C, int numSms, int FT
    fp.offIM = o;
    if (!imTmem) o = al(o + NKC * 16384);
    fp.wStride = al(wB);
-   for (int sl = 0; sl < 3; sl++) {
+   for (int sl = 0; sl < 4; sl++) {
       fp.offW[sl] = o;
       if (sl < nW) o = al(o + wB);
    }
@@ -1807,13 +1801,13 @@ FusePlan fuse_plan_for(const LcaGeom &g, int S, int P, int C, int numSms, int FT
 }
 
 // The default: 256-feature tiles (or the largest multiple of 64 dividing F), the deepest V ring
-// that fits with two weight slots.
+// (4 or 2 slots) that fits with two weight slots.
 FusePlan make_fuse_plan(const LcaGeom &g, int S, int P, int C, int numSms) {
    FusePlan fp;
    std::memset(&fp, 0, sizeof(fp));
    for (int FT = std::min(256, g.F); FT >= 64; FT -= 64) {
       if (g.F % FT || FT % 64) continue;
-      for (int nV = 4; nV >= 1; nV--) {
+      for (int nV = 4; nV >= 2; nV -= 2) {
          fp = fuse_plan_for(g, S, P, C, numSms, FT, nV, 2);
          if (fp.total && fp.total <= kSmemBudget) return fp;
       }
@@ -1951,7 +1945,7 @@ struct Launcher {
    static pvgpu_status launch_F(const StepArgs &a, int mode, int writeA, const float *rin, float *bout,
                                 cudaStream_t st, bool programmatic) {
       cudaLaunchAttribute attr[1];
-      cudaLaunchConfig_t c = config(a.fp.G, a.fp.total, st, programmatic, attr, 608);
+      cudaLaunchConfig_t c = config(a.fp.G, a.fp.total, st, programmatic, attr, kFuseThreads);
       cudaError_t e = cudaLaunchKernelEx(&c, step_tc_kernel<S, P, C>, *a.tmW, a.g, a.fp, mode, writeA, rin, bout,
                                          (const float *)a.xpad, a.V, a.A, a.Alo, a.err);
       return e == cudaSuccess ? PVGPU_OK : pvgpu::record_cuda_error(e, "lca fused step");
@@ -2521,8 +2515,8 @@ extern "C" pvgpu_status pvgpu_lca_solver_autotune(pvgpu_lca_solver *s, const flo
       s->sched.fused = 1;
       double bestMs = 1e30;
       for (int FT = 64; FT <= 512 && FT <= s->g.F; FT += 64) {
-         for (int nV = 1; nV <= 4; nV++) {
-            for (int nW = 2; nW <= 3; nW++) {
+         for (int nV = 2; nV <= 4; nV += 2) {
+            for (int nW = 2; nW <= 4; nW++) {
                FusePlan fp = fuse_plan_for(s->g, s->S, s->P, s->C, g_num_sms, FT, nV, nW);
                if (!fp.total || fp.total > kSmemBudget) continue;
                if ((size_t)s->g.nb * s->g.MB * (s->g.F / FT) * fp.bandFloats > s->bandsPerBuf) continue;

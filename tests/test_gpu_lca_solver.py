@@ -338,8 +338,8 @@ def test_lca_fused_plan_shapes(torch, oracle):
     s.set_schedule(fused=True)
     per_tile = {}
     for ft in (64, 128):
-        for nv in (1, 2, 3):
-            for nw in (2, 3):
+        for nv in (2, 4):
+            for nw in (2, 3, 4):
                 try:
                     s.set_fused_plan(ft, nv, nw)
                 except capi.PvgpuError:
@@ -354,14 +354,17 @@ def test_lca_fused_plan_shapes(torch, oracle):
     assert set(per_tile) == {64, 128}
     with pytest.raises(capi.PvgpuError):
         s.set_fused_plan(96, 2, 2)  # not a multiple of 64
+    for nv, nw in ((1, 2), (3, 2), (2, 5)):  # odd V rings (the two epilogue groups own every other slot)
+        with pytest.raises(capi.PvgpuError):
+            s.set_fused_plan(64, nv, nw)
 
 
 def test_lca_config3_geometry_every_fused_shape(torch, oracle):
     """The batched configuration's geometry -- 32x32x3 inputs (1/f spectrum, unit std) -> V1
     16x16x512 at stride 2, 512 features of 8x8x3, VThresh = AShift = 0.15 -- on 4 images for 100
     timesteps with the last 12 in BF16x3.  Every fused-kernel shape the solver accepts (feature
-    tiles 64..512, among them the 512-feature tile with 3 V and 3 weight slots the autotuner
-    picks for the full batch) against the two-kernel form: V within 1e-3 of max|V|; the final
+    tiles 64..512, V rings of 2 and 4 slots, weight rings of 2 to 4, among them the 512-feature
+    tile with 4 V and 3 weight slots) against the two-kernel form: V within 1e-3 of max|V|; the final
     energy within 1e-3 relative of the FP64 oracle for each, and for the autotuner's own pick;
     no bounded device wait gives up."""
     from openpv_gb300 import capi
@@ -395,8 +398,8 @@ def test_lca_config3_geometry_every_fused_shape(torch, oracle):
     s.set_schedule(fused=True)
     accepted = []
     for ft in (64, 128, 256, 512):
-        for nv in (1, 2, 3):
-            for nw in (2, 3):
+        for nv in (2, 4):
+            for nw in (2, 3, 4):
                 try:
                     s.set_fused_plan(ft, nv, nw)
                 except capi.PvgpuError:
@@ -405,7 +408,7 @@ def test_lca_config3_geometry_every_fused_shape(torch, oracle):
                 accepted.append((ft, nv, nw))
                 assert np.abs(v - ref).max() <= 1e-3 * np.abs(ref).max(), (ft, nv, nw)
                 assert rel < 1e-3, (ft, nv, nw, rel)
-    assert (512, 3, 3) in accepted, accepted
+    assert (512, 4, 3) in accepted and (512, 2, 4) in accepted, accepted
     s.autotune(xd, trial_steps=2)
     _, rel = solve()
     assert rel < 1e-3, (rel, s.fused_plan_info(), s.schedule())
