@@ -886,7 +886,8 @@ __global__ void __launch_bounds__(kFuseThreads, 1)
    extern __shared__ uint8_t smem_raw[];
    uint8_t *smem = align1024(smem_raw);
    __shared__ __align__(8) uint64_t stFull, stEmpty, imFull, imEmpty, wFull[kMaxW], wEmpty[kMaxW], vFull[kMaxVF],
-         vEmpty[kMaxVF], accFull[kAccF], accEmpty[kAccF], aFull[2], aEmpty[2], d2Full, d2Empty, foldFree, drain;
+         vEmpty[kMaxVF], accFull[kAccF], accEmpty[kAccF], aFull[2], aEmpty[2], d2Full, d2Empty, foldFree, xFull,
+         drain;
    __shared__ uint32_t tmemBase;
    __shared__ volatile int abortFlag;
 
@@ -925,6 +926,7 @@ __global__ void __launch_bounds__(kFuseThreads, 1)
       mbar_init(&d2Full, 1);
       mbar_init(&d2Empty, TT / 32);  // one arrival per tile warp (its D2 reads are done)
       mbar_init(&foldFree, 1);
+      mbar_init(&xFull, 1);
       mbar_init(&drain, 1);
       abortFlag = 0;
       fence_mbar_init();
@@ -1254,25 +1256,41 @@ __global__ void __launch_bounds__(kFuseThreads, 1)
          return true;
       };
       // the fold of tile t's D2 into its band (in the stage, which tile t + 1's im2col has
-      // read), starting from x on the owned rows and 0 elsewhere, and the band store
+      // read), starting from x on the owned rows (a bulk copy) and 0 elsewhere, and the band store
+      int xUses = 0;         // bulk copies of x waited for (thread 0): xFull's phase
+      bool xPending = false;  // one issued and not yet waited for
       auto fold_tile = [&](int t) {
          int b, mb, fh;
          tile_of(t, b, mb, fh);
          // thread 0 passes this barrier only after the previous fold's band store has read the
          // stage (bulk_wait_read_all below); a CTA's last two folds follow each other directly
          named_bar_sync(1, TT);
-         {
-            const int n4 = (int)fp.bandFloats / 4, x4 = fh == 0 ? owned_rows(mb) * RP / 4 : 0;
-            float4 *f4 = reinterpret_cast<float4 *>(fold);
-            const float4 *src =
-                  reinterpret_cast<const float4 *>(xpad + ((size_t)b * fp.rowsPad + (size_t)S * mb * rpb) * RP);
-            for (int i = tt; i < n4; i += TT) f4[i] = i < x4 ? __ldg(src + i) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+         const int xRows = fh == 0 ? owned_rows(mb) : 0;
+         if (tt == 0 && xRows > 0) {
+            const uint32_t xb = (uint32_t)(xRows * RP * 4);
+            mbar_arrive_expect_tx(&xFull, xb);
+            bulk_load(fold, xpad + ((size_t)b * fp.rowsPad + (size_t)S * mb * rpb) * RP, xb, &xFull);
+            xPending = true;
          }
-         if (tt == 0) wait_or_abort(&d2Full, (uint32_t)(t & 1));
+         {
+            const int n4 = (int)fp.bandFloats / 4;
+            float4 *f4 = reinterpret_cast<float4 *>(fold);
+            for (int i = xRows * RP / 4 + tt; i < n4; i += TT) f4[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+         }
+         if (tt == 0) {
+            if (xPending && wait_or_abort(&xFull, (uint32_t)(xUses & 1))) {
+               xUses++;
+               xPending = false;
+            }
+            wait_or_abort(&d2Full, (uint32_t)(t & 1));
+         }
          if (named_bar_or(1, TT, abortFlag != 0)) return false;
          tc_fence_after();
          const uint32_t lanes = tmemD2 + ((uint32_t)(tq * 32) << 16);
          const int yImg0 = S * (mb * rpb + yl) - (P - S) / 2, xImg0 = S * xl - (P - S) / 2;
+         constexpr int SEG = S * C, SEG2 = SEG / 2;  // floats of one patch row in one tap group
+         // P/S x P/S tap groups (ty, tx), one barrier each; within a group no two threads touch
+         // one pixel, and every pixel sees its taps in the order of the groups
 #pragma unroll 1
          for (int ty = 0; ty < P / S; ty++) {
 #pragma unroll 1
@@ -1288,34 +1306,36 @@ __global__ void __launch_bounds__(kFuseThreads, 1)
                }
 #pragma unroll
                for (int tx = 0; tx < P / S; tx++) {
-                  // the group's pixels of this thread: all loads, then all stores (they are
-                  // distinct, so the adds need not wait on one another)
-                  float old[FD][S][C];
-                  bool in[FD][S];
+                  // the group's pixels of this thread, S*C contiguous floats per patch row, read
+                  // and written as pairs (they are distinct, so the adds need not wait on one
+                  // another); pixels outside the image keep their value
+                  float2 old[FD][SEG2];
+                  bool rowIn[FD];
 #pragma unroll
                   for (int dd = 0; dd < FD; dd++) {
                      const int ky = S * ty + hf * FD + dd;
                      const int py = yImg0 + ky;
+                     rowIn[dd] = py >= 0 && py < g.inNy;
+                     const float2 *o2 =
+                           reinterpret_cast<const float2 *>(fold + (S * yl + ky) * RP + (S * xl + S * tx) * C);
 #pragma unroll
-                     for (int dx = 0; dx < S; dx++) {
-                        const int kx = S * tx + dx;
-                        const int px = xImg0 + kx;
-                        in[dd][dx] = py >= 0 && py < g.inNy && px >= 0 && px < g.inNx;
-                        const int o = (S * yl + ky) * RP + (S * xl + kx) * C;
-#pragma unroll
-                        for (int c = 0; c < C; c++) old[dd][dx][c] = in[dd][dx] ? fold[o + c] : 0.0f;
-                     }
+                     for (int j = 0; j < SEG2; j++) old[dd][j] = rowIn[dd] ? o2[j] : make_float2(0.0f, 0.0f);
                   }
 #pragma unroll
                   for (int dd = 0; dd < FD; dd++) {
                      const int ky = S * ty + hf * FD + dd;
+                     if (rowIn[dd]) {
+                        float2 *o2 = reinterpret_cast<float2 *>(fold + (S * yl + ky) * RP + (S * xl + S * tx) * C);
 #pragma unroll
-                     for (int dx = 0; dx < S; dx++) {
-                        const int kx = S * tx + dx;
-                        const int o = (S * yl + ky) * RP + (S * xl + kx) * C;
-                        if (in[dd][dx]) {
+                        for (int j = 0; j < SEG2; j++) {
+                           float e2[2] = {old[dd][j].x, old[dd][j].y};
 #pragma unroll
-                           for (int c = 0; c < C; c++) fold[o + c] = __fadd_rn(old[dd][dx][c], -rowv[dd][kx * C + c]);
+                           for (int h = 0; h < 2; h++) {
+                              const int e = 2 * j + h, dx = e / C;
+                              const int px = xImg0 + S * tx + dx;
+                              if (px >= 0 && px < g.inNx) e2[h] = __fadd_rn(e2[h], -rowv[dd][S * tx * C + e]);
+                           }
+                           o2[j] = make_float2(e2[0], e2[1]);
                         }
                      }
                   }
@@ -1342,7 +1362,11 @@ __global__ void __launch_bounds__(kFuseThreads, 1)
             if (ok) ok = fold_tile(t);
          }
       }
-      if (tt == 0) bulk_wait_all();
+      if (tt == 0) {
+         bulk_wait_all();
+         // an x copy still in flight (a wait that gave up) lands before shared memory goes away
+         if (xPending) mbar_wait(&xFull, (uint32_t)(xUses & 1));
+      }
    } else if (warp < EW) {
       // ============================== epilogue (warps 0-15) ==============================
       const int gi = warp >> 3, qd = warp & 3, hh = (warp >> 2) & 1;
@@ -1356,8 +1380,20 @@ __global__ void __launch_bounds__(kFuseThreads, 1)
       }
       if (ti < myTiles) tile_of(ti, b, mb, fh);
       bool dead = false;
+      // with four V slots a slot is next loaded two of this group's blocks later, so its release
+      // waits for the top of the group's next block (the store has long read it by then); with
+      // two it is the group's next block's slot and goes back as soon as the store has read it
+      int pendingV = -1;
+      auto release_v = [&](int slot) {
+         if (lane == 0) {
+            bulk_wait_read_all();
+            mbar_arrive(&vEmpty[slot]);
+         }
+      };
       for (int q = gi, k = 0; q < Q; q += 2, k++) {
          const int f0 = fh * fp.FT + nb * kPostNT, rowV = b * g.Npos + mb * 128;
+         if (pendingV >= 0) release_v(pendingV);
+         pendingV = -1;
          int okw = !dead;
          if (lane == 0 && okw)
             okw = wait_or_abort(&accFull[gi], (uint32_t)(k & 1)) && wait_or_abort(&vFull[sv], (uint32_t)(uv & 1));
@@ -1440,8 +1476,12 @@ __global__ void __launch_bounds__(kFuseThreads, 1)
                // store has read it
                bulk_store(V + v_index(g, b, mb * 128 + 32 * qd, f0 + 32 * hh), vsub, 4096);
                bulk_commit();
-               bulk_wait_read_all();
-               mbar_arrive(&vEmpty[sv]);
+            }
+            if (oka) {
+               if (nV == 2)
+                  release_v(sv);
+               else
+                  pendingV = sv;
             }
             dead = !oka;
          }
@@ -1456,6 +1496,7 @@ __global__ void __launch_bounds__(kFuseThreads, 1)
             if (++ti < myTiles) tile_of(ti, b, mb, fh);
          }
       }
+      if (pendingV >= 0) release_v(pendingV);
       if (lane == 0) bulk_wait_all();
    }
    __syncthreads();
@@ -2387,7 +2428,6 @@ extern "C" pvgpu_status pvgpu_lca_solver_energy(pvgpu_lca_solver *s, const float
 extern "C" pvgpu_status pvgpu_lca_solver_state(pvgpu_lca_solver *s, float *v, float *a, void *stream) {
    if (!s) return PVGPU_ERR_BAD_ARG;
    cudaStream_t st = pvgpu::as_stream(stream);
-   size_t n = (size_t)s->g.nb * s->g.Npos * s->g.F;
    if (v) {
       v_layout_kernel<<<152 * 8, 256, 0, st>>>(s->g, s->V, v, 0);
       PVGPU_CHECK_LAUNCH("lca state");
