@@ -858,9 +858,12 @@ struct FusePlan {
 
 constexpr int kFuseThreads = 736;
 
-template <int S, int P, int C>
+// SIMPLE: the threshold is the plain shift (g.simple); WRITEA: the launch also writes A and its
+// low half for the kernels of a later unfused step.  Compile-time, so that each instance holds
+// only the epilogue code it runs (the roles' code competes for the instruction cache).
+template <int S, int P, int C, bool SIMPLE, bool WRITEA>
 __global__ void __launch_bounds__(kFuseThreads, 1)
-      step_tc_kernel(const __grid_constant__ CUtensorMap tmW, LcaGeom g, FusePlan fp, int mode, int writeA,
+      step_tc_kernel(const __grid_constant__ CUtensorMap tmW, LcaGeom g, FusePlan fp, int mode,
                      const float *__restrict__ rin, float *__restrict__ bandsOut, const float *__restrict__ xpad,
                      float *__restrict__ V, bf16 *__restrict__ A, bf16 *__restrict__ Alo, int *__restrict__ err) {
    constexpr int KP = P * P * C, NKC = KP / 64;
@@ -1421,7 +1424,7 @@ __global__ void __launch_bounds__(kFuseThreads, 1)
                   v[4 * qq + 3] = t4.w;
                }
                float an[16];
-               if (g.simple) {
+               if constexpr (SIMPLE) {
 #pragma unroll
                   for (int jj = 0; jj < 16; jj++) {
                      const float ao = v[jj] < g.VThresh ? g.AMin : v[jj] - g.AShift;
@@ -1441,7 +1444,7 @@ __global__ void __launch_bounds__(kFuseThreads, 1)
                         make_float4(v[4 * qq], v[4 * qq + 1], v[4 * qq + 2], v[4 * qq + 3]);
 #pragma unroll
                for (int j = 0; j < 8; j++) ap[8 * sub + j] = pack2(an[2 * j], an[2 * j + 1]);
-               if (writeA) {  // the activity for the kernels of a later unfused step
+               if constexpr (WRITEA) {  // the activity for the kernels of a later unfused step
                   const size_t o = (size_t)(rowV + pw) * g.F + f0 + 32 * hh + 16 * sub;
                   st_global_32B(A + o, make_uint4(ap[8 * sub], ap[8 * sub + 1], ap[8 * sub + 2], ap[8 * sub + 3]),
                                 make_uint4(ap[8 * sub + 4], ap[8 * sub + 5], ap[8 * sub + 6], ap[8 * sub + 7]));
@@ -1935,12 +1938,15 @@ template <int S, int P, int C>
 struct Launcher {
    // shared-memory limits of both kernels (once, at create: not inside a stream capture)
    static pvgpu_status set_attrs(const pvgpu_lca_solver *) {
-      const void *fns[5] = {reinterpret_cast<const void *>(recon_tc_kernel<S, P, C, false>),
+      const void *fns[8] = {reinterpret_cast<const void *>(recon_tc_kernel<S, P, C, false>),
                             reinterpret_cast<const void *>(recon_tc_kernel<S, P, C, true>),
                             reinterpret_cast<const void *>(post_tc_kernel<S, P, C, false>),
                             reinterpret_cast<const void *>(post_tc_kernel<S, P, C, true>),
-                            reinterpret_cast<const void *>(step_tc_kernel<S, P, C>)};
-      for (int i = 0; i < 5; i++) {
+                            reinterpret_cast<const void *>(step_tc_kernel<S, P, C, false, false>),
+                            reinterpret_cast<const void *>(step_tc_kernel<S, P, C, false, true>),
+                            reinterpret_cast<const void *>(step_tc_kernel<S, P, C, true, false>),
+                            reinterpret_cast<const void *>(step_tc_kernel<S, P, C, true, true>)};
+      for (int i = 0; i < 8; i++) {
          cudaError_t e = cudaFuncSetAttribute(fns[i], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBudget);
          if (e != cudaSuccess) return pvgpu::record_cuda_error(e, "lca kernel attributes");
       }
@@ -1987,8 +1993,10 @@ struct Launcher {
                                 cudaStream_t st, bool programmatic) {
       cudaLaunchAttribute attr[1];
       cudaLaunchConfig_t c = config(a.fp.G, a.fp.total, st, programmatic, attr, kFuseThreads);
-      cudaError_t e = cudaLaunchKernelEx(&c, step_tc_kernel<S, P, C>, *a.tmW, a.g, a.fp, mode, writeA, rin, bout,
-                                         (const float *)a.xpad, a.V, a.A, a.Alo, a.err);
+      auto fn = a.g.simple ? (writeA ? step_tc_kernel<S, P, C, true, true> : step_tc_kernel<S, P, C, true, false>)
+                           : (writeA ? step_tc_kernel<S, P, C, false, true> : step_tc_kernel<S, P, C, false, false>);
+      cudaError_t e = cudaLaunchKernelEx(&c, fn, *a.tmW, a.g, a.fp, mode, rin, bout, (const float *)a.xpad, a.V, a.A,
+                                         a.Alo, a.err);
       return e == cudaSuccess ? PVGPU_OK : pvgpu::record_cuda_error(e, "lca fused step");
    }
    // recon CTAs that can be resident at once (one CTA per SM)
