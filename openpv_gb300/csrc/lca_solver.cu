@@ -1554,10 +1554,25 @@ __global__ void __launch_bounds__(256) energy_kernel(LcaGeom g, int C, const flo
       }
    }
    const double tw = cp0 + cp1, maxc = 0.5 * tw, qc = 0.5 / tw;
-   const float *vb = V + (size_t)b * g.Npos * g.F;
-   for (int i = threadIdx.x; i < g.Npos * g.F; i += 256) {
-      double a = fabs((double)thresh(vb[i], g));
-      cost += costKind == 1 ? a : (a < tw ? a * (1.0 - qc * a) : maxc);
+   // V in 8-element runs (two float4; an image's V is a whole number of 64-feature chunks);
+   // the L1 cost sums each run in FP32 (eight nonnegative terms) before the FP64 total
+   const float4 *v4 = reinterpret_cast<const float4 *>(V + (size_t)b * g.Npos * g.F);
+   const int n8 = g.Npos * g.F / 8;
+   for (int i = threadIdx.x; i < n8; i += 256) {
+      const float4 p = v4[2 * i], q = v4[2 * i + 1];
+      const float e8[8] = {p.x, p.y, p.z, p.w, q.x, q.y, q.z, q.w};
+      if (costKind == 1) {
+         float s8 = 0.0f;
+#pragma unroll
+         for (int k = 0; k < 8; k++) s8 += fabsf(thresh(e8[k], g));
+         cost += (double)s8;
+      } else {
+#pragma unroll
+         for (int k = 0; k < 8; k++) {
+            const double a = fabs((double)thresh(e8[k], g));
+            cost += a < tw ? a * (1.0 - qc * a) : maxc;
+         }
+      }
    }
    __shared__ double s1[256], s2[256];
    s1[threadIdx.x] = l2;
@@ -1606,14 +1621,30 @@ __device__ __forceinline__ size_t v_of(const LcaGeom &g, size_t i) {
    return v_index(g, (int)(bp / g.Npos), (int)(bp % g.Npos), f);
 }
 
+// eight features per thread: two float4 of V (each four features contiguous in its layout),
+// 16-byte stores of A and its low half, two of the FP32 activity
 __global__ void init_activity_kernel(LcaGeom g, const float *__restrict__ V, bf16 *A, bf16 *Alo, float *A32) {
-   size_t n = (size_t)g.nb * g.Npos * g.F;
-   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-      float a = thresh(V[v_of(g, i)], g);
-      bf16 h = __float2bfloat16_rn(a);
-      A[i] = h;
-      Alo[i] = __float2bfloat16_rn(a - __bfloat162float(h));
-      A32[i] = a;
+   const size_t n8 = (size_t)g.nb * g.Npos * g.F / 8;
+   for (size_t i8 = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i8 < n8; i8 += (size_t)gridDim.x * blockDim.x) {
+      const size_t i = i8 * 8;
+      const size_t bp = i / g.F;
+      const int f = (int)(i % g.F);
+      const int b = (int)(bp / g.Npos), pos = (int)(bp % g.Npos);
+      const float4 p = *reinterpret_cast<const float4 *>(V + v_index(g, b, pos, f));
+      const float4 q = *reinterpret_cast<const float4 *>(V + v_index(g, b, pos, f + 4));
+      const float v8[8] = {p.x, p.y, p.z, p.w, q.x, q.y, q.z, q.w};
+      float a[8], l[8];
+#pragma unroll
+      for (int k = 0; k < 8; k++) {
+         a[k] = thresh(v8[k], g);
+         l[k] = a[k] - __bfloat162float(__float2bfloat16_rn(a[k]));
+      }
+      *reinterpret_cast<uint4 *>(A + i) =
+            make_uint4(pack2(a[0], a[1]), pack2(a[2], a[3]), pack2(a[4], a[5]), pack2(a[6], a[7]));
+      *reinterpret_cast<uint4 *>(Alo + i) =
+            make_uint4(pack2(l[0], l[1]), pack2(l[2], l[3]), pack2(l[4], l[5]), pack2(l[6], l[7]));
+      *reinterpret_cast<float4 *>(A32 + i) = make_float4(a[0], a[1], a[2], a[3]);
+      *reinterpret_cast<float4 *>(A32 + i + 4) = make_float4(a[4], a[5], a[6], a[7]);
    }
 }
 
