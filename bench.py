@@ -408,6 +408,7 @@ def delivery_bench(torch, capi, reps=5):
                        "best_ms": min(ms, tms), "best": "sparse" if ms <= tms else "tensor-core",
                        "sparse_vs_tc_max_rel_diff": rel}
     capi.deliver_tc_check_error()
+    out["cpu_baseline"] = delivery_cpu_baseline(w)
     # postsynaptic perspective, dense activity (p = 0.2 from above), post weights on the device
     wpost = torch.zeros_like(w)
     capi.transpose_weights(conn, w, wpost)
@@ -416,6 +417,59 @@ def delivery_bench(torch, capi, reps=5):
     out["post"] = {"fp32_ms": fp32_ms, "tc_ms": tc_ms, "fp32_TFLOP_s": dense_flops / fp32_ms / 1e9,
                    "tc_TFLOP_s": dense_flops / tc_ms / 1e9, "speedup_tc_over_fp32": fp32_ms / tc_ms,
                    "tc_tf32_products_per_term": 3}
+    return out
+
+
+def delivery_cpu_baseline(w):
+    """The reference's CPU deliveries for the delivery workload, as the oracle's ports of
+    PresynapticPerspectiveConvolveDelivery (SparseList branch) and
+    PostsynapticPerspectiveConvolveDelivery (each pinned bit for bit to the reference's own code
+    compiled from its tree): one image per thread, on one core and on all host cores.  Bounded
+    samples: the presynaptic delivery of one full image at p = 0.01 (the timed density) per
+    thread; the postsynaptic delivery of a 32x32 crop of the same connection per thread, scaled
+    to a 128x128 image by the output count (its cost per output does not depend on the size)."""
+    import concurrent.futures as cf
+    from oracle import oracle as O
+    cores = os.cpu_count() or 1
+    wn = w.detach().cpu().numpy().reshape(256, 7, 7, 64)
+    pre1 = O.Loc.make(1, 128, 128, 256, 3)
+    post1 = O.Loc.make(1, 128, 128, 64, 0)
+    rng = np.random.default_rng(1234 + 2)
+    core = (rng.random((128, 128, 256)) < 0.01) * (1.0 - rng.random((128, 128, 256)))
+    a1 = np.zeros(pre1.ext_shape(), np.float32)
+    a1[0, 3:131, 3:131, :] = core
+    ent, num = O.compact(a1)
+
+    def pre_one(_):
+        t0 = time.perf_counter()
+        O.deliver_pre(pre1, post1, 7, 7, wn, entries=ent, num_active=num)
+        return time.perf_counter() - t0
+
+    # 32x32 crop for the postsynaptic loop (dense activity, p = 0.2 as in the GPU figure)
+    preC = O.Loc.make(1, 32, 32, 256, 3)
+    postC = O.Loc.make(1, 32, 32, 64, 0)
+    aC = np.zeros(preC.ext_shape(), np.float32)
+    aC[0, 3:35, 3:35, :] = (rng.random((32, 32, 256)) < 0.2) * (1.0 - rng.random((32, 32, 256)))
+    w_post = O.transpose_shared(preC, postC, 7, 7, wn)
+
+    def post_one(_):
+        t0 = time.perf_counter()
+        O.deliver_post(preC, postC, 7, 7, w_post, aC)
+        return time.perf_counter() - t0
+
+    out = {}
+    for name, fn, scale in (("pre_sparse_p0.01", pre_one, 1.0), ("post_dense", post_one, 16.0)):
+        t1 = fn(0)  # one core, one image (post: 16 crops = one 128x128 image)
+        with cf.ThreadPoolExecutor(cores) as ex:
+            t0 = time.perf_counter()
+            list(ex.map(fn, range(cores)))
+            tall = time.perf_counter() - t0
+        ms_batch_1 = 16 * scale * t1 * 1e3               # 16 images on one core
+        ms_batch_all = 16 * scale * tall / cores * 1e3   # 16 images spread over all cores
+        out[name] = {"ms_per_16_image_batch_1_core": ms_batch_1,
+                     "ms_per_16_image_batch_all_cores": ms_batch_all, "cores": cores, "kind": "port",
+                     "sample": ("one 128x128x256 image at p = 0.01 per thread" if scale == 1.0 else
+                                "a 32x32 crop per thread, scaled by 16 to a 128x128 image")}
     return out
 
 
