@@ -89,7 +89,7 @@ pvgpu_status pvgpu_selftest_wait_expiry(uint64_t limitNs, long long *hostOut2, v
  * runs on the host after a device->host copy.  Stable: entries of each batch element are in
  * ascending extended index, value = the exact activity float; numActive[b] (long in the
  * reference) receives the count.  entries has capacity numExt per batch element.
- * One pass over the activity (chunks of 8192 values; a decoupled look-back carries the chunk
+ * One pass over the activity (chunks of 16384 values; a decoupled look-back carries the chunk
  * prefixes).  Scratch: `scratch` (device, 8-byte aligned, >= pvgpu_compact_scratch_bytes) holds
  * a ticket word and one status word per chunk; the call clears it on the stream first.
  * entries must be 8-byte aligned.  numActive[b] = -1 reports a look-back that gave up waiting
@@ -111,7 +111,7 @@ pvgpu_status pvgpu_compact_active(
  * hosts whose device memory all belongs to their own pool allocator.  The ticket and chunk
  * statuses live in a fixed 1 MiB array inside the library's device image (loaded once per
  * device, kept until the process exits), which limits a call to
- * nbatch * ceil(numExt / 8192) <= 131071; larger calls return PVGPU_ERR_BAD_ARG with a message
+ * nbatch * ceil(numExt / 16384) <= 131071; larger calls return PVGPU_ERR_BAD_ARG with a message
  * in pvgpu_last_error().  Each call clears the part of the array it uses (cudaMemsetAsync on the
  * stream) before its kernel reads it.  The first call on a device looks up the array's device
  * address (cudaGetSymbolAddress, with that device current) and caches it per device ordinal for

@@ -1,7 +1,7 @@
 // compact.cu -- a1: stable active-index compaction (DataStore::updateActiveIndices,
 // columns/DataStore.cpp:46-66) on the device, in one pass over the activity.
 //
-// Each batch element's extended activity is cut into chunks of kChunk = 8192 floats (32 KB).
+// Each batch element's extended activity is cut into chunks of kChunk = 16384 floats (64 KB).
 // Entries must come out in ascending extended index.  Per chunk:
 //   * every thread holds a fixed set of units of the chunk (float4s, or single floats when the
 //     images are not 16-byte aligned) at unit index k * threads + t, so a warp's units of one k
@@ -21,8 +21,8 @@
 // always ends.  Its spin is bounded in time all the same; a chunk that gives up publishes an
 // error status that propagates down the image's chain and makes the image's count -1.
 //
-// One CTA per chunk: 128 threads with float4 units (images 16-byte aligned), else 512 threads
-// with scalar units; every load of the chunk is issued before any is used.  (Tried and not
+// One CTA per chunk of 512 threads, float4 units (images 16-byte aligned) or scalar units;
+// every load of the chunk is issued before any is used.  (Tried and not
 // kept: a persistent kernel streaming chunks through a shared-memory ring -- its consumers
 // take their chunks in order, so a chunk's total is published late and look-backs convoy
 // across CTAs, 0.21 ms against 0.10 ms on 16 x 134x134x256 values; a dedicated look-back warp
@@ -41,7 +41,7 @@ namespace {
 using pvgpu::tc::global_ns;
 using pvgpu::tc::kWaitNs;
 
-constexpr int kChunk = 8192;
+constexpr int kChunk = 16384;
 constexpr uint64_t kFlagAgg = 1ull << 62, kFlagPre = 2ull << 62, kFlagErr = 3ull << 62;
 
 __device__ __forceinline__ void st_release(uint64_t *p, uint64_t v) {
@@ -156,20 +156,21 @@ __device__ __forceinline__ uint32_t look_back(uint64_t *st, int c, uint32_t tota
 }
 
 // ---- one CTA per chunk -------------------------------------------------------------------------
-// VEC = 4: float4 units (images 16-byte aligned), 128 threads x 16 units: small CTAs, five per
-// SM, so that while one CTA is in its serial phases (look-back, writes) the others keep their
-// loads in flight (with 512-thread CTAs, ncu showed the warps mostly parked at the barrier
-// behind the look-back and DRAM at 29 % of peak).  VEC = 1: scalar units, 512 threads x 16
-// units.  Every load of the chunk is issued before any is used.
+// 512 threads, two CTAs per SM: 64 KB of a chunk's float4 loads in flight per CTA (8 per
+// thread), the look-back once per 64 KB.  Measured on 16 x 131x131x256 values at p = 0.01 / 0.2:
+// 8192-value chunks on 128-thread CTAs (five per SM) 0.103 / 0.124 ms, on 256-thread CTAs
+// 0.110 / 0.129, 4096-value chunks 0.137 / 0.157, 16384-value chunks on 256 threads 0.095 /
+// 0.118 (register spills) or 0.100 / 0.119 (two per SM), 32768 on 512 threads 0.100 / 0.118,
+// this shape 0.095 / 0.113.  VEC = 1: scalar units, 512 threads x 32 units, one CTA per SM.
 template <int VEC>
 struct Shape {
-   static constexpr int kThreads = VEC == 4 ? 128 : 512;
+   static constexpr int kThreads = 512;
    static constexpr int kWarps = kThreads / 32;
-   static constexpr int KU = kChunk / (kThreads * VEC);  // units per thread (16)
+   static constexpr int KU = kChunk / (kThreads * VEC);  // units per thread (8 float4 or 32 floats)
 };
 
 template <int VEC>
-__global__ void __launch_bounds__(Shape<VEC>::kThreads, VEC == 4 ? 5 : 3)
+__global__ void __launch_bounds__(Shape<VEC>::kThreads, VEC == 4 ? 2 : 1)
       compact_kernel(const float *__restrict__ a, int64_t numExt, int nbatch, int nchunks,
                      uint64_t *__restrict__ scratch, pvgpu_entry *__restrict__ entries,
                      int64_t *__restrict__ numActive) {
@@ -329,7 +330,7 @@ extern "C" pvgpu_status pvgpu_compact_active(const float *aExt, int nbatch, int6
 // latency-critical loops that cannot afford the implicit device synchronisation that
 // cudaMalloc / cudaFree may cause, and hosts whose device memory is entirely owned by their own
 // pool allocator.  For them the ticket and the chunk statuses live in a fixed array in this
-// library's device image: kNoAllocWords 8-byte words, i.e. nbatch * ceil(numExt / 8192) <=
+// library's device image: kNoAllocWords 8-byte words, i.e. nbatch * ceil(numExt / 16384) <=
 // 131071 chunks (up to about 2^30 activity values per call).  The array is loaded with the
 // library, once per device, and held until the process exits.
 // ---------------------------------------------------------------------------------------------
@@ -374,7 +375,7 @@ extern "C" pvgpu_status pvgpu_compact_active_noalloc(const float *aExt, int nbat
    if (st != PVGPU_OK) return st;
    if ((int64_t)nbatch * chunks_of(numExt) > kNoAllocMaxChunks)
       return pvgpu::record_message(PVGPU_ERR_BAD_ARG,
-                                   "compact_active_noalloc: nbatch * ceil(numExt / 8192) exceeds the fixed scratch "
+                                   "compact_active_noalloc: nbatch * ceil(numExt / 16384) exceeds the fixed scratch "
                                    "of 131071 chunk statuses; use pvgpu_compact_active with caller scratch");
    uint64_t *scratch = nullptr;
    st = noalloc_scratch(&scratch);

@@ -48,14 +48,15 @@ def sparse_activity(rng, loc, p, zero_halo=True):
 
 # ---- a1: compaction --------------------------------------------------------------------
 
-# Sizes: float4 units (n % 4 == 0) and scalar units, one chunk of 8192 and long look-back
-# chains (the delivery microbenchmark's 16 x 134x134x256 extended activity: 562 chunks per
+# Sizes: float4 units (n % 4 == 0) and scalar units, one chunk of 16384 and long look-back
+# chains (the delivery microbenchmark's 16 x 134x134x256 extended activity: 281 chunks per
 # image), empty and full activity.  `offset` starts the activity one float past an aligned
 # address, which forces scalar units on an aligned size.
 @pytest.mark.parametrize("nb,n,p,offset", [(3, 25600, 0.05, 0), (2, 4097, 0.5, 0), (1, 4096, 1.0, 0),
                                            (4, 777, 0.0, 0), (2, 204800, 0.02, 0), (1, 1, 1.0, 0),
                                            (16, 134 * 134 * 256, 0.01, 0), (5, 1000003, 0.3, 0),
-                                           (3, 25600, 0.05, 1), (2, 8192 * 3, 1.0, 1)])
+                                           (3, 25600, 0.05, 1), (2, 8192 * 3, 1.0, 1), (2, 16384 * 3, 1.0, 0),
+                                           (2, 16384 * 3 + 5, 0.4, 1)])
 def test_compaction_bitexact(cuda, oracle, nb, n, p, offset):
     torch = cuda
     from openpv_gb300 import capi

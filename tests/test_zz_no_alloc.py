@@ -45,7 +45,7 @@ def test_noalloc_compaction_equals_scratch_version(torch, nb, n, p_seq):
 
 def test_noalloc_rejects_sizes_beyond_its_fixed_scratch(torch):
     from openpv_gb300 import capi
-    nb, n = 65, 4096 * 4096  # 65 * 2048 chunks of 8192 values > 131071
+    nb, n = 129, 4096 * 4096  # 129 * 1024 chunks of 16384 values > 131071
     a = torch.zeros(1, device="cuda")
     e = torch.zeros(1, device="cuda")
     num = torch.zeros(nb, dtype=torch.int64, device="cuda")
