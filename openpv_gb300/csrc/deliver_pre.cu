@@ -234,6 +234,24 @@ struct VecF<4> {
    }
 };
 
+// acc[q] += a * w[q] for the lane's FPL features: pairs of features by the packed FP32 FMA (one
+// instruction, each element rounded once, as fmaf), a single feature by fmaf
+template <int FPL>
+__device__ __forceinline__ void fma_row(float *acc, float a, const float *w) {
+   if constexpr (FPL % 2 == 0) {
+      const float2 a2 = make_float2(a, a);
+#pragma unroll
+      for (int q = 0; q < FPL; q += 2) {
+         const float2 r = __ffma2_rn(a2, make_float2(w[q], w[q + 1]), make_float2(acc[q], acc[q + 1]));
+         acc[q] = r.x;
+         acc[q + 1] = r.y;
+      }
+   } else {
+#pragma unroll
+      for (int q = 0; q < FPL; q++) acc[q] = fmaf(a, w[q], acc[q]);
+   }
+}
+
 // More than 16 accumulators per lane (NYP x FPL) do not fit the 64 registers of four CTAs per SM
 // next to the entry pipeline; those instantiations take two CTAs per SM (128 registers) instead.
 template <int FPL, int NYP, bool SPARSE>
@@ -338,12 +356,8 @@ __global__ void __launch_bounds__(kWarps * 32, (FPL * NYP > 16) ? 2 : 4) deliver
 #pragma unroll
                for (int ky = 0; ky < NYP; ky++) {
                   if (ky >= kyMin && ky <= kyMax) {
-#pragma unroll
-                     for (int q = 0; q < FPL; q++) acc[ky][q] = fmaf(a1, w1[ky][q], acc[ky][q]);
-                     if (two) {
-#pragma unroll
-                        for (int q = 0; q < FPL; q++) acc[ky][q] = fmaf(a2, w2[ky][q], acc[ky][q]);
-                     }
+                     fma_row<FPL>(acc[ky], a1, w1[ky]);
+                     if (two) fma_row<FPL>(acc[ky], a2, w2[ky]);
                   }
                }
             }
