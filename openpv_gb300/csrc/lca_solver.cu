@@ -1425,11 +1425,19 @@ __global__ void __launch_bounds__(kFuseThreads, 1)
                }
                float an[16];
                if constexpr (SIMPLE) {
+                  // element pairs on the packed FP32 pipe: t = d + si*ao, t = om*t, v = e*v + t
+                  const float2 si2 = make_float2(g.si, g.si), om2 = make_float2(om, om), e2 = make_float2(g.e, g.e);
 #pragma unroll
-                  for (int jj = 0; jj < 16; jj++) {
-                     const float ao = v[jj] < g.VThresh ? g.AMin : v[jj] - g.AShift;
-                     v[jj] = fmaf(g.e, v[jj], om * (d[16 * sub + jj] + g.si * ao));
+                  for (int jj = 0; jj < 16; jj += 2) {
+                     const float ao0 = v[jj] < g.VThresh ? g.AMin : v[jj] - g.AShift;
+                     const float ao1 = v[jj + 1] < g.VThresh ? g.AMin : v[jj + 1] - g.AShift;
+                     float2 t = __ffma2_rn(si2, make_float2(ao0, ao1), make_float2(d[16 * sub + jj], d[16 * sub + jj + 1]));
+                     t = __fmul2_rn(om2, t);
+                     const float2 vn = __ffma2_rn(e2, make_float2(v[jj], v[jj + 1]), t);
+                     v[jj] = vn.x;
+                     v[jj + 1] = vn.y;
                      an[jj] = v[jj] < g.VThresh ? g.AMin : v[jj] - g.AShift;
+                     an[jj + 1] = v[jj + 1] < g.VThresh ? g.AMin : v[jj + 1] - g.AShift;
                   }
                } else {
 #pragma unroll
