@@ -422,7 +422,9 @@ __device__ __forceinline__ uint32_t pack2(float lo, float hi) {
    return *reinterpret_cast<uint32_t *>(&h);
 }
 
-template <int S, int P, int C, bool X3>
+// SIMPLE: the threshold is the plain shift (g.simple), compile-time so that the instance holds
+// only the update code it runs
+template <int S, int P, int C, bool X3, bool SIMPLE>
 __global__ void __launch_bounds__(320, 1) post_tc_kernel(const __grid_constant__ CUtensorMap tmW,
                                                          const __grid_constant__ CUtensorMap tmWlo,
                                                          const __grid_constant__ CUtensorMap tmAst, LcaGeom g,
@@ -712,12 +714,20 @@ __global__ void __launch_bounds__(320, 1) post_tc_kernel(const __grid_constant__
             }
             float vn[32], an[32];
             const float om = 1.0f - g.e;
-            if (g.simple) {  // AMax = +inf, VWidth = 0: A = V < VThresh ? AMin : V - AShift
+            if constexpr (SIMPLE) {  // AMax = +inf, VWidth = 0: A = V < VThresh ? AMin : V - AShift
+               // element pairs on the packed FP32 pipe: t = d + si*ao, t = om*t, v = e*v + t
+               const float2 si2 = make_float2(g.si, g.si), om2 = make_float2(om, om), e2 = make_float2(g.e, g.e);
 #pragma unroll
-               for (int jj = 0; jj < 32; jj++) {
-                  const float ao = vo[jj] < g.VThresh ? g.AMin : vo[jj] - g.AShift;
-                  vn[jj] = fmaf(g.e, vo[jj], om * (d[jj] + g.si * ao));
+               for (int jj = 0; jj < 32; jj += 2) {
+                  const float ao0 = vo[jj] < g.VThresh ? g.AMin : vo[jj] - g.AShift;
+                  const float ao1 = vo[jj + 1] < g.VThresh ? g.AMin : vo[jj + 1] - g.AShift;
+                  float2 t = __ffma2_rn(si2, make_float2(ao0, ao1), make_float2(d[jj], d[jj + 1]));
+                  t = __fmul2_rn(om2, t);
+                  const float2 v2 = __ffma2_rn(e2, make_float2(vo[jj], vo[jj + 1]), t);
+                  vn[jj] = v2.x;
+                  vn[jj + 1] = v2.y;
                   an[jj] = vn[jj] < g.VThresh ? g.AMin : vn[jj] - g.AShift;
+                  an[jj + 1] = vn[jj + 1] < g.VThresh ? g.AMin : vn[jj + 1] - g.AShift;
                }
             } else {
 #pragma unroll
@@ -1977,15 +1987,17 @@ template <int S, int P, int C>
 struct Launcher {
    // shared-memory limits of both kernels (once, at create: not inside a stream capture)
    static pvgpu_status set_attrs(const pvgpu_lca_solver *) {
-      const void *fns[8] = {reinterpret_cast<const void *>(recon_tc_kernel<S, P, C, false>),
+      const void *fns[10] = {reinterpret_cast<const void *>(recon_tc_kernel<S, P, C, false>),
                             reinterpret_cast<const void *>(recon_tc_kernel<S, P, C, true>),
-                            reinterpret_cast<const void *>(post_tc_kernel<S, P, C, false>),
-                            reinterpret_cast<const void *>(post_tc_kernel<S, P, C, true>),
+                            reinterpret_cast<const void *>(post_tc_kernel<S, P, C, false, false>),
+                            reinterpret_cast<const void *>(post_tc_kernel<S, P, C, true, false>),
+                            reinterpret_cast<const void *>(post_tc_kernel<S, P, C, false, true>),
+                            reinterpret_cast<const void *>(post_tc_kernel<S, P, C, true, true>),
                             reinterpret_cast<const void *>(step_tc_kernel<S, P, C, false, false>),
                             reinterpret_cast<const void *>(step_tc_kernel<S, P, C, false, true>),
                             reinterpret_cast<const void *>(step_tc_kernel<S, P, C, true, false>),
                             reinterpret_cast<const void *>(step_tc_kernel<S, P, C, true, true>)};
-      for (int i = 0; i < 8; i++) {
+      for (int i = 0; i < 10; i++) {
          cudaError_t e = cudaFuncSetAttribute(fns[i], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBudget);
          if (e != cudaSuccess) return pvgpu::record_cuda_error(e, "lca kernel attributes");
       }
@@ -2021,10 +2033,10 @@ struct Launcher {
    static pvgpu_status launch_P(const StepArgs &a, bool x3, cudaStream_t st, bool programmatic) {
       cudaLaunchAttribute attr[1];
       cudaLaunchConfig_t c = config(a.pl.G, a.pl.total, st, programmatic, attr);
-      cudaError_t e = x3 ? cudaLaunchKernelEx(&c, post_tc_kernel<S, P, C, true>, *a.tmW, *a.tmWlo, *a.tmAst, a.g,
-                                              a.pl, (const float *)a.rpad, a.V, a.A, a.Alo, a.err)
-                         : cudaLaunchKernelEx(&c, post_tc_kernel<S, P, C, false>, *a.tmW, *a.tmWlo, *a.tmAst, a.g,
-                                              a.pl, (const float *)a.rpad, a.V, a.A, a.Alo, a.err);
+      auto fn = x3 ? (a.g.simple ? post_tc_kernel<S, P, C, true, true> : post_tc_kernel<S, P, C, true, false>)
+                   : (a.g.simple ? post_tc_kernel<S, P, C, false, true> : post_tc_kernel<S, P, C, false, false>);
+      cudaError_t e = cudaLaunchKernelEx(&c, fn, *a.tmW, *a.tmWlo, *a.tmAst, a.g, a.pl, (const float *)a.rpad, a.V,
+                                         a.A, a.Alo, a.err);
       return e == cudaSuccess ? PVGPU_OK : pvgpu::record_cuda_error(e, "lca post");
    }
    // kernel F: a whole timestep; mode 0 reads kernel R's residual, mode 1 the bands in rin
