@@ -299,6 +299,62 @@ def taus_next(st):
     return st
 
 
+def taus_draws(count, seed, n):
+    """n successive outputs (s0) of count generators seeded seed, seed + 1, ...
+    (columns/Random.cpp:90-106 randomUInt): [n][count] uint32."""
+    st = taus_init(count, seed)
+    out = np.zeros((n, count), np.uint32)
+    for i in range(n):
+        st = taus_next(st)
+        out[i] = st["s0"]
+    return out
+
+
+def uniform_random_v(nx, ny, nf, vmin, vmax, seed):
+    """UniformRandomV::calcV (initv/UniformRandomV.cpp:44-60) for one batch element of a
+    layer on one process: one generator per (x, y) position, seeded seed + y*nx + x
+    (columns/Random.cpp:40-85 with nf = 1, restricted), drawn once per feature in feature order;
+    each value min + u * (max - min) with u = s0 / (float)UINT_MAX (columns/Random.hpp:37-39,
+    Random.cpp:100-103), every operation rounded to float.  Returns V [ny][nx][nf]."""
+    d = taus_draws(nx * ny, seed, nf)                     # [f][xy]
+    u = d.astype(np.float32) / np.float32(4294967295.0)   # (float)s0 / (float)UINT_MAX
+    lo, hi = np.float32(vmin), np.float32(vmax)
+    v = (lo + (u * np.float32(hi - lo)).astype(np.float32)).astype(np.float32)
+    return np.ascontiguousarray(v.T.reshape(ny, nx, nf))
+
+
+def uniform_random_weights(num_patches, patch_size, wmin, wmax, sparse_fraction, seed):
+    """InitUniformRandomWeights::randomWeights (weightinit/InitUniformRandomWeights.cpp:63-106)
+    for shared weights with minNNZ = 0: one generator per data patch, seeded seed + patch
+    (InitRandomWeights::initRNGs, weightinit/InitRandomWeights.cpp:39-50); per weight, in patch
+    order, one draw for the value wMin + (float)(p * draw) with p = (wMax - wMin) / 2^32 in
+    double, then one draw that zeroes it when below sparseFraction * 2^32 (a float).
+    Returns [num_patches][patch_size] float32."""
+    d = taus_draws(num_patches, seed, 2 * patch_size)     # [draw][patch]
+    p = (float(np.float32(wmax)) - float(np.float32(wmin))) / (1.0 + 4294967295.0)
+    cut = float(np.float32(np.float32(sparse_fraction) * np.float32(4294967296.0)))
+    w = np.zeros((num_patches, patch_size), np.float32)
+    for n in range(patch_size):
+        val = (np.float32(wmin) + (p * d[2 * n].astype(np.float64)).astype(np.float32)).astype(np.float32)
+        w[:, n] = np.where(d[2 * n + 1].astype(np.float64) < cut, np.float32(0.0), val)
+    return w
+
+
+def normalize_l2(w, strength=1.0):
+    """NormalizeL2::normalizeWeights (normalizers/NormalizeL2.cpp:53-155) for one connection,
+    one arbor, normalizeFromPostPerspective off, no rMin / cutoff / non-negativity: per data
+    patch the float sum of squares in patch order (NormalizeBase.cpp:184-193), l2 = sqrtf(sum),
+    every weight multiplied by strength / l2 (NormalizeMultiply.cpp:251-254).
+    w: [num_patches][...]; returns a normalised copy."""
+    shp = w.shape
+    w = np.ascontiguousarray(w, np.float32).reshape(shp[0], -1).copy()
+    s = np.zeros(shp[0], np.float32)
+    for k in range(w.shape[1]):
+        s = (s + (w[:, k] * w[:, k]).astype(np.float32)).astype(np.float32)
+    mult = (np.float32(strength) / np.sqrt(s)).astype(np.float32)
+    return (w * mult[:, None]).astype(np.float32).reshape(shp)
+
+
 def lif_update(method, loc, params, dt, state, gsyn_head, a_ext):
     """One LIF step (LIFActivityComponent.cpp:332-942).  state: dict of rnd, V, Vth, GE, GI, GIB
     (updated copies returned); gsyn_head: [3][nbatch*nx*ny*nf] EXC, INH, INHB; returns
