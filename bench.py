@@ -654,15 +654,18 @@ def lif_bench(torch, capi, steps=1000, cpu_sample=True):
            "exc_lif_update_GB_s": exc_n * 88 / (t_lif / k) / 1e6}
     if cpu_sample:
         out["cpu_oracle"] = lif_cpu_sample()
+        t = max(1, min(nb, os.cpu_count() or 1))
+        out["cpu_baseline"] = lif_cpu_sample(steps=6, images=nb, threads=t)
     return out
 
 
-def lif_cpu_sample(steps=6):
-    """The same network for one image on one host core through the oracle (its LIF update and
-    presynaptic delivery, pinned to the reference's own loops): a bounded sample of timesteps."""
+def lif_cpu_sample(steps=6, images=1, threads=1):
+    """The same network through the oracle (its LIF update and presynaptic delivery, pinned to the
+    reference's own loops): a bounded sample of `steps` timesteps for each of `images` images,
+    one image per host thread."""
+    from multiprocessing.pool import ThreadPool
     from oracle import oracle as O
     O.build()
-    rng = np.random.default_rng(1234 + 5)
     n, ne, ni = 256, 32, 8
     inp, exc, inh = O.Loc.make(1, n, n, 1, 5, 5), O.Loc.make(1, n, n, ne, 2, 2), O.Loc.make(1, n // 2, n // 2, ni, 2, 2)
     exc_r, inh_r = O.Loc.make(1, n, n, ne, 0, 0), O.Loc.make(1, n // 2, n // 2, ni, 0, 0)
@@ -680,24 +683,35 @@ def lif_cpu_sample(steps=6):
         return {"rnd": O.taus_init(m, seed), "V": np.full(m, -70.0, np.float32), "Vth": np.full(m, -55.0, np.float32),
                 "GE": np.zeros(m, np.float32), "GI": np.zeros(m, np.float32), "GIB": np.zeros(m, np.float32)}
 
-    se, sh = state(exc, 17), state(inh, 18)
-    ae, ah = np.zeros(exc.ext_shape(), np.float32), np.zeros(inh.ext_shape(), np.float32)
-    rates = rng.uniform(5, 50, (1, n, n, 1))
+    def run_image(i):
+        rng = np.random.default_rng(1234 + 5 + i)
+        se, sh = state(exc, 17 + 2 * i), state(inh, 18 + 2 * i)
+        ae, ah = np.zeros(exc.ext_shape(), np.float32), np.zeros(inh.ext_shape(), np.float32)
+        rates = rng.uniform(5, 50, (1, n, n, 1))
+        for _ in range(steps):
+            x = np.zeros(inp.ext_shape(), np.float32)
+            x[:, 5:5 + n, 5:5 + n, :] = (rng.random((1, n, n, 1)) < rates * 1e-3).astype(np.float32)
+            e, c = O.compact(x.reshape(1, -1))
+            eh, ch = O.compact(ah.reshape(1, -1))
+            g0 = O.deliver_pre(inp, exc_r, 11, 11, w_ie, entries=e, num_active=c)
+            g1 = O.deliver_pre(inh, exc_r, 8, 8, w_he, entries=eh, num_active=ch)
+            se, ae = O.lif_update("a", exc, prm, 1.0, se, np.stack([g0.reshape(-1), g1.reshape(-1), 0 * g0.reshape(-1)]),
+                                  ae)
+            ee, ce = O.compact(ae.reshape(1, -1))
+            gi = O.deliver_pre(exc, inh_r, 3, 3, w_ei, entries=ee, num_active=ce).reshape(-1)
+            sh, ah = O.lif_update("a", inh, prm, 1.0, sh, np.stack([gi, 0 * gi, 0 * gi]), ah)
+
     t0 = time.perf_counter()
-    for _ in range(steps):
-        x = np.zeros(inp.ext_shape(), np.float32)
-        x[:, 5:5 + n, 5:5 + n, :] = (rng.random((1, n, n, 1)) < rates * 1e-3).astype(np.float32)
-        e, c = O.compact(x.reshape(1, -1))
-        eh, ch = O.compact(ah.reshape(1, -1))
-        g0 = O.deliver_pre(inp, exc_r, 11, 11, w_ie, entries=e, num_active=c)
-        g1 = O.deliver_pre(inh, exc_r, 8, 8, w_he, entries=eh, num_active=ch)
-        se, ae = O.lif_update("a", exc, prm, 1.0, se, np.stack([g0.reshape(-1), g1.reshape(-1), 0 * g0.reshape(-1)]), ae)
-        ee, ce = O.compact(ae.reshape(1, -1))
-        gi = O.deliver_pre(exc, inh_r, 3, 3, w_ei, entries=ee, num_active=ce).reshape(-1)
-        sh, ah = O.lif_update("a", inh, prm, 1.0, sh, np.stack([gi, 0 * gi, 0 * gi]), ah)
+    if threads > 1:
+        with ThreadPool(threads) as pool:
+            pool.map(run_image, range(images))
+    else:
+        for i in range(images):
+            run_image(i)
     dt = time.perf_counter() - t0
-    return {"value": steps / dt, "unit": "image-steps/s", "cores": 1, "kind": "port",
-            "sample": f"oracle, the whole network for 1 image x {steps} timesteps ({dt:.2f} s)"}
+    return {"value": images * steps / dt, "unit": "image-steps/s", "cores": threads, "kind": "port",
+            "sample": f"oracle, the whole network for {images} image(s) x {steps} timesteps, one image per thread on "
+                      f"{threads} host thread(s) ({dt:.2f} s)"}
 
 
 # ---------------------------------------------------------------------------------------------
