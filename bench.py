@@ -927,6 +927,8 @@ def run_ours(args, rank, world, local_rank):
         "unit": "images*steps/s",
         "final_energy_rel_err_vs_fp64": rel_bf16,
         "speedup_bf16_over_fp32_form": value / world / value32,
+        # against an FP32 form running at its FMA ceiling (the same FLOPs at fp32_fma_ceiling_tflops)
+        "speedup_bf16_over_fp32_fma_ceiling": value / world / (fp32_peak_tflops * 1e12 / flop_unit),
         "fp32_form": {"value": value32, "unit": "images*steps/s", "final_energy_rel_err_vs_fp64": rel_fp32,
                       "TFLOP_s": fp32_tflops, "fp32_fma_ceiling_tflops": fp32_peak_tflops,
                       "frac_of_fp32_fma_ceiling": fp32_tflops / fp32_peak_tflops},
