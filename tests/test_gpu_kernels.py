@@ -96,6 +96,9 @@ PRE_CASES = [
     ((2, 20, 36, 6, 4), (20, 36, 64, 0), 5, 9),     # unequal patch axes
     ((1, 30, 40, 1, 5), (30, 40, 32, 0), 11, 11),   # 11x11 (Gauss2D-style LIF input), 32 features
     ((2, 20, 36, 4, 6), (20, 36, 64, 0), 13, 13),   # tallest patch of the row-sliding kernel
+    # the reference's GPU system tests (tests/GPUSystemTest/input), their layer sizes:
+    ((1, 32, 32, 3, 1), (64, 64, 3, 0), 6, 6),      # preTest.params: TransposeConn of a 3x3 many-to-one, one-to-many x2
+    ((4, 32, 32, 3, 8), (16, 16, 64, 0), 9, 9),     # preRecvBatch.params: batch 4, many-to-one x2, 9x9
 ]
 
 
@@ -193,6 +196,12 @@ POST_CASES = [
     ((1, 24, 24, 16, 3), (24, 24, 8, 0), 7, 7),     # one-to-one
     ((2, 8, 8, 6, 2), (16, 16, 4, 1), 4, 4),        # one-to-many x2 (kernel phases)
     ((1, 64, 64, 1, 6), (16, 16, 32, 2), 4, 4),     # stride-4 dictionary, 16x16 receptive field
+    # the reference's GPU system tests (tests/GPUSystemTest/input), their layer sizes:
+    ((1, 64, 64, 3, 8), (32, 32, 64, 0), 9, 9),     # postTest.params: TransposeConn of an 18x18 dictionary
+    ((16, 64, 64, 3, 8), (32, 32, 64, 0), 9, 9),    # postRecvBatch.params: batch 16
+    ((1, 32, 32, 64, 8), (64, 64, 3, 0), 18, 18),   # postTestOneToMany.params: one-to-many x2
+    ((1, 32, 32, 3, 5), (16, 16, 192, 0), 6, 6),    # oneToTwo.params / twoToOneAccumulation.params, 192 features
+    ((1, 32, 32, 3, 3), (16, 16, 192, 0), 4, 4),
 ]
 
 
