@@ -236,24 +236,42 @@ def test_deliver_post_matches_oracle(cuda, oracle, case):
             np.testing.assert_allclose(out, ref, rtol=RTOL_FP32, atol=1e-5 * np.abs(ref).max())
 
 
-def test_pre_and_post_perspective_agree(cuda, oracle):
+# (pre nbatch, nx, ny, nf), (post nx, ny, nf), patch of the pre -> post connection
+PRE_POST_CASES = [
+    ((2, 32, 32, 8), (16, 16, 16), 4),
+    # tests/ReceiveFromPostTest/input of the reference, their layer sizes:
+    ((1, 32, 32, 3), (16, 16, 10), 2),     # manyToOnePatchSizeTest.params
+    ((1, 4, 4, 3), (8, 8, 10), 4),         # oneToManyPatchSizeTest.params
+    ((1, 16, 16, 96), (8, 8, 384), 3),     # postTest.params: TransposeConn of a 6x6x96 one-to-many
+    ((1, 32, 32, 3), (16, 16, 3), 3),      # postTest_ManyToOne.params
+    ((1, 16, 16, 3), (32, 32, 3), 10),     # postTest_OneToMany.params
+]
+
+
+@pytest.mark.parametrize("case", PRE_POST_CASES)
+def test_pre_and_post_perspective_agree(cuda, oracle, case):
     """ReceiveFromPostTest's property: pre- and post-perspective delivery of the same
-    connection give the same GSyn (tolerance n*2^-24, input/postTest.params:176)."""
+    connection give the same GSyn, to the rounding of the terms summed per element
+    (n * 2^-24 of the largest value; postTest.params:176 allows 3e-3)."""
     torch = cuda
     from openpv_gb300 import capi
-    pre = capi.Loc.make(2, 32, 32, 8, 3)
-    post = capi.Loc.make(2, 16, 16, 16, 0)
+    (nb, nx, ny, nf), (qx, qy, qf), p = case
+    pp = oracle.post_patch_size(p, nx, qx)
+    h = max(oracle.required_margin(nx, qx, p), oracle.required_margin(qx, nx, pp))
+    pre = capi.Loc.make(nb, nx, ny, nf, h)
+    post = capi.Loc.make(nb, qx, qy, qf, 0)
     rng = np.random.default_rng(5)
     a = sparse_activity(rng, pre, 0.3)
-    w = rng.normal(0, 0.1, (4 * 8, 4, 4, 16)).astype(np.float32)
-    conn = capi.conn_desc(pre, post, 4, 4)
+    nk = (nx // qx if nx > qx else 1) * (ny // qy if ny > qy else 1) * nf
+    w = rng.normal(0, 0.1, (nk, p, p, qf)).astype(np.float32)
+    conn = capi.conn_desc(pre, post, p, p)
     g_pre = torch.zeros(post.res_shape(), device="cuda")
     capi.deliver_pre(conn, T(torch, w), g_pre, a_ext=T(torch, a))
     w_post = torch.zeros(w.size, device="cuda")
     capi.transpose_weights(conn, T(torch, w), w_post)
     g_post = torch.zeros(post.res_shape(), device="cuda")
     capi.deliver_post(conn, T(torch, a), w_post, g_post)
-    n_inputs = 8 * 8 * 8
+    n_inputs = pp * pp * nf
     np.testing.assert_allclose(H(g_pre), H(g_post), atol=n_inputs * 2.0 ** -24 * np.abs(H(g_pre)).max())
 
 
