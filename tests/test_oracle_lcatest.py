@@ -94,3 +94,17 @@ def test_random_initial_state_matches_the_gpu_lca_test_files(oracle):
     n = L.NXP * L.NXP
     w_file = np.stack([np.frombuffer(raw, np.float32, n, 104 + k * (8 + 4 * n) + 8) for k in range(L.V1_NF)])
     assert np.abs(w_file.reshape(w.shape) - w).max() <= 1e-7
+
+
+def test_host_timescale_stand_in_matches_the_oracle(oracle):
+    """The host-side time-scale update the GPU test uses in place of the column's probe equals
+    the oracle's AdaptiveTimeScaleController restatement step for step: resets (-1), repeated
+    energies, growth up to the cap, an energy increase."""
+    energies = [-1.0, 3171.0, 3190.1, 3176.5, 3100.0, 3050.0, 3049.9, 3049.9, 3000.0, 3500.0, 3400.0, -1.0, 2900.0,
+                2800.0, 2700.0, 2650.0, 2640.0, 2639.0]
+    py = [L.BASE_MIN, L.BASE_MAX, -1.0]
+    c = np.array([[L.BASE_MIN, L.BASE_MAX, -1.0]])
+    for e in energies:
+        py = L.timescale_update(py, e)
+        c = oracle.adaptive_timescale(c, [e], L.BASE_MAX, L.BASE_MIN, L.TAU_FACTOR, L.GROWTH)
+        assert py == list(c[0]), (e, py, c[0])
