@@ -1,7 +1,7 @@
-"""CPU model check of the mbarrier protocols of the LCA solver's persistent kernels
-(openpv_gb300/csrc/lca_solver.cu): the reconstruction kernel R (recon_tc_kernel), the
-post-delivery + update kernel P (post_tc_kernel) and the fused timestep kernel F
-(step_tc_kernel).
+"""CPU model check of the mbarrier protocols of the persistent tensor-core kernels: the LCA
+solver's reconstruction kernel R (recon_tc_kernel), post-delivery + update kernel P
+(post_tc_kernel) and fused timestep kernel F (step_tc_kernel) in openpv_gb300/csrc/lca_solver.cu,
+and the tensor-core delivery (conv_tf32x3_kernel) in openpv_gb300/csrc/deliver_tc.cu.
 
 Every role of one CTA runs as a coroutine over exact mbarrier semantics (a wait for phase k
 tests parity k & 1 and passes once the barrier has completed a phase of the other parity; a
@@ -466,6 +466,118 @@ def run_kernel_f(n_blk, n_v, n_w, tiles, seed, group_slots=True):
 
 
 # ---------------------------------------------------------------------------------------------
+# the tensor-core delivery (conv_tf32x3_kernel, openpv_gb300/csrc/deliver_tc.cu): TMA producer,
+# MMA issuer, 4 split warps (each on its own), 4 epilogue warps (each on its own)
+# ---------------------------------------------------------------------------------------------
+def run_conv_tc(R, NS, NR, NB, KX, KY, nFC, units, seed):
+    """R target rows per unit, NS split-row slots, NR raw-row slots, NB weight-tile slots,
+    KX x KY patch, nFC 32-feature source chunks, units of this CTA."""
+    s = _Sim(seed)
+    for i in range(NR):
+        s.mk(f"rawFull{i}")
+        s.mk(f"rawEmpty{i}", 4)
+    for i in range(NS):
+        s.mk(f"aReady{i}", 4)
+        s.mk(f"aEmpty{i}")
+    for i in range(NB):
+        s.mk(f"bFull{i}")
+        s.mk(f"bEmpty{i}")
+    for i in range(2):
+        s.mk(f"chainFull{i}")
+        s.mk(f"chainEmpty{i}", 4)
+    rows_per_fc = R + KY - 1
+    groups_per_unit = nFC * KY
+    groups_per_chain = max(1, min(KY, (7 + KX - 1) // KX))
+    chains_per_unit = (groups_per_unit + groups_per_chain - 1) // groups_per_chain
+
+    def producer():
+        ca = cb = 0
+        for _ in range(units):
+            for _ in range(nFC):
+                def load_a():
+                    nonlocal ca
+                    rr = ca % NR
+                    if ca >= NR:
+                        yield from s.wait(f"rawEmpty{rr}", ca // NR - 1)
+                    s.async_q.append(f"rawFull{rr}")
+                    ca += 1
+                    yield "step"
+
+                def load_b():
+                    nonlocal cb
+                    d = cb % NB
+                    if cb >= NB:
+                        yield from s.wait(f"bEmpty{d}", cb // NB - 1)
+                    s.async_q.append(f"bFull{d}")  # the hi and lo weight rows
+                    cb += 1
+                    yield "step"
+
+                for _ in range(R - 1):
+                    yield from load_a()
+                for _ in range(KY):
+                    yield from load_a()
+                    for _ in range(KX):
+                        yield from load_b()
+
+    def mma():
+        cbase = cb = cc = 0
+        slot_base = 0
+        for _ in range(units):
+            grp = 0
+            for _ in range(nFC):
+                for ky in range(KY):
+                    if grp % groups_per_chain == 0 and cc >= 2:
+                        yield from s.wait(f"chainEmpty{cc & 1}", (cc >> 1) - 1)
+                    for j in range(0 if ky == 0 else ky + R - 1, ky + R):
+                        c = cbase + j
+                        yield from s.wait(f"aReady{c % NS}", c // NS)
+                    slot_ky = (slot_base + ky) % NS
+                    for _ in range(KX):
+                        yield from s.wait(f"bFull{cb % NB}", cb // NB)
+                        s.commit_q.append(f"bEmpty{cb % NB}")
+                        cb += 1
+                        yield "step"
+                    s.commit_q.append(f"aEmpty{slot_ky}")  # row ky has no later use
+                    if (grp + 1) % groups_per_chain == 0 or grp + 1 == groups_per_unit:
+                        s.commit_q.append(f"chainFull{cc & 1}")
+                        cc += 1
+                    grp += 1
+                for j in range(KY, rows_per_fc):
+                    s.commit_q.append(f"aEmpty{(slot_base + j) % NS}")
+                cbase += rows_per_fc
+                slot_base = (slot_base + rows_per_fc) % NS
+
+    def split(w):
+        c = 0
+        for _ in range(units):
+            for _ in range(nFC):
+                for _ in range(rows_per_fc):
+                    rr, sl = c % NR, c % NS
+                    yield from s.wait(f"rawFull{rr}", c // NR)
+                    if c >= NS:
+                        yield from s.wait(f"aEmpty{sl}", c // NS - 1)
+                    yield "step"  # hi / lo split of the row
+                    s.arrive(f"aReady{sl}")
+                    s.arrive(f"rawEmpty{rr}")
+                    c += 1
+
+    def epilogue(w):
+        cc = 0
+        for _ in range(units):
+            for _ in range(chains_per_unit):
+                yield from s.wait(f"chainFull{cc & 1}", cc >> 1)
+                yield "step"  # the chain's sums
+                s.arrive(f"chainEmpty{cc & 1}")
+                cc += 1
+
+    roles = {"tma": producer(), "mma": mma()}
+    for w in range(4):
+        roles[f"split{w}"] = split(w)
+        roles[f"epi{w}"] = epilogue(w)
+    return s.run(roles)
+
+
+# ---------------------------------------------------------------------------------------------
 @pytest.mark.parametrize("n_stage", [2, 3, 4])
 def test_kernel_r_protocol(n_stage):
     """Kernel R: every ring depth the solver uses, 1-2 position blocks per image, 0-5 images
@@ -518,3 +630,17 @@ def test_kernel_p_early_im2col_is_caught():
     found = [run_kernel_p(4, 1, 1, 2, seed, k_im=0) for seed in range(4)]
     assert any(r.startswith("deadlock") for r in found), found
     assert all(run_kernel_p(4, 1, 1, 2, seed) == "ok" for seed in range(4))
+
+
+@pytest.mark.parametrize("R", [1, 2, 3, 4])
+def test_conv_tc_protocol(R):
+    """The tensor-core delivery: split-row rings of R + 1 and R + 2 slots, one or two raw rows,
+    2-8 weight-tile slots, patches of 1x1 to 9x9, 1-3 source chunks, 0-3 units per CTA."""
+    for NS in (R + 1, R + 2):
+        for NR in (1, 2):
+            for NB in (2, 3, 8):
+                for KX, KY in ((1, 1), (3, 3), (7, 7), (9, 5)):
+                    for nFC in (1, 3):
+                        for units in (0, 1, 3):
+                            r = run_conv_tc(R, NS, NR, NB, KX, KY, nFC, units, seed=R + NS + NB + KX + units)
+                            assert r == "ok", (R, NS, NR, NB, KX, KY, nFC, units, r)
