@@ -597,12 +597,22 @@ def dictlearn_bench(torch, capi, reps=5):
     O.lca_run(p, w, x_np[None, :cores], cpu_steps, np.zeros((cores,) + v1, np.float32), threads=cores,
               want_recon=False)
     cpu_s = time.perf_counter() - t0
+    emulated = bool(grad.emulated_fp32())
+    fp32_tf = flops / (ms / 1000.0) / 1e12
+    # the emulated FP32 GEMM issues 9 BF16 products per FP32 product (each operand in three BF16
+    # parts); averaged over the whole gradient (the fold / im2col / update kernels included)
+    issued = fp32_tf * (9 if emulated else 1)
+    pk = peaks()
+    roofline = ({"bound": "tensor", "achieved": issued, "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
+                 "frac": issued / pk["bf16_tflops"], "peak_source": pk.get("source", "fallback"),
+                 "what": "BF16 products issued by the GEMMs, averaged over the whole gradient"}
+                if emulated else None)
     return {"workload": "32 x 64x64x1 -> V1 16x16x256 stride 4, 256 x 16x16x1 dictionary, 100 unrolled "
                         "timesteps (checkpoint every 10), gradient of 0.5||x - W^T a||^2 + 0.1||a||_1 w.r.t. W",
             "ms_per_gradient": ms, "image_steps_per_s": nb * T / (ms / 1000.0), "loss": float(loss.item()),
             "grad_norm": float(dw.norm().item()), "dtype": "f32",
-            "gemm_math": "fp32 emulated on bf16 tensor cores" if grad.emulated_fp32() else "fp32",
-            "gemm_tflops_fp32_equivalent": flops / (ms / 1000.0) / 1e12,
+            "gemm_math": "fp32 emulated on bf16 tensor cores" if emulated else "fp32",
+            "gemm_tflops_fp32_equivalent": fp32_tf, "roofline": roofline,
             "cpu_baseline": {"value": cores * cpu_steps / cpu_s, "unit": "image-steps/s", "cores": cores,
                              "kind": "port", "sample": f"oracle LCA solve (forward only) of {cores} images x "
                                                        f"{cpu_steps} timesteps, one image per thread "
