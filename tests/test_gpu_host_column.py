@@ -174,7 +174,6 @@ def test_one_to_one_gpu_delivery_in_the_column(capi, oracle, post):
     """A one-to-one HyPerConn with 32 / 64 features: the postsynaptic GPU keyword runs the
     tensor-core delivery, the presynaptic one the sparse kernel; both within 1e-5 of the oracle's
     FP32 delivery of the input frame (HyPerLayer: V = GSyn)."""
-    from tests.test_gpu_kernels import OL
     nb, nx, ny, cin, cout, p = 2, 40, 12, 32, 64, 5
     rng = np.random.default_rng(17)
     x = ((rng.random((nb, ny, nx, cin)) < 0.3) * rng.uniform(0, 1, (nb, ny, nx, cin))).astype(np.float32)
@@ -217,7 +216,6 @@ def test_lif_network_from_params_with_pvp_input_and_output(capi, oracle, tmp_pat
     into the EXC channel of a LIFLayer (Heun method), and both layers write their activity to
     <outputPath>/<layer>.pvp every step from t = 0.  The written frames equal the oracle's network
     composed from the pinned pieces, bit for bit."""
-    from tests.test_gpu_kernels import OL
     nb, n, p, steps, F = 2, 24, 5, 5, 6
     rng = np.random.default_rng(41)
     frames = (rng.random((F, n, n, 1)) < 0.08).astype(np.float32)
