@@ -1,7 +1,7 @@
 // standin_framework.hpp -- stand-ins for the OpenPV framework classes that the adapters in
 // adapters/ touch (layer buffers, publisher, weights, arbor list, CUDA device and buffer, the
 // delivery and component base classes), so that the very same adapter translation units can be
-// compiled and driven on a GPU machine that has no reference tree.  Only the members the adapters
+// compiled and driven on a GPU host without the reference's source tree.  Only the members the adapters
 // use exist; their meaning follows the reference's (columns/BaseObject.hpp,
 // components/{BasePublisherComponent,ComponentBuffer,LayerInputBuffer,Weights,WeightsPair,
 // ArborList}.hpp, arch/cuda/{CudaBuffer,CudaDevice}.hpp, delivery/HyPerDelivery.hpp).  Buffers

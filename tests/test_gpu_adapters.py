@@ -1,6 +1,6 @@
 """The drop-in adapters of adapters/ -- the replacement bodies of the reference's GPU delivery and
 update translation units -- compiled unchanged against stand-ins of the framework classes
-(tests/adapter_standins; the GPU machine has no reference tree) and driven through the framework's
+(tests/adapter_standins; a GPU host need not have the reference's source tree) and driven through the framework's
 life cycle (communicateInitInfo, setCudaDevice, allocateDataStructures, copyInitialStateToGPU,
 deliver / runKernel) on device buffers, against the oracle (whose loops are pinned bit for bit
 to the reference's own compiled code):
