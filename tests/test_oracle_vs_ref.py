@@ -231,6 +231,40 @@ def test_deliver_post_bitexact_vs_reference(oracle, case):
     assert np.array_equal(mine.view(np.uint32), ref.view(np.uint32))
 
 
+# ReceiveFromPostTest (tests/ReceiveFromPostTest/input of the reference): the layer sizes of its
+# params files -- (pre nbatch, nx, ny, nf), (post nx, ny, nf), patch of the pre -> post connection
+RECEIVE_FROM_POST_CASES = [
+    ((1, 32, 32, 3), (16, 16, 10), 2),     # manyToOnePatchSizeTest.params
+    ((1, 4, 4, 3), (8, 8, 10), 4),         # oneToManyPatchSizeTest.params
+    ((1, 16, 16, 96), (8, 8, 384), 3),     # postTest.params
+    ((1, 32, 32, 3), (16, 16, 3), 3),      # postTest_ManyToOne.params
+    ((1, 16, 16, 3), (32, 32, 3), 10),     # postTest_OneToMany.params
+]
+
+
+@pytest.mark.parametrize("case", RECEIVE_FROM_POST_CASES)
+def test_transpose_is_what_the_reference_post_delivery_expects(oracle, case):
+    """The oracle's transpose of shared weights (TransposeWeights::transposeShared,
+    utils/TransposeWeights.cpp:56-115; the GPU transpose equals it bit for bit) fed to the
+    reference's own postsynaptic delivery reproduces the reference's own presynaptic delivery of
+    the original weights to the rounding of the terms summed per element -- ReceiveFromPostTest's
+    check, here with the reference's compiled delivery loops on both sides."""
+    (nb, nx, ny, nf), (qx, qy, qf), p = case
+    pp = oracle.post_patch_size(p, nx, qx)
+    h = max(oracle.required_margin(nx, qx, p), oracle.required_margin(qx, nx, pp))
+    pre, post = L(oracle, nb, nx, ny, nf, h), L(oracle, nb, qx, qy, qf, 0)
+    rng = np.random.default_rng(7)
+    a = _activity(rng, pre, 0.3)
+    nk = (nx // qx if nx > qx else 1) * (ny // qy if ny > qy else 1) * nf
+    w = rng.normal(0, 0.1, (nk, p, p, qf)).astype(np.float32)
+    g_pre = refbuild.deliver_pre(pre, post, p, p, w, a_ext=a, gsyn=np.zeros(post.res_shape(), np.float32))
+    w_post = oracle.transpose_shared(pre, post, p, p, w)
+    g_post = refbuild.deliver_post(pre, post, pp, pp, w_post, a, gsyn=np.zeros(post.res_shape(), np.float32))
+    n_inputs = pp * pp * nf
+    np.testing.assert_allclose(g_post, g_pre, atol=n_inputs * 2.0 ** -24 * np.abs(g_pre).max())
+    assert np.abs(g_pre).max() > 0
+
+
 def lif_state(oracle, loc, rng, seed):
     n = loc.nbatch * loc.nx * loc.ny * loc.nf
     return {"rnd": oracle.taus_init(n, seed),
