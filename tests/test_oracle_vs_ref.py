@@ -178,6 +178,10 @@ DELIVERY_CASES = [  # (pre nb,nx,ny,nf,halo), (post nx,ny,nf,halo), nxp, nyp
     ((2, 32, 32, 2, 6), (8, 8, 3, 0), 4, 4),       # many-to-one x4
     ((1, 12, 8, 3, 1), (24, 16, 2, 2), 6, 4),      # one-to-many, unequal axes
     ((1, 16, 16, 4, 2), (64, 64, 1, 6), 16, 16),   # one-to-many x4
+    # the layer sizes of the reference's GPU system tests (tests/GPUSystemTest/input)
+    ((1, 32, 32, 3, 1), (64, 64, 3, 0), 6, 6),     # preTest.params
+    ((2, 32, 32, 3, 8), (16, 16, 64, 0), 9, 9),    # preRecvBatch.params
+    ((1, 32, 32, 64, 4), (64, 64, 3, 0), 18, 18),  # the reconstruction of postTestOneToMany.params
 ]
 
 
@@ -212,6 +216,10 @@ POST_CASES = [  # connection pre -> post, delivered from the post perspective
     ((1, 24, 24, 5, 3), (24, 24, 4, 0), 7, 7),
     ((2, 8, 8, 3, 2), (16, 16, 2, 1), 4, 4),
     ((1, 64, 64, 1, 6), (16, 16, 4, 2), 4, 4),
+    # the layer sizes of the reference's GPU system tests (tests/GPUSystemTest/input)
+    ((1, 64, 64, 3, 8), (32, 32, 64, 0), 9, 9),    # postTest.params
+    ((1, 32, 32, 64, 8), (64, 64, 3, 0), 18, 18),  # postTestOneToMany.params
+    ((1, 32, 32, 3, 5), (16, 16, 192, 0), 6, 6),   # oneToTwo.params / twoToOneAccumulation.params
 ]
 
 
