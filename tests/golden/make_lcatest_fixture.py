@@ -1,8 +1,11 @@
-"""Writes tests/golden/lcatest_correct.npz from the reference's LCA system test
-(tests/LCATest/input of the OpenPV tree, LCATest.params): the two input frames the test's
-PvpLayer "Input" shows (inputImages.pvp) and the frames of the known-answer reconstruction
-(correct.pvp, 40 frames, compared by the test with the Reconstruction layer at every timestep
-to 1e-6) at the timesteps listed in STEPS.  Run once where the reference tree is mounted:
+"""Writes the known-answer fixtures of the reference's LCA system tests (OpenPV tree):
+  tests/golden/lcatest_correct.npz from tests/LCATest/input (LCATest.params): the two input
+  frames the test's PvpLayer "Input" shows (inputImages.pvp) and the frames of the known-answer
+  reconstruction (correct.pvp, 40 frames, compared by the test with the Reconstruction layer at
+  every timestep to 1e-6) at the timesteps listed in STEPS;
+  tests/golden/momentumlcatest_correct.npz from tests/MomentumLCATest/input
+  (MomentumLCATest.params): the test image and all 10 known-answer reconstruction frames.
+Run once where the reference tree is mounted:
 
     python tests/golden/make_lcatest_fixture.py /path/to/OpenPV
 """
@@ -34,7 +37,20 @@ def read_dense_pvp(path):
     return frames, times
 
 
+def momentum_fixture(ref_root):
+    """tests/MomentumLCATest/input: the 60x60 test image and all 10 known-answer frames."""
+    d = os.path.join(ref_root, "tests", "MomentumLCATest", "input")
+    x, xt = read_dense_pvp(os.path.join(d, "testimage.pvp"))
+    c, ct = read_dense_pvp(os.path.join(d, "correct.pvp"))
+    assert x.shape == (1, 60, 60, 1) and c.shape == (10, 60, 60, 1)
+    assert np.array_equal(ct, np.arange(1, 11, dtype=np.float64))
+    out = os.path.join(os.path.dirname(os.path.abspath(__file__)), "momentumlcatest_correct.npz")
+    np.savez_compressed(out, input_frame=x, correct=c)
+    print("wrote", out)
+
+
 def main(ref_root):
+    momentum_fixture(ref_root)
     d = os.path.join(ref_root, "tests", "LCATest", "input")
     x, xt = read_dense_pvp(os.path.join(d, "inputImages.pvp"))
     c, ct = read_dense_pvp(os.path.join(d, "correct.pvp"))

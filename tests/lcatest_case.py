@@ -56,7 +56,7 @@ def locs(O_or_capi):
     return L.make(1, V1_NX, V1_NY, V1_NF, 4), L.make(1, IN_NX, IN_NY, 1, 8)
 
 
-def timescale_update(state, energy):
+def timescale_update(state, energy, base_max=BASE_MAX, base_min=BASE_MIN, tau_factor=TAU_FACTOR, growth=GROWTH):
     """AdaptiveTimeScaleController::calcTimesteps (components/AdaptiveTimeScaleController.cpp:57-86)
     for one batch element; state = [timeScale, timeScaleMax, timeScaleTrue], energy = the total
     energy of the previous timestep, or -1 where the trigger layer updates this timestep."""
@@ -65,11 +65,11 @@ def timescale_update(state, energy):
         return state
     dE = (e0 - energy) / ts
     if dE < 0.0 or e0 <= 0.0 or energy <= 0.0:
-        return [BASE_MIN, BASE_MAX, energy]
-    ts = TAU_FACTOR * (e0 / dE)
+        return [base_min, base_max, energy]
+    ts = tau_factor * (e0 / dE)
     if ts >= tsmax:
         ts = tsmax
-        tsmax = tsmax * (1 + GROWTH)
+        tsmax = tsmax * (1 + growth)
     return [ts, tsmax, energy]
 
 

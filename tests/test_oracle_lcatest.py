@@ -108,3 +108,30 @@ def test_host_timescale_stand_in_matches_the_oracle(oracle):
         py = L.timescale_update(py, e)
         c = oracle.adaptive_timescale(c, [e], L.BASE_MAX, L.BASE_MIN, L.TAU_FACTOR, L.GROWTH)
         assert py == list(c[0]), (e, py, c[0])
+
+
+def test_momentum_lca_module_reproduces_momentumlcatest_bit_for_bit(oracle):
+    """The reference's momentum-LCA system test (tests/MomentumLCATest, described in
+    tests/momentumlcatest_case.py): V1 feeding the residual directly (its initial activity at
+    timestep 1), MomentumLCALayer, the time step triggered by the input every 5 steps.  The
+    oracle's composition from its pinned primitives reproduces all 10 known-answer frames bit for
+    bit (the test itself allows 1e-4)."""
+    from tests import momentumlcatest_case as M
+    x, correct = M.fixture()
+    v0, w = M.initial_state(oracle)
+    steps = M.oracle_steps(oracle, x, v0, w)
+    for t in range(M.STEPS):
+        got = steps[t]["rec"].reshape(M.IN_N, M.IN_N)
+        assert np.array_equal(got.view(np.uint32), correct[t, :, :, 0].view(np.uint32)), t
+    assert steps[0]["dt"] == M.BASE_MIN and steps[M.DISPLAY]["dt"] == M.BASE_MIN
+    c, _ = _reference_file("MomentumLCATest", "correct.pvp")
+    if c is not None:
+        assert np.array_equal(c, correct)
+
+
+def _reference_file(test, name):
+    path = os.path.join(REF_ROOT, "tests", test, "input", name)
+    if not os.path.exists(path):
+        return None, None
+    from tests.golden.make_lcatest_fixture import read_dense_pvp
+    return read_dense_pvp(path)
