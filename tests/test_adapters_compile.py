@@ -18,6 +18,8 @@ OBJS = {
     "PostsynapticPerspectiveGPUDelivery": ["pvgpu_deliver_post", "pvgpu_deliver_post_tc",
                                            "pvgpu_deliver_tc_workspace_bytes"],
     "HyPerLCAInternalStateBuffer": ["pvgpu_lca_update"],
+    "MomentumLCAInternalStateBuffer": ["pvgpu_momentum_lca_update"],
+    "ISTAInternalStateBuffer": ["pvgpu_ista_update"],
     "ANNActivityBuffer": ["pvgpu_ann_vertices"],
     "GSynAccumulator": ["pvgpu_gsyn_accumulate"],
     "CudaKernel": [],
